@@ -1,0 +1,283 @@
+/*
+ * e8g.h — C ABI of the GB300 path-tracing core.
+ *
+ * Every entry point returns an e8g_status and never throws. Pointers are plain host pointers
+ * unless the function name ends in `_dev`, in which case they are CUDA device pointers and the
+ * call is asynchronous on the stream passed in (NULL = the context's own stream).
+ *
+ * The entry points replace, one for one, the reference interfaces of e8yescg's corelib
+ * (paths relative to the reference project):
+ *
+ *   e8g_scene_upload + e8g_scene_build_bvh
+ *       if_path_space::load / bvh_path_space_layout::commit   corelib/src/pathspace.cpp:15-19, :292-328
+ *       if_material_container::load                           corelib/src/materialcontainer.cpp:19-23
+ *       if_light_sources::load / basic_light_sources::commit  corelib/src/lightsources.cpp:11-18, :45-52
+ *       camera_container / pinhole_camera::transform          corelib/src/camera.cpp:63-71
+ *   e8g_trace_closest   bvh_path_space_layout::intersect      corelib/src/pathspace.cpp:330-413
+ *   e8g_trace_any       bvh_path_space_layout::has_intersect  corelib/src/pathspace.cpp:415-456
+ *   e8g_camera_rays     pinhole_camera::sample                corelib/src/camera.cpp:38-48
+ *   e8g_render          pt_image_renderer::render             corelib/src/renderer.cpp:106-166
+ *   e8g_render_paths    if_path_tracer::sample (one ray per call, as the reference's own
+ *                       furnace test drives it)              corelib/src/pathtracer.h:59-63,
+ *                                                            corelib/test/tst_pathtracer/tst_pathtracer.cpp:58-86
+ *   e8g_forward / e8g_backward, e8g_batch_render: no counterpart in the reference (new).
+ */
+#ifndef E8G_H
+#define E8G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum e8g_status {
+    E8G_OK = 0,
+    E8G_ERR_INVALID_ARG = 1,
+    E8G_ERR_CUDA = 2,
+    E8G_ERR_OUT_OF_MEMORY = 3,
+    E8G_ERR_NO_SCENE = 4,
+    E8G_ERR_NOT_BUILT = 5,
+    E8G_ERR_UNSUPPORTED = 6,
+    E8G_ERR_TIMEOUT = 7,
+    E8G_ERR_INTERNAL = 8,
+    E8G_ERR_NO_DEVICE = 9
+} e8g_status;
+
+typedef struct e8g_ctx e8g_ctx;
+
+typedef struct e8g_device_opts {
+    int device;     /* CUDA ordinal */
+    uint32_t flags; /* reserved, 0 */
+} e8g_device_opts;
+
+/* ---------------------------------------------------------------- scene ---- */
+
+/* Material types: corelib/src/material.h:96-199. */
+enum {
+    E8G_MAT_FAIL_SAFE = 0,  /* mat_fail_safe: Lambert rho=0.8, no cosine cut   material.cpp:54-76 */
+    E8G_MAT_OREN_NAYAR = 1, /* oren_nayar(albedo, sigma)                       material.cpp:108-169 */
+    E8G_MAT_COOK_TORR = 2,  /* cook_torr(albedo, roughness, complex ior)       material.cpp:171-252 */
+    E8G_MAT_MIXTURE = 3     /* mat_mixture(mix0, mix1, ratio)                   material.cpp:78-106 */
+};
+
+typedef struct e8g_material {
+    uint32_t type;
+    float albedo[3];
+    float roughness; /* oren_nayar: sigma; cook_torr: r, alpha^2 = 2 r^2 (material.cpp:176) */
+    float ior_re;    /* cook_torr complex index of refraction */
+    float ior_im;
+    int32_t mix0; /* mixture: indices of two non-mixture materials */
+    int32_t mix1;
+    float ratio; /* mixture: probability of mix0 */
+} e8g_material;
+
+/* area_light on a mesh of the scene: light.cpp:17-71. */
+typedef struct e8g_light {
+    uint32_t mesh;
+    float radiance[3];
+} e8g_light;
+
+/* pinhole_camera after transform(): camera.cpp:23-30, :63-71.
+ * rot is the 3x3 upper-left block of the camera transform, row-major. */
+typedef struct e8g_camera {
+    float origin[3];
+    float rot[9];
+    float sensor_size;
+    float focal_len;
+    float aspect;
+} e8g_camera;
+
+/*
+ * A scene is a list of triangle meshes (corelib trimesh), given in the order of the reference
+ * path space's std::map, i.e. ascending object id. Meshes are already in world space.
+ * Lights are given in ascending object id order (the order basic_light_sources::commit walks).
+ * All arrays are caller-owned host memory and are copied by e8g_scene_upload.
+ */
+typedef struct e8g_scene_desc {
+    uint32_t num_meshes;
+    const uint32_t *mesh_vert_offset; /* num_meshes + 1 prefix offsets into positions/normals */
+    const uint32_t *mesh_tri_offset;  /* num_meshes + 1 prefix offsets into triangles */
+    const int32_t *mesh_material;     /* per mesh: index into materials, -1 = fail-safe */
+    const float *positions;           /* 3 * V */
+    const float *normals;             /* 3 * V */
+    const uint32_t *triangles;        /* 3 * T, mesh-local vertex indices */
+    uint32_t num_materials;
+    const e8g_material *materials;
+    uint32_t num_lights;
+    const e8g_light *lights;
+    e8g_camera camera;
+} e8g_scene_desc;
+
+typedef struct e8g_bvh_opts {
+    uint32_t max_leaf_prims; /* reference BVH_MAX_PRIMS = 4   pathspace.cpp:121 */
+    uint32_t num_bins;       /* reference BVH_BUCKET_COUNT = 20 pathspace.cpp:122 */
+    float tri_cost;          /* reference BVH_RAY_TRIANGLE_COST = 8 */
+    float node_cost;         /* reference BVH_RAY_BOX_COST = 1 */
+    uint32_t num_threads;    /* host build threads, 0 = all */
+} e8g_bvh_opts;
+
+typedef struct e8g_bvh_stats {
+    uint32_t num_nodes;
+    uint32_t num_leaves;
+    uint32_t max_depth;
+    uint32_t num_tris;
+    double avg_leaf_depth;
+    double build_ms;
+    uint64_t node_bytes;
+    uint64_t tri_bytes;
+} e8g_bvh_stats;
+
+/* ----------------------------------------------------------- traversal ---- */
+
+typedef struct e8g_ray {
+    float o[3];
+    float d[3];
+} e8g_ray;
+
+/* Closest hit. mesh = -1 on a miss. b1, b2 are the barycentrics of ray::intersect
+ * (corelib/src/tensor.h:688-725); b0 = 1 - b1 - b2. */
+typedef struct e8g_hit {
+    float t;
+    int32_t mesh;
+    int32_t tri; /* mesh-local triangle index */
+    float b1;
+    float b2;
+} e8g_hit;
+
+/* ------------------------------------------------------------- render ---- */
+
+enum {
+    E8G_MODE_REF_UNI = 0,     /* unidirect_path_tracer        pathtracer.cpp:528-585 */
+    E8G_MODE_REF_LT1 = 1,     /* unidirect_lt1_path_tracer    pathtracer.cpp:587-653 */
+    E8G_MODE_MIS = 2,         /* NEE + BSDF sampling, power-heuristic MIS (new) */
+    E8G_MODE_REF_BDPT = 3,    /* bidirect_mis_path_tracer     pathtracer.cpp:754-803 */
+    E8G_MODE_BDPT_POWER = 4,  /* bidirectional, power-heuristic MIS (new) */
+    E8G_MODE_REF_DIRECT = 5,  /* direct_path_tracer           pathtracer.cpp:508-526 */
+    E8G_MODE_NORMAL = 6,      /* normal_tracer                pathtracer.cpp:492-506 */
+    E8G_MODE_POSITION = 7     /* position_tracer              pathtracer.cpp:474-490 */
+};
+
+enum { E8G_INTEGRATOR_MEGAKERNEL = 0, E8G_INTEGRATOR_WAVEFRONT = 1 };
+
+enum {
+    E8G_RNG_MINSTD = 0, /* the reference's std::minstd_rand0 stream, one stream per path */
+    E8G_RNG_PHILOX = 1  /* Philox4x32-10 counter-based stream */
+};
+
+typedef struct e8g_render_params {
+    uint32_t mode;
+    uint32_t integrator;
+    uint32_t rng;
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint64_t seed;
+    uint32_t max_depth;     /* 0 = unlimited (the reference) */
+    uint32_t rr_start;      /* first depth with Russian roulette (reference: 2) */
+    float rr_prob;          /* survival probability (reference: 0.5) */
+    uint32_t bdpt_max_len;  /* subpath vertex cap (reference: 8, pathtracer.h:201) */
+    uint32_t firefly;       /* 8-neighbour firefly clamp, renderer.cpp:46-83 */
+    uint32_t sample_offset; /* first sample index (progressive rendering) */
+} e8g_render_params;
+
+/* Fill p with the reference's defaults for a mode: rr_start 2, rr_prob 0.5, unlimited depth,
+ * bdpt_max_len 8, minstd stream for reference modes and Philox otherwise. */
+void e8g_default_params(e8g_render_params *p, uint32_t mode, uint32_t width, uint32_t height,
+                        uint32_t spp);
+
+/* Per-path seed of the minstd stream for (seed, pixel, sample): the value an oracle feeds to
+ * e8util::rng(unsigned) so both sides draw the same sequence. */
+uint32_t e8g_path_seed(uint64_t seed, uint32_t pixel, uint32_t sample);
+
+typedef struct e8g_render_stats {
+    double ms;          /* device time of the render, CUDA events */
+    double kernel_ms;   /* device time of the dominant kernel */
+    uint64_t paths;
+    uint64_t rays;      /* extension + shadow rays traced (when counted) */
+    uint64_t nodes;     /* BVH nodes whose box was fetched (when counted) */
+    uint64_t tris;      /* triangles tested (when counted) */
+    uint32_t launches;  /* kernels launched by the call */
+    uint32_t counted;   /* 1 when rays/nodes/tris are filled */
+} e8g_render_stats;
+
+/* ------------------------------------------------------------ batch ---- */
+
+typedef struct e8g_batch_item {
+    const e8g_scene_desc *scene;
+    e8g_render_params params;
+    float *rgba_out; /* host, width*height*4 */
+} e8g_batch_item;
+
+/* ----------------------------------------------------------- functions ---- */
+
+e8g_status e8g_create(e8g_ctx **ctx, const e8g_device_opts *opts);
+e8g_status e8g_destroy(e8g_ctx *ctx);
+const char *e8g_last_error(const e8g_ctx *ctx);
+const char *e8g_version(void);
+
+e8g_status e8g_scene_upload(e8g_ctx *ctx, const e8g_scene_desc *desc);
+e8g_status e8g_scene_build_bvh(e8g_ctx *ctx, const e8g_bvh_opts *opts);
+e8g_status e8g_bvh_get_stats(const e8g_ctx *ctx, e8g_bvh_stats *stats);
+void e8g_default_bvh_opts(e8g_bvh_opts *opts);
+
+e8g_status e8g_camera_rays(e8g_ctx *ctx, uint32_t width, uint32_t height, e8g_ray *rays_out);
+
+e8g_status e8g_trace_closest(e8g_ctx *ctx, const e8g_ray *rays, uint32_t n, e8g_hit *hits);
+e8g_status e8g_trace_any(e8g_ctx *ctx, const e8g_ray *rays, const float *t_min, const float *t_max,
+                         uint32_t n, uint8_t *occluded);
+e8g_status e8g_trace_closest_dev(e8g_ctx *ctx, const e8g_ray *d_rays, uint32_t n, e8g_hit *d_hits,
+                                 void *stream);
+
+/* Image render: rgba_out is host memory of width*height*4 floats (alpha = 1). */
+e8g_status e8g_render(e8g_ctx *ctx, const e8g_render_params *params, float *rgba_out);
+/* Same, writing a device buffer; the caller synchronises. */
+e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
+                          void *stream);
+e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
+
+/* Per-path radiance for an explicit list of (pixel, sample) pairs: rgb_out is 3*n floats. */
+e8g_status e8g_render_paths(e8g_ctx *ctx, const e8g_render_params *params, const uint32_t *pixel,
+                            const uint32_t *sample, uint32_t n, float *rgb_out);
+
+/* Differentiable render (path-replay adjoint). e8g_forward renders like e8g_render and keeps
+ * the parameters; e8g_backward replays every path and accumulates dLoss/d(albedo) (3 floats per
+ * material) and dLoss/d(roughness) (1 float per material) given dLoss/d(image) (width*height*3).
+ * Gradients are with respect to e8g_material::albedo and e8g_material::roughness. */
+e8g_status e8g_forward(e8g_ctx *ctx, const e8g_render_params *params, float *rgba_out);
+e8g_status e8g_backward(e8g_ctx *ctx, const float *dl_dimage, float *d_albedo, float *d_roughness);
+/* Overwrite material parameters of the uploaded scene without re-uploading geometry. */
+e8g_status e8g_set_materials(e8g_ctx *ctx, const e8g_material *materials, uint32_t n);
+
+/* Render many independent scenes in one persistent launch (wavefront, batched). */
+e8g_status e8g_batch_render(e8g_ctx *ctx, const e8g_batch_item *items, uint32_t n,
+                            e8g_render_stats *stats);
+
+/* Host-side scene generators (no GPU needed): fill a scene owned by the library. */
+typedef struct e8g_host_scene e8g_host_scene;
+enum {
+    E8G_GEN_CORNELL = 0,        /* unit Cornell box, two rotated boxes, 0.25^2 light */
+    E8G_GEN_DISPLACED_ICO = 1,  /* displaced icosphere on a ground plane, 4 quad lights */
+    E8G_GEN_SOUP = 2,           /* random triangle soup in an enclosing box */
+    E8G_GEN_FURNACE = 3         /* inward uv_sphere, Lambert 0.7, L = 1 (tst_pathtracer.cpp:24-56) */
+};
+typedef struct e8g_gen_opts {
+    uint32_t kind;
+    uint64_t seed;
+    uint32_t level;         /* icosphere subdivision level / uv_sphere resolution */
+    uint32_t num_tris;      /* soup size */
+    uint32_t num_materials; /* icosphere materials */
+    float amplitude;        /* displacement amplitude */
+    float roughness_lo, roughness_hi;
+    uint32_t width, height; /* camera aspect */
+} e8g_gen_opts;
+e8g_status e8g_gen_scene(const e8g_gen_opts *opts, e8g_host_scene **out);
+e8g_status e8g_host_scene_desc(const e8g_host_scene *s, e8g_scene_desc *desc);
+void e8g_host_scene_free(e8g_host_scene *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* E8G_H */

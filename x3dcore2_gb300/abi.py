@@ -1,0 +1,175 @@
+"""ctypes mirror of include/e8g.h and the loader of the in-tree native library.
+
+The native library (libe8g.so, built by x3dcore2_gb300.build) holds the CUDA kernels and the
+C++ host code. There is no fallback: if the library is missing, loading raises.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libe8g.so")
+
+# status codes
+E8G_OK = 0
+STATUS_NAMES = {
+    0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "NO_SCENE", 5: "NOT_BUILT",
+    6: "UNSUPPORTED", 7: "TIMEOUT", 8: "INTERNAL", 9: "NO_DEVICE",
+}
+
+# materials
+MAT_FAIL_SAFE, MAT_OREN_NAYAR, MAT_COOK_TORR, MAT_MIXTURE = 0, 1, 2, 3
+# integrator modes
+MODE_REF_UNI, MODE_REF_LT1, MODE_MIS, MODE_REF_BDPT, MODE_BDPT_POWER = 0, 1, 2, 3, 4
+MODE_REF_DIRECT, MODE_NORMAL, MODE_POSITION = 5, 6, 7
+INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT = 0, 1
+RNG_MINSTD, RNG_PHILOX = 0, 1
+# generators
+GEN_CORNELL, GEN_DISPLACED_ICO, GEN_SOUP, GEN_FURNACE = 0, 1, 2, 3
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("albedo", C.c_float * 3), ("roughness", C.c_float),
+                ("ior_re", C.c_float), ("ior_im", C.c_float), ("mix0", C.c_int32),
+                ("mix1", C.c_int32), ("ratio", C.c_float)]
+
+
+class Light(C.Structure):
+    _fields_ = [("mesh", C.c_uint32), ("radiance", C.c_float * 3)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("rot", C.c_float * 9), ("sensor_size", C.c_float),
+                ("focal_len", C.c_float), ("aspect", C.c_float)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_meshes", C.c_uint32),
+                ("mesh_vert_offset", C.POINTER(C.c_uint32)),
+                ("mesh_tri_offset", C.POINTER(C.c_uint32)),
+                ("mesh_material", C.POINTER(C.c_int32)),
+                ("positions", C.POINTER(C.c_float)),
+                ("normals", C.POINTER(C.c_float)),
+                ("triangles", C.POINTER(C.c_uint32)),
+                ("num_materials", C.c_uint32),
+                ("materials", C.POINTER(Material)),
+                ("num_lights", C.c_uint32),
+                ("lights", C.POINTER(Light)),
+                ("camera", Camera)]
+
+
+class BvhOpts(C.Structure):
+    _fields_ = [("max_leaf_prims", C.c_uint32), ("num_bins", C.c_uint32), ("tri_cost", C.c_float),
+                ("node_cost", C.c_float), ("num_threads", C.c_uint32)]
+
+
+class BvhStats(C.Structure):
+    _fields_ = [("num_nodes", C.c_uint32), ("num_leaves", C.c_uint32), ("max_depth", C.c_uint32),
+                ("num_tris", C.c_uint32), ("avg_leaf_depth", C.c_double), ("build_ms", C.c_double),
+                ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64)]
+
+
+class Ray(C.Structure):
+    _fields_ = [("o", C.c_float * 3), ("d", C.c_float * 3)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("t", C.c_float), ("mesh", C.c_int32), ("tri", C.c_int32), ("b1", C.c_float),
+                ("b2", C.c_float)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("integrator", C.c_uint32), ("rng", C.c_uint32),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("seed", C.c_uint64), ("max_depth", C.c_uint32), ("rr_start", C.c_uint32),
+                ("rr_prob", C.c_float), ("bdpt_max_len", C.c_uint32), ("firefly", C.c_uint32),
+                ("sample_offset", C.c_uint32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("ms", C.c_double), ("kernel_ms", C.c_double), ("paths", C.c_uint64),
+                ("rays", C.c_uint64), ("nodes", C.c_uint64), ("tris", C.c_uint64),
+                ("launches", C.c_uint32), ("counted", C.c_uint32)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("scene", C.POINTER(SceneDesc)), ("params", RenderParams),
+                ("rgba_out", C.POINTER(C.c_float))]
+
+
+class GenOpts(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("level", C.c_uint32),
+                ("num_tris", C.c_uint32), ("num_materials", C.c_uint32), ("amplitude", C.c_float),
+                ("roughness_lo", C.c_float), ("roughness_hi", C.c_float), ("width", C.c_uint32),
+                ("height", C.c_uint32)]
+
+
+_P = C.c_void_p
+_U32 = C.c_uint32
+_ST = C.c_int
+
+# name -> (restype, argtypes); every symbol include/e8g.h declares
+SIGNATURES = {
+    "e8g_create": (_ST, [C.POINTER(_P), _P]),
+    "e8g_destroy": (_ST, [_P]),
+    "e8g_last_error": (C.c_char_p, [_P]),
+    "e8g_version": (C.c_char_p, []),
+    "e8g_scene_upload": (_ST, [_P, C.POINTER(SceneDesc)]),
+    "e8g_scene_build_bvh": (_ST, [_P, C.POINTER(BvhOpts)]),
+    "e8g_bvh_get_stats": (_ST, [_P, C.POINTER(BvhStats)]),
+    "e8g_default_bvh_opts": (None, [C.POINTER(BvhOpts)]),
+    "e8g_camera_rays": (_ST, [_P, _U32, _U32, _P]),
+    "e8g_trace_closest": (_ST, [_P, _P, _U32, _P]),
+    "e8g_trace_any": (_ST, [_P, _P, _P, _P, _U32, _P]),
+    "e8g_trace_closest_dev": (_ST, [_P, _P, _U32, _P, _P]),
+    "e8g_render": (_ST, [_P, C.POINTER(RenderParams), _P]),
+    "e8g_render_dev": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
+    "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
+    "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
+    "e8g_forward": (_ST, [_P, C.POINTER(RenderParams), _P]),
+    "e8g_backward": (_ST, [_P, _P, _P, _P]),
+    "e8g_set_materials": (_ST, [_P, C.POINTER(Material), _U32]),
+    "e8g_batch_render": (_ST, [_P, C.POINTER(BatchItem), _U32, C.POINTER(RenderStats)]),
+    "e8g_default_params": (None, [C.POINTER(RenderParams), _U32, _U32, _U32, _U32]),
+    "e8g_path_seed": (_U32, [C.c_uint64, _U32, _U32]),
+    "e8g_gen_scene": (_ST, [C.POINTER(GenOpts), C.POINTER(_P)]),
+    "e8g_host_scene_desc": (_ST, [_P, C.POINTER(SceneDesc)]),
+    "e8g_host_scene_free": (None, [_P]),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Load libe8g.so (once). Raises OSError if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"native library {p} is missing: build it with "
+                      "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            if path is None:
+                raise OSError(f"{p} does not export {name}")
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class E8GError(RuntimeError):
+    pass
+
+
+def check(status, ctx=None, what=""):
+    if status != E8G_OK:
+        msg = ""
+        if ctx is not None:
+            err = load().e8g_last_error(ctx)
+            msg = err.decode() if err else ""
+        raise E8GError(f"{what}: {STATUS_NAMES.get(status, status)} {msg}".strip())
