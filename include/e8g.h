@@ -236,6 +236,9 @@ e8g_status e8g_render(e8g_ctx *ctx, const e8g_render_params *params, float *rgba
 e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
                           void *stream);
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
+/* Runs the render once with traversal counters on (not for timing) and returns the number of
+ * rays traced, BVH nodes whose box was fetched and triangles tested. */
+e8g_status e8g_count_traversal(e8g_ctx *ctx, const e8g_render_params *params, e8g_render_stats *stats);
 
 /* Per-path radiance for an explicit list of (pixel, sample) pairs: rgb_out is 3*n floats. */
 e8g_status e8g_render_paths(e8g_ctx *ctx, const e8g_render_params *params, const uint32_t *pixel,

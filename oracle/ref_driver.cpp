@@ -312,6 +312,25 @@ void r_minstd_draws(uint32_t seed, uint32_t n, float *out) {
         out[i] = rng.draw();
 }
 
+// The reference's uv_sphere generator (geometry.cpp:162-241): vertex, normal and index arrays.
+uint32_t r_uv_sphere(float r, uint32_t res, int flip, float *pos_out, float *nrm_out, uint32_t *tris_out) {
+    e8::uv_sphere sp("sphere", e8util::vec3{0.0f, 0.0f, 0.0f}, r, res, flip != 0);
+    auto const &v = sp.vertices();
+    auto const &n = sp.normals();
+    auto const &t = sp.triangles();
+    if (pos_out) {
+        for (size_t i = 0; i < v.size(); i++)
+            for (int k = 0; k < 3; k++) {
+                pos_out[3 * i + k] = v[i](k);
+                nrm_out[3 * i + k] = n[i](k);
+            }
+        for (size_t i = 0; i < t.size(); i++)
+            for (int k = 0; k < 3; k++)
+                tris_out[3 * i + k] = t[i](k);
+    }
+    return static_cast<uint32_t>(t.size());
+}
+
 uint32_t r_bvh_num_nodes(r_scene const *s) { return s->bvh->num_nodes(); }
 uint32_t r_bvh_max_depth(r_scene const *s) { return s->bvh->max_depth(); }
 

@@ -1,0 +1,124 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+Runs only where the reference sources exist (the oracle Makefile compiles them, unmodified, into
+oracle/_ref/libe8ref.so). Every fixture stores its scene arrays too, so consumers never depend on
+regenerating geometry bit for bit on another machine.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from x3dcore2_gb300 import abi, scene as S  # noqa: E402
+import oracle_bind as ob  # noqa: E402
+
+MODES = {"uni": abi.MODE_REF_UNI, "lt1": abi.MODE_REF_LT1, "bdpt": abi.MODE_REF_BDPT,
+         "direct": abi.MODE_REF_DIRECT, "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION}
+
+
+def scene_arrays(sc):
+    mats = np.array([[m.type, *m.albedo, m.roughness, m.ior_re, m.ior_im, m.mix0, m.mix1, m.ratio]
+                     for m in sc.material_list()], np.float64)
+    lights = np.array([[sc.lights[i].mesh, *sc.lights[i].radiance] for i in range(sc.num_lights)],
+                      np.float64)
+    cam = np.array(list(sc.camera.origin) + list(sc.camera.rot) +
+                   [sc.camera.sensor_size, sc.camera.focal_len, sc.camera.aspect], np.float32)
+    return dict(voff=sc.voff, toff=sc.toff, mesh_mat=sc.mesh_mat, pos=sc.pos, nrm=sc.nrm, tris=sc.tris,
+                mats=mats, lights=lights, cam=cam)
+
+
+def paths_fixture(name, sc, w, h, npaths, seed, modes, rng_seed=0):
+    ref = ob.RefScene(sc)
+    rng = np.random.default_rng(rng_seed)
+    px = rng.integers(0, w * h, npaths).astype(np.uint32)
+    samples = np.arange(npaths, dtype=np.uint32)
+    seeds = np.array([ob.oracle().o_path_seed(seed, int(p), int(k)) for p, k in zip(px, samples)], np.uint32)
+    out = dict(scene_arrays(sc), width=np.uint32(w), height=np.uint32(h), seed=np.uint64(seed), pixels=px,
+               samples=samples, seeds=seeds)
+    for mname in modes:
+        out["rad_" + mname] = ref.render_paths(MODES[mname], w, h, px, seeds)
+    rays = ref.camera_rays(w, h)
+    hits = ref.trace_closest(rays)
+    out.update(rays=rays, hit_t=hits["t"], hit_mesh=hits["mesh"], hit_tri=hits["tri"],
+               hit_normal=hits["normal"], hit_vertex=hits["vertex"])
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print(name, {k: v.shape for k, v in out.items() if hasattr(v, "shape")})
+
+
+def bsdf_fixture():
+    # tst_material.cpp:28-179: cook_torr(0.787, r 0.2/0.25, ior 2.93) and oren_nayar(sigma 0.078)
+    mats = [S.material(abi.MAT_COOK_TORR, (0.787, 0.787, 0.787), 0.25, (2.93, 0.0)),
+            S.material(abi.MAT_COOK_TORR, (0.787, 0.787, 0.787), 0.2, (2.93, 0.0)),
+            S.material(abi.MAT_OREN_NAYAR, (0.725, 0.710, 0.680), 0.078),
+            S.material(abi.MAT_MIXTURE, mix=(0, 2), ratio=0.3),
+            S.material(abi.MAT_FAIL_SAFE)]
+    sc = S.cornell(8, 8)
+    sc = sc.with_materials(mats)
+    ref = ob.RefScene(sc)
+    n = np.array([0.0, 0.0, 1.0], np.float32)
+    o = np.array([0.57735026, 0.57735026, 0.57735026], np.float32)  # (1,1,1).normalize()
+    out = dict(scene_arrays(sc), n=n, o=o)
+    for mi in range(len(mats)):
+        d, p = ref.bsdf_sample(mi, 13, n, o, 1000)
+        out[f"dirs_{mi}"] = d
+        out[f"pdf_{mi}"] = p
+        ev = np.array([ref.bsdf_eval(mi, n, o, dd) for dd in d[:200]], np.float32)
+        out[f"eval_{mi}"] = ev
+    # special-case vectors of tst_material.cpp:142-144
+    i = np.array([0.983719, 0.0456052, 0.173832], np.float32)
+    oo = np.array([0.687788, 0.361631, 0.629421], np.float32)
+    nn = np.array([0.687654, 0.361558, 0.62961], np.float32)
+    out["special"] = np.array([ref.bsdf_eval(mi, nn, oo, i) for mi in range(len(mats))], np.float32)
+    out["special_vecs"] = np.stack([i, oo, nn])
+    np.savez_compressed(os.path.join(HERE, "bsdf.npz"), **out)
+    print("bsdf.npz")
+
+
+def draws_fixture():
+    r = ob.reference()
+    seeds = [0, 1, 13, 12345, 2147483646, 4294967295]
+    out = {}
+    for s in seeds:
+        a = np.zeros(64, np.float32)
+        r.r_minstd_draws(s, 64, ob.ptr(a))
+        out[f"seed_{s}"] = a
+    np.savez_compressed(os.path.join(HERE, "draws.npz"), **out)
+    print("draws.npz")
+
+
+def uv_sphere_fixture():
+    r = ob.reference()
+    nt = r.r_uv_sphere(10.0, 30, 1, None, None, None)
+    nv = (30 - 2) * 30 + 2
+    pos = np.zeros((nv, 3), np.float32)
+    nrm = np.zeros((nv, 3), np.float32)
+    tris = np.zeros((nt, 3), np.uint32)
+    r.r_uv_sphere(10.0, 30, 1, ob.ptr(pos), ob.ptr(nrm), ob.ptr(tris))
+    np.savez_compressed(os.path.join(HERE, "uv_sphere.npz"), pos=pos, nrm=nrm, tris=tris)
+    print("uv_sphere.npz")
+
+
+def main():
+    subprocess.run(["make", "-s", "-C", ob.ORACLE_DIR, "all", "ref"], check=True)
+    draws_fixture()
+    uv_sphere_fixture()
+    bsdf_fixture()
+    all_modes = list(MODES)
+    paths_fixture("cornell.npz", S.cornell(64, 48), 64, 48, 512, 7, all_modes)
+    paths_fixture("furnace.npz", S.furnace(), 32, 32, 256, 11, ["uni", "lt1", "bdpt", "direct"])
+    paths_fixture("ico.npz", S.displaced_icosphere(level=3, seed=5, num_materials=16, width=48, height=27),
+                  48, 27, 384, 3, ["uni", "lt1", "bdpt", "direct"])
+    paths_fixture("soup.npz", S.soup(3000, seed=2, width=40, height=40), 40, 40, 256, 9,
+                  ["lt1", "bdpt", "direct"])
+
+
+if __name__ == "__main__":
+    main()

@@ -98,6 +98,7 @@ def reference(timing=False):
             "r_minstd_draws": (None, [_U, _U, _P]),
             "r_bvh_num_nodes": (_U, [_P]),
             "r_bvh_max_depth": (_U, [_P]),
+            "r_uv_sphere": (_U, [C.c_float, _U, C.c_int, _P, _P, _P]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)

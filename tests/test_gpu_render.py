@@ -1,0 +1,83 @@
+"""Image rendering on the GPU: the image is the mean of the same per-path estimates the oracle
+computes (identical draw streams), the furnace expectation of the reference's own test, and
+basic invariants of pt_image_renderer::render."""
+import numpy as np
+import pytest
+
+import golden_util as G
+import oracle_bind as ob
+from x3dcore2_gb300 import abi
+from x3dcore2_gb300 import scene as S
+from x3dcore2_gb300.core import default_params
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_mse(img, ref, eps=1e-2):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT])
+def test_image_matches_oracle_same_streams(ctx, mode):
+    sc = S.cornell(48, 48)
+    ctx.upload(sc)
+    osc = ob.OracleScene(sc)
+    p = default_params(mode, 48, 48, 8, seed=9, max_depth=6 if mode == abi.MODE_MIS else 0)
+    img = ctx.render(p)[..., :3]
+    pol = ob.OPolicy(p.max_depth, p.rr_start, p.rr_prob, 8)
+    ref = osc.render(mode, 48, 48, 8, seed=9, policy=pol, rng=p.rng)[..., :3]
+    assert np.all(np.isfinite(img)) and np.all(img >= 0)
+    assert rel_mse(img, ref) < 1e-4, rel_mse(img, ref)
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_MIS])
+def test_furnace(ctx, mode):
+    """tst_pathtracer.cpp:58-86 on the GPU: E[sum RGB] = 1 / (1 - 0.7) * 3 = 10 within 0.3."""
+    ctx.upload(S.furnace(30))
+    p = default_params(mode, 16, 16, 256, seed=13)
+    img = ctx.render(p)
+    mu = img[..., :3].sum(axis=-1).mean()
+    assert abs(mu - 10.0) < 0.3, mu
+
+
+def test_cornell_sanity_like_tst_renderer(ctx):
+    """tst_renderer.cpp:117-168: no NaN/inf/negative pixels and enough total radiance."""
+    ctx.upload(S.cornell(200, 150))
+    p = default_params(abi.MODE_REF_LT1, 200, 150, 4)
+    img = ctx.render(p)
+    assert np.all(np.isfinite(img)) and np.all(img >= 0)
+    assert np.all(img[..., :3].sum(axis=(0, 1)) > 1000)
+
+
+def test_progressive_samples_add_up(ctx):
+    ctx.upload(S.cornell(32, 32))
+    full = ctx.render(default_params(abi.MODE_MIS, 32, 32, 8, seed=4))
+    a = ctx.render(default_params(abi.MODE_MIS, 32, 32, 4, seed=4, sample_offset=0))
+    b = ctx.render(default_params(abi.MODE_MIS, 32, 32, 4, seed=4, sample_offset=4))
+    assert np.allclose(full, 0.5 * (a + b), rtol=1e-4, atol=1e-5)
+
+
+def test_normal_and_position_tracers(ctx):
+    d = G.load("cornell.npz")
+    sc = G.scene_from(d)
+    ctx.upload(sc)
+    osc = ob.OracleScene(sc)
+    for mode in (abi.MODE_NORMAL, abi.MODE_POSITION):
+        img = ctx.render(default_params(mode, 64, 48, 1))
+        ref = osc.render(mode, 64, 48, 1)
+        assert np.allclose(img, ref, atol=1e-6)
+
+
+def test_invalid_params(ctx):
+    from x3dcore2_gb300.abi import E8GError
+    ctx.upload(S.cornell(8, 8))
+    for bad in (dict(width=1), dict(mode=42), dict(rr_prob=0.0), dict(rng=7)):
+        p = default_params(abi.MODE_REF_LT1, 8, 8, 1, **bad)
+        with pytest.raises(E8GError, match="INVALID_ARG"):
+            ctx.render(p)
+
+
+def test_zero_spp_renders_black(ctx):
+    ctx.upload(S.cornell(8, 8))
+    img = ctx.render(default_params(abi.MODE_REF_LT1, 8, 8, 0))
+    assert np.all(img[..., :3] == 0)

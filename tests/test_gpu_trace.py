@@ -1,0 +1,92 @@
+"""Closest-hit and any-hit traversal on the GPU against the reference (golden fixtures) and the
+oracle: primitive ids on >= 99.99% of rays, hit distance within 1e-5 relative."""
+import numpy as np
+import pytest
+
+import golden_util as G
+import oracle_bind as ob
+from x3dcore2_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz"]
+
+
+def compare_hits(g, ref_mesh, ref_tri, ref_t, min_match=0.9999):
+    same_mesh = g["mesh"] == ref_mesh
+    same = same_mesh & (g["tri"] == ref_tri)
+    assert same.mean() >= min_match, f"id match {same.mean():.6f}"
+    hit = same & (ref_mesh >= 0)
+    rel = np.abs(g["t"][hit] - ref_t[hit]) / np.maximum(np.abs(ref_t[hit]), 1e-30)
+    assert np.all(rel <= 1e-5), rel.max()
+    return same.mean()
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_closest_hits_match_reference_golden(ctx, name):
+    d = G.load(name)
+    ctx.upload(G.scene_from(d))
+    g = ctx.trace_closest(d["rays"])
+    compare_hits(g, d["hit_mesh"], d["hit_tri"], d["hit_t"], min_match=1.0)
+    # bitwise distances: same triangle, same arithmetic, no FMA contraction
+    hit = d["hit_mesh"] >= 0
+    assert np.array_equal(g["t"][hit].view(np.uint32), d["hit_t"][hit].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_camera_rays_match_reference_golden(ctx, name):
+    d = G.load(name)
+    ctx.upload(G.scene_from(d))
+    r = ctx.camera_rays(int(d["width"]), int(d["height"]))
+    assert np.allclose(r, d["rays"], rtol=0, atol=2e-7)
+
+
+def random_rays(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    dd = rng.normal(size=(n, 3)).astype(np.float32)
+    dd /= np.linalg.norm(dd, axis=1, keepdims=True)
+    # a few axis-aligned and degenerate-component directions
+    dd[:64] = np.eye(3, dtype=np.float32)[np.arange(64) % 3] * np.where(np.arange(64) % 2, 1, -1)[:, None]
+    return ob.rays_array(o, dd)
+
+
+@pytest.mark.parametrize("kind,size", [("ico", 6), ("soup", 100_000), ("ico", 7)])
+def test_closest_and_any_hit_match_oracle_on_large_scenes(ctx, kind, size):
+    sc = (S.displaced_icosphere(level=size, seed=2, num_materials=64, width=64, height=36) if kind == "ico"
+          else S.soup(size, seed=4, width=64, height=64))
+    ctx.upload(sc)
+    osc = ob.OracleScene(sc)
+    rays = random_rays(20000, -1.0, 1.0, seed=size)
+    g = ctx.trace_closest(rays)
+    o = osc.trace_closest(rays)
+    compare_hits(g, o["mesh"], o["tri"], o["t"])
+    tmin = np.full(len(rays), 1e-4, np.float32)
+    tmax = np.random.default_rng(1).uniform(1e-3, 2.5, len(rays)).astype(np.float32)
+    ga = ctx.trace_any(rays, tmin, tmax)
+    oa = osc.trace_any(rays, tmin, tmax)
+    assert np.mean(ga == oa) >= 0.9999
+
+
+def test_trace_edge_cases(ctx):
+    sc = S.cornell(32, 32)
+    ctx.upload(sc)
+    osc = ob.OracleScene(sc)
+    # empty batch
+    assert ctx.trace_closest(np.zeros((0, 6), np.float32))["t"].shape == (0,)
+    # rays starting on a wall, grazing along walls, pointing out of the box, and beyond t=1000
+    o = np.array([[0.5, 0.0, 0.5], [0.0, 0.5, 0.5], [0.5, 0.5, 0.5], [0.5, 0.5, 0.5], [0.5, 0.5, -2000.0],
+                  [1e-7, 0.5, 0.5], [0.5, 1.0, 0.5]], np.float32)
+    d = np.array([[0, 1, 0], [0, 1, 0], [0, 0, 1], [0, 0, -1], [0, 0, 1], [0, 0, -1], [0, -1, 0]], np.float32)
+    rays = ob.rays_array(o, d)
+    g, r = ctx.trace_closest(rays), osc.trace_closest(rays)
+    assert np.array_equal(g["mesh"], r["mesh"]) and np.array_equal(g["tri"], r["tri"])
+    assert g["mesh"][4] == -1  # nothing within 1000
+
+
+def test_trace_without_scene_is_an_error(lib):
+    from x3dcore2_gb300.core import Context
+    from x3dcore2_gb300.abi import E8GError
+    with Context(0) as c:
+        with pytest.raises(E8GError, match="NO_SCENE"):
+            c.trace_closest(np.zeros((1, 6), np.float32))

@@ -1,0 +1,80 @@
+"""Builds the in-tree native library x3dcore2_gb300/libe8g.so for sm_103a.
+
+Host C++ (scene generators, packer, BVH builder) is compiled with g++; the CUDA translation
+units with nvcc for compute_103a/sm_103a only. Float-sensitive code is built with FMA contraction
+off (-ffp-contract=off on the host, --fmad=false on the device) so results follow the reference's
+operation order. Objects are rebuilt only when a source or header changed.
+"""
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libe8g.so")
+ROOT = os.path.dirname(HERE)
+
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wextra",
+            f"-I{os.path.join(ROOT, 'include')}"]
+NVFLAGS = ["-std=c++17", "-O3", ARCH, "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+           "-Xptxas", "-warn-spills", f"-I{os.path.join(ROOT, 'include')}"]
+
+
+def _nvcc():
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found")
+    return p
+
+
+def _stale(obj, deps):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("compile failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stderr
+
+
+def build(verbose=False, jobs=None):
+    os.makedirs(BUILD, exist_ok=True)
+    headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
+        [os.path.join(ROOT, "include", "e8g.h")]
+    nvcc = _nvcc()
+    tasks = []
+    objs = []
+    for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            tasks.append(["g++"] + CXXFLAGS + ["-c", src, "-o", obj])
+    for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            tasks.append([nvcc] + NVFLAGS + ["-c", src, "-o", obj])
+    if tasks:
+        with cf.ThreadPoolExecutor(max_workers=jobs or min(len(tasks), os.cpu_count() or 4)) as ex:
+            for err in ex.map(_compile, tasks):
+                if verbose and err:
+                    sys.stderr.write(err)
+    if tasks or not os.path.exists(LIB):
+        tmp = LIB + ".tmp"
+        _compile([nvcc, ARCH, "-shared", "-o", tmp] + objs + ["-lpthread"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    print(LIB)

@@ -1,0 +1,149 @@
+"""Python view of the C ABI: one Context per GPU, owning an uploaded scene and its BVH.
+
+Mirrors the reference's split between scene commit (path space / lights / materials actuators,
+corelib/src/pathspace.cpp:292-328) and rendering (pt_image_renderer::render,
+corelib/src/renderer.cpp:106-166). Every call goes through libe8g.so; nothing here computes.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+_P = C.c_void_p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P)
+
+
+def default_params(mode, width, height, spp, **overrides):
+    p = abi.RenderParams()
+    abi.load().e8g_default_params(C.byref(p), mode, width, height, spp)
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def path_seed(seed, pixel, sample):
+    return abi.load().e8g_path_seed(seed, pixel, sample)
+
+
+class Context:
+    def __init__(self, device=0):
+        self.lib = abi.load()
+        self.h = _P()
+        opts = (C.c_int32 * 2)(device, 0)
+        st = self.lib.e8g_create(C.byref(self.h), C.cast(opts, _P))
+        abi.check(st, None, "e8g_create")
+        self.scene = None
+
+    def close(self):
+        if self.h:
+            self.lib.e8g_destroy(self.h)
+            self.h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        abi.check(st, self.h, what)
+
+    # ---- scene commit -------------------------------------------------------------------
+    def upload(self, scene, build=True, bvh_opts=None):
+        self._check(self.lib.e8g_scene_upload(self.h, C.byref(scene.desc)), "e8g_scene_upload")
+        self.scene = scene
+        if build:
+            self.build_bvh(bvh_opts)
+        return self
+
+    def build_bvh(self, opts=None):
+        if opts is None:
+            opts = abi.BvhOpts()
+            self.lib.e8g_default_bvh_opts(C.byref(opts))
+        self._check(self.lib.e8g_scene_build_bvh(self.h, C.byref(opts)), "e8g_scene_build_bvh")
+
+    def bvh_stats(self):
+        s = abi.BvhStats()
+        self._check(self.lib.e8g_bvh_get_stats(self.h, C.byref(s)), "e8g_bvh_get_stats")
+        return {k: getattr(s, k) for k, _ in abi.BvhStats._fields_}
+
+    # ---- traversal ----------------------------------------------------------------------
+    def camera_rays(self, w, h):
+        out = np.empty((w * h, 6), np.float32)
+        self._check(self.lib.e8g_camera_rays(self.h, w, h, _ptr(out)), "e8g_camera_rays")
+        return out
+
+    def trace_closest(self, rays):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        n = len(rays)
+        raw = np.zeros((n, 5), np.float32)
+        self._check(self.lib.e8g_trace_closest(self.h, _ptr(rays), n, _ptr(raw)), "e8g_trace_closest")
+        return dict(t=raw[:, 0].copy(), mesh=raw[:, 1].view(np.int32).copy(),
+                    tri=raw[:, 2].view(np.int32).copy(), b=raw[:, 3:5].copy())
+
+    def trace_any(self, rays, tmin, tmax):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        n = len(rays)
+        out = np.zeros(n, np.uint8)
+        tmin = np.ascontiguousarray(np.broadcast_to(tmin, (n,)), np.float32)
+        tmax = np.ascontiguousarray(np.broadcast_to(tmax, (n,)), np.float32)
+        self._check(self.lib.e8g_trace_any(self.h, _ptr(rays), _ptr(tmin), _ptr(tmax), n, _ptr(out)),
+                    "e8g_trace_any")
+        return out
+
+    # ---- rendering ----------------------------------------------------------------------
+    def render(self, params):
+        out = np.zeros((params.height, params.width, 4), np.float32)
+        self._check(self.lib.e8g_render(self.h, C.byref(params), _ptr(out)), "e8g_render")
+        return out
+
+    def render_dev(self, params, d_out_ptr, stream=None):
+        self._check(self.lib.e8g_render_dev(self.h, C.byref(params), _P(d_out_ptr), _P(stream)),
+                    "e8g_render_dev")
+
+    def render_paths(self, params, pixels, samples):
+        pixels = np.ascontiguousarray(pixels, np.uint32)
+        samples = np.ascontiguousarray(np.broadcast_to(samples, pixels.shape), np.uint32)
+        out = np.zeros((len(pixels), 3), np.float32)
+        self._check(self.lib.e8g_render_paths(self.h, C.byref(params), _ptr(pixels), _ptr(samples),
+                                              len(pixels), _ptr(out)), "e8g_render_paths")
+        return out
+
+    def stats(self):
+        s = abi.RenderStats()
+        self._check(self.lib.e8g_get_render_stats(self.h, C.byref(s)), "e8g_get_render_stats")
+        return {k: getattr(s, k) for k, _ in abi.RenderStats._fields_}
+
+    def count_traversal(self, params):
+        s = abi.RenderStats()
+        self._check(self.lib.e8g_count_traversal(self.h, C.byref(params), C.byref(s)),
+                    "e8g_count_traversal")
+        return {k: getattr(s, k) for k, _ in abi.RenderStats._fields_}
+
+    # ---- differentiable rendering -------------------------------------------------------
+    def forward(self, params):
+        out = np.zeros((params.height, params.width, 4), np.float32)
+        self._check(self.lib.e8g_forward(self.h, C.byref(params), _ptr(out)), "e8g_forward")
+        return out
+
+    def backward(self, dl_dimage):
+        nm = self.scene.num_materials
+        dl = np.ascontiguousarray(dl_dimage, np.float32)
+        da = np.zeros((nm, 3), np.float32)
+        dr = np.zeros(nm, np.float32)
+        self._check(self.lib.e8g_backward(self.h, _ptr(dl), _ptr(da), _ptr(dr)), "e8g_backward")
+        return da, dr
+
+    def set_materials(self, materials):
+        arr = (abi.Material * len(materials))(*materials)
+        self._check(self.lib.e8g_set_materials(self.h, arr, len(materials)), "e8g_set_materials")

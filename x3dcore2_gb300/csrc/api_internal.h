@@ -1,0 +1,72 @@
+// Context and helpers shared by the C ABI translation units.
+#pragma once
+
+#include "../../include/e8g.h"
+#include "host_scene.h"
+#include "launch.h"
+#include "scene_pack.h"
+
+#include <string>
+#include <vector>
+
+namespace e8g {
+
+struct dev_buffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n);
+    void release();
+};
+
+} // namespace e8g
+
+struct e8g_ctx {
+    int device = 0;
+    int num_sms = 1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    std::string err;
+    bool uploaded = false, built = false;
+    e8g::packed_scene pack;
+    std::vector<e8g_material> materials;
+    e8g::DevScene dev{};
+    e8g_bvh_stats bvh_stats{};
+    e8g_render_stats stats{};
+    uint32_t launches = 0;
+    // scene
+    e8g::dev_buffer b_nlo, b_nhi, b_tri, b_tidx, b_vpos, b_vnrm, b_mesh_mat, b_mesh_light, b_mesh_toff, b_mesh_area,
+        b_tri_cum, b_mats, b_light_mesh, b_light_rad, b_light_cum, b_light_pnorm;
+    // render scratch
+    e8g::dev_buffer b_fh, b_accum, b_work, b_img, b_io0, b_io1, b_counts;
+    // wavefront queues and adjoint state
+    e8g::dev_buffer b_wf, b_grad;
+    e8g_render_params fwd_params{};
+    bool have_forward = false;
+
+    std::vector<e8g::dev_buffer *> all_buffers() {
+        return {&b_nlo, &b_nhi, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
+                &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
+                &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad};
+    }
+};
+
+namespace e8g {
+
+e8g_status fail(e8g_ctx *ctx, e8g_status st, std::string const &msg);
+e8g_status cuda_fail(e8g_ctx *ctx, cudaError_t e, char const *what);
+e8g_status check_ready(e8g_ctx *c);
+e8g_status validate_params(e8g_ctx *c, e8g_render_params const *p);
+RenderArgs make_args(e8g_render_params const *p);
+e8g_status first_hits(e8g_ctx *c, uint32_t w, uint32_t h);
+int persistent_grid(e8g_ctx *c, int blocks_per_sm);
+void fill_dev_scene(e8g_ctx *c);
+
+// Renders an image into d_rgba (device). counts (host, 3 values) requests the instrumented run.
+e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts);
+// Per-path radiance for device lists of pixels and samples into d_rgb (3 floats per path).
+e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,
+                       uint32_t n, float *d_rgb);
+
+} // namespace e8g
+
+extern "C" e8g_status e8g_count_traversal(e8g_ctx *c, e8g_render_params const *p, e8g_render_stats *out);

@@ -1,0 +1,39 @@
+// Host BVH builder: binned SAH over triangles, flattened to 32-byte nodes in two
+// structure-of-arrays halves (lo: min xyz + link, hi: max xyz + count), children stored as
+// adjacent pairs so one interior visit reads 64 contiguous bytes per half-array pair.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace e8g {
+
+// Traversal stacks live in shared memory with this many entries per thread; the builder never
+// makes the tree deeper than this, so a push can never overflow.
+constexpr uint32_t kMaxTreeDepth = 32;
+
+struct bvh_build_opts {
+    uint32_t max_leaf_prims = 4; // reference BVH_MAX_PRIMS (pathspace.cpp:121)
+    uint32_t num_bins = 20;      // reference BVH_BUCKET_COUNT (pathspace.cpp:122)
+    float tri_cost = 8.0f;       // reference BVH_RAY_TRIANGLE_COST
+    float node_cost = 1.0f;      // reference BVH_RAY_BOX_COST
+    uint32_t num_threads = 0;
+};
+
+struct flat_bvh {
+    // node i: lo[i] = (min.x, min.y, min.z, link), hi[i] = (max.x, max.y, max.z, count)
+    // count == 0: interior, children at link and link + 1; count > 0: leaf of `count`
+    // triangles starting at position `link` of tri_order.
+    std::vector<float> lo;      // 4 per node
+    std::vector<float> hi;      // 4 per node
+    std::vector<uint32_t> tri_order; // BVH position -> global triangle index
+    uint32_t num_nodes = 0;
+    uint32_t num_leaves = 0;
+    uint32_t max_depth = 0;
+    double avg_leaf_depth = 0;
+};
+
+// tris: 3 global vertex indices per triangle; pos: 3 floats per vertex.
+flat_bvh build_bvh(float const *pos, uint32_t const *tris, uint32_t num_tris, bvh_build_opts const &o);
+
+} // namespace e8g

@@ -1,0 +1,28 @@
+// Kernel launchers (defined in the .cu files, called by the C ABI in api.cu).
+#pragma once
+
+#include "device.cuh"
+
+namespace e8g {
+
+struct LaunchCfg {
+    int grid;
+    cudaStream_t stream;
+};
+
+void launch_first_hits(DevScene const &S, uint32_t w, uint32_t h, FirstHit *out, cudaStream_t st);
+void launch_camera_rays(DevScene const &S, uint32_t w, uint32_t h, float *rays6, cudaStream_t st);
+void launch_trace_closest(DevScene const &S, float const *rays6, uint32_t n, float *hits5, cudaStream_t st);
+void launch_trace_any(DevScene const &S, float const *rays6, float const *tmin, float const *tmax, uint32_t n,
+                      uint8_t *occ, cudaStream_t st);
+void launch_trace_closest_counted(DevScene const &S, float const *rays6, uint32_t n, float *hits5,
+                                  unsigned long long *counters, cudaStream_t st);
+void launch_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rgba, cudaStream_t st);
+
+// Megakernel integrator (one thread per path, persistent threads refilled warp-wide).
+// counters (when non-null): [0] rays, [1] nodes, [2] tris.
+void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                       unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+int megakernel_blocks_per_sm();
+
+} // namespace e8g

@@ -1,0 +1,41 @@
+// Host-side packing of an e8g_scene_desc into the GPU layout (arrays uploaded as-is).
+#pragma once
+
+#include "../../include/e8g.h"
+#include "bvh.h"
+#include "layout.h"
+
+#include <cstdint>
+#include <vector>
+
+namespace e8g {
+
+struct packed_scene {
+    uint32_t nm = 0, nv = 0, nt = 0, nmat = 0, nl = 0;
+    std::vector<float> vpos, vnrm;  // 4 floats per vertex
+    std::vector<uint32_t> tidx;     // 4 per triangle: global vertex indices, mesh
+    std::vector<int32_t> mesh_mat;  // fail-safe remapped to nmat
+    std::vector<int32_t> mesh_light;
+    std::vector<uint32_t> mesh_toff;
+    std::vector<float> mesh_area;   // trimesh::update_face_cdf (geometry.cpp:105-118)
+    std::vector<float> tri_cum;
+    std::vector<DevMaterial> mats;  // nmat + 1
+    std::vector<uint32_t> light_mesh;
+    std::vector<float> light_rad;   // 4 per light
+    std::vector<float> light_cum, light_pnorm;
+    float total_power = 0;
+    float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+    DevCamera cam{};
+    // BVH (after build)
+    flat_bvh bvh;
+    std::vector<float> tri;         // 12 floats per BVH position
+    double build_ms = 0;
+};
+
+// Fills everything but the BVH. Float arithmetic follows the reference (built with
+// -ffp-contract=off) so light areas, powers and the light CDF are bit-identical to corelib's.
+void pack_scene(e8g_scene_desc const &d, packed_scene &out);
+void pack_materials(e8g_material const *m, uint32_t n, std::vector<DevMaterial> &out);
+void build_scene_bvh(packed_scene &s, bvh_build_opts const &o);
+
+} // namespace e8g

@@ -252,7 +252,8 @@ e8g_host_scene *cornell(e8g_gen_opts const &o) {
              {0.625, 0.999, 0.375}, {0, -1, 0}, 3);
     s->lights.push_back(e8g_light{lm, {17.0f, 12.0f, 4.0f}});
     float aspect = o.height ? static_cast<float>(o.width) / static_cast<float>(o.height) : 1.0f;
-    double d = 0.5 / std::tan(20.0 * M_PI / 180.0);
+    // 3% margin around the opening so no primary ray grazes its edges exactly
+    double d = 0.515 / std::tan(20.0 * M_PI / 180.0);
     s->cam = look_at({0.5, 0.5, 1.0 + d}, {0.5, 0.5, 0.0}, {0, 1, 0}, 40.0f, aspect);
     return s;
 }

@@ -1,0 +1,135 @@
+// Primary-hit, ray-batch traversal and resolve kernels.
+#include "launch.h"
+
+namespace e8g {
+
+// compute_first_hit (pathtracer.cpp:456-472): camera ray, closest hit, back-facing hits become
+// misses, emitter lookup.
+__global__ void __launch_bounds__(kBlock) k_first_hits(DevScene S, uint32_t w, uint32_t h, FirstHit *out) {
+    __shared__ uint32_t sn[kStack * kBlock];
+    __shared__ float st[kStack * kBlock];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h)
+        return;
+    float3 o, d;
+    camera_ray(S.cam, i % w, i / w, w, h, o, d);
+    Hit hit = trace_closest<false>(S, o, d, sn + threadIdx.x, st + threadIdx.x, nullptr);
+    FirstHit f;
+    f.d = make_float4(d.x, d.y, d.z, 0.0f);
+    int32_t mesh = -1, light = -1;
+    float3 p = f3(0, 0, 0), n = f3(0, 0, 0);
+    if (hit.tri != 0xFFFFFFFFu) {
+        Vert v = make_vert(S, hit);
+        if (dot(v.n, neg(d)) > 0) {
+            mesh = v.mesh;
+            p = v.p;
+            n = v.n;
+            light = __ldg(&S.mesh_light[mesh]);
+        }
+    }
+    f.p = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
+    f.n = make_float4(n.x, n.y, n.z, __int_as_float(light));
+    out[i] = f;
+}
+
+__global__ void k_camera_rays(DevScene S, uint32_t w, uint32_t h, float *rays6) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h)
+        return;
+    float3 o, d;
+    camera_ray(S.cam, i % w, i / w, w, h, o, d);
+    float *r = rays6 + 6 * static_cast<size_t>(i);
+    r[0] = o.x;
+    r[1] = o.y;
+    r[2] = o.z;
+    r[3] = d.x;
+    r[4] = d.y;
+    r[5] = d.z;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_trace_closest(DevScene S, float const *rays6, uint32_t n, float *hits5,
+                                                          unsigned long long *counters) {
+    __shared__ uint32_t sn[kStack * kBlock];
+    __shared__ float st[kStack * kBlock];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    TraceCounters c{0, 0};
+    if (i < n) {
+        float const *r = rays6 + 6 * static_cast<size_t>(i);
+        float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
+        Hit h = trace_closest<COUNT>(S, o, d, sn + threadIdx.x, st + threadIdx.x, &c);
+        float *out = hits5 + 5 * static_cast<size_t>(i);
+        if (h.tri == 0xFFFFFFFFu) {
+            out[0] = 0.0f;
+            out[1] = __int_as_float(-1);
+            out[2] = __int_as_float(-1);
+            out[3] = 0.0f;
+            out[4] = 0.0f;
+        } else {
+            uint4 ti = __ldg(&S.tidx[h.tri]);
+            out[0] = h.t;
+            out[1] = __int_as_float(static_cast<int>(ti.w));
+            out[2] = __int_as_float(static_cast<int>(h.tri - __ldg(&S.mesh_toff[ti.w])));
+            out[3] = h.b1;
+            out[4] = h.b2;
+        }
+    }
+    if (COUNT) {
+        unsigned long long a = c.nodes, b = c.tris;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(~0u, a, off);
+            b += __shfl_down_sync(~0u, b, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&counters[1], a);
+            atomicAdd(&counters[2], b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_trace_any(DevScene S, float const *rays6, float const *tmin,
+                                                      float const *tmax, uint32_t n, uint8_t *occ) {
+    __shared__ uint32_t sn[kStack * kBlock];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float const *r = rays6 + 6 * static_cast<size_t>(i);
+    float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
+    occ[i] = trace_any<false>(S, o, d, tmin[i], tmax[i], sn + threadIdx.x, nullptr) ? 1 : 0;
+}
+
+__global__ void k_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rgba) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix)
+        return;
+    float4 a = accum[i];
+    reinterpret_cast<float4 *>(rgba)[i] = make_float4(a.x * inv_spp, a.y * inv_spp, a.z * inv_spp, 1.0f);
+}
+
+static inline int blocks(uint32_t n, int b) { return static_cast<int>((n + b - 1) / b); }
+
+void launch_first_hits(DevScene const &S, uint32_t w, uint32_t h, FirstHit *out, cudaStream_t st) {
+    k_first_hits<<<blocks(w * h, kBlock), kBlock, 0, st>>>(S, w, h, out);
+}
+void launch_camera_rays(DevScene const &S, uint32_t w, uint32_t h, float *rays6, cudaStream_t st) {
+    k_camera_rays<<<blocks(w * h, 256), 256, 0, st>>>(S, w, h, rays6);
+}
+void launch_trace_closest(DevScene const &S, float const *rays6, uint32_t n, float *hits5, cudaStream_t st) {
+    if (n)
+        k_trace_closest<false><<<blocks(n, kBlock), kBlock, 0, st>>>(S, rays6, n, hits5, nullptr);
+}
+void launch_trace_closest_counted(DevScene const &S, float const *rays6, uint32_t n, float *hits5,
+                                  unsigned long long *counters, cudaStream_t st) {
+    if (n)
+        k_trace_closest<true><<<blocks(n, kBlock), kBlock, 0, st>>>(S, rays6, n, hits5, counters);
+}
+void launch_trace_any(DevScene const &S, float const *rays6, float const *tmin, float const *tmax, uint32_t n,
+                      uint8_t *occ, cudaStream_t st) {
+    if (n)
+        k_trace_any<<<blocks(n, kBlock), kBlock, 0, st>>>(S, rays6, tmin, tmax, n, occ);
+}
+void launch_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rgba, cudaStream_t st) {
+    k_resolve<<<blocks(npix, 256), 256, 0, st>>>(accum, npix, inv_spp, rgba);
+}
+
+} // namespace e8g
