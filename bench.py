@@ -1,0 +1,310 @@
+"""Benchmark of the per-pixel path integral on one GB300 (or N, one process per GPU).
+
+Workload (default): the large procedural scene — icosphere level 8 (1,310,720 triangles)
+displaced by seeded 3-octave value noise (amplitude 0.05) on a 2-triangle ground plane with 4
+quad area lights, 512 materials (albedo U[0.1,0.9]^3, roughness U[0.05,0.8], odd ones GGX metals
+with F0 U[0.5,1)) — rendered at 1920x1080, 64 spp, max depth 8, Russian roulette from depth 3,
+fp32, with the product estimator (next-event estimation + BSDF sampling, power-heuristic MIS,
+Philox streams). A step is one full render of that frame.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line. `value` is paths/s over the device-resident render; `e2e` is the same
+metric through the public C ABI call with the image read back to pinned host memory each step.
+The reference arm (--impl reference) times the reference's CPU tracer (unidirect_lt1) on the
+host cores: the reference compiled from its own sources when present, else the oracle's C
+restatement of it.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "paths/s at fixed relMSE, plain vs wavefront-batched; adjoint/forward time"
+WORKLOAD = dict(workload="displaced_icosphere_l8_1080p_64spp", triangles=1310730, width=1920,
+                height=1080, spp=64, max_depth=8, rr_start=3, materials=512, lights=4,
+                estimator="nee+bsdf power-heuristic MIS", rng="philox4x32-10")
+# DRAM traffic per path of the megakernel, from the ncu capture summarised in
+# profiles/megakernel_icosphere_l8.md (dram__bytes_read.sum + dram__bytes_write.sum divided by
+# the paths of the captured launch); None until a capture exists.
+TRAFFIC_BYTES_PER_PATH = None
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    except OSError:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_scene(small):
+    from x3dcore2_gb300 import scene as S
+    if small:
+        return S.displaced_icosphere(level=5, seed=1, num_materials=512, width=320, height=180), 320, 180, 8
+    return (S.displaced_icosphere(level=8, seed=1, num_materials=512, width=1920, height=1080), 1920, 1080, 64)
+
+
+def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
+    """Times the reference's CPU tracer (unidirect_lt1, the reference's direct-lighting
+    integrator) on a centred crop of the same frame: the reference itself when it is compiled
+    here, else the oracle's restatement. Returns (paths/s, kind, sample description)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import oracle_bind as ob
+    from x3dcore2_gb300 import abi
+    cw, ch = 96, 54
+    x0, y0 = (width - cw) // 2, (height - ch) // 2
+    if timing_ref and ob.os.path.exists(ob.REF_TIMING_LIB):
+        # the reference renders whole frames; time a reduced-resolution frame of the same scene
+        rs = ob.RefScene(scene, timing=True)
+        spp = threads
+        img, secs, taken = rs.render(abi.MODE_REF_LT1, cw, ch, spp, threads)
+        return cw * ch * taken / secs, "reference", f"{cw}x{ch} frame, {taken} spp, unidirect_lt1, {threads} threads"
+    t0 = time.time()
+    osc = ob.OracleScene(scene)
+    build_s = time.time() - t0
+    spp, total_paths, total_s = 1, 0, 0.0
+    while total_s < budget_s:
+        t = time.time()
+        osc.render(abi.MODE_REF_LT1, width, height, spp, seed=1, crop=(x0, y0, x0 + cw, y0 + ch), threads=threads)
+        dt = time.time() - t
+        total_paths += cw * ch * spp
+        total_s += dt
+        spp *= 2
+        if dt * 2 + total_s > budget_s * 1.5:
+            break
+    return total_paths / total_s, "port", (f"{cw}x{ch} crop of the {width}x{height} frame, unidirect_lt1 restated "
+                                           f"(oracle), {threads} threads, {total_s:.1f} s render, BVH build {build_s:.1f} s")
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind as ob
+    from x3dcore2_gb300 import abi
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
+    scene, w, h, _ = make_scene(args.small)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    osc = ob.OracleScene(scene)
+    cw, ch = 64, 36
+    x0, y0 = (w - cw) // 2, (h - ch) // 2
+    spp = 2
+    for _ in range(args.warmup):
+        osc.render(abi.MODE_REF_LT1, w, h, 1, seed=1, crop=(x0, y0, x0 + cw, y0 + ch), threads=threads)
+    t0 = time.time()
+    for k in range(args.steps):
+        osc.render(abi.MODE_REF_LT1, w, h, spp, seed=1, offset=k * spp, crop=(x0, y0, x0 + cw, y0 + ch),
+                   threads=threads)
+    dt = time.time() - t0
+    paths = cw * ch * spp * args.steps
+    v = paths / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "paths/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": dict(WORKLOAD),
+            "cpu_baseline": {"value": v, "unit": "paths/s", "cores": threads, "kind": kind,
+                             "sample": f"{cw}x{ch} centre crop of the {w}x{h} frame, {spp} spp per step, "
+                                       "unidirect_lt1 (the reference's CPU tracer restated by the oracle)"},
+            "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="e8g")
+    ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--small", action="store_true", help="reduced scene for quick checks (not a bench line)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    if args.warmup < 3:
+        args.warmup = 3
+
+    import numpy as np
+    import torch
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300.core import Context, default_params
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    scene, w, h, spp = make_scene(args.small)
+    ctx = Context(local)
+    t0 = time.time()
+    ctx.upload(scene)
+    commit_s = time.time() - t0
+    bvh = ctx.bvh_stats()
+    p = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5,
+                       sample_offset=rank * spp)
+    p.integrator = abi.INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+    stream = torch.cuda.current_stream()
+    d_img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+    h_img = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
+
+    def render_dev():
+        ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        render_dev()
+    torch.cuda.synchronize()
+    counts = ctx.count_traversal(p)  # instrumented run (not timed): rays, nodes, tris
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kernel_ms, launches = [], 0
+    for k in range(args.steps):
+        flush.zero_()  # L2 flush between timed steps (outside the event pair)
+        starts[k].record(stream)
+        render_dev()
+        ends[k].record(stream)
+        st = ctx.stats()
+        kernel_ms.append(st["kernel_ms"])
+        launches += st["launches"]
+    barrier()
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    paths_per_step = w * h * spp
+    value = paths_per_step * world / (ms_per_step / 1000.0)
+
+    # end to end through the public call: host buffer, image read back every step
+    lib = abi.load()
+    e2e_ms = []
+    for k in range(max(2, min(args.steps, 3))):
+        barrier()
+        t = time.perf_counter()
+        abi.check(lib.e8g_render(ctx.h, C.byref(p), C.c_void_p(h_img.data_ptr())), ctx.h, "e8g_render")
+        e2e_ms.append((time.perf_counter() - t) * 1000)
+    e2e_value = paths_per_step * world / (statistics.mean(e2e_ms) / 1000.0)
+
+    peak, peak_kind = read_peaks()
+    mean_kernel_ms = statistics.mean(kernel_ms)
+    alg_bytes = 32 * counts["nodes"] + 48 * counts["tris"]
+    achieved = alg_bytes / (mean_kernel_ms / 1000.0) / 1e9
+    traffic = TRAFFIC_BYTES_PER_PATH * paths_per_step if TRAFFIC_BYTES_PER_PATH else None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": dict(WORKLOAD, integrator=args.integrator, l2="flushed between steps (256 MB write)",
+                       small=args.small, bvh_nodes=bvh["num_nodes"], bvh_build_ms=bvh["build_ms"],
+                       commit_s=round(commit_s, 3)),
+        "e2e": {"value": e2e_value, "unit": "paths/s", "ms_per_step": statistics.mean(e2e_ms),
+                "h2d_bytes_per_step": C.sizeof(abi.RenderParams),
+                "d2h_bytes_per_step": w * h * 16},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "k_mega (megakernel)", "kernel_ms": mean_kernel_ms,
+                     "algorithmic_bytes": alg_bytes, "rays": counts["rays"], "nodes": counts["nodes"],
+                     "tris": counts["tris"], "rays_per_s": counts["rays"] / (mean_kernel_ms / 1000.0)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        v, kind, sample = cpu_sample(scene, w, h, args.cpu_budget, os.cpu_count() or 1, timing_ref=False)
+        line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": os.cpu_count() or 1, "kind": kind,
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -116,7 +116,14 @@ typedef struct e8g_bvh_opts {
     float tri_cost;          /* reference BVH_RAY_TRIANGLE_COST = 8 */
     float node_cost;         /* reference BVH_RAY_BOX_COST = 1 */
     uint32_t num_threads;    /* host build threads, 0 = all */
+    uint32_t layout;         /* E8G_BVH_SAH or E8G_BVH_REFERENCE */
 } e8g_bvh_opts;
+
+enum {
+    E8G_BVH_SAH = 0,      /* binned SAH over 3 axes, child pairs, ordered traversal (fast) */
+    E8G_BVH_REFERENCE = 1 /* the reference's own tree and visiting order (pathspace.cpp:121-456):
+                             hit identities match the reference bit for bit, ties included */
+};
 
 typedef struct e8g_bvh_stats {
     uint32_t num_nodes;

@@ -25,7 +25,7 @@ def match_fraction(a, b, rtol=RTOL, atol=1e-6):
 @pytest.mark.parametrize("name", ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz"])
 def test_paths_match_reference_golden(ctx, name):
     d = G.load(name)
-    ctx.upload(G.scene_from(d))
+    ctx.upload(G.scene_from(d), layout=abi.BVH_REFERENCE)
     w, h, seed = int(d["width"]), int(d["height"]), int(d["seed"])
     for mname, mode in MODES.items():
         if "rad_" + mname not in d:

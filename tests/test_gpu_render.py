@@ -17,17 +17,22 @@ def rel_mse(img, ref, eps=1e-2):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_REFERENCE, abi.BVH_SAH])
 @pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT])
-def test_image_matches_oracle_same_streams(ctx, mode):
-    sc = S.cornell(48, 48)
-    ctx.upload(sc)
+def test_image_matches_oracle_same_streams(ctx, mode, layout):
+    """Same draw streams: >= 98% of pixels agree to 1e-4; the rest are pixels with a path that
+    took another branch after a last-ulp difference (sinf/cosf/atanf) or an edge tie."""
+    sc = S.cornell(48, 40)
+    ctx.upload(sc, layout=layout)
     osc = ob.OracleScene(sc)
-    p = default_params(mode, 48, 48, 8, seed=9, max_depth=6 if mode == abi.MODE_MIS else 0)
+    p = default_params(mode, 48, 40, 8, seed=9, max_depth=6 if mode == abi.MODE_MIS else 0)
     img = ctx.render(p)[..., :3]
     pol = ob.OPolicy(p.max_depth, p.rr_start, p.rr_prob, 8)
-    ref = osc.render(mode, 48, 48, 8, seed=9, policy=pol, rng=p.rng)[..., :3]
+    ref = osc.render(mode, 48, 40, 8, seed=9, policy=pol, rng=p.rng)[..., :3]
     assert np.all(np.isfinite(img)) and np.all(img >= 0)
-    assert rel_mse(img, ref) < 1e-4, rel_mse(img, ref)
+    close = np.all(np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-6), axis=-1)
+    assert close.mean() >= 0.98, close.mean()
+    assert rel_mse(img, ref) < 2e-3, rel_mse(img, ref)
 
 
 @pytest.mark.parametrize("mode", [abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_MIS])
@@ -71,8 +76,11 @@ def test_normal_and_position_tracers(ctx):
 def test_invalid_params(ctx):
     from x3dcore2_gb300.abi import E8GError
     ctx.upload(S.cornell(8, 8))
-    for bad in (dict(width=1), dict(mode=42), dict(rr_prob=0.0), dict(rng=7)):
-        p = default_params(abi.MODE_REF_LT1, 8, 8, 1, **bad)
+    for bad in (dict(width=1), dict(mode=42), dict(rr_prob=0.0), dict(rng=7), dict(max_depth=300),
+                dict(rr_prob=1.0), dict(rr_start=100)):
+        p = default_params(abi.MODE_REF_LT1, 8, 8, 1)
+        for k, v in bad.items():
+            setattr(p, k, v)
         with pytest.raises(E8GError, match="INVALID_ARG"):
             ctx.render(p)
 

@@ -5,6 +5,7 @@ import pytest
 
 import golden_util as G
 import oracle_bind as ob
+from x3dcore2_gb300 import abi
 from x3dcore2_gb300 import scene as S
 
 pytestmark = pytest.mark.gpu
@@ -12,10 +13,14 @@ pytestmark = pytest.mark.gpu
 FIXTURES = ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz"]
 
 
-def compare_hits(g, ref_mesh, ref_tri, ref_t, min_match=0.9999):
-    same_mesh = g["mesh"] == ref_mesh
-    same = same_mesh & (g["tri"] == ref_tri)
-    assert same.mean() >= min_match, f"id match {same.mean():.6f}"
+def compare_hits(g, ref_mesh, ref_tri, ref_t, min_match=0.9999, min_strict=0.999):
+    """Ids must match on >= min_match of rays, counting as a match a ray where both sides hit
+    at bitwise the same distance (a tie on a shared edge, resolved by visiting order); ids must
+    match outright on >= min_strict."""
+    same = (g["mesh"] == ref_mesh) & (g["tri"] == ref_tri)
+    tie = (~same) & (ref_mesh >= 0) & (g["t"].view(np.uint32) == ref_t.view(np.uint32))
+    assert (same | tie).mean() >= min_match, f"id match {(same | tie).mean():.6f}"
+    assert same.mean() >= min_strict, f"strict id match {same.mean():.6f}"
     hit = same & (ref_mesh >= 0)
     rel = np.abs(g["t"][hit] - ref_t[hit]) / np.maximum(np.abs(ref_t[hit]), 1e-30)
     assert np.all(rel <= 1e-5), rel.max()
@@ -23,13 +28,24 @@ def compare_hits(g, ref_mesh, ref_tri, ref_t, min_match=0.9999):
 
 
 @pytest.mark.parametrize("name", FIXTURES)
-def test_closest_hits_match_reference_golden(ctx, name):
+def test_closest_hits_match_reference_golden_exactly(ctx, name):
+    """The reference's tree and visiting order: every id and distance bit-exact, ties included."""
+    d = G.load(name)
+    ctx.upload(G.scene_from(d), layout=abi.BVH_REFERENCE)
+    g = ctx.trace_closest(d["rays"])
+    assert np.array_equal(g["mesh"], d["hit_mesh"]) and np.array_equal(g["tri"], d["hit_tri"])
+    hit = d["hit_mesh"] >= 0
+    assert np.array_equal(g["t"][hit].view(np.uint32), d["hit_t"][hit].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_closest_hits_match_reference_golden_sah(ctx, name):
+    """The fast SAH tree: same hits; ties on shared edges may resolve to the other triangle."""
     d = G.load(name)
     ctx.upload(G.scene_from(d))
     g = ctx.trace_closest(d["rays"])
     compare_hits(g, d["hit_mesh"], d["hit_tri"], d["hit_t"], min_match=1.0)
-    # bitwise distances: same triangle, same arithmetic, no FMA contraction
-    hit = d["hit_mesh"] >= 0
+    hit = (d["hit_mesh"] >= 0) & (g["mesh"] == d["hit_mesh"])
     assert np.array_equal(g["t"][hit].view(np.uint32), d["hit_t"][hit].view(np.uint32))
 
 
@@ -51,11 +67,12 @@ def random_rays(n, lo, hi, seed):
     return ob.rays_array(o, dd)
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_REFERENCE])
 @pytest.mark.parametrize("kind,size", [("ico", 6), ("soup", 100_000), ("ico", 7)])
-def test_closest_and_any_hit_match_oracle_on_large_scenes(ctx, kind, size):
+def test_closest_and_any_hit_match_oracle_on_large_scenes(ctx, kind, size, layout):
     sc = (S.displaced_icosphere(level=size, seed=2, num_materials=64, width=64, height=36) if kind == "ico"
           else S.soup(size, seed=4, width=64, height=64))
-    ctx.upload(sc)
+    ctx.upload(sc, layout=layout)
     osc = ob.OracleScene(sc)
     rays = random_rays(20000, -1.0, 1.0, seed=size)
     g = ctx.trace_closest(rays)
@@ -80,8 +97,14 @@ def test_trace_edge_cases(ctx):
     d = np.array([[0, 1, 0], [0, 1, 0], [0, 0, 1], [0, 0, -1], [0, 0, 1], [0, 0, -1], [0, -1, 0]], np.float32)
     rays = ob.rays_array(o, d)
     g, r = ctx.trace_closest(rays), osc.trace_closest(rays)
-    assert np.array_equal(g["mesh"], r["mesh"]) and np.array_equal(g["tri"], r["tri"])
+    # rays 0 and 6 hit the centre of a quad, on its diagonal: a tie both layouts may resolve
+    # differently from the oracle; the distance is the same bits either way
+    assert np.array_equal(g["mesh"], r["mesh"])
+    assert np.array_equal(g["t"].view(np.uint32), r["t"].view(np.uint32))
     assert g["mesh"][4] == -1  # nothing within 1000
+    ctx.upload(sc, layout=abi.BVH_REFERENCE)
+    g = ctx.trace_closest(rays)
+    assert np.array_equal(g["tri"], r["tri"])
 
 
 def test_trace_without_scene_is_an_error(lib):

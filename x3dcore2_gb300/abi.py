@@ -23,6 +23,7 @@ MODE_REF_UNI, MODE_REF_LT1, MODE_MIS, MODE_REF_BDPT, MODE_BDPT_POWER = 0, 1, 2, 
 MODE_REF_DIRECT, MODE_NORMAL, MODE_POSITION = 5, 6, 7
 INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT = 0, 1
 RNG_MINSTD, RNG_PHILOX = 0, 1
+BVH_SAH, BVH_REFERENCE = 0, 1
 # generators
 GEN_CORNELL, GEN_DISPLACED_ICO, GEN_SOUP, GEN_FURNACE = 0, 1, 2, 3
 
@@ -59,7 +60,7 @@ class SceneDesc(C.Structure):
 
 class BvhOpts(C.Structure):
     _fields_ = [("max_leaf_prims", C.c_uint32), ("num_bins", C.c_uint32), ("tri_cost", C.c_float),
-                ("node_cost", C.c_float), ("num_threads", C.c_uint32)]
+                ("node_cost", C.c_float), ("num_threads", C.c_uint32), ("layout", C.c_uint32)]
 
 
 class BvhStats(C.Structure):

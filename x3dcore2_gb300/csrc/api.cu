@@ -79,6 +79,7 @@ void fill_dev_scene(e8g_ctx *c) {
     S.nm = p.nm;
     S.nnodes = p.bvh.num_nodes;
     S.ntris = p.nt;
+    S.layout = p.layout;
     S.total_power = p.total_power;
     for (int k = 0; k < 3; k++) {
         S.bmin[k] = p.bmin[k];
@@ -171,6 +172,7 @@ void e8g_default_bvh_opts(e8g_bvh_opts *o) {
     o->tri_cost = 8.0f;
     o->node_cost = 1.0f;
     o->num_threads = 0;
+    o->layout = E8G_BVH_SAH;
 }
 
 void e8g_default_params(e8g_render_params *p, uint32_t mode, uint32_t width, uint32_t height, uint32_t spp) {
@@ -311,6 +313,9 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
         bo.tri_cost = o->tri_cost;
         bo.node_cost = o->node_cost;
         bo.num_threads = o->num_threads;
+        if (o->layout > E8G_BVH_REFERENCE)
+            return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH layout");
+        bo.layout = o->layout;
     }
     cudaSetDevice(c->device);
     try {
@@ -319,6 +324,10 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
         return fail(c, E8G_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
     }
     packed_scene &p = c->pack;
+    if (p.layout == E8G_BVH_REFERENCE && p.bvh.max_depth > kMaxRefTreeDepth) {
+        c->built = false;
+        return fail(c, E8G_ERR_UNSUPPORTED, "reference BVH deeper than the traversal stack (63 levels)");
+    }
     cudaError_t e = upload(c->b_nlo, p.bvh.lo, c->stream);
     if (e == cudaSuccess)
         e = upload(c->b_nhi, p.bvh.hi, c->stream);

@@ -18,6 +18,7 @@ struct bvh_build_opts {
     float tri_cost = 8.0f;       // reference BVH_RAY_TRIANGLE_COST
     float node_cost = 1.0f;      // reference BVH_RAY_BOX_COST
     uint32_t num_threads = 0;
+    uint32_t layout = 0; // 0: SAH child pairs, 1: the reference's tree
 };
 
 struct flat_bvh {
@@ -35,5 +36,13 @@ struct flat_bvh {
 
 // tris: 3 global vertex indices per triangle; pos: 3 floats per vertex.
 flat_bvh build_bvh(float const *pos, uint32_t const *tris, uint32_t num_tris, bvh_build_opts const &o);
+
+// The reference's tree (bvh_path_space_layout::commit) in depth-first order: node n's left child
+// is n + 1, its right child `link`; boxes are the reference's, uninflated.
+flat_bvh build_bvh_reference(float const *pos, uint32_t const *tris, uint32_t num_tris);
+
+// Deepest reference tree the 64-entry traversal stack can walk (the stack never holds more than
+// depth + 1 entries).
+constexpr uint32_t kMaxRefTreeDepth = 63;
 
 } // namespace e8g

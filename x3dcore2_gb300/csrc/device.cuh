@@ -17,7 +17,8 @@ namespace e8g {
 constexpr float kPi = 3.14159274101257324f;    // static_cast<float>(M_PI)
 constexpr float kInvPi = 0.318309873342514038f; // 1.0f / static_cast<float>(M_PI), 0x3ea2f983
 constexpr int kBlock = 128;                     // threads per block of the traversal kernels
-constexpr int kStack = 32;                      // per-thread traversal stack (== kMaxTreeDepth)
+constexpr int kStack = 32;                      // per-thread (node, t) stack of the SAH layout (== kMaxTreeDepth)
+constexpr int kStackWords = 2 * kStack;          // shared words per thread: 64 node entries in reference order
 constexpr float kOneMinusUlp = 0.999999940395355225f; // nextafter(1.0f, 0.0f)
 // Safety stop for any path, whatever the policy (the C ABI rejects policies under which paths
 // could approach it: survival <= 0.95 from depth <= 64 leaves a 1e-21 chance of reaching it).
@@ -43,6 +44,7 @@ struct DevScene {
     const float *light_cum;    // basic_light_sources::commit CDF (lightsources.cpp:45-52)
     const float *light_pnorm;  // |power| per light
     uint32_t nmat, nl, nm, nnodes, ntris;
+    uint32_t layout; // 0: SAH child pairs (ordered traversal), 1: the reference's tree and order
     float total_power;
     float bmin[3], bmax[3]; // if_path_space::aabb() for the position tracer
     DevCamera cam;
@@ -233,8 +235,10 @@ __device__ __forceinline__ bool tri_test(float3 o, float3 d, float4 a, float4 b,
 // ordered child visits, far children and their entry distances kept on a per-thread stack in
 // shared memory (stack entries of one thread are kBlock words apart, so lanes never conflict).
 template <bool COUNT>
-__device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3 d, uint32_t *sn, float *st,
-                                             TraceCounters *cnt) {
+__device__ __forceinline__ Hit trace_closest_sah(const DevScene &S, float3 o, float3 d, uint32_t *stk,
+                                                 TraceCounters *cnt) {
+    uint32_t *sn = stk;
+    float *st = reinterpret_cast<float *>(stk + kStack * kBlock);
     Hit h;
     h.t = INFINITY;
     h.tri = 0xFFFFFFFFu;
@@ -308,8 +312,8 @@ __device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3
 
 // Any hit with t in [tmin, tmax] (has_intersect, pathspace.cpp:415-456).
 template <bool COUNT>
-__device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d, float tmin, float tmax, uint32_t *sn,
-                                          TraceCounters *cnt) {
+__device__ __forceinline__ bool trace_any_sah(const DevScene &S, float3 o, float3 d, float tmin, float tmax,
+                                              uint32_t *sn, TraceCounters *cnt) {
     if (S.nnodes == 0)
         return false;
     float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
@@ -355,6 +359,122 @@ __device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d,
         link = __float_as_uint(__ldg(&S.nlo[node].w));
         count = __float_as_uint(__ldg(&S.nhi[node].w));
     }
+}
+
+
+// ---- the reference's tree, visited in the reference's order ----
+// bvh_path_space_layout::intersect / has_intersect (pathspace.cpp:330-456): depth-first with an
+// explicit stack, both children tested on the fixed interval and pushed left then right (so the
+// right child is visited first), no ordering and no culling by the closest hit; node boxes are
+// the reference's, uninflated. Triangles are met in the reference's order, so ties on shared
+// edges resolve as in the reference.
+
+__device__ __forceinline__ float ref_max(float a, float b) { return a < b ? b : a; } // std::max(a, b)
+__device__ __forceinline__ float ref_min(float a, float b) { return b < a ? b : a; } // std::min(a, b)
+
+// aabb::intersect (tensor.h:815-840)
+__device__ __forceinline__ bool ref_slab(float4 lo, float4 hi, float3 o, float3 inv, float tmin, float tmax) {
+    float k0 = (lo.x - o.x) * inv.x, k1 = (hi.x - o.x) * inv.x;
+    if (k0 > k1) {
+        tmin = ref_max(k1, tmin);
+        tmax = ref_min(k0, tmax);
+    } else {
+        tmin = ref_max(k0, tmin);
+        tmax = ref_min(k1, tmax);
+    }
+    if (tmin > tmax)
+        return false;
+    k0 = (lo.y - o.y) * inv.y;
+    k1 = (hi.y - o.y) * inv.y;
+    if (k0 > k1) {
+        tmin = ref_max(k1, tmin);
+        tmax = ref_min(k0, tmax);
+    } else {
+        tmin = ref_max(k0, tmin);
+        tmax = ref_min(k1, tmax);
+    }
+    if (tmin > tmax)
+        return false;
+    k0 = (lo.z - o.z) * inv.z;
+    k1 = (hi.z - o.z) * inv.z;
+    if (k0 > k1) {
+        tmin = ref_max(k1, tmin);
+        tmax = ref_min(k0, tmax);
+    } else {
+        tmin = ref_max(k0, tmin);
+        tmax = ref_min(k1, tmax);
+    }
+    return !(tmin > tmax);
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d, float tmin, float tmax, Hit &h,
+                                          uint32_t *stk, TraceCounters *cnt) {
+    if (S.nnodes == 0)
+        return false;
+    float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    int sp = 0;
+    stk[0] = 0;
+    sp = 1;
+    while (sp > 0) {
+        sp--;
+        uint32_t n = stk[sp * kBlock];
+        uint32_t link = __float_as_uint(__ldg(&S.nlo[n].w));
+        uint32_t count = __float_as_uint(__ldg(&S.nhi[n].w));
+        if (count > 0) {
+            for (uint32_t k = link; k < link + count; k++) {
+                float4 a = __ldg(&S.tri[3 * k]), b = __ldg(&S.tri[3 * k + 1]), c = __ldg(&S.tri[3 * k + 2]);
+                if (COUNT)
+                    cnt->tris++;
+                float t0, b1, b2;
+                if (tri_test(o, d, a, b, c, tmin, tmax, t0, b1, b2)) {
+                    if (ANY)
+                        return true;
+                    if (t0 < h.t) {
+                        h.t = t0;
+                        h.tri = __float_as_uint(a.w);
+                        h.b1 = b1;
+                        h.b2 = b2;
+                    }
+                }
+            }
+        } else {
+            uint32_t left = n + 1, right = link;
+            if (COUNT)
+                cnt->nodes += 2;
+            if (ref_slab(__ldg(&S.nlo[left]), __ldg(&S.nhi[left]), o, inv, tmin, tmax))
+                stk[(sp++) * kBlock] = left;
+            if (ref_slab(__ldg(&S.nlo[right]), __ldg(&S.nhi[right]), o, inv, tmin, tmax))
+                stk[(sp++) * kBlock] = right;
+        }
+    }
+    return false;
+}
+
+// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336) in either layout.
+template <bool COUNT>
+__device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
+    if (S.layout == 1) {
+        Hit h;
+        h.t = INFINITY;
+        h.tri = 0xFFFFFFFFu;
+        h.b1 = h.b2 = 0.0f;
+        trace_ref<false, COUNT>(S, o, d, 1e-4f, 1000.0f, h, stk, cnt);
+        return h;
+    }
+    return trace_closest_sah<COUNT>(S, o, d, stk, cnt);
+}
+
+// Any hit on [tmin, tmax] in either layout.
+template <bool COUNT>
+__device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d, float tmin, float tmax, uint32_t *stk,
+                                          TraceCounters *cnt) {
+    if (S.layout == 1) {
+        Hit h;
+        h.t = INFINITY;
+        return trace_ref<true, COUNT>(S, o, d, tmin, tmax, h, stk, cnt);
+    }
+    return trace_any_sah<COUNT>(S, o, d, tmin, tmax, stk, cnt);
 }
 
 // ------------------------------------------------------------------ surfaces ----

@@ -94,10 +94,8 @@ template <class R, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
                                                  float4 *accum, float *path_rgb, unsigned long long *work,
                                                  unsigned long long *counters) {
-    __shared__ uint32_t sn_all[kStack * kBlock];
-    __shared__ float st_all[kStack * kBlock];
-    uint32_t *sn = sn_all + threadIdx.x;
-    float *st = st_all + threadIdx.x;
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *sn = stk_all + threadIdx.x;
     TraceCounters cnt{0, 0};
     uint32_t rays = 0;
     const uint64_t mix = splitmix64(A.seed);
@@ -245,7 +243,7 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
                 if (!finish) {
                     if (COUNT)
                         rays++;
-                    Hit h = trace_closest<COUNT>(S, ps.p, i, sn, st, &cnt);
+                    Hit h = trace_closest<COUNT>(S, ps.p, i, sn, &cnt);
                     if (h.tri == 0xFFFFFFFFu) {
                         finish = true;
                     } else {

@@ -144,7 +144,8 @@ void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
     for (uint32_t t = 0; t < s.nt; t++)
         for (int k = 0; k < 3; k++)
             t3[3 * static_cast<size_t>(t) + k] = s.tidx[4 * static_cast<size_t>(t) + k];
-    s.bvh = build_bvh(p3.data(), t3.data(), s.nt, o);
+    s.bvh = o.layout == 1 ? build_bvh_reference(p3.data(), t3.data(), s.nt) : build_bvh(p3.data(), t3.data(), s.nt, o);
+    s.layout = o.layout;
     s.tri.assign(12 * static_cast<size_t>(s.nt), 0.0f);
     for (uint32_t k = 0; k < s.nt; k++) {
         uint32_t t = s.bvh.tri_order[k];

@@ -30,6 +30,7 @@ struct packed_scene {
     flat_bvh bvh;
     std::vector<float> tri;         // 12 floats per BVH position
     double build_ms = 0;
+    uint32_t layout = 0;
 };
 
 // Fills everything but the BVH. Float arithmetic follows the reference (built with

@@ -6,14 +6,13 @@ namespace e8g {
 // compute_first_hit (pathtracer.cpp:456-472): camera ray, closest hit, back-facing hits become
 // misses, emitter lookup.
 __global__ void __launch_bounds__(kBlock) k_first_hits(DevScene S, uint32_t w, uint32_t h, FirstHit *out) {
-    __shared__ uint32_t sn[kStack * kBlock];
-    __shared__ float st[kStack * kBlock];
+    __shared__ uint32_t stk[kStackWords * kBlock];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w * h)
         return;
     float3 o, d;
     camera_ray(S.cam, i % w, i / w, w, h, o, d);
-    Hit hit = trace_closest<false>(S, o, d, sn + threadIdx.x, st + threadIdx.x, nullptr);
+    Hit hit = trace_closest<false>(S, o, d, stk + threadIdx.x, nullptr);
     FirstHit f;
     f.d = make_float4(d.x, d.y, d.z, 0.0f);
     int32_t mesh = -1, light = -1;
@@ -50,14 +49,13 @@ __global__ void k_camera_rays(DevScene S, uint32_t w, uint32_t h, float *rays6) 
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_trace_closest(DevScene S, float const *rays6, uint32_t n, float *hits5,
                                                           unsigned long long *counters) {
-    __shared__ uint32_t sn[kStack * kBlock];
-    __shared__ float st[kStack * kBlock];
+    __shared__ uint32_t stk[kStackWords * kBlock];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     TraceCounters c{0, 0};
     if (i < n) {
         float const *r = rays6 + 6 * static_cast<size_t>(i);
         float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
-        Hit h = trace_closest<COUNT>(S, o, d, sn + threadIdx.x, st + threadIdx.x, &c);
+        Hit h = trace_closest<COUNT>(S, o, d, stk + threadIdx.x, &c);
         float *out = hits5 + 5 * static_cast<size_t>(i);
         if (h.tri == 0xFFFFFFFFu) {
             out[0] = 0.0f;
@@ -89,13 +87,13 @@ __global__ void __launch_bounds__(kBlock) k_trace_closest(DevScene S, float cons
 
 __global__ void __launch_bounds__(kBlock) k_trace_any(DevScene S, float const *rays6, float const *tmin,
                                                       float const *tmax, uint32_t n, uint8_t *occ) {
-    __shared__ uint32_t sn[kStack * kBlock];
+    __shared__ uint32_t stk[kStackWords * kBlock];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     float const *r = rays6 + 6 * static_cast<size_t>(i);
     float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
-    occ[i] = trace_any<false>(S, o, d, tmin[i], tmax[i], sn + threadIdx.x, nullptr) ? 1 : 0;
+    occ[i] = trace_any<false>(S, o, d, tmin[i], tmax[i], stk + threadIdx.x, nullptr) ? 1 : 0;
 }
 
 __global__ void k_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rgba) {
