@@ -13,7 +13,7 @@ from x3dcore2_gb300.core import default_params
 pytestmark = pytest.mark.gpu
 
 MODES = {"uni": abi.MODE_REF_UNI, "lt1": abi.MODE_REF_LT1, "direct": abi.MODE_REF_DIRECT,
-         "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION}
+         "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION, "bdpt": abi.MODE_REF_BDPT}
 RTOL = 1e-4
 
 
@@ -37,6 +37,23 @@ def test_paths_match_reference_golden(ctx, name):
 
 
 POLICIES = [dict(), dict(max_depth=5, rr_start=3), dict(max_depth=8, rr_start=3, rr_prob=0.75)]
+
+
+@pytest.mark.parametrize("max_len", [8, 6, 3])
+def test_bdpt_paths_match_oracle(ctx, max_len):
+    """bidirect_mis with the subpath cap as a policy knob (the reference fixes it at 8)."""
+    d = G.load("ico.npz")
+    sc = G.scene_from(d)
+    ctx.upload(sc, layout=abi.BVH_REFERENCE)
+    osc = ob.OracleScene(sc)
+    w, h = int(d["width"]), int(d["height"])
+    px = np.random.default_rng(8).integers(0, w * h, 800).astype(np.uint32)
+    samples = np.arange(len(px), dtype=np.uint32)
+    p = default_params(abi.MODE_REF_BDPT, w, h, 1, seed=5, bdpt_max_len=max_len)
+    got = ctx.render_paths(p, px, samples)
+    seeds = np.array([ob.oracle().o_path_seed(5, int(a), int(b)) for a, b in zip(px, samples)], np.uint32)
+    ref = osc.render_paths(abi.MODE_REF_BDPT, w, h, px, seeds, policy=ob.OPolicy(0, 2, 0.5, max_len))
+    assert match_fraction(got, ref) >= 0.99
 
 
 @pytest.mark.parametrize("pol", POLICIES)

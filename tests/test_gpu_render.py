@@ -18,7 +18,8 @@ def rel_mse(img, ref, eps=1e-2):
 
 
 @pytest.mark.parametrize("layout", [abi.BVH_REFERENCE, abi.BVH_SAH])
-@pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT])
+@pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT,
+                                  abi.MODE_REF_BDPT])
 def test_image_matches_oracle_same_streams(ctx, mode, layout):
     """Same draw streams: >= 98% of pixels agree to 1e-4; the rest are pixels with a path that
     took another branch after a last-ulp difference (sinf/cosf/atanf) or an edge tie."""
@@ -35,7 +36,7 @@ def test_image_matches_oracle_same_streams(ctx, mode, layout):
     assert rel_mse(img, ref) < 2e-3, rel_mse(img, ref)
 
 
-@pytest.mark.parametrize("mode", [abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_MIS])
+@pytest.mark.parametrize("mode", [abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_MIS, abi.MODE_REF_BDPT])
 def test_furnace(ctx, mode):
     """tst_pathtracer.cpp:58-86 on the GPU: E[sum RGB] = 1 / (1 - 0.7) * 3 = 10 within 0.3."""
     ctx.upload(S.furnace(30))

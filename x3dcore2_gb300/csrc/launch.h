@@ -25,4 +25,9 @@ void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *f
                        unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
 int megakernel_blocks_per_sm();
 
+// Bidirectional path tracing (reference uniform weights), one thread per path.
+void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                 unsigned long long *work, int grid, cudaStream_t st);
+int bdpt_blocks_per_sm();
+
 } // namespace e8g

@@ -13,9 +13,13 @@ e8g_status run_integrator(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
     if (e != cudaSuccess)
         return cuda_fail(c, e, "work counter");
     auto *work = static_cast<unsigned long long *>(c->b_work.ptr);
-    int grid = persistent_grid(c, megakernel_blocks_per_sm());
-    launch_megakernel(c->dev, A, static_cast<FirstHit const *>(c->b_fh.ptr), accum, path_rgb, work, d_counts, grid,
-                      c->stream);
+    auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
+    if (A.mode == E8G_MODE_REF_BDPT) {
+        launch_bdpt(c->dev, A, fh, accum, path_rgb, work, persistent_grid(c, bdpt_blocks_per_sm()), c->stream);
+    } else {
+        int grid = persistent_grid(c, megakernel_blocks_per_sm());
+        launch_megakernel(c->dev, A, fh, accum, path_rgb, work, d_counts, grid, c->stream);
+    }
     c->launches++;
     return E8G_OK;
 }
@@ -23,8 +27,10 @@ e8g_status run_integrator(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
 } // namespace
 
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts) {
-    if (p->mode == E8G_MODE_REF_BDPT || p->mode == E8G_MODE_BDPT_POWER)
-        return fail(c, E8G_ERR_UNSUPPORTED, "bidirectional modes are not available yet");
+    if (p->mode == E8G_MODE_BDPT_POWER)
+        return fail(c, E8G_ERR_UNSUPPORTED, "power-heuristic BDPT is not available yet");
+    if (counts && p->mode == E8G_MODE_REF_BDPT)
+        return fail(c, E8G_ERR_UNSUPPORTED, "traversal counters cover the unidirectional integrators");
     c->launches = 0;
     size_t npix = static_cast<size_t>(p->width) * p->height;
     cudaError_t e = c->b_accum.reserve(npix * sizeof(float4));
@@ -76,8 +82,8 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
 
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,
                        uint32_t n, float *d_rgb) {
-    if (p->mode == E8G_MODE_REF_BDPT || p->mode == E8G_MODE_BDPT_POWER)
-        return fail(c, E8G_ERR_UNSUPPORTED, "bidirectional modes are not available yet");
+    if (p->mode == E8G_MODE_BDPT_POWER)
+        return fail(c, E8G_ERR_UNSUPPORTED, "power-heuristic BDPT is not available yet");
     c->launches = 0;
     e8g_status s = first_hits(c, p->width, p->height);
     if (s != E8G_OK)
