@@ -192,6 +192,9 @@ def main():
     ap.add_argument("--small", action="store_true", help="reduced scene for quick checks (not a bench line)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--res", default=None, help="WxH override, e.g. 480x270 (profiling a smaller launch)")
+    ap.add_argument("--spp", type=int, default=None, help="spp override (profiling)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -209,6 +212,12 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     scene, w, h, spp = make_scene(args.small)
+    if args.res:
+        w, h = (int(x) for x in args.res.lower().split("x"))
+        scene.camera.aspect = w / h
+        scene.desc.camera = scene.camera
+    if args.spp:
+        spp = args.spp
     ctx = Context(local)
     t0 = time.time()
     ctx.upload(scene)
@@ -264,11 +273,13 @@ def main():
     # end to end through the public call: host buffer, image read back every step
     lib = abi.load()
     e2e_ms = []
-    for k in range(max(2, min(args.steps, 3))):
+    for k in range(0 if args.no_e2e else max(2, min(args.steps, 3))):
         barrier()
         t = time.perf_counter()
         abi.check(lib.e8g_render(ctx.h, C.byref(p), C.c_void_p(h_img.data_ptr())), ctx.h, "e8g_render")
         e2e_ms.append((time.perf_counter() - t) * 1000)
+    if not e2e_ms:
+        e2e_ms = [float("nan")]
     e2e_value = paths_per_step * world / (statistics.mean(e2e_ms) / 1000.0)
 
     peak, peak_kind = read_peaks()
