@@ -243,6 +243,23 @@ e8g_status e8g_render(e8g_ctx *ctx, const e8g_render_params *params, float *rgba
 e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
                           void *stream);
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
+
+/* Largest image (width * height) e8g_render_dev_noalloc accepts. */
+#define E8G_NOALLOC_MAX_PIXELS 65536u
+
+/* Same render as e8g_render_dev, but it allocates no device memory: its scratch (first-hit cache,
+ * accumulator, counters) lives in one statically sized device array, 4 MiB held on every GPU
+ * that loads the library until exit. For callers that cannot call cudaMalloc at render time
+ * (cudaMalloc synchronises the device and can fail once a process has budgeted all of its device
+ * memory up front). No counterpart in the reference.
+ *   - width * height must not exceed E8G_NOALLOC_MAX_PIXELS (else E8G_ERR_INVALID_ARG);
+ *   - the scene must already be uploaded and built (those calls allocate, once, beforehand);
+ *   - the first call on a device looks up the array's device address: make it before any
+ *     stream capture;
+ *   - all calls share the one array: calls that overlap on the GPU race, so serialise them.
+ * Asynchronous on `stream` (NULL = the context's stream); the caller synchronises. */
+e8g_status e8g_render_dev_noalloc(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
+                                  void *stream);
 /* Runs the render once with traversal counters on (not for timing) and returns the number of
  * rays traced, BVH nodes whose box was fetched and triangles tested. */
 e8g_status e8g_count_traversal(e8g_ctx *ctx, const e8g_render_params *params, e8g_render_stats *stats);

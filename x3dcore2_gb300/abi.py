@@ -124,6 +124,7 @@ SIGNATURES = {
     "e8g_trace_closest_dev": (_ST, [_P, _P, _U32, _P, _P]),
     "e8g_render": (_ST, [_P, C.POINTER(RenderParams), _P]),
     "e8g_render_dev": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
+    "e8g_render_dev_noalloc": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
     "e8g_count_traversal": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(RenderStats)]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
