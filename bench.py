@@ -188,7 +188,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="e8g")
-    ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--integrator", default="both", choices=["megakernel", "wavefront", "both"])
     ap.add_argument("--small", action="store_true", help="reduced scene for quick checks (not a bench line)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -211,6 +211,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    integrators = ["megakernel", "wavefront"] if args.integrator == "both" else [args.integrator]
     scene, w, h, spp = make_scene(args.small)
     if args.res:
         w, h = (int(x) for x in args.res.lower().split("x"))
@@ -225,53 +226,69 @@ def main():
     bvh = ctx.bvh_stats()
     p = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5,
                        sample_offset=rank * spp)
-    p.integrator = abi.INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
     stream = torch.cuda.current_stream()
     d_img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
     h_img = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
-
-    def render_dev():
-        ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
-
-    for _ in range(args.warmup):
-        render_dev()
-    torch.cuda.synchronize()
-    counts = ctx.count_traversal(p)  # instrumented run (not timed): rays, nodes, tris
+    lib = abi.load()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    tune = None
+    if "wavefront" in integrators:
+        r = abi.TuneResult()
+        pw = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
+        abi.check(lib.e8g_wavefront_tune(ctx.h, C.byref(pw), C.byref(r)), ctx.h, "e8g_wavefront_tune")
+        tune = {"capacity": r.capacity, "bounces_per_graph": r.bounces_per_graph,
+                "candidates": [[r.cand_capacity[i], r.cand_bounces[i], round(r.cand_ms[i], 3)]
+                               for i in range(r.num_candidates)]}
+
+    results = {}
     clocks = ClockSampler(local)
     clocks.start()
-    barrier()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kernel_ms, launches = [], 0
-    for k in range(args.steps):
-        flush.zero_()  # L2 flush between timed steps (outside the event pair)
-        starts[k].record(stream)
-        render_dev()
-        ends[k].record(stream)
-        st = ctx.stats()
-        kernel_ms.append(st["kernel_ms"])
-        launches += st["launches"]
-    barrier()
+    for integ in integrators:
+        p.integrator = abi.INTEGRATOR_WAVEFRONT if integ == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+        for _ in range(args.warmup):
+            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+        barrier()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kernel_ms, launches = [], 0
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (outside the event pair)
+            starts[k].record(stream)
+            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+            ends[k].record(stream)
+            st = ctx.stats()
+            kernel_ms.append(st["kernel_ms"])
+            launches += st["launches"]
+        barrier()
+        total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+        if world > 1:
+            t = torch.tensor([total_ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(t.item())
+        results[integ] = dict(ms_per_step=total_ms / args.steps, kernel_ms=statistics.mean(kernel_ms),
+                              launches=launches)
     clk = clocks.stop()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
     paths_per_step = w * h * spp
-    value = paths_per_step * world / (ms_per_step / 1000.0)
+    for r in results.values():
+        r["paths_per_s"] = paths_per_step * world / (r["ms_per_step"] / 1000.0)
+    best = max(results, key=lambda k: results[k]["paths_per_s"])
+    value = results[best]["paths_per_s"]
+    ms_per_step = results[best]["ms_per_step"]
+    launches = results[best]["launches"]
+    p.integrator = abi.INTEGRATOR_WAVEFRONT if best == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+
+    # traversal counts for the roofline: instrumented run of the megakernel (same paths, same rays)
+    pc = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
+    counts = ctx.count_traversal(pc)
+    mega_kernel_ms = results.get("megakernel", results[best])["kernel_ms"]
 
     # end to end through the public call: host buffer, image read back every step
-    lib = abi.load()
     e2e_ms = []
     for k in range(0 if args.no_e2e else max(2, min(args.steps, 3))):
         barrier()
@@ -283,7 +300,7 @@ def main():
     e2e_value = paths_per_step * world / (statistics.mean(e2e_ms) / 1000.0)
 
     peak, peak_kind = read_peaks()
-    mean_kernel_ms = statistics.mean(kernel_ms)
+    mean_kernel_ms = mega_kernel_ms
     alg_bytes = 32 * counts["nodes"] + 48 * counts["tris"]
     achieved = alg_bytes / (mean_kernel_ms / 1000.0) / 1e9
     traffic = TRAFFIC_BYTES_PER_PATH * paths_per_step if TRAFFIC_BYTES_PER_PATH else None
@@ -292,7 +309,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": dict(WORKLOAD, integrator=args.integrator, l2="flushed between steps (256 MB write)",
+        "config": dict(WORKLOAD, integrator=best, l2="flushed between steps (256 MB write)",
+                       integrators={k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in r.items()}
+                                    for k, r in results.items()}, wavefront_tune=tune,
                        small=args.small, bvh_nodes=bvh["num_nodes"], bvh_build_ms=bvh["build_ms"],
                        commit_s=round(commit_s, 3)),
         "e2e": {"value": e2e_value, "unit": "paths/s", "ms_per_step": statistics.mean(e2e_ms),

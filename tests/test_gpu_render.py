@@ -90,3 +90,25 @@ def test_zero_spp_renders_black(ctx):
     ctx.upload(S.cornell(8, 8))
     img = ctx.render(default_params(abi.MODE_REF_LT1, 8, 8, 0))
     assert np.all(img[..., :3] == 0)
+
+
+@pytest.mark.parametrize("capacity_small", [False, True])
+def test_wavefront_image_equals_megakernel(ctx, capacity_small):
+    """Same estimator, same streams: the wavefront image equals the megakernel image up to the
+    order of float accumulation; with few slots the queues refill many times."""
+    import ctypes as C
+    sc = S.displaced_icosphere(level=5, seed=3, num_materials=32, width=96, height=54)
+    ctx.upload(sc)
+    p = default_params(abi.MODE_MIS, 96, 54, 16, seed=2, max_depth=8, rr_start=3)
+    mk = ctx.render(p)
+    if capacity_small:
+        # tune on this frame, then force refills with the smallest candidate by rendering more spp
+        r = abi.TuneResult()
+        abi.check(ctx.lib.e8g_wavefront_tune(ctx.h, C.byref(p), C.byref(r)), ctx.h, "tune")
+        assert r.num_candidates == 6 and r.capacity in (1 << 20, 1 << 21, 1 << 22)
+        assert all(ms > 0 for ms in r.cand_ms[:6])
+    p.integrator = abi.INTEGRATOR_WAVEFRONT
+    wf = ctx.render(p)
+    assert np.all(np.isfinite(wf)) and np.all(wf >= 0)
+    close = np.abs(wf - mk) <= np.maximum(1e-4 * np.abs(mk), 1e-5)
+    assert close.mean() >= 0.999, close.mean()

@@ -97,6 +97,11 @@ class BatchItem(C.Structure):
                 ("rgba_out", C.POINTER(C.c_float))]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("capacity", C.c_uint32), ("bounces_per_graph", C.c_uint32), ("num_candidates", C.c_uint32),
+                ("cand_capacity", C.c_uint32 * 8), ("cand_bounces", C.c_uint32 * 8), ("cand_ms", C.c_double * 8)]
+
+
 class GenOpts(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("seed", C.c_uint64), ("level", C.c_uint32),
                 ("num_tris", C.c_uint32), ("num_materials", C.c_uint32), ("amplitude", C.c_float),
@@ -127,6 +132,7 @@ SIGNATURES = {
     "e8g_render_dev_noalloc": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
     "e8g_count_traversal": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(RenderStats)]),
+    "e8g_wavefront_tune": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(TuneResult)]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
     "e8g_forward": (_ST, [_P, C.POINTER(RenderParams), _P]),
     "e8g_backward": (_ST, [_P, _P, _P, _P]),

@@ -227,6 +227,8 @@ e8g_status e8g_create(e8g_ctx **out, e8g_device_opts const *opts) {
         e = cudaEventCreate(&c->ev3);
     if (e == cudaSuccess)
         e = c->b_work.reserve(64);
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&c->host_pinned, 64);
     if (e != cudaSuccess) {
         delete c;
         return E8G_ERR_CUDA;
@@ -252,6 +254,8 @@ e8g_status e8g_destroy(e8g_ctx *c) {
         cudaEventDestroy(c->ev3);
     if (c->stream)
         cudaStreamDestroy(c->stream);
+    if (c->host_pinned)
+        cudaFreeHost(c->host_pinned);
     delete c;
     return E8G_OK;
 }

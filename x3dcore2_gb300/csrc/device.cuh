@@ -451,7 +451,32 @@ __device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d,
     return false;
 }
 
-// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336) in either layout.
+// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336); LAYOUT 0 = SAH, 1 = reference tree.
+template <int LAYOUT, bool COUNT>
+__device__ __forceinline__ Hit trace_closest_l(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
+    if (LAYOUT == 1) {
+        Hit h;
+        h.t = INFINITY;
+        h.tri = 0xFFFFFFFFu;
+        h.b1 = h.b2 = 0.0f;
+        trace_ref<false, COUNT>(S, o, d, 1e-4f, 1000.0f, h, stk, cnt);
+        return h;
+    }
+    return trace_closest_sah<COUNT>(S, o, d, stk, cnt);
+}
+
+template <int LAYOUT, bool COUNT>
+__device__ __forceinline__ bool trace_any_l(const DevScene &S, float3 o, float3 d, float tmin, float tmax,
+                                            uint32_t *stk, TraceCounters *cnt) {
+    if (LAYOUT == 1) {
+        Hit h;
+        h.t = INFINITY;
+        return trace_ref<true, COUNT>(S, o, d, tmin, tmax, h, stk, cnt);
+    }
+    return trace_any_sah<COUNT>(S, o, d, tmin, tmax, stk, cnt);
+}
+
+// Closest hit in the scene's layout, chosen at run time (kernels off the hot path).
 template <bool COUNT>
 __device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
     if (S.layout == 1) {

@@ -69,7 +69,7 @@ __device__ __forceinline__ void emit(RenderArgs const &A, float4 *accum, float *
 }
 
 // transport_direct_illum with one light sample (pathtracer.cpp:152-242).
-template <class R, bool COUNT>
+template <class R, bool COUNT, int LAYOUT>
 __device__ __forceinline__ float3 ref_direct(DevScene const &S, R &rng, const DevMaterial &m, float3 p, float3 n,
                                              float3 o, uint32_t *sn, TraceCounters *cnt, uint32_t &rays) {
     float pmf;
@@ -84,13 +84,13 @@ __device__ __forceinline__ float3 ref_direct(DevScene const &S, R &rng, const De
         float3 i = divs(neg(l), dist);
         if (COUNT)
             rays++;
-        if (!trace_any<COUNT>(S, p, i, 1e-4f, dist - 1e-3f, sn, cnt))
+        if (!trace_any_l<LAYOUT, COUNT>(S, p, i, 1e-4f, dist - 1e-3f, sn, cnt))
             c = mul(illum, bsdf_eval(S, m, n, o, i));
     }
     return divs(divs(c, s.area_dens), 1.0f);
 }
 
-template <class R, bool COUNT>
+template <class R, bool COUNT, int LAYOUT>
 __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
                                                  float4 *accum, float *path_rgb, unsigned long long *work,
                                                  unsigned long long *counters) {
@@ -106,8 +106,12 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
     R rng;
 
     while (true) {
-        uint32_t need = __ballot_sync(~0u, !active && !done);
-        if (need) {
+        // refill: lanes without a path keep drawing until they hold one with a valid first hit
+        // (sky pixels end at once) or the work is exhausted; one atomic per warp per round
+        while (true) {
+            uint32_t need = __ballot_sync(~0u, !active && !done);
+            if (!need)
+                break;
             int leader = __ffs(need) - 1;
             unsigned long long base = 0;
             if (static_cast<int>(lane) == leader)
@@ -164,7 +168,7 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
         bool finish = false;
         const DevMaterial &m = vert_mat(S, ps.mesh);
         if (A.mode == E8G_MODE_REF_DIRECT) {
-            float3 r = ref_direct<R, COUNT>(S, rng, m, ps.p, ps.n, ps.o, sn, &cnt, rays);
+            float3 r = ref_direct<R, COUNT, LAYOUT>(S, rng, m, ps.p, ps.n, ps.o, sn, &cnt, rays);
             int32_t light = __ldg(&S.mesh_light[ps.mesh]);
             if (light >= 0)
                 r = add(r, light_projected(S, light, ps.o, ps.n));
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
                 float pdf;
                 float3 i;
                 if (A.mode == E8G_MODE_REF_LT1) {
-                    ps.L = add(ps.L, mul(bl, ref_direct<R, COUNT>(S, rng, m, ps.p, ps.n, ps.o, sn, &cnt, rays)));
+                    ps.L = add(ps.L, mul(bl, ref_direct<R, COUNT, LAYOUT>(S, rng, m, ps.p, ps.n, ps.o, sn, &cnt, rays)));
                     i = bsdf_sample_ref(S, m, rng, pdf, ps.n, ps.o);
                     if (pdf == 0.0f)
                         finish = true;
@@ -219,7 +223,7 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
                             float p_b = bsdf_pdf(S, m, ps.n, ps.o, wi);
                             if (COUNT)
                                 rays++;
-                            if (!trace_any<COUNT>(S, ps.p, wi, 1e-4f, dist - 1e-3f, sn, &cnt)) {
+                            if (!trace_any_l<LAYOUT, COUNT>(S, ps.p, wi, 1e-4f, dist - 1e-3f, sn, &cnt)) {
                                 float w = power_heuristic(p_l, p_b);
                                 ps.L = add(ps.L, scale(mul(mul(ps.beta, f), light_rad(S, light)), cos_x * w / p_l));
                             }
@@ -243,7 +247,7 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
                 if (!finish) {
                     if (COUNT)
                         rays++;
-                    Hit h = trace_closest<COUNT>(S, ps.p, i, sn, &cnt);
+                    Hit h = trace_closest_l<LAYOUT, COUNT>(S, ps.p, i, sn, &cnt);
                     if (h.tri == 0xFFFFFFFFu) {
                         finish = true;
                     } else {
@@ -307,24 +311,33 @@ __global__ void __launch_bounds__(kBlock) k_mega(DevScene S, RenderArgs A, First
 
 int megakernel_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mega<RngPhilox, false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mega<RngPhilox, false, 0>, kBlock, 0);
     return n > 0 ? n : 1;
+}
+
+template <int LAYOUT>
+static void launch_layout(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                          unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st) {
+    bool minstd = A.rng == E8G_RNG_MINSTD;
+    if (counters) {
+        if (minstd)
+            k_mega<RngMinstd, true, LAYOUT><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
+        else
+            k_mega<RngPhilox, true, LAYOUT><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
+    } else {
+        if (minstd)
+            k_mega<RngMinstd, false, LAYOUT><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
+        else
+            k_mega<RngPhilox, false, LAYOUT><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
+    }
 }
 
 void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                        unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st) {
-    bool minstd = A.rng == E8G_RNG_MINSTD;
-    if (counters) {
-        if (minstd)
-            k_mega<RngMinstd, true><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
-        else
-            k_mega<RngPhilox, true><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
-    } else {
-        if (minstd)
-            k_mega<RngMinstd, false><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
-        else
-            k_mega<RngPhilox, false><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
-    }
+    if (S.layout == 1)
+        launch_layout<1>(S, A, fh, accum, path_rgb, work, counters, grid, st);
+    else
+        launch_layout<0>(S, A, fh, accum, path_rgb, work, counters, grid, st);
 }
 
 } // namespace e8g

@@ -1,14 +1,25 @@
-// Render orchestration: first hits, integrator dispatch, resolve, timing.
+// Render orchestration: first hits, integrator dispatch (megakernel, wavefront, BDPT), resolve,
+// timing, and the wavefront autotuner.
 #include "api_internal.h"
+#include "wavefront.h"
 
 #include <algorithm>
+#include <chrono>
+#include <cstring>
 
 namespace e8g {
 
 namespace {
 
-e8g_status run_integrator(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb,
+struct WfCounters { // mirrors the device Counters of wavefront.cu
+    unsigned long long next_path;
+    uint32_t shadow_n, ext_n, busy, pad[3];
+};
+
+e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs const &A, float4 *accum, float *path_rgb,
                           unsigned long long *d_counts) {
+    if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_MIS && !d_counts)
+        return run_wavefront(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces);
     cudaError_t e = cudaMemsetAsync(c->b_work.ptr, 0, 64, c->stream);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "work counter");
@@ -25,6 +36,61 @@ e8g_status run_integrator(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
 }
 
 } // namespace
+
+e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
+                         uint32_t bounces) {
+    uint64_t want = std::max<uint64_t>(A.total_paths, 1024);
+    uint32_t Q = static_cast<uint32_t>(std::min<uint64_t>(capacity, (want + 255) / 256 * 256));
+    cudaError_t e = c->b_wf.reserve(wf_total_bytes(Q));
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront slots");
+    WfSlots W = wf_carve(c->b_wf.ptr, Q);
+    e = wf_init(W, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront init");
+    int shade_grid = static_cast<int>(std::min<uint64_t>((Q + 255) / 256, static_cast<uint64_t>(c->num_sms) * 8));
+    int trace_grid = persistent_grid(c, wf_trace_blocks_per_sm());
+    auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
+    // capture `bounces` bounces once, replay until no slot is busy and no path is left
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront capture");
+    for (uint32_t k = 0; k < bounces; k++)
+        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, c->stream);
+    e = cudaStreamEndCapture(c->stream, &graph);
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return cuda_fail(c, e, "wavefront graph");
+    }
+    auto *host = static_cast<WfCounters *>(c->host_pinned);
+    // every path needs at most kHardDepth + 2 bounces; slots refill continuously
+    uint64_t max_replays = ((A.total_paths + Q - 1) / Q + 1) * (kHardDepth + 2) / bounces + 16;
+    uint64_t r = 0;
+    for (; r < max_replays; r++) {
+        e = cudaGraphLaunch(exec, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(host, W.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess)
+            break;
+        c->launches += 4 * bounces;
+        if (host->busy == 0 && host->next_path >= A.total_paths)
+            break;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront run");
+    if (r == max_replays)
+        return fail(c, E8G_ERR_INTERNAL, "wavefront did not drain");
+    return E8G_OK;
+}
 
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts) {
     if (p->mode == E8G_MODE_BDPT_POWER)
@@ -50,7 +116,7 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
         return cuda_fail(c, e, "render clear");
     RenderArgs A = make_args(p);
     cudaEventRecord(c->ev2, c->stream);
-    s = run_integrator(c, A, static_cast<float4 *>(c->b_accum.ptr), nullptr, d_counts);
+    s = run_integrator(c, p, A, static_cast<float4 *>(c->b_accum.ptr), nullptr, d_counts);
     if (s != E8G_OK)
         return s;
     cudaEventRecord(c->ev3, c->stream);
@@ -92,7 +158,12 @@ e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d
     A.list_pixel = d_pixel;
     A.list_sample = d_sample;
     A.total_paths = n;
-    s = run_integrator(c, A, nullptr, d_rgb, nullptr);
+    if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_MIS) {
+        cudaError_t e = cudaMemsetAsync(d_rgb, 0, static_cast<size_t>(n) * 3 * sizeof(float), c->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "path output clear");
+    }
+    s = run_integrator(c, p, A, nullptr, d_rgb, nullptr);
     if (s != E8G_OK)
         return s;
     cudaError_t e = cudaGetLastError();
@@ -102,6 +173,57 @@ e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d
 } // namespace e8g
 
 extern "C" {
+
+e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_tune_result *res) {
+    using namespace e8g;
+    e8g_status s = check_ready(c);
+    if (s != E8G_OK)
+        return s;
+    s = validate_params(c, params);
+    if (s != E8G_OK)
+        return s;
+    if (params->mode != E8G_MODE_MIS)
+        return fail(c, E8G_ERR_INVALID_ARG, "the wavefront integrator runs E8G_MODE_MIS");
+    e8g_render_params p = *params;
+    p.integrator = E8G_INTEGRATOR_WAVEFRONT;
+    p.spp = std::max<uint32_t>(1, std::min<uint32_t>(p.spp, 2));
+    size_t bytes = static_cast<size_t>(p.width) * p.height * 4 * sizeof(float);
+    cudaError_t e = c->b_img.reserve(bytes);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "image buffer");
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
+    const uint32_t bnc[] = {4, 8};
+    e8g_tune_result r{};
+    double best = 1e300;
+    for (uint32_t cap : caps)
+        for (uint32_t b : bnc) {
+            c->wf_capacity = cap;
+            c->wf_bounces = b;
+            double ms = 1e300;
+            for (int rep = 0; rep < 2; rep++) { // first run warms caches and builds nothing twice
+                s = render_image(c, &p, static_cast<float *>(c->b_img.ptr), nullptr);
+                if (s != E8G_OK)
+                    return s;
+                ms = std::min(ms, c->stats.kernel_ms);
+            }
+            if (r.num_candidates < 8) {
+                r.cand_capacity[r.num_candidates] = cap;
+                r.cand_bounces[r.num_candidates] = b;
+                r.cand_ms[r.num_candidates] = ms;
+                r.num_candidates++;
+            }
+            if (ms < best) {
+                best = ms;
+                r.capacity = cap;
+                r.bounces_per_graph = b;
+            }
+        }
+    c->wf_capacity = r.capacity;
+    c->wf_bounces = r.bounces_per_graph;
+    if (res)
+        *res = r;
+    return E8G_OK;
+}
 
 e8g_status e8g_forward(e8g_ctx *c, e8g_render_params const *, float *) {
     return e8g::fail(c, E8G_ERR_UNSUPPORTED, "adjoint not available yet");

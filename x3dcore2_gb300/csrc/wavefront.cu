@@ -1,0 +1,394 @@
+// Wavefront integrator for the product estimator (E8G_MODE_MIS).
+//
+// Path states live in structure-of-arrays slots (capacity Q). One bounce of the whole wavefront
+// is three kernels:
+//   k_wf_shade   every slot: finish the pending extension hit (emission with MIS weight, or
+//                termination), refill empty slots with new paths (warp-aggregated fetch), then
+//                shade the vertex: Russian roulette, one light sample whose shadow ray goes to
+//                the shadow queue, one BSDF sample whose ray goes to the extension queue;
+//   k_wf_shadow  drains the shadow queue: any-hit, adds unoccluded contributions to the image;
+//   k_wf_extend  drains the extension queue: closest hit into the slot.
+// Queue kernels are persistent (grid = SMs x resident blocks, grid-stride over the device-side
+// queue length). The bounce loop is captured once as a CUDA graph of `k` bounces and replayed
+// until no slot is busy. Per path, draws happen in the same order as in the megakernel, so
+// both integrators produce the same per-path radiance.
+#include "../../include/e8g.h"
+#include "wavefront.h"
+
+namespace e8g {
+
+namespace {
+
+enum : uint32_t { kEmpty = 0, kAtVertex = 1, kWaitHit = 2 };
+
+struct Counters {
+    unsigned long long next_path; // global path counter
+    uint32_t shadow_n, ext_n;      // queue lengths of the current bounce
+    uint32_t busy;                 // slots holding a path after the last shade
+    uint32_t pad[3];
+};
+
+__device__ __forceinline__ void emit_to(RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t out, float3 c) {
+    if (path_rgb) {
+        atomicAdd(&path_rgb[3 * static_cast<size_t>(out)], c.x);
+        atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 1], c.y);
+        atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 2], c.z);
+    } else {
+        atomicAdd(&accum[out], make_float4(c.x, c.y, c.z, 0.0f));
+    }
+}
+
+// Warp-aggregated append: one atomic per warp for all lanes with `want`.
+__device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
+    uint32_t mask = __ballot_sync(__activemask(), want);
+    if (!want)
+        return 0;
+    uint32_t lane = lane_id();
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (static_cast<int>(lane) == leader)
+        base = atomicAdd(counter, static_cast<uint32_t>(__popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+template <class R> struct RngSlot;
+template <> struct RngSlot<RngMinstd> {
+    __device__ static RngMinstd load(RenderArgs const &, uint32_t, uint32_t, uint32_t word) {
+        RngMinstd r;
+        r.x = word;
+        return r;
+    }
+    __device__ static uint32_t store(RngMinstd const &r) { return r.x; }
+    __device__ static RngMinstd fresh(RenderArgs const &, uint64_t mix, uint32_t px, uint32_t s) {
+        RngMinstd r;
+        r.seed(path_seed(mix, px, s));
+        return r;
+    }
+};
+template <> struct RngSlot<RngPhilox> {
+    // the slot keeps the number of draws taken; the 4-word block is regenerated on resume
+    __device__ static RngPhilox load(RenderArgs const &A, uint32_t px, uint32_t s, uint32_t drawn) {
+        RngPhilox r;
+        r.seed(A.seed, px, s);
+        r.block = drawn >> 2;
+        uint32_t skip = drawn & 3u;
+        if (skip) {
+            r.refill();
+            for (uint32_t k = 0; k < skip; k++) {
+                r.buf[0] = r.buf[1];
+                r.buf[1] = r.buf[2];
+                r.buf[2] = r.buf[3];
+            }
+            r.lane = skip;
+        }
+        return r;
+    }
+    __device__ static uint32_t store(RngPhilox const &r) { return r.lane == 4 ? r.block * 4 : (r.block - 1) * 4 + r.lane; }
+    __device__ static RngPhilox fresh(RenderArgs const &A, uint64_t, uint32_t px, uint32_t s) {
+        RngPhilox r;
+        r.seed(A.seed, px, s);
+        return r;
+    }
+};
+
+__device__ __forceinline__ bool wf_coords(RenderArgs const &A, uint64_t idx, uint32_t &pixel, uint32_t &sample,
+                                          uint32_t &out) {
+    if (A.list_pixel) {
+        pixel = A.list_pixel[idx];
+        sample = A.list_sample[idx];
+        out = static_cast<uint32_t>(idx);
+        return true;
+    }
+    uint32_t s = static_cast<uint32_t>(idx / A.paths_per_sample);
+    uint32_t j = static_cast<uint32_t>(idx - static_cast<uint64_t>(s) * A.paths_per_sample);
+    uint32_t tile = j >> 5, w = j & 31u;
+    uint32_t x = (tile % A.tiles_x) * 8 + (w & 7u), y = (tile / A.tiles_x) * 4 + (w >> 3);
+    if (x >= A.width || y >= A.height)
+        return false;
+    pixel = y * A.width + x;
+    sample = A.sample_offset + s;
+    out = pixel;
+    return true;
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh, WfSlots W,
+                                                  Counters *cnt, float4 *accum, float *path_rgb) {
+    const uint64_t mix = splitmix64(A.seed);
+    uint32_t busy_local = 0;
+    for (uint32_t s0 = blockIdx.x * blockDim.x; s0 < W.capacity; s0 += gridDim.x * blockDim.x) {
+        uint32_t s = s0 + threadIdx.x;
+        bool in = s < W.capacity;
+        uint32_t state = in ? W.state[s] : kEmpty;
+        uint32_t pixel = 0, sample = 0, out = 0;
+        float3 beta = f3(0, 0, 0), p = f3(0, 0, 0), n = f3(0, 0, 0), o = f3(0, 0, 0);
+        int32_t mesh = 0;
+        uint32_t depth = 0;
+        float last_pdf = 0.0f;
+        R rng;
+        if (state != kEmpty) {
+            pixel = W.pixel[s];
+            sample = W.sample[s];
+            out = W.out[s];
+            float4 b = W.beta_pdf[s];
+            beta = xyz(b);
+            last_pdf = b.w;
+            float4 pm = W.p_mesh[s];
+            p = xyz(pm);
+            mesh = __float_as_int(pm.w);
+            float4 nd = W.n_depth[s];
+            n = xyz(nd);
+            depth = __float_as_uint(nd.w);
+            o = xyz(W.o[s]);
+            rng = RngSlot<R>::load(A, pixel, sample, W.rng[s]);
+        }
+        if (state == kWaitHit) { // complete the extension ray shot last bounce
+            float4 hv = W.hit[s];
+            Hit h;
+            h.t = hv.x;
+            h.tri = __float_as_uint(hv.y);
+            h.b1 = hv.z;
+            h.b2 = hv.w;
+            float3 i = neg(o);
+            state = kEmpty;
+            if (h.tri != 0xFFFFFFFFu) {
+                Vert nv = make_vert(S, h);
+                if (dot(nv.n, neg(i)) > 0.0f) {
+                    int32_t hl = __ldg(&S.mesh_light[nv.mesh]);
+                    if (hl >= 0) {
+                        float cos_l2 = dot(nv.n, neg(i));
+                        float pl = __ldg(&S.light_pnorm[hl]) / S.total_power;
+                        float inv_area = 1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]);
+                        float p_l = pl * inv_area * (nv.t * nv.t) / cos_l2;
+                        float w = power_heuristic(last_pdf, p_l);
+                        emit_to(A, accum, path_rgb, out, scale(mul(beta, light_rad(S, hl)), w));
+                    }
+                    p = nv.p;
+                    n = nv.n;
+                    mesh = nv.mesh;
+                    depth++;
+                    state = kAtVertex;
+                }
+            }
+        }
+        // refill empty slots, one atomic per warp
+        bool want = in && state == kEmpty;
+        uint32_t mask = __ballot_sync(~0u, want);
+        if (mask) {
+            int leader = __ffs(mask) - 1;
+            unsigned long long base = 0;
+            if (static_cast<int>(lane_id()) == leader)
+                base = atomicAdd(&cnt->next_path, static_cast<unsigned long long>(__popc(mask)));
+            base = __shfl_sync(~0u, base, leader);
+            if (want) {
+                uint64_t idx = base + __popc(mask & ((1u << lane_id()) - 1u));
+                if (idx < A.total_paths && wf_coords(A, idx, pixel, sample, out)) {
+                    FirstHit f = fh[pixel];
+                    int32_t m = __float_as_int(f.p.w);
+                    if (m >= 0) {
+                        p = xyz(f.p);
+                        n = xyz(f.n);
+                        o = neg(xyz(f.d));
+                        mesh = m;
+                        depth = 0;
+                        beta = f3(1.0f, 1.0f, 1.0f);
+                        rng = RngSlot<R>::fresh(A, mix, pixel, sample);
+                        int32_t light = __float_as_int(f.n.w);
+                        if (light >= 0)
+                            emit_to(A, accum, path_rgb, out, light_radiance(S, light, o, n));
+                        state = kAtVertex;
+                    }
+                }
+            }
+        }
+        // shade the vertex
+        bool push_shadow = false, push_ext = false;
+        float3 sh_dir = f3(0, 0, 0), sh_c = f3(0, 0, 0);
+        float sh_tmax = 0.0f;
+        if (state == kAtVertex) {
+            state = kEmpty;
+            bool go = !((A.max_depth && depth >= A.max_depth) || depth >= kHardDepth);
+            if (go && depth >= A.rr_start) {
+                if (rng.next() >= A.rr_prob)
+                    go = false;
+                else
+                    beta = divs(beta, A.rr_prob);
+            }
+            if (go) {
+                const DevMaterial &m = vert_mat(S, mesh);
+                float pmf;
+                int light = sample_light(S, rng, pmf);
+                Surf ls = mesh_sample(S, __ldg(&S.light_mesh[light]), rng, true);
+                float3 l = sub(p, ls.p);
+                float r2 = dot(l, l);
+                float dist = sqrtf(r2);
+                float3 ln = divs(l, dist);
+                float cos_l = dot(ls.n, ln);
+                float3 wi = neg(ln);
+                float cos_x = dot(n, wi);
+                if (cos_l > 0.0f && cos_x > 0.0f) {
+                    float3 f = bsdf_eval(S, m, n, o, wi);
+                    if (!vequals0(f)) {
+                        float p_l = pmf * ls.area_dens * r2 / cos_l;
+                        float p_b = bsdf_pdf(S, m, n, o, wi);
+                        float w = power_heuristic(p_l, p_b);
+                        sh_c = scale(mul(mul(beta, f), light_rad(S, light)), cos_x * w / p_l);
+                        sh_dir = wi;
+                        sh_tmax = dist - 1e-3f;
+                        push_shadow = true;
+                    }
+                }
+                float pdf;
+                float3 i = bsdf_sample_mis(S, m, rng, pdf, n, o);
+                if (pdf > 0.0f) {
+                    float cw = dot(n, i);
+                    if (cw > 0.0f) {
+                        float3 f = bsdf_eval(S, m, n, o, i);
+                        beta = mul(beta, scale(f, cw / pdf));
+                        o = neg(i);
+                        last_pdf = pdf;
+                        push_ext = true;
+                        state = kWaitHit;
+                    }
+                }
+            }
+        }
+        uint32_t sq = warp_append(&cnt->shadow_n, push_shadow);
+        if (push_shadow) {
+            W.sh_o[sq] = make_float4(p.x, p.y, p.z, __uint_as_float(out));
+            W.sh_d[sq] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, sh_tmax);
+            W.sh_c[sq] = make_float4(sh_c.x, sh_c.y, sh_c.z, 0.0f);
+        }
+        uint32_t eq = warp_append(&cnt->ext_n, push_ext);
+        if (push_ext)
+            W.ext_slot[eq] = s;
+        if (in) {
+            W.state[s] = state;
+            if (state != kEmpty) {
+                W.pixel[s] = pixel;
+                W.sample[s] = sample;
+                W.out[s] = out;
+                W.beta_pdf[s] = make_float4(beta.x, beta.y, beta.z, last_pdf);
+                W.p_mesh[s] = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
+                W.n_depth[s] = make_float4(n.x, n.y, n.z, __uint_as_float(depth));
+                W.o[s] = make_float4(o.x, o.y, o.z, 0.0f);
+                W.rng[s] = RngSlot<R>::store(rng);
+                busy_local++;
+            }
+        }
+    }
+    // busy count for the host's termination test
+    for (int off = 16; off > 0; off >>= 1)
+        busy_local += __shfl_down_sync(~0u, busy_local, off);
+    if (lane_id() == 0 && busy_local)
+        atomicAdd(&cnt->busy, busy_local);
+}
+
+__global__ void __launch_bounds__(kBlock) k_wf_shadow(DevScene S, RenderArgs A, WfSlots W, Counters const *cnt,
+                                                      float4 *accum, float *path_rgb) {
+    __shared__ uint32_t stk[kStackWords * kBlock];
+    uint32_t n = cnt->shadow_n;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float4 so = W.sh_o[q], sd = W.sh_d[q];
+        if (!trace_any<false>(S, xyz(so), xyz(sd), 1e-4f, sd.w, stk + threadIdx.x, nullptr))
+            emit_to(A, accum, path_rgb, __float_as_uint(so.w), xyz(W.sh_c[q]));
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Counters const *cnt) {
+    __shared__ uint32_t stk[kStackWords * kBlock];
+    uint32_t n = cnt->ext_n;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        uint32_t s = W.ext_slot[q];
+        float3 p = xyz(W.p_mesh[s]);
+        float3 d = neg(xyz(W.o[s]));
+        Hit h = trace_closest<false>(S, p, d, stk + threadIdx.x, nullptr);
+        W.hit[s] = make_float4(h.t, __uint_as_float(h.tri), h.b1, h.b2);
+    }
+}
+
+__global__ void k_wf_reset(Counters *cnt) {
+    cnt->shadow_n = 0;
+    cnt->ext_n = 0;
+    cnt->busy = 0;
+}
+
+} // namespace
+
+size_t wf_bytes_per_slot() {
+    // state, pixel, sample, out, rng (5 x 4) + beta_pdf, p_mesh, n_depth, o, hit (5 x 16)
+    // + shadow queue entry (3 x 16) + extension queue entry (4)
+    return 20 + 80 + 48 + 4;
+}
+
+WfSlots wf_carve(void *base, uint32_t capacity) {
+    WfSlots W{};
+    W.capacity = capacity;
+    char *p = static_cast<char *>(base);
+    auto take = [&](size_t bytes) {
+        char *r = p;
+        p += (bytes + 255) & ~static_cast<size_t>(255);
+        return r;
+    };
+    size_t Q = capacity;
+    W.state = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.pixel = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.sample = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.out = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.rng = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.beta_pdf = reinterpret_cast<float4 *>(take(Q * 16));
+    W.p_mesh = reinterpret_cast<float4 *>(take(Q * 16));
+    W.n_depth = reinterpret_cast<float4 *>(take(Q * 16));
+    W.o = reinterpret_cast<float4 *>(take(Q * 16));
+    W.hit = reinterpret_cast<float4 *>(take(Q * 16));
+    W.sh_o = reinterpret_cast<float4 *>(take(Q * 16));
+    W.sh_d = reinterpret_cast<float4 *>(take(Q * 16));
+    W.sh_c = reinterpret_cast<float4 *>(take(Q * 16));
+    W.ext_slot = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.counters = take(sizeof(Counters));
+    return W;
+}
+
+size_t wf_total_bytes(uint32_t capacity) {
+    size_t Q = capacity, total = 0;
+    size_t sizes[] = {Q * 4, Q * 4, Q * 4, Q * 4, Q * 4, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 4,
+                      sizeof(Counters)};
+    for (size_t s : sizes)
+        total += (s + 255) & ~static_cast<size_t>(255);
+    return total;
+}
+
+int wf_trace_blocks_per_sm() {
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
+    int n = a < b ? a : b;
+    return n > 0 ? n : 1;
+}
+
+// One bounce: reset queue lengths, shade, shadow, extend.
+void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
+                       float *path_rgb, int shade_grid, int trace_grid, cudaStream_t st) {
+    auto *cnt = reinterpret_cast<Counters *>(W.counters);
+    k_wf_reset<<<1, 1, 0, st>>>(cnt);
+    if (A.rng == E8G_RNG_MINSTD)
+        k_wf_shade<RngMinstd><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
+    else
+        k_wf_shade<RngPhilox><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
+    k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
+    k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);
+}
+
+cudaError_t wf_init(WfSlots const &W, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(W.state, 0, static_cast<size_t>(W.capacity) * 4, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(W.counters, 0, sizeof(Counters), st);
+    return e;
+}
+
+// Busy slots after the last bounce (read back by the host between graph replays).
+uint32_t *wf_busy_ptr(WfSlots const &W) { return &reinterpret_cast<Counters *>(W.counters)->busy; }
+unsigned long long *wf_next_ptr(WfSlots const &W) { return &reinterpret_cast<Counters *>(W.counters)->next_path; }
+
+} // namespace e8g

@@ -1,0 +1,26 @@
+// Wavefront integrator: slot arrays, queues and the per-bounce kernels (wavefront.cu).
+#pragma once
+
+#include "device.cuh"
+
+namespace e8g {
+
+struct WfSlots {
+    uint32_t capacity;
+    uint32_t *state, *pixel, *sample, *out, *rng;
+    float4 *beta_pdf, *p_mesh, *n_depth, *o, *hit;
+    float4 *sh_o, *sh_d, *sh_c; // shadow queue: origin | out, direction | tmax, contribution
+    uint32_t *ext_slot;         // extension queue: slot indices
+    void *counters;
+};
+
+size_t wf_total_bytes(uint32_t capacity);
+WfSlots wf_carve(void *base, uint32_t capacity);
+cudaError_t wf_init(WfSlots const &W, cudaStream_t st);
+int wf_trace_blocks_per_sm();
+void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
+                       float *path_rgb, int shade_grid, int trace_grid, cudaStream_t st);
+uint32_t *wf_busy_ptr(WfSlots const &W);
+unsigned long long *wf_next_ptr(WfSlots const &W);
+
+} // namespace e8g
