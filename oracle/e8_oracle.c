@@ -1765,19 +1765,251 @@ void o_render(const o_scene *s, uint32_t mode, uint32_t rng_kind, uint64_t seed,
 }
 
 /* ------------------------------------------------- FP64 adjoint reference -- */
+/* Double-precision restatement of the product estimator (mis_path above) and of the path-replay
+ * gradient the GPU computes: same draws and discrete decisions (light, triangle, Russian
+ * roulette, hits), contributions and derivatives carried in double. Not in the reference: it is
+ * the checker of the GPU adjoint. */
+
+typedef struct dv3 {
+    double x, y, z;
+} dv3;
+static inline dv3 D3(double x, double y, double z) {
+    dv3 r = {x, y, z};
+    return r;
+}
+static inline dv3 dfrom(v3 a) { return D3(a.x, a.y, a.z); }
+static inline v3 dto(dv3 a) { return V((float)a.x, (float)a.y, (float)a.z); }
+static inline dv3 dadd(dv3 a, dv3 b) { return D3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline dv3 dsub(dv3 a, dv3 b) { return D3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline dv3 dmul(dv3 a, dv3 b) { return D3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline dv3 dscale(dv3 a, double k) { return D3(a.x * k, a.y * k, a.z * k); }
+static inline double ddot(dv3 a, dv3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline dv3 dcross(dv3 a, dv3 b) { return D3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static inline dv3 dnorm(dv3 a) { return dscale(a, 1.0 / sqrt(ddot(a, a))); }
+
+static void dbasis(dv3 n, dv3 *u, dv3 *v) {
+    dv3 ref = fabs(n.x) > .1 ? D3(0, 1, 0) : D3(1, 1, 1);
+    *u = dnorm(dcross(ref, n));
+    *v = dcross(n, *u);
+}
+
+static double d_ggx(double a2, dv3 n, dv3 h) {
+    double c = ddot(n, h), c2 = c * c, t2 = (1 - c2) / c2, k = 1 + t2 / a2;
+    return 1.0 / (M_PI * a2 * c2 * c2 * k * k);
+}
+static double d_lambda(double a2, dv3 n, dv3 w) {
+    double c = ddot(n, w), c2 = c * c, t2 = (1 - c2) / c2;
+    return (-1 + sqrt(1 + a2 * t2)) / 2;
+}
+
+/* f (per channel) of a leaf material; *g receives d ln f / d r for cook_torr */
+static dv3 d_eval_leaf(const omat *m, dv3 n, dv3 o, dv3 i, double *dlog_dr) {
+    *dlog_dr = 0;
+    dv3 alb = dfrom(m->albedo);
+    if (m->type == E8G_MAT_OREN_NAYAR) {
+        double ci = ddot(i, n), co = ddot(o, n);
+        ci = ci < 0 ? 0 : (ci > 1 ? 1 : ci);
+        co = co < 0 ? 0 : (co > 1 ? 1 : co);
+        if (ci <= 1e-5 || co <= 1e-5)
+            return D3(0, 0, 0);
+        double ca = ci < co ? ci : co, cb = ci < co ? co : ci;
+        double sa = sqrt(1 - ca * ca), sb = sqrt(1 - cb * cb);
+        double cio = ca * cb + sa * sb;
+        return dscale(alb, (m->a + m->b * (cio > 0 ? cio : 0) * sa * (sb / co)) / M_PI);
+    }
+    if (m->type == E8G_MAT_COOK_TORR) {
+        double co = ddot(n, o), ci = ddot(n, i);
+        if (ci <= 1e-5 || co <= 1e-5)
+            return D3(0, 0, 0);
+        dv3 h = dadd(i, o);
+        if (fabs(h.x) <= 1e-5 && fabs(h.y) <= 1e-5 && fabs(h.z) <= 1e-5)
+            return D3(0, 0, 0);
+        h = dnorm(h);
+        double a2 = (double)m->alpha2;
+        double fl = 1 - ddot(i, h), f5 = fl * fl * fl * fl * fl;
+        double re = m->ior_re, im = m->ior_im;
+        double F = ((re - 1) * (re - 1) + 4 * re * f5 + im * im) / ((re + 1) * (re + 1) + im * im);
+        double D = d_ggx(a2, n, h);
+        double li = d_lambda(a2, n, i), lo = d_lambda(a2, n, o);
+        double G = 1 / (1 + li + lo);
+        double c = ddot(n, h), c2 = c * c, t2 = (1 - c2) / c2, k = 1 + t2 / a2;
+        double dlnD = -1 / a2 + 2 * t2 / (a2 * a2 * k);
+        double ti = (1 - ci * ci) / (ci * ci), to = (1 - co * co) / (co * co);
+        double dli = ti / (4 * sqrt(1 + a2 * ti)), dlo = to / (4 * sqrt(1 + a2 * to));
+        double dlnG = -(dli + dlo) / (1 + li + lo);
+        double r = sqrt(a2 / 2);
+        *dlog_dr = (dlnD + dlnG) * 4 * r;
+        return dscale(alb, F * D * G / (4 * ci * co));
+    }
+    return dscale(alb, 1.0 / M_PI);
+}
+
+static double d_pdf_leaf(const omat *m, dv3 n, dv3 o, dv3 i) {
+    if (m->type == E8G_MAT_COOK_TORR) {
+        if (ddot(i, n) < 0)
+            return 0;
+        dv3 h = dnorm(dadd(i, o));
+        double hdo = ddot(h, o), ch = ddot(n, h);
+        if (hdo <= 0 || ch <= 0)
+            return 0;
+        return d_ggx((double)m->alpha2, n, h) * ch / (4 * hdo);
+    }
+    double c = ddot(i, n);
+    return c > 0 ? c / M_PI : 0;
+}
+
+static void d_grad(const o_scene *s, int32_t mesh, dv3 C, double dlr, const float w[3], double *da, double *dr) {
+    int32_t mi = s->mesh_mat[mesh];
+    if (mi < 0 || (uint32_t)mi >= s->nmat)
+        return;
+    const omat *m = &s->mats[mi];
+    if (m->type != E8G_MAT_OREN_NAYAR && m->type != E8G_MAT_COOK_TORR)
+        return;
+    double c[3] = {C.x, C.y, C.z};
+    double alb[3] = {m->albedo.x, m->albedo.y, m->albedo.z};
+    for (int k = 0; k < 3; k++)
+        if (alb[k] > 0)
+            da[3 * mi + k] += w[k] * c[k] / alb[k];
+    if (m->type == E8G_MAT_COOK_TORR)
+        dr[mi] += (w[0] * c[0] + w[1] * c[1] + w[2] * c[2]) * dlr;
+}
+
+static dv3 d_replay(const o_scene *s, uint64_t seed, const o_policy *pol, const ofirst *f, uint32_t pixel,
+                    uint32_t sample, int grad, dv3 Ltot, const float w[3], double *da, double *dr) {
+    orng rng;
+    philox_seed(&rng, seed, pixel, sample);
+    dv3 L = D3(0, 0, 0);
+    if (f->light >= 0) {
+        v3 le = light_radiance(s, f->light, vneg(f->ray.v), f->hit.normal);
+        L = dfrom(le);
+    }
+    dv3 beta = D3(1, 1, 1);
+    dv3 p = dfrom(f->hit.vertex), n = dfrom(f->hit.normal), o = dscale(dfrom(f->ray.v), -1);
+    int32_t mesh = f->hit.mesh;
+    for (unsigned depth = 0;; depth++) {
+        if (pol->max_depth && depth >= pol->max_depth)
+            break;
+        if (depth >= pol->rr_start) {
+            if (draw(&rng) >= pol->rr_prob)
+                break;
+            beta = dscale(beta, 1.0 / pol->rr_prob);
+        }
+        const omat *m = find_mat(s, s->mesh_mat[mesh]);
+        /* light sample (float draws, double geometry) */
+        float pmf;
+        int light = sample_light(s, &rng, &pmf);
+        uint32_t lm = s->lights[light].mesh;
+        uint32_t ntris = s->toff[lm + 1] - s->toff[lm];
+        float q = draw(&rng);
+        float e = q * s->mesh_area[lm];
+        unsigned lo = 0, hi = ntris;
+        const float *cum = s->tri_cum + s->toff[lm];
+        while (lo < hi) {
+            unsigned mi = (lo + hi) >> 1;
+            if (cum[mi] <= e)
+                lo = mi + 1;
+            else
+                hi = mi;
+        }
+        if (lo >= ntris)
+            lo = ntris - 1;
+        uint32_t t = s->toff[lm] + lo;
+        double u = draw(&rng), vv = draw(&rng);
+        double r = sqrt(u), b0 = 1 - r, b1 = r * vv, b2 = 1 - b0 - b1;
+        uint32_t i0 = s->tri[3 * t], i1 = s->tri[3 * t + 1], i2 = s->tri[3 * t + 2];
+        dv3 lp = dadd(dadd(dscale(dfrom(s->pos[i0]), b0), dscale(dfrom(s->pos[i1]), b1)), dscale(dfrom(s->pos[i2]), b2));
+        dv3 lnrm = dnorm(dadd(dadd(dscale(dfrom(s->nrm[i0]), b0), dscale(dfrom(s->nrm[i1]), b1)), dscale(dfrom(s->nrm[i2]), b2)));
+        dv3 l = dsub(p, lp);
+        double r2 = ddot(l, l), dist = sqrt(r2);
+        dv3 ln = dscale(l, 1 / dist);
+        double cos_l = ddot(lnrm, ln);
+        dv3 wi = dscale(ln, -1);
+        double cos_x = ddot(n, wi);
+        if (cos_l > 0 && cos_x > 0) {
+            double dlr;
+            dv3 fv = d_eval_leaf(m, n, o, wi, &dlr);
+            if (!(fabs(fv.x) <= 1e-5 && fabs(fv.y) <= 1e-5 && fabs(fv.z) <= 1e-5)) {
+                double p_l = pmf * (1.0 / s->mesh_area[lm]) * r2 / cos_l;
+                double p_b = d_pdf_leaf(m, n, o, wi);
+                oray sr = mkray(dto(p), dto(wi));
+                if (!has_intersect(s, &sr, 1e-4f, (float)dist - 1e-3f)) {
+                    double wgt = p_l * p_l / (p_l * p_l + p_b * p_b);
+                    dv3 c = dscale(dmul(dmul(beta, fv), dfrom(light_rad(s, light))), cos_x * wgt / p_l);
+                    L = dadd(L, c);
+                    if (grad)
+                        d_grad(s, mesh, c, dlr, w, da, dr);
+                }
+            }
+        }
+        /* BSDF sample (draw order of sample_leaf) */
+        dv3 i;
+        double pdf;
+        if (m->type == E8G_MAT_COOK_TORR) {
+            dv3 uu, vb;
+            dbasis(n, &uu, &vb);
+            double theta = 2.0 * M_PI * draw(&rng);
+            double tt = draw(&rng);
+            double phi = atan(sqrt((double)m->alpha2 * tt / (1 - tt)));
+            dv3 h = dadd(dadd(dscale(uu, sin(phi) * cos(theta)), dscale(vb, sin(phi) * sin(theta))), dscale(n, cos(phi)));
+            double hdo = ddot(h, o);
+            i = dsub(dscale(h, 2 * hdo), o);
+            if (ddot(i, n) < 0)
+                break;
+            pdf = d_ggx((double)m->alpha2, n, h) * cos(phi) / (4 * hdo);
+        } else if (m->type == E8G_MAT_MIXTURE) {
+            break; /* mixtures are not part of the gradient check scenes */
+        } else {
+            double e1 = draw(&rng), e0 = draw(&rng);
+            dv3 uu, vb;
+            dbasis(n, &uu, &vb);
+            double z = sqrt(e1), rr = sqrt(1 - z * z), ph = e0 * 2 * M_PI;
+            i = dadd(dadd(dscale(uu, rr * cos(ph)), dscale(vb, rr * sin(ph))), dscale(n, z));
+            pdf = ddot(i, n) / M_PI;
+        }
+        if (!(pdf > 0))
+            break;
+        double cw = ddot(n, i);
+        if (cw <= 0)
+            break;
+        double dlr;
+        dv3 fv = d_eval_leaf(m, n, o, i, &dlr);
+        if (grad)
+            d_grad(s, mesh, dsub(Ltot, L), dlr, w, da, dr);
+        beta = dmul(beta, dscale(fv, cw / pdf));
+        oray rr_ = mkray(dto(p), dto(i));
+        overt nv = intersect(s, &rr_);
+        if (!nv.valid)
+            break;
+        dv3 nn = dfrom(nv.normal);
+        if (ddot(nn, dscale(i, -1)) <= 0)
+            break;
+        int hl = vert_light(s, &nv);
+        if (hl >= 0) {
+            double cos_l2 = ddot(nn, dscale(i, -1));
+            double pl = (double)s->light_pnorm[hl] / s->total_power;
+            double t2 = (double)nv.t * nv.t;
+            double p_l = pl * (1.0 / s->mesh_area[s->lights[hl].mesh]) * t2 / cos_l2;
+            double wgt = pdf * pdf / (pdf * pdf + p_l * p_l);
+            L = dadd(L, dscale(dmul(beta, dfrom(light_rad(s, hl))), wgt));
+        }
+        p = dfrom(nv.vertex);
+        n = nn;
+        mesh = nv.mesh;
+        o = dscale(i, -1);
+    }
+    return L;
+}
 
 void o_path_gradient_f64(const o_scene *s, uint64_t seed, const o_policy *pol, uint32_t width,
                          uint32_t height, uint32_t pixel, uint32_t sample, const float w[3],
                          double *d_albedo, double *d_roughness, double rgb_out[3]) {
-    (void)s;
-    (void)seed;
-    (void)pol;
-    (void)width;
-    (void)height;
-    (void)pixel;
-    (void)sample;
-    (void)w;
-    (void)d_albedo;
-    (void)d_roughness;
+    ofirst f = first_hit(s, pixel % width, pixel / width, width, height);
     rgb_out[0] = rgb_out[1] = rgb_out[2] = 0.0;
+    if (!f.hit.valid)
+        return;
+    dv3 Ltot = d_replay(s, seed, pol, &f, pixel, sample, 0, D3(0, 0, 0), w, d_albedo, d_roughness);
+    d_replay(s, seed, pol, &f, pixel, sample, 1, Ltot, w, d_albedo, d_roughness);
+    rgb_out[0] = Ltot.x;
+    rgb_out[1] = Ltot.y;
+    rgb_out[2] = Ltot.z;
 }

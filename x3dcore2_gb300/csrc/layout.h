@@ -13,7 +13,8 @@ struct DevMaterial {
     float ior_re, ior_im;
     int32_t mix0, mix1;
     float ratio;
-    uint32_t pad[4];
+    float rough; // the roughness parameter r itself (gradients are taken with respect to it)
+    uint32_t pad[3];
 };
 static_assert(sizeof(DevMaterial) == 64, "DevMaterial is one 64-byte line");
 

@@ -1,6 +1,7 @@
 // Render orchestration: first hits, integrator dispatch (megakernel, wavefront, BDPT), resolve,
 // timing, and the wavefront autotuner.
 #include "api_internal.h"
+#include "adjoint.h"
 #include "wavefront.h"
 
 #include <algorithm>
@@ -225,14 +226,107 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     return E8G_OK;
 }
 
-e8g_status e8g_forward(e8g_ctx *c, e8g_render_params const *, float *) {
-    return e8g::fail(c, E8G_ERR_UNSUPPORTED, "adjoint not available yet");
+e8g_status e8g_forward(e8g_ctx *c, e8g_render_params const *p, float *rgba_out) {
+    using namespace e8g;
+    e8g_status s = check_ready(c);
+    if (s != E8G_OK)
+        return s;
+    s = validate_params(c, p);
+    if (s != E8G_OK)
+        return s;
+    if (p->mode != E8G_MODE_MIS || p->rng != E8G_RNG_PHILOX)
+        return fail(c, E8G_ERR_INVALID_ARG, "the adjoint replays E8G_MODE_MIS paths from Philox streams");
+    c->have_forward = false;
+    s = e8g_render(c, p, rgba_out);
+    if (s != E8G_OK)
+        return s;
+    c->fwd_params = *p;
+    c->have_forward = true;
+    return E8G_OK;
 }
-e8g_status e8g_backward(e8g_ctx *c, float const *, float *, float *) {
-    return e8g::fail(c, E8G_ERR_UNSUPPORTED, "adjoint not available yet");
+
+e8g_status e8g_backward(e8g_ctx *c, float const *dl_dimage, float *d_albedo, float *d_roughness) {
+    using namespace e8g;
+    e8g_status s = check_ready(c);
+    if (s != E8G_OK)
+        return s;
+    if (!c->have_forward)
+        return fail(c, E8G_ERR_INVALID_ARG, "e8g_backward needs a preceding e8g_forward");
+    if (!dl_dimage || !d_albedo || !d_roughness)
+        return fail(c, E8G_ERR_INVALID_ARG, "NULL buffers");
+    e8g_render_params const &p = c->fwd_params;
+    cudaSetDevice(c->device);
+    size_t npix = static_cast<size_t>(p.width) * p.height, nm = c->pack.nmat;
+    size_t gb = npix * 3 * sizeof(float), ab = nm * 3 * sizeof(float), rb = nm * sizeof(float);
+    cudaError_t e = c->b_io0.reserve(gb);
+    if (e == cudaSuccess)
+        e = c->b_grad.reserve(ab + rb + 16);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "adjoint buffers");
+    float *d_dl = static_cast<float *>(c->b_io0.ptr);
+    float *d_a = static_cast<float *>(c->b_grad.ptr), *d_r = d_a + nm * 3;
+    cudaEventRecord(c->ev0, c->stream);
+    e = cudaMemcpyAsync(d_dl, dl_dimage, gb, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(d_a, 0, ab + rb, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(c->b_work.ptr, 0, 64, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "adjoint upload");
+    s = first_hits(c, p.width, p.height);
+    if (s != E8G_OK)
+        return s;
+    RenderArgs A = make_args(&p);
+    cudaEventRecord(c->ev2, c->stream);
+    e = launch_adjoint(c->dev, A, static_cast<FirstHit const *>(c->b_fh.ptr), d_dl,
+                       p.spp ? 1.0f / static_cast<float>(p.spp) : 0.0f, static_cast<unsigned long long *>(c->b_work.ptr),
+                       d_a, d_r, nullptr, c->num_sms, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "adjoint launch");
+    cudaEventRecord(c->ev3, c->stream);
+    e = cudaMemcpyAsync(d_albedo, d_a, ab, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_roughness, d_r, rb, cudaMemcpyDeviceToHost, c->stream);
+    cudaEventRecord(c->ev1, c->stream);
+    if (e == cudaSuccess)
+        e = cudaEventSynchronize(c->ev1);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "adjoint");
+    float ms = 0, kms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    cudaEventElapsedTime(&kms, c->ev2, c->ev3);
+    c->stats.ms = ms;
+    c->stats.kernel_ms = kms;
+    c->stats.paths = npix * p.spp;
+    c->stats.launches = 2;
+    return E8G_OK;
 }
-e8g_status e8g_set_materials(e8g_ctx *c, e8g_material const *, uint32_t) {
-    return e8g::fail(c, E8G_ERR_UNSUPPORTED, "not available yet");
+
+e8g_status e8g_set_materials(e8g_ctx *c, e8g_material const *m, uint32_t n) {
+    using namespace e8g;
+    if (!c || !m)
+        return E8G_ERR_INVALID_ARG;
+    if (!c->uploaded)
+        return fail(c, E8G_ERR_NO_SCENE, "no scene uploaded");
+    if (n != c->pack.nmat)
+        return fail(c, E8G_ERR_INVALID_ARG, "material count differs from the uploaded scene");
+    for (uint32_t i = 0; i < n; i++) {
+        if (m[i].type > E8G_MAT_MIXTURE)
+            return fail(c, E8G_ERR_INVALID_ARG, "unknown material type");
+        if (m[i].type == E8G_MAT_MIXTURE &&
+            (m[i].mix0 < 0 || m[i].mix1 < 0 || static_cast<uint32_t>(m[i].mix0) >= n ||
+             static_cast<uint32_t>(m[i].mix1) >= n || m[m[i].mix0].type == E8G_MAT_MIXTURE ||
+             m[m[i].mix1].type == E8G_MAT_MIXTURE))
+            return fail(c, E8G_ERR_INVALID_ARG, "bad mixture components");
+    }
+    cudaSetDevice(c->device);
+    pack_materials(m, n, c->pack.mats);
+    c->materials.assign(m, m + n);
+    cudaError_t e = cudaMemcpyAsync(c->b_mats.ptr, c->pack.mats.data(), c->pack.mats.size() * sizeof(DevMaterial),
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "material upload");
 }
 e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *, uint32_t, e8g_render_stats *) {
     return e8g::fail(c, E8G_ERR_UNSUPPORTED, "batched rendering not available yet");

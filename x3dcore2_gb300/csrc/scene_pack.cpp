@@ -31,6 +31,7 @@ void pack_materials(e8g_material const *m, uint32_t n, std::vector<DevMaterial> 
             d.b = 0.45f * sigma2 / (sigma2 + 0.09f);
         } else if (m[i].type == E8G_MAT_COOK_TORR) { // cook_torr ctor, material.cpp:171-176
             d.alpha2 = 2 * m[i].roughness * m[i].roughness;
+            d.rough = m[i].roughness;
             d.ior_re = m[i].ior_re;
             d.ior_im = m[i].ior_im;
         } else if (m[i].type == E8G_MAT_MIXTURE) {
