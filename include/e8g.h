@@ -244,16 +244,19 @@ e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *
                           void *stream);
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
 
-/* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity and
- * bounces-per-graph on a short render of `params` (at most 2 spp) and keeps the fastest for this
- * context. Without it the wavefront uses 2^21 slots and 8 bounces per graph. */
+/* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity,
+ * bounces-per-graph and warp refill threshold (the number of idle lanes at which a trace kernel
+ * hands its idle lanes new rays) on a short render of `params` (at most 2 spp), and keeps the
+ * fastest for this context. Without it: 2^21 slots, 8 bounces per graph, threshold 16. */
 typedef struct e8g_tune_result {
     uint32_t capacity;          /* chosen number of path slots */
     uint32_t bounces_per_graph; /* chosen bounces captured in one CUDA graph */
+    uint32_t threshold;         /* chosen warp refill threshold of the trace kernels (0 = off) */
     uint32_t num_candidates;
-    uint32_t cand_capacity[8];
-    uint32_t cand_bounces[8];
-    double cand_ms[8];
+    uint32_t cand_capacity[16];
+    uint32_t cand_bounces[16];
+    uint32_t cand_threshold[16];
+    double cand_ms[16];
 } e8g_tune_result;
 e8g_status e8g_wavefront_tune(e8g_ctx *ctx, const e8g_render_params *params, e8g_tune_result *result);
 

@@ -77,8 +77,9 @@ def test_albedo_gradients_match_finite_differences(ctx):
 
 def test_roughness_gradients_match_finite_differences(ctx):
     """Roughness moves the sampled GGX directions, so CRN finite differences and the replayed
-    gradient agree in expectation only: 4096 spp, the two largest gradients, within 5%."""
-    sc, base, p, target = setup(ctx, 32, 24, 4096)
+    gradient (sampling held fixed) agree in expectation only: 96x72 pixels at 4096 spp (28M paths
+    per render), the two largest gradients, within 3%."""
+    sc, base, p, target = setup(ctx, 96, 72, 4096)
     img = ctx.forward(p)
     _, dl = loss_and_grad(img, target)
     da, dr = ctx.backward(dl)
@@ -90,7 +91,7 @@ def test_roughness_gradients_match_finite_differences(ctx):
         plus[m].roughness += h
         minus[m].roughness -= h
         fd = (render_loss(ctx, plus, p, target) - render_loss(ctx, minus, p, target)) / (2 * h)
-        assert abs(fd - dr[m]) <= 0.05 * abs(fd), (m, fd, dr[m])
+        assert abs(fd - dr[m]) <= 0.03 * abs(fd), (m, fd, dr[m])
     ctx.set_materials(base)
 
 

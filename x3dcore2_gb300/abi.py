@@ -98,8 +98,10 @@ class BatchItem(C.Structure):
 
 
 class TuneResult(C.Structure):
-    _fields_ = [("capacity", C.c_uint32), ("bounces_per_graph", C.c_uint32), ("num_candidates", C.c_uint32),
-                ("cand_capacity", C.c_uint32 * 8), ("cand_bounces", C.c_uint32 * 8), ("cand_ms", C.c_double * 8)]
+    _fields_ = [("capacity", C.c_uint32), ("bounces_per_graph", C.c_uint32), ("threshold", C.c_uint32),
+                ("num_candidates", C.c_uint32), ("cand_capacity", C.c_uint32 * 16),
+                ("cand_bounces", C.c_uint32 * 16), ("cand_threshold", C.c_uint32 * 16),
+                ("cand_ms", C.c_double * 16)]
 
 
 class GenOpts(C.Structure):

@@ -149,3 +149,19 @@ class Context:
     def set_materials(self, materials):
         arr = (abi.Material * len(materials))(*materials)
         self._check(self.lib.e8g_set_materials(self.h, arr, len(materials)), "e8g_set_materials")
+
+
+def render_batch(ctx, scenes, params):
+    """e8g_batch_render: many scenes in one persistent launch; returns images and stats."""
+    n = len(scenes)
+    items = (abi.BatchItem * n)()
+    outs = []
+    for k, (sc, p) in enumerate(zip(scenes, params)):
+        img = np.zeros((p.height, p.width, 4), np.float32)
+        outs.append(img)
+        items[k].scene = C.pointer(sc.desc)
+        items[k].params = p
+        items[k].rgba_out = img.ctypes.data_as(C.POINTER(C.c_float))
+    st = abi.RenderStats()
+    abi.check(ctx.lib.e8g_batch_render(ctx.h, items, n, C.byref(st)), ctx.h, "e8g_batch_render")
+    return outs, {k: getattr(st, k) for k, _ in abi.RenderStats._fields_}

@@ -43,7 +43,7 @@ struct e8g_ctx {
     e8g_render_params fwd_params{};
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
-    uint32_t wf_capacity = 1u << 21, wf_bounces = 8;
+    uint32_t wf_capacity = 1u << 21, wf_bounces = 8, wf_threshold = 16;
     void *host_pinned = nullptr;
 
     std::vector<e8g::dev_buffer *> all_buffers() {
@@ -68,7 +68,7 @@ void fill_dev_scene(e8g_ctx *c);
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts);
 // Wavefront integrator over the image or a path list (E8G_MODE_MIS).
 e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
-                         uint32_t bounces);
+                         uint32_t bounces, uint32_t threshold);
 
 // Per-path radiance for device lists of pixels and samples into d_rgb (3 floats per path).
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,

@@ -502,6 +502,91 @@ __device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d,
     return trace_any_sah<COUNT>(S, o, d, tmin, tmax, stk, cnt);
 }
 
+// ---- resumable traversal (SAH layout): one node per call ----
+// Lets a persistent trace kernel give a lane a new ray as soon as its ray is done, instead of
+// holding the lane until the warp's slowest ray finishes.
+struct TravState {
+    float3 o, d, inv;
+    float tmin, cull;     // closest: min(best, 1000); any: tmax
+    uint32_t link, count; // current node (count == 0: interior)
+    int sp;
+    bool found;           // any-hit: an occluder was found
+    Hit best;
+};
+
+__device__ __forceinline__ void trav_begin(const DevScene &S, TravState &T, float3 o, float3 d, float tmin, float tmax) {
+    T.o = o;
+    T.d = d;
+    T.inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    T.tmin = tmin;
+    T.cull = tmax;
+    T.sp = 0;
+    T.found = false;
+    T.best.t = INFINITY;
+    T.best.tri = 0xFFFFFFFFu;
+    T.best.b1 = T.best.b2 = 0.0f;
+    T.link = __float_as_uint(__ldg(&S.nlo[0].w));
+    T.count = __float_as_uint(__ldg(&S.nhi[0].w));
+}
+
+// Visits one node; returns true when the ray is finished (stack empty, or any-hit found).
+// Same tests, order and culling as trace_closest_sah / trace_any_sah.
+template <bool ANY>
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint32_t *stk) {
+    uint32_t *sn = stk;
+    float *st = reinterpret_cast<float *>(stk + kStack * kBlock);
+    if (T.count == 0) {
+        float4 l0 = __ldg(&S.nlo[T.link]), h0 = __ldg(&S.nhi[T.link]);
+        float4 l1 = __ldg(&S.nlo[T.link + 1]), h1 = __ldg(&S.nhi[T.link + 1]);
+        float tn0, tn1;
+        bool hit0 = slab(l0, h0, T.o, T.inv, T.tmin, T.cull, tn0);
+        bool hit1 = slab(l1, h1, T.o, T.inv, T.tmin, T.cull, tn1);
+        if (hit0 && hit1) {
+            bool swap = tn1 < tn0;
+            sn[T.sp * kBlock] = swap ? T.link : T.link + 1;
+            if (!ANY)
+                st[T.sp * kBlock] = swap ? tn0 : tn1;
+            T.sp++;
+            float4 nl = swap ? l1 : l0, nh = swap ? h1 : h0;
+            T.link = __float_as_uint(nl.w);
+            T.count = __float_as_uint(nh.w);
+            return false;
+        }
+        if (hit0 || hit1) {
+            T.link = __float_as_uint(hit0 ? l0.w : l1.w);
+            T.count = __float_as_uint(hit0 ? h0.w : h1.w);
+            return false;
+        }
+    } else {
+        for (uint32_t k = T.link; k < T.link + T.count; k++) {
+            float4 a = __ldg(&S.tri[3 * k]), b = __ldg(&S.tri[3 * k + 1]), c = __ldg(&S.tri[3 * k + 2]);
+            float t0, b1, b2;
+            if (ANY) {
+                if (tri_test(T.o, T.d, a, b, c, T.tmin, T.cull, t0, b1, b2)) {
+                    T.found = true;
+                    return true;
+                }
+            } else if (tri_test(T.o, T.d, a, b, c, T.tmin, 1000.0f, t0, b1, b2) && t0 < T.best.t) {
+                T.best.t = t0;
+                T.best.tri = __float_as_uint(a.w);
+                T.best.b1 = b1;
+                T.best.b2 = b2;
+                T.cull = fminf(t0, 1000.0f);
+            }
+        }
+    }
+    while (T.sp > 0) {
+        T.sp--;
+        uint32_t node = sn[T.sp * kBlock];
+        if (ANY || st[T.sp * kBlock] <= T.cull) {
+            T.link = __float_as_uint(__ldg(&S.nlo[node].w));
+            T.count = __float_as_uint(__ldg(&S.nhi[node].w));
+            return false;
+        }
+    }
+    return true;
+}
+
 // ------------------------------------------------------------------ surfaces ----
 
 struct Vert {

@@ -25,6 +25,23 @@ void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *f
                        unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
 int megakernel_blocks_per_sm();
 
+// Many scenes, one persistent launch (SAH layout, Philox streams).
+struct BatchDev {
+    DevScene const *scenes;      // per scene
+    RenderArgs const *args;      // per scene
+    uint64_t const *path_prefix; // n + 1 prefix sums of each scene's path count
+    uint64_t const *pix_prefix;  // n + 1 prefix sums of each scene's pixel count
+    uint32_t n;
+    uint64_t total_paths;
+};
+void launch_megakernel_batch(BatchDev const &B, FirstHit const *fh_all, float4 *accum_all, unsigned long long *work,
+                             int grid, cudaStream_t st);
+int megakernel_batch_blocks_per_sm();
+void launch_first_hits_batch(BatchDev const &B, DevScene const *h_scenes, RenderArgs const *h_args,
+                             uint64_t const *h_pix_prefix, FirstHit *fh_all, cudaStream_t st);
+void launch_resolve_batch(BatchDev const &B, uint64_t total_pix, float4 const *accum_all, float *rgba_all,
+                          cudaStream_t st);
+
 // Bidirectional path tracing (reference uniform weights), one thread per path.
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                  unsigned long long *work, int grid, cudaStream_t st);

@@ -20,7 +20,7 @@ struct WfCounters { // mirrors the device Counters of wavefront.cu
 e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs const &A, float4 *accum, float *path_rgb,
                           unsigned long long *d_counts) {
     if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_MIS && !d_counts)
-        return run_wavefront(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces);
+        return run_wavefront(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces, c->wf_threshold);
     cudaError_t e = cudaMemsetAsync(c->b_work.ptr, 0, 64, c->stream);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "work counter");
@@ -39,7 +39,7 @@ e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs con
 } // namespace
 
 e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
-                         uint32_t bounces) {
+                         uint32_t bounces, uint32_t threshold) {
     uint64_t want = std::max<uint64_t>(A.total_paths, 1024);
     uint32_t Q = static_cast<uint32_t>(std::min<uint64_t>(capacity, (want + 255) / 256 * 256));
     cudaError_t e = c->b_wf.reserve(wf_total_bytes(Q));
@@ -59,7 +59,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront capture");
     for (uint32_t k = 0; k < bounces; k++)
-        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, c->stream);
+        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, threshold, c->stream);
     e = cudaStreamEndCapture(c->stream, &graph);
     if (e == cudaSuccess)
         e = cudaGraphInstantiate(&exec, graph, 0);
@@ -192,14 +192,17 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     cudaError_t e = c->b_img.reserve(bytes);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "image buffer");
-    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
+    const uint32_t caps[] = {1u << 21, 1u << 22};
     const uint32_t bnc[] = {4, 8};
+    const uint32_t thr[] = {0, 8, 16, 24};
     e8g_tune_result r{};
     double best = 1e300;
     for (uint32_t cap : caps)
-        for (uint32_t b : bnc) {
+        for (uint32_t b : bnc)
+            for (uint32_t th : thr) {
             c->wf_capacity = cap;
             c->wf_bounces = b;
+            c->wf_threshold = th;
             double ms = 1e300;
             for (int rep = 0; rep < 2; rep++) { // first run warms caches and builds nothing twice
                 s = render_image(c, &p, static_cast<float *>(c->b_img.ptr), nullptr);
@@ -207,9 +210,10 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                     return s;
                 ms = std::min(ms, c->stats.kernel_ms);
             }
-            if (r.num_candidates < 8) {
+            if (r.num_candidates < 16) {
                 r.cand_capacity[r.num_candidates] = cap;
                 r.cand_bounces[r.num_candidates] = b;
+                r.cand_threshold[r.num_candidates] = th;
                 r.cand_ms[r.num_candidates] = ms;
                 r.num_candidates++;
             }
@@ -217,10 +221,12 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                 best = ms;
                 r.capacity = cap;
                 r.bounces_per_graph = b;
+                r.threshold = th;
             }
-        }
+            }
     c->wf_capacity = r.capacity;
     c->wf_bounces = r.bounces_per_graph;
+    c->wf_threshold = r.threshold;
     if (res)
         *res = r;
     return E8G_OK;
@@ -327,9 +333,6 @@ e8g_status e8g_set_materials(e8g_ctx *c, e8g_material const *m, uint32_t n) {
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
     return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "material upload");
-}
-e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *, uint32_t, e8g_render_stats *) {
-    return e8g::fail(c, E8G_ERR_UNSUPPORTED, "batched rendering not available yet");
 }
 
 } // extern "C"

@@ -131,3 +131,76 @@ void launch_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rg
 }
 
 } // namespace e8g
+
+namespace e8g {
+
+// Batched first hits: the pixel index runs over every scene's pixels.
+__global__ void __launch_bounds__(kBlock) k_first_hits_batch(BatchDev B, uint64_t total_pix, FirstHit *out) {
+    __shared__ uint32_t stk[kStackWords * kBlock];
+    uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= total_pix)
+        return;
+    uint32_t lo = 0, hi = B.n;
+    while (hi - lo > 1) {
+        uint32_t mi = (lo + hi) >> 1;
+        if (B.pix_prefix[mi] <= i)
+            lo = mi;
+        else
+            hi = mi;
+    }
+    DevScene const &S = B.scenes[lo];
+    RenderArgs const &A = B.args[lo];
+    uint32_t px = static_cast<uint32_t>(i - B.pix_prefix[lo]);
+    float3 o, d;
+    camera_ray(S.cam, px % A.width, px / A.width, A.width, A.height, o, d);
+    Hit hit = trace_closest_l<0, false>(S, o, d, stk + threadIdx.x, nullptr);
+    FirstHit f;
+    f.d = make_float4(d.x, d.y, d.z, 0.0f);
+    int32_t mesh = -1, light = -1;
+    float3 p = f3(0, 0, 0), n = f3(0, 0, 0);
+    if (hit.tri != 0xFFFFFFFFu) {
+        Vert v = make_vert(S, hit);
+        if (dot(v.n, neg(d)) > 0) {
+            mesh = v.mesh;
+            p = v.p;
+            n = v.n;
+            light = __ldg(&S.mesh_light[mesh]);
+        }
+    }
+    f.p = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
+    f.n = make_float4(n.x, n.y, n.z, __int_as_float(light));
+    out[i] = f;
+}
+
+__global__ void k_resolve_batch(BatchDev B, uint64_t total_pix, float4 const *accum, float *rgba) {
+    uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= total_pix)
+        return;
+    uint32_t lo = 0, hi = B.n;
+    while (hi - lo > 1) {
+        uint32_t mi = (lo + hi) >> 1;
+        if (B.pix_prefix[mi] <= i)
+            lo = mi;
+        else
+            hi = mi;
+    }
+    uint32_t spp = B.args[lo].spp;
+    float inv = spp ? 1.0f / static_cast<float>(spp) : 0.0f;
+    float4 a = accum[i];
+    reinterpret_cast<float4 *>(rgba)[i] = make_float4(a.x * inv, a.y * inv, a.z * inv, 1.0f);
+}
+
+void launch_first_hits_batch(BatchDev const &B, DevScene const *, RenderArgs const *, uint64_t const *h_pix_prefix,
+                             FirstHit *fh_all, cudaStream_t st) {
+    uint64_t total = h_pix_prefix[B.n];
+    if (total)
+        k_first_hits_batch<<<static_cast<unsigned>((total + kBlock - 1) / kBlock), kBlock, 0, st>>>(B, total, fh_all);
+}
+
+void launch_resolve_batch(BatchDev const &B, uint64_t total_pix, float4 const *accum_all, float *rgba_all,
+                          cudaStream_t st) {
+    if (total_pix)
+        k_resolve_batch<<<static_cast<unsigned>((total_pix + 255) / 256), 256, 0, st>>>(B, total_pix, accum_all, rgba_all);
+}
+
+} // namespace e8g

@@ -25,7 +25,8 @@ struct Counters {
     unsigned long long next_path; // global path counter
     uint32_t shadow_n, ext_n;      // queue lengths of the current bounce
     uint32_t busy;                 // slots holding a path after the last shade
-    uint32_t pad[3];
+    uint32_t shadow_head, ext_head; // next queue entry to hand out (dynamic fetch)
+    uint32_t pad;
 };
 
 __device__ __forceinline__ void emit_to(RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t out, float3 c) {
@@ -308,10 +309,71 @@ __global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Cou
     }
 }
 
+// Persistent trace kernel with per-lane dynamic fetch: a lane whose ray is finished takes the
+// next queue entry; lanes are refilled together (one atomic) once at least `threshold` of them
+// are idle, or when none is busy.
+template <bool ANY>
+__global__ void __launch_bounds__(kBlock) k_wf_trace_dyn(DevScene S, RenderArgs A, WfSlots W, Counters *cnt,
+                                                         float4 *accum, float *path_rgb, uint32_t threshold) {
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *stk = stk_all + threadIdx.x;
+    const uint32_t n = ANY ? cnt->shadow_n : cnt->ext_n;
+    uint32_t *head = ANY ? &cnt->shadow_head : &cnt->ext_head;
+    const uint32_t lane = lane_id();
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    uint32_t q = kNone;
+    bool exhausted = false;
+    TravState T;
+    while (true) {
+        bool idle = q == kNone && !exhausted;
+        uint32_t im = __ballot_sync(~0u, idle);
+        uint32_t busy = __ballot_sync(~0u, q != kNone);
+        if (im && (__popc(im) >= threshold || busy == 0)) {
+            int leader = __ffs(im) - 1;
+            uint32_t base = 0;
+            if (static_cast<int>(lane) == leader)
+                base = atomicAdd(head, static_cast<uint32_t>(__popc(im)));
+            base = __shfl_sync(~0u, base, leader);
+            if (idle) {
+                uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
+                if (qq < n) {
+                    q = qq;
+                    if (ANY) {
+                        float4 so = W.sh_o[q], sd = W.sh_d[q];
+                        trav_begin(S, T, xyz(so), xyz(sd), 1e-4f, sd.w);
+                    } else {
+                        uint32_t s = W.ext_slot[q];
+                        trav_begin(S, T, xyz(W.p_mesh[s]), neg(xyz(W.o[s])), 1e-4f, 1000.0f);
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+            busy = __ballot_sync(~0u, q != kNone);
+        }
+        if (busy == 0) {
+            if (__ballot_sync(~0u, !exhausted) == 0)
+                break;
+            continue;
+        }
+        if (q != kNone && trav_step<ANY>(S, T, stk)) {
+            if (ANY) {
+                if (!T.found)
+                    emit_to(A, accum, path_rgb, __float_as_uint(W.sh_o[q].w), xyz(W.sh_c[q]));
+            } else {
+                W.hit[W.ext_slot[q]] = make_float4(T.best.t, __uint_as_float(T.best.tri), T.best.b1, T.best.b2);
+            }
+            q = kNone;
+        }
+    }
+}
+
 __global__ void k_wf_reset(Counters *cnt) {
     cnt->shadow_n = 0;
     cnt->ext_n = 0;
     cnt->busy = 0;
+    cnt->shadow_head = 0;
+    cnt->ext_head = 0;
 }
 
 } // namespace
@@ -360,24 +422,33 @@ size_t wf_total_bytes(uint32_t capacity) {
 }
 
 int wf_trace_blocks_per_sm() {
-    int a = 0, b = 0;
+    int a = 0, b = 0, c = 0, d = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
-    int n = a < b ? a : b;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_trace_dyn<true>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_wf_trace_dyn<false>, kBlock, 0);
+    int n = a;
+    for (int x : {b, c, d})
+        n = x < n ? x : n;
     return n > 0 ? n : 1;
 }
 
 // One bounce: reset queue lengths, shade, shadow, extend.
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
-                       float *path_rgb, int shade_grid, int trace_grid, cudaStream_t st) {
+                       float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, cudaStream_t st) {
     auto *cnt = reinterpret_cast<Counters *>(W.counters);
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
     if (A.rng == E8G_RNG_MINSTD)
         k_wf_shade<RngMinstd><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
     else
         k_wf_shade<RngPhilox><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
-    k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
-    k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);
+    if (threshold > 0 && S.layout == 0) {
+        k_wf_trace_dyn<true><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_dyn<false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+    } else {
+        k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
+        k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);
+    }
 }
 
 cudaError_t wf_init(WfSlots const &W, cudaStream_t st) {

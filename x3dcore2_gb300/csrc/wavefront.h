@@ -18,8 +18,10 @@ size_t wf_total_bytes(uint32_t capacity);
 WfSlots wf_carve(void *base, uint32_t capacity);
 cudaError_t wf_init(WfSlots const &W, cudaStream_t st);
 int wf_trace_blocks_per_sm();
+// threshold > 0: trace kernels refill idle lanes with new rays during traversal once that many
+// lanes of a warp are idle; 0: one ray per thread.
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
-                       float *path_rgb, int shade_grid, int trace_grid, cudaStream_t st);
+                       float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, cudaStream_t st);
 uint32_t *wf_busy_ptr(WfSlots const &W);
 unsigned long long *wf_next_ptr(WfSlots const &W);
 
