@@ -147,6 +147,62 @@ def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
                                            f"(oracle), {threads} threads, {total_s:.1f} s render, BVH build {build_s:.1f} s")
 
 
+def batch_leg(ctx, seed=1):
+    """64 independent scenes in one persistent launch: seeded random soups in an enclosing box,
+    triangles log-uniform in [1k, 500k], resolution from {128, 256, 512, 1024}^2, spp from
+    {4, 16, 64}, max depth 4-10, GGX roughness U[0.02, 1]. Compared with rendering the same 64
+    scenes one call at a time (device time of the integrator kernels in both)."""
+    import numpy as np
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300 import scene as S
+    from x3dcore2_gb300.core import default_params, render_batch
+    rng = np.random.default_rng(seed)
+    scenes, params = [], []
+    for k in range(64):
+        ntri = int(np.exp(rng.uniform(np.log(1000), np.log(500000))))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = int(rng.choice([4, 16, 64]))
+        depth = int(rng.integers(4, 11))
+        scenes.append(S.soup(ntri, seed=1000 + k, width=res, height=res, roughness_lo=0.02, roughness_hi=1.0))
+        params.append(default_params(abi.MODE_MIS, res, res, spp, seed=k + 1, max_depth=depth, rr_start=3))
+    paths = sum(p.width * p.height * p.spp for p in params)
+    render_batch(ctx, scenes, params)  # warm-up
+    _, st = render_batch(ctx, scenes, params)
+    sep_ms = 0.0
+    for sc, p in zip(scenes, params):
+        ctx.upload(sc)
+        ctx.render(p)
+        sep_ms += ctx.stats()["ms"]
+    return {"scenes": 64, "paths": paths, "triangles": int(sum(s.num_tris for s in scenes)),
+            "batched_ms": st["ms"], "batched_paths_per_s": paths / (st["ms"] / 1000.0),
+            "separate_ms": sep_ms, "separate_paths_per_s": paths / (sep_ms / 1000.0),
+            "launches": st["launches"]}
+
+
+def adjoint_leg(ctx):
+    """Differentiable render: displaced icosphere level 7 (327,680 triangles), 256 materials,
+    512x512, 32 spp, max depth 6; forward render vs path-replay backward of an L2 loss."""
+    import numpy as np
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300 import scene as S
+    from x3dcore2_gb300.core import default_params
+    sc = S.displaced_icosphere(level=7, seed=5, num_materials=256, width=512, height=512)
+    ctx.upload(sc)
+    p = default_params(abi.MODE_MIS, 512, 512, 32, seed=1, max_depth=6, rr_start=3)
+    fwd, bwd = [], []
+    dl = np.ones((512, 512, 3), np.float32)
+    for k in range(4):
+        ctx.forward(p)
+        f = ctx.stats()["ms"]
+        ctx.backward(dl)
+        b = ctx.stats()["ms"]
+        if k:
+            fwd.append(f)
+            bwd.append(b)
+    return {"triangles": sc.num_tris, "materials": 256, "forward_ms": statistics.mean(fwd),
+            "backward_ms": statistics.mean(bwd), "ratio": statistics.mean(bwd) / statistics.mean(fwd)}
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -195,6 +251,7 @@ def main():
     ap.add_argument("--res", default=None, help="WxH override, e.g. 480x270 (profiling a smaller launch)")
     ap.add_argument("--spp", type=int, default=None, help="spp override (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the 64-scene batch and adjoint legs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -325,6 +382,9 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if rank == 0 and not args.no_extras and world == 1:
+        line["batch"] = batch_leg(ctx)
+        line["adjoint"] = adjoint_leg(ctx)
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         v, kind, sample = cpu_sample(scene, w, h, args.cpu_budget, os.cpu_count() or 1, timing_ref=False)
         line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": os.cpu_count() or 1, "kind": kind,

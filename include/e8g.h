@@ -185,7 +185,9 @@ typedef struct e8g_render_params {
     uint32_t rr_start;      /* first depth with Russian roulette (reference: 2) */
     float rr_prob;          /* survival probability (reference: 0.5) */
     uint32_t bdpt_max_len;  /* subpath vertex cap (reference: 8, pathtracer.h:201) */
-    uint32_t firefly;       /* 8-neighbour firefly clamp, renderer.cpp:46-83 */
+    uint32_t firefly;       /* nonzero: pt_image_renderer's 8-neighbour firefly clamp on every
+                               sample image (renderer.cpp:46-83); not taken by
+                               e8g_render_dev_noalloc or e8g_batch_render */
     uint32_t sample_offset; /* first sample index (progressive rendering) */
 } e8g_render_params;
 

@@ -1558,6 +1558,212 @@ static v3 mis_path(octx *c, const oray *cam_ray, const overt *first, int first_l
     return L;
 }
 
+/* ---- product mode: bidirectional with power-heuristic MIS (new; not in the reference) ----
+ * Camera subpath from the cached first hit, light subpath from an area-weighted emission
+ * sample with a cosine direction, every (s light, t camera) connection with t >= 1, weighted by
+ * the power heuristic over all strategies that could produce the same path. Densities are kept
+ * in area measure per vertex: fwd (from the predecessor in its own subpath) and rev (from the
+ * successor); the connection updates the four densities it changes (Veach's recurrence). */
+
+typedef struct obv {
+    v3 p, n;
+    int32_t mesh;
+    v3 beta;
+    float fwd, rev;
+} obv;
+
+static inline float to_area(float pdf_w, v3 from, v3 to, v3 n_to) {
+    v3 d = vsub(to, from);
+    float d2 = vdot(d, d);
+    if (d2 <= 0.0f)
+        return 0.0f;
+    float c = fabsf(vdot(n_to, d)) / sqrtf(d2);
+    return pdf_w * c / d2;
+}
+
+/* BSDF density at vertex v of going out along `wi` given the other direction `wo` */
+static inline float vpdf(const o_scene *s, const obv *v, v3 wo, v3 wi) {
+    return bsdf_pdf(s, find_mat(s, s->mesh_mat[v->mesh]), v->n, wo, wi);
+}
+
+static unsigned bdp_walk(octx *c, obv *path, unsigned len, unsigned max_len, v3 wo) {
+    const o_scene *s = c->s;
+    while (len < max_len) {
+        obv *cur = &path[len - 1];
+        const omat *m = find_mat(s, s->mesh_mat[cur->mesh]);
+        float pdf;
+        v3 i = bsdf_sample_mis(s, m, c->rng, &pdf, cur->n, wo);
+        if (!(pdf > 0.0f))
+            break;
+        float cw = vdot(cur->n, i);
+        if (cw <= 0.0f)
+            break;
+        v3 f = bsdf_eval(s, m, cur->n, wo, i);
+        oray r = mkray(cur->p, i);
+        overt nv = intersect(s, &r);
+        if (!nv.valid || vdot(nv.normal, vneg(i)) <= 0.0f)
+            break;
+        obv *nx = &path[len];
+        nx->p = nv.vertex;
+        nx->n = nv.normal;
+        nx->mesh = nv.mesh;
+        nx->beta = vmul(cur->beta, vscale(f, cw / pdf));
+        nx->fwd = to_area(pdf, cur->p, nx->p, nx->n);
+        nx->rev = 0.0f;
+        /* density of sampling cur from nx (reverse direction) */
+        float prev_w = vpdf(s, cur, i, wo);
+        if (len >= 2)
+            cur[-1].rev = to_area(prev_w, cur->p, cur[-1].p, cur[-1].n);
+        wo = vneg(i);
+        len++;
+    }
+    return len;
+}
+
+static v3 bdpt_power_path(octx *c, const oray *cam_ray, const overt *first) {
+    const o_scene *s = c->s;
+    unsigned maxlen = c->pol->bdpt_max_len;
+    if (maxlen > 16)
+        maxlen = 16;
+    obv cam[16], lp[16];
+    unsigned clen = 0, llen = 0;
+    v3 o0 = vneg(cam_ray->v);
+    if (first->valid && maxlen) {
+        cam[0].p = first->vertex;
+        cam[0].n = first->normal;
+        cam[0].mesh = first->mesh;
+        cam[0].beta = V(1, 1, 1);
+        cam[0].fwd = 1.0f;
+        cam[0].rev = 0.0f;
+        clen = bdp_walk(c, cam, 1, maxlen, o0);
+    }
+    /* emission sample: light (CDF), area-weighted point, cosine direction */
+    float pmf;
+    int light = sample_light(s, c->rng, &pmf);
+    osurf em = mesh_sample(s, s->lights[light].mesh, c->rng, 1);
+    v3 w = cos_hemisphere(em.n, c->rng);
+    float pdf_w = vdot(em.n, w) / PI_F;
+    if (maxlen) {
+        lp[0].p = em.p;
+        lp[0].n = em.n;
+        lp[0].mesh = (int32_t)s->lights[light].mesh;
+        lp[0].fwd = pmf * em.area_dens;
+        lp[0].rev = 0.0f;
+        lp[0].beta = V(1.0f / lp[0].fwd, 1.0f / lp[0].fwd, 1.0f / lp[0].fwd);
+        llen = 1;
+        if (pdf_w > 0.0f && maxlen > 1) {
+            oray r0 = mkray(em.p, w);
+            overt v0 = intersect(s, &r0);
+            if (v0.valid && vdot(v0.normal, vneg(w)) > 0.0f) {
+                lp[1].p = v0.vertex;
+                lp[1].n = v0.normal;
+                lp[1].mesh = v0.mesh;
+                /* beta_1 = Le cos / (pmf pA pdf_w) */
+                lp[1].beta = vscale(light_rad(s, light), vdot(em.n, w) / (pdf_w * lp[0].fwd));
+                lp[1].fwd = to_area(pdf_w, em.p, lp[1].p, lp[1].n);
+                lp[1].rev = 0.0f;
+                llen = bdp_walk(c, lp, 2, maxlen, vneg(w));
+            }
+        }
+    }
+    if (clen == 0)
+        return V0;
+    v3 L = V0;
+    for (unsigned t = 1; t <= clen; t++) {
+        for (unsigned sl = 0; sl <= llen; sl++) {
+            obv *cv = &cam[t - 1];
+            v3 wo_c = t >= 2 ? vnormalize(vsub(cam[t - 2].p, cv->p)) : o0;
+            v3 contrib = V0;
+            /* densities the connection changes (restored after) */
+            float save_c_rev = cv->rev, save_c2_rev = t >= 2 ? cam[t - 2].rev : 0.0f;
+            float save_l_rev = sl >= 1 ? lp[sl - 1].rev : 0.0f, save_l2_rev = sl >= 2 ? lp[sl - 2].rev : 0.0f;
+            if (sl == 0) {
+                int hl = s->mesh_light[cv->mesh];
+                if (hl < 0)
+                    continue;
+                v3 le = light_radiance(s, hl, wo_c, cv->n);
+                if (vequals0(le))
+                    continue;
+                contrib = vmul(cv->beta, le);
+                float pl = s->light_pnorm[hl] / s->total_power;
+                cv->rev = pl * (1.0f / s->mesh_area[s->lights[hl].mesh]);
+                if (t >= 2) {
+                    float ew = fmaxf(vdot(cv->n, wo_c), 0.0f) / PI_F;
+                    cam[t - 2].rev = to_area(ew, cv->p, cam[t - 2].p, cam[t - 2].n);
+                }
+            } else {
+                obv *lv = &lp[sl - 1];
+                v3 d = vsub(lv->p, cv->p);
+                float d2 = vdot(d, d);
+                if (d2 <= 0.0f)
+                    continue;
+                float dist = sqrtf(d2);
+                v3 dir = vdivs(d, dist); /* from camera vertex to light vertex */
+                float cos_c = vdot(cv->n, dir);
+                float cos_l = vdot(lv->n, vneg(dir));
+                if (cos_c <= 0.0f || cos_l <= 0.0f)
+                    continue;
+                const omat *mc = find_mat(s, s->mesh_mat[cv->mesh]);
+                v3 fc = bsdf_eval(s, mc, cv->n, wo_c, dir);
+                if (vequals0(fc))
+                    continue;
+                v3 fl;
+                v3 wo_l = V0;
+                if (sl == 1) {
+                    fl = light_radiance(s, light, vneg(dir), lv->n);
+                } else {
+                    wo_l = vnormalize(vsub(lp[sl - 2].p, lv->p));
+                    fl = bsdf_eval(s, find_mat(s, s->mesh_mat[lv->mesh]), lv->n, vneg(dir), wo_l);
+                }
+                if (vequals0(fl))
+                    continue;
+                oray sr = mkray(cv->p, dir);
+                if (has_intersect(s, &sr, 1e-4f, dist - 1e-3f))
+                    continue;
+                float G = cos_c * cos_l / d2;
+                contrib = vscale(vmul(vmul(vmul(cv->beta, fc), fl), lv->beta), G);
+                /* reverse densities of the connection */
+                float pc = vpdf(s, cv, wo_c, dir);       /* camera vertex generating the light vertex */
+                lv->rev = to_area(pc, cv->p, lv->p, lv->n);
+                if (sl == 1)
+                    cv->rev = to_area(cos_l / PI_F, lv->p, cv->p, cv->n);
+                else
+                    cv->rev = to_area(vpdf(s, lv, wo_l, vneg(dir)), lv->p, cv->p, cv->n);
+                if (t >= 2)
+                    cam[t - 2].rev = to_area(vpdf(s, cv, dir, wo_c), cv->p, cam[t - 2].p, cam[t - 2].n);
+                if (sl >= 2)
+                    lp[sl - 2].rev = to_area(vpdf(s, lv, vneg(dir), wo_l), lv->p, lp[sl - 2].p, lp[sl - 2].n);
+            }
+            /* power-heuristic weight over strategies producing this path */
+            /* strategies whose subpaths would exceed the cap are impossible: stop there */
+            double sum = 0.0, ri = 1.0;
+            for (int i = (int)t - 1; i >= 1; i--) {
+                if (sl + t - (unsigned)i > maxlen)
+                    break;
+                ri *= (cam[i].fwd > 0.0f) ? (double)cam[i].rev / cam[i].fwd : 0.0;
+                sum += ri * ri;
+            }
+            ri = 1.0;
+            for (int i = (int)sl - 1; i >= 0; i--) {
+                if (t + sl - (unsigned)i > maxlen)
+                    break;
+                ri *= (lp[i].fwd > 0.0f) ? (double)lp[i].rev / lp[i].fwd : 0.0;
+                sum += ri * ri;
+            }
+            float wgt = (float)(1.0 / (1.0 + sum));
+            L = vadd(L, vscale(contrib, wgt));
+            cv->rev = save_c_rev;
+            if (t >= 2)
+                cam[t - 2].rev = save_c2_rev;
+            if (sl >= 1)
+                lp[sl - 1].rev = save_l_rev;
+            if (sl >= 2)
+                lp[sl - 2].rev = save_l2_rev;
+        }
+    }
+    return L;
+}
+
 /* ---------------------------------------------------------- path driver -- */
 
 typedef struct ofirst {
@@ -1607,6 +1813,8 @@ static v3 path_radiance(const o_scene *s, uint32_t mode, const o_policy *pol, or
         return bdpt_path(&c, &f->ray, &f->hit, f->light);
     case E8G_MODE_MIS:
         return mis_path(&c, &f->ray, &f->hit, f->light);
+    case E8G_MODE_BDPT_POWER:
+        return bdpt_power_path(&c, &f->ray, &f->hit);
     case E8G_MODE_NORMAL: /* normal_tracer, :492-506 */
         if (!f->hit.valid)
             return V0;
@@ -1762,6 +1970,87 @@ void o_render(const o_scene *s, uint32_t mode, uint32_t rng_kind, uint64_t seed,
     pthread_mutex_init(&j.mu, NULL);
     run_threads(image_worker, &j, num_threads);
     pthread_mutex_destroy(&j.mu);
+}
+
+/* pt_image_renderer::sampling_task::run, the firefly clamp (renderer.cpp:46-83) applied to one
+ * sample image est (w*h rgb): an interior pixel whose squared norm (vec::norm2, tensor.h:213)
+ * exceeds each of its 8 neighbours' by more than FireFlyMinDiff = 1.5 (renderer.h:118) has every
+ * channel capped (vec::at_most, tensor.h:284-289) at the neighbours' mean squared norm plus 1.5.
+ * Border pixels pass unchanged. The result is added to acc (w*h rgb). */
+static float sqn(const float *v) {
+    float r = 0.0f;
+    r += v[0] * v[0];
+    r += v[1] * v[1];
+    r += v[2] * v[2];
+    return r;
+}
+
+void o_firefly_add(const float *est, uint32_t w, uint32_t h, float *acc) {
+    const float diff = 1.5f;
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) {
+            size_t k = (size_t)y * w + x;
+            const float *e = est + 3 * k;
+            float *a = acc + 3 * k;
+            if (x > 0 && x < w - 1 && y > 0 && y < h - 1) {
+                float r00 = sqn(est + 3 * (k - w - 1)), r10 = sqn(est + 3 * (k - w)), r20 = sqn(est + 3 * (k - w + 1));
+                float r01 = sqn(est + 3 * (k - 1)), r11 = sqn(e), r21 = sqn(est + 3 * (k + 1));
+                float r02 = sqn(est + 3 * (k + w - 1)), r12 = sqn(est + 3 * (k + w)), r22 = sqn(est + 3 * (k + w + 1));
+                int ff = (r11 - r00) > diff && (r11 - r10) > diff && (r11 - r20) > diff && (r11 - r01) > diff &&
+                         (r11 - r21) > diff && (r11 - r02) > diff && (r11 - r12) > diff && (r11 - r22) > diff;
+                if (ff) {
+                    float cap = 1.0f / 8.0f * (r00 + r10 + r20 + r01 + r21 + r02 + r12 + r22) + diff;
+                    for (int i = 0; i < 3; i++)
+                        a[i] += cap < e[i] ? cap : e[i];
+                    continue;
+                }
+            }
+            for (int i = 0; i < 3; i++)
+                a[i] += e[i];
+        }
+}
+
+/* pt_image_renderer::render (renderer.cpp:106-166) with a single sampling task: the task's
+ * stream is std::minstd_rand0 seeded task_seed (i*1361+33 for task i, renderer.cpp:102); each of
+ * the spp samples runs the integrator over every pixel in row-major order drawing from that one
+ * stream (for example unidirect_lt1_path_tracer::sample, pathtracer.cpp:630-653), passes the
+ * sample image through the firefly clamp when asked (renderer.cpp:46-83), and adds it to the
+ * task's estimate. The compositor receives (estimate, 1) and scales it by 1/spp, so alpha is
+ * 1/spp, as in the reference. */
+void o_render_task(const o_scene *s, uint32_t mode, const o_policy *pol, uint32_t w, uint32_t h, uint32_t spp,
+                   int firefly, uint32_t task_seed, float *rgba_out) {
+    size_t npix = (size_t)w * h;
+    ofirst *f = (ofirst *)malloc(sizeof(ofirst) * npix);
+    float *est = (float *)malloc(sizeof(float) * 3 * npix);
+    float *acc = (float *)calloc(3 * npix, sizeof(float));
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++)
+            f[(size_t)y * w + x] = first_hit(s, x, y, w, h);
+    orng rng;
+    memset(&rng, 0, sizeof(rng));
+    minstd_seed(&rng, task_seed);
+    for (uint32_t k = 0; k < spp; k++) {
+        for (size_t i = 0; i < npix; i++) {
+            v3 L = path_radiance(s, mode, pol, &rng, &f[i]);
+            est[3 * i] = L.x;
+            est[3 * i + 1] = L.y;
+            est[3 * i + 2] = L.z;
+        }
+        if (firefly)
+            o_firefly_add(est, w, h, acc);
+        else
+            for (size_t i = 0; i < 3 * npix; i++)
+                acc[i] += est[i];
+    }
+    float scale = 1.0f / (float)spp;
+    for (size_t i = 0; i < npix; i++) {
+        for (int c = 0; c < 3; c++)
+            rgba_out[4 * i + c] = (0.0f + acc[3 * i + c]) * scale;
+        rgba_out[4 * i + 3] = (0.0f + 1.0f) * scale;
+    }
+    free(f);
+    free(est);
+    free(acc);
 }
 
 /* ------------------------------------------------- FP64 adjoint reference -- */

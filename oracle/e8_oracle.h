@@ -72,6 +72,14 @@ void o_render(const o_scene *s, uint32_t mode, uint32_t rng_kind, uint64_t seed,
               uint32_t sample_offset, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
               float *rgba_out, int num_threads);
 
+/* The firefly clamp of pt_image_renderer (renderer.cpp:46-83) on one sample image est (w*h
+ * rgb), added to acc (w*h rgb). */
+void o_firefly_add(const float *est, uint32_t w, uint32_t h, float *acc);
+/* pt_image_renderer::render with one sampling task whose sequential minstd stream is seeded
+ * task_seed (renderer.cpp:35-166): rgba_out as the reference's compositor holds it. */
+void o_render_task(const o_scene *s, uint32_t mode, const o_policy *pol, uint32_t w, uint32_t h, uint32_t spp,
+                   int firefly, uint32_t task_seed, float *rgba_out);
+
 /* Seed of the per-path minstd stream; the same function as e8g_path_seed. */
 uint32_t o_path_seed(uint64_t seed, uint32_t pixel, uint32_t sample);
 /* First n draws of the minstd stream with this seed (tensor.h:987-1001 + libstdc++

@@ -264,14 +264,14 @@ void r_render_paths(r_scene const *s, uint32_t mode, uint32_t w, uint32_t h, uin
 // pt_image_renderer::render with num_threads threads; returns wall seconds and the number of
 // samples per pixel actually taken (spp rounded up to a multiple of the thread count).
 double r_render(r_scene const *s, uint32_t mode, uint32_t w, uint32_t h, uint32_t spp,
-                uint32_t num_threads, float *rgba_out, uint32_t *samples_taken) {
+                uint32_t num_threads, float *rgba_out, uint32_t *samples_taken, int firefly) {
     e8::pt_image_renderer renderer(
         std::make_unique<e8::pathtracer_factory>(tracer_type(mode), e8::pathtracer_factory::options()),
         num_threads);
     mem_compositor comp(w, h);
     auto t0 = std::chrono::steady_clock::now();
     e8::pt_image_renderer::numerical_stats st =
-        renderer.render(&comp, *s->bvh, *s->mc, *s->ls, *s->cam, spp, false);
+        renderer.render(&comp, *s->bvh, *s->mc, *s->ls, *s->cam, spp, firefly != 0);
     auto t1 = std::chrono::steady_clock::now();
     for (uint32_t y = 0; y < h; y++)
         for (uint32_t x = 0; x < w; x++)

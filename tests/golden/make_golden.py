@@ -4,7 +4,8 @@ Runs only where the reference sources exist (the oracle Makefile compiles them, 
 oracle/_ref/libe8ref.so). Every fixture stores its scene arrays too, so consumers never depend on
 regenerating geometry bit for bit on another machine.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # every fixture
+    python tests/golden/make_golden.py renderer     # only the named ones
 """
 import os
 import subprocess
@@ -106,19 +107,44 @@ def uv_sphere_fixture():
     print("uv_sphere.npz")
 
 
-def main():
+def renderer_fixture():
+    """pt_image_renderer::render with one thread (one sampling task, stream seed 33), with and
+    without the firefly clamp, on the Cornell fixture's scene."""
+    import golden_util as G
+    sc = G.scene_from(G.load("cornell.npz"))
+    ref = ob.RefScene(sc)
+    w, h, spp = 64, 48, 4
+    out = dict(scene_arrays(sc), width=np.uint32(w), height=np.uint32(h), spp=np.uint32(spp))
+    for mname in ("lt1", "uni"):
+        for ff in (0, 1):
+            img, _, taken = ref.render(MODES[mname], w, h, spp, 1, firefly=bool(ff))
+            assert taken == spp
+            out[f"img_{mname}_ff{ff}"] = img
+    np.savez_compressed(os.path.join(HERE, "renderer.npz"), **out)
+    print("renderer.npz")
+
+
+def main(only=()):
     subprocess.run(["make", "-s", "-C", ob.ORACLE_DIR, "all", "ref"], check=True)
-    draws_fixture()
-    uv_sphere_fixture()
-    bsdf_fixture()
     all_modes = list(MODES)
-    paths_fixture("cornell.npz", S.cornell(64, 48), 64, 48, 512, 7, all_modes)
-    paths_fixture("furnace.npz", S.furnace(), 32, 32, 256, 11, ["uni", "lt1", "bdpt", "direct"])
-    paths_fixture("ico.npz", S.displaced_icosphere(level=3, seed=5, num_materials=16, width=48, height=27),
-                  48, 27, 384, 3, ["uni", "lt1", "bdpt", "direct"])
-    paths_fixture("soup.npz", S.soup(3000, seed=2, width=40, height=40), 40, 40, 256, 9,
-                  ["lt1", "bdpt", "direct"])
+    jobs = {
+        "draws": draws_fixture,
+        "uv_sphere": uv_sphere_fixture,
+        "bsdf": bsdf_fixture,
+        "cornell": lambda: paths_fixture("cornell.npz", S.cornell(64, 48), 64, 48, 512, 7, all_modes),
+        "furnace": lambda: paths_fixture("furnace.npz", S.furnace(), 32, 32, 256, 11,
+                                         ["uni", "lt1", "bdpt", "direct"]),
+        "ico": lambda: paths_fixture("ico.npz", S.displaced_icosphere(level=3, seed=5, num_materials=16,
+                                                                      width=48, height=27),
+                                     48, 27, 384, 3, ["uni", "lt1", "bdpt", "direct"]),
+        "soup": lambda: paths_fixture("soup.npz", S.soup(3000, seed=2, width=40, height=40), 40, 40, 256, 9,
+                                      ["lt1", "bdpt", "direct"]),
+        "renderer": renderer_fixture,  # reads cornell.npz, so it runs after it
+    }
+    for name, fn in jobs.items():
+        if not only or name in only:
+            fn()
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

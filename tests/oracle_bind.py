@@ -59,6 +59,8 @@ def oracle():
             "o_render": (None, [_P, _U, _U, C.c_uint64, C.POINTER(OPolicy), _U, _U, _U, _U, _U,
                                 _U, _U, _U, _P, C.c_int]),
             "o_path_seed": (_U, [C.c_uint64, _U, _U]),
+            "o_firefly_add": (None, [_P, _U, _U, _P]),
+            "o_render_task": (None, [_P, _U, C.POINTER(OPolicy), _U, _U, _U, C.c_int, _U, _P]),
             "o_minstd_draws": (None, [_U, _U, _P]),
             "o_philox_draws": (None, [C.c_uint64, _U, _U, _U, _P]),
             "o_bsdf_eval": (None, [_P, C.c_int32, _P, _P, _P, _P]),
@@ -92,7 +94,7 @@ def reference(timing=False):
             "r_trace_any": (None, [_P, _P, _P, _P, _U, C.c_int, _P]),
             "r_camera_rays": (None, [_P, _U, _U, _P]),
             "r_render_paths": (None, [_P, _U, _U, _U, _P, _P, _U, _P]),
-            "r_render": (C.c_double, [_P, _U, _U, _U, _U, _U, _P, _P]),
+            "r_render": (C.c_double, [_P, _U, _U, _U, _U, _U, _P, _P, C.c_int]),
             "r_bsdf_eval": (None, [_P, C.c_int32, _P, _P, _P, _P]),
             "r_bsdf_sample": (None, [_P, C.c_int32, _U, _P, _P, _U, _P, _P]),
             "r_minstd_draws": (None, [_U, _U, _P]),
@@ -177,6 +179,12 @@ class OracleScene:
                           y1, ptr(out), threads)
         return out.reshape(y1 - y0, x1 - x0, 4)
 
+    def render_task(self, mode, w, h, spp, firefly=False, task_seed=33, policy=REF_POLICY):
+        """pt_image_renderer::render with one task: the reference's own sequential stream."""
+        out = np.zeros((w * h, 4), dtype=np.float32)
+        self.lib.o_render_task(self.h, mode, C.byref(policy), w, h, spp, int(firefly), task_seed, ptr(out))
+        return out.reshape(h, w, 4)
+
     def bsdf_eval(self, m, n, o, i):
         f = np.zeros(3, np.float32)
         self.lib.o_bsdf_eval(self.h, m, ptr(np.asarray(n, np.float32)), ptr(np.asarray(o, np.float32)),
@@ -194,6 +202,13 @@ class OracleScene:
         a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
         self.lib.o_bvh_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
         return dict(nodes=a.value, max_depth=b.value, leaves=c.value)
+
+
+def firefly_add(est, acc):
+    """The reference's firefly clamp on one sample image est (h, w, 3), added to acc in place."""
+    est = np.ascontiguousarray(est, np.float32)
+    assert acc.dtype == np.float32 and acc.flags.c_contiguous and acc.shape == est.shape
+    oracle().o_firefly_add(ptr(est), est.shape[1], est.shape[0], ptr(acc))
 
 
 class RefScene:
@@ -239,10 +254,10 @@ class RefScene:
         self.lib.r_render_paths(self.h, mode, w, h, ptr(pixels), ptr(seeds), len(pixels), ptr(out))
         return out
 
-    def render(self, mode, w, h, spp, threads):
+    def render(self, mode, w, h, spp, threads, firefly=False):
         out = np.zeros((w * h, 4), dtype=np.float32)
         taken = C.c_uint32()
-        secs = self.lib.r_render(self.h, mode, w, h, spp, threads, ptr(out), C.byref(taken))
+        secs = self.lib.r_render(self.h, mode, w, h, spp, threads, ptr(out), C.byref(taken), int(firefly))
         return out.reshape(h, w, 4), secs, taken.value
 
     def bsdf_eval(self, m, n, o, i):

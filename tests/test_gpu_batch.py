@@ -37,3 +37,22 @@ def test_batch_rejects_bad_items(ctx):
     p = default_params(abi.MODE_REF_BDPT, 16, 16, 1)
     with pytest.raises(E8GError, match="UNSUPPORTED"):
         render_batch(ctx, [sc], [p])
+    p = default_params(abi.MODE_MIS, 16, 16, 1, firefly=1)
+    with pytest.raises(E8GError, match="UNSUPPORTED"):
+        render_batch(ctx, [sc], [p])
+
+
+def test_batch_mixes_stream_kinds(ctx):
+    """A batch whose scenes use different stream kinds (the reference's minstd, Philox) runs
+    one launch; each scene's image equals its separate render."""
+    scenes = [S.cornell(24, 24), S.cornell(24, 24)]
+    params = [default_params(abi.MODE_REF_LT1, 24, 24, 4, seed=3, rng=abi.RNG_MINSTD),
+              default_params(abi.MODE_REF_LT1, 24, 24, 4, seed=3, rng=abi.RNG_PHILOX)]
+    imgs, st = render_batch(ctx, scenes, params)
+    assert st["launches"] == 3
+    assert not np.allclose(imgs[0], imgs[1])
+    for sc, p, img in zip(scenes, params, imgs):
+        ctx.upload(sc)
+        ref = ctx.render(p)
+        close = np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-5)
+        assert close.mean() >= 0.999, close.mean()

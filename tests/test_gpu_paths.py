@@ -127,3 +127,26 @@ def test_wavefront_paths_match_oracle(ctx, rng):
     else:
         ref = osc.render_paths(abi.MODE_MIS, w, h, px, samples, policy=pol, rng=abi.RNG_PHILOX, seed=31)
     assert match_fraction(got, ref) >= 0.99
+
+
+@pytest.mark.parametrize("rng", [abi.RNG_PHILOX, abi.RNG_MINSTD])
+@pytest.mark.parametrize("max_len", [6, 3])
+def test_bdpt_power_paths_match_oracle(ctx, rng, max_len):
+    """Bidirectional with power-heuristic MIS (product mode): per-path radiance equals the
+    oracle's restatement fed the same stream."""
+    d = G.load("ico.npz")
+    sc = G.scene_from(d)
+    ctx.upload(sc)
+    osc = ob.OracleScene(sc)
+    w, h = int(d["width"]), int(d["height"])
+    px = np.random.default_rng(12).integers(0, w * h, 1500).astype(np.uint32)
+    samples = np.arange(len(px), dtype=np.uint32)
+    p = default_params(abi.MODE_BDPT_POWER, w, h, 1, seed=17, rng=rng, bdpt_max_len=max_len)
+    got = ctx.render_paths(p, px, samples)
+    pol = ob.OPolicy(0, 2, 0.5, max_len)
+    if rng == abi.RNG_MINSTD:
+        seeds = np.array([ob.oracle().o_path_seed(17, int(a), int(b)) for a, b in zip(px, samples)], np.uint32)
+        ref = osc.render_paths(abi.MODE_BDPT_POWER, w, h, px, seeds, policy=pol)
+    else:
+        ref = osc.render_paths(abi.MODE_BDPT_POWER, w, h, px, samples, policy=pol, rng=abi.RNG_PHILOX, seed=17)
+    assert match_fraction(got, ref) >= 0.99

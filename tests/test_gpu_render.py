@@ -19,7 +19,7 @@ def rel_mse(img, ref, eps=1e-2):
 
 @pytest.mark.parametrize("layout", [abi.BVH_REFERENCE, abi.BVH_SAH])
 @pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT,
-                                  abi.MODE_REF_BDPT])
+                                  abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER])
 def test_image_matches_oracle_same_streams(ctx, mode, layout):
     """Same draw streams: >= 98% of pixels agree to 1e-4; the rest are pixels with a path that
     took another branch after a last-ulp difference (sinf/cosf/atanf) or an edge tie."""
@@ -36,7 +36,8 @@ def test_image_matches_oracle_same_streams(ctx, mode, layout):
     assert rel_mse(img, ref) < 2e-3, rel_mse(img, ref)
 
 
-@pytest.mark.parametrize("mode", [abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_MIS, abi.MODE_REF_BDPT])
+@pytest.mark.parametrize("mode", [abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_MIS, abi.MODE_REF_BDPT,
+                                  abi.MODE_BDPT_POWER])
 def test_furnace(ctx, mode):
     """tst_pathtracer.cpp:58-86 on the GPU: E[sum RGB] = 1 / (1 - 0.7) * 3 = 10 within 0.3."""
     ctx.upload(S.furnace(30))
@@ -113,3 +114,45 @@ def test_wavefront_image_equals_megakernel(ctx, capacity_small):
     assert np.all(np.isfinite(wf)) and np.all(wf >= 0)
     close = np.abs(wf - mk) <= np.maximum(1e-4 * np.abs(mk), 1e-5)
     assert close.mean() >= 0.999, close.mean()
+
+
+def test_bdpt_power_converges_to_mis(ctx):
+    """Two unbiased estimators of the same truncated integral (paths of at most 6 surface
+    vertices): power-heuristic BDPT with subpaths capped at 3 and MIS with depth 5 agree on the
+    Cornell box at 1024 spp to within 1% of the frame mean."""
+    ctx.upload(S.cornell(64, 64))
+    a = ctx.render(default_params(abi.MODE_BDPT_POWER, 64, 64, 1024, seed=2, bdpt_max_len=3))[..., :3]
+    b = ctx.render(default_params(abi.MODE_MIS, 64, 64, 1024, seed=3, max_depth=5, rr_start=100, rr_prob=0.5))[..., :3]
+    assert abs(a.mean() - b.mean()) <= 0.01 * b.mean(), (a.mean(), b.mean())
+    assert rel_mse(a, b) < 5e-3
+
+
+@pytest.mark.parametrize("mode,rng", [(abi.MODE_REF_UNI, abi.RNG_MINSTD), (abi.MODE_REF_LT1, abi.RNG_MINSTD),
+                                      (abi.MODE_MIS, abi.RNG_PHILOX)])
+def test_firefly_clamp_matches_oracle(ctx, mode, rng):
+    """firefly = 1 (renderer.cpp:46-83): every sample image is clamped against its neighbours
+    before it is accumulated. The oracle renders the same paths (same streams), applies its
+    restatement of the clamp per sample and averages; the GPU image equals it on >= 98% of
+    pixels, and the clamp changes the image."""
+    sc = S.cornell(40, 32)
+    ctx.upload(sc)
+    w, h, spp = 40, 32, 6
+    p = default_params(mode, w, h, spp, seed=5, rng=rng, firefly=1)
+    got = ctx.render(p)[..., :3]
+    p.firefly = 0
+    plain = ctx.render(p)[..., :3]
+    osc = ob.OracleScene(sc)
+    pol = ob.REF_POLICY  # e8g_default_params: the reference's policy for every mode
+    px = np.arange(w * h, dtype=np.uint32)
+    acc = np.zeros((h, w, 3), np.float32)
+    for s in range(spp):
+        if rng == abi.RNG_MINSTD:
+            seeds = np.array([ob.oracle().o_path_seed(5, int(q), s) for q in px], np.uint32)
+            est = osc.render_paths(mode, w, h, px, seeds, policy=pol)
+        else:
+            est = osc.render_paths(mode, w, h, px, np.full(w * h, s, np.uint32), policy=pol, rng=rng, seed=5)
+        ob.firefly_add(est.reshape(h, w, 3), acc)
+    ref = acc * np.float32(1.0 / spp)
+    close = np.all(np.abs(got - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-6), axis=-1)
+    assert close.mean() >= 0.98, close.mean()
+    assert not np.allclose(got, plain)

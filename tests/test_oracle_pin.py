@@ -152,3 +152,48 @@ def test_oracle_matches_live_reference(reference, seed):
         a = osc.render_paths(mode, 40, 30, px, seeds)
         b = rsc.render_paths(mode, 40, 30, px, seeds)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), mode
+
+
+def test_renderer_matches_reference_golden(oracle):
+    """pt_image_renderer::render with one thread (renderer.cpp:35-166), the reference's own
+    sequential stream and its firefly clamp (renderer.cpp:46-83): the oracle reproduces the
+    compositor's buffer bit for bit, and the clamp changes the image."""
+    d = G.load("renderer.npz")
+    osc = ob.OracleScene(G.scene_from(d))
+    w, h, spp = int(d["width"]), int(d["height"]), int(d["spp"])
+    for name, mode in (("lt1", abi.MODE_REF_LT1), ("uni", abi.MODE_REF_UNI)):
+        for ff in (0, 1):
+            got = osc.render_task(mode, w, h, spp, firefly=bool(ff))
+            assert np.array_equal(got, d[f"img_{name}_ff{ff}"]), (name, ff)
+    assert not np.array_equal(d["img_uni_ff0"], d["img_uni_ff1"])
+
+
+def test_firefly_clamp_rule(oracle):
+    """The clamp on a hand-made image: an interior pixel brighter than all 8 neighbours by more
+    than 1.5 in squared norm is capped per channel at their mean squared norm + 1.5; a pixel
+    with one neighbour as bright, and border pixels, pass unchanged."""
+    est = np.full((5, 6, 3), 0.5, np.float32)
+    est[2, 2] = (3.0, 0.2, 1.0)   # squared norm 10.04 > 0.75 + 1.5 against every neighbour
+    est[0, 4] = (9.0, 9.0, 9.0)   # border
+    est[3, 4] = (2.0, 2.0, 2.0)   # interior, but its neighbour (3, 5) is as bright
+    est[3, 5] = (2.0, 2.0, 2.0)   # border
+    acc = np.zeros_like(est)
+    ob.firefly_add(est, acc)
+    cap = np.float32(0.125) * np.float32(8 * 0.75) + np.float32(1.5)
+    assert np.allclose(acc[2, 2], np.minimum(est[2, 2], cap))
+    assert acc[2, 2, 0] == cap and acc[2, 2, 1] == np.float32(0.2)
+    keep = np.ones((5, 6), bool)
+    keep[2, 2] = False
+    assert np.array_equal(acc[keep], est[keep])
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_REF_DIRECT, abi.MODE_REF_BDPT,
+                                  abi.MODE_NORMAL])
+def test_renderer_matches_live_reference(reference, mode):
+    d = G.load("furnace.npz")
+    sc = G.scene_from(d)
+    osc, rsc = ob.OracleScene(sc), ob.RefScene(sc)
+    for ff in (False, True):
+        a = osc.render_task(mode, 24, 20, 3, firefly=ff)
+        b, _, taken = rsc.render(mode, 24, 20, 3, 1, firefly=ff)
+        assert taken == 3 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), ff

@@ -177,7 +177,7 @@ gpu_image_renderer::~gpu_image_renderer() {
 e8::pt_image_renderer::numerical_stats
 gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space const &path_space,
                            e8::if_material_container const &mats, e8::if_light_sources const &light_sources,
-                           e8::if_camera const &cam, unsigned num_samps, bool /*firefly_filter*/) {
+                           e8::if_camera const &cam, unsigned num_samps, bool firefly_filter) {
     auto const &ps = dynamic_cast<gpu_path_space_layout const &>(path_space);
     auto const &mc = dynamic_cast<gpu_material_container const &>(mats);
     auto const &ls = dynamic_cast<gpu_light_sources const &>(light_sources);
@@ -211,6 +211,7 @@ gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space cons
     e8g_render_params p;
     e8g_default_params(&p, mode, w, h, num_samps);
     p.seed = 1361 + m_frame++;
+    p.firefly = firefly_filter ? 1u : 0u;
     std::vector<float> rgba(static_cast<size_t>(w) * h * 4);
     if (e8g_render(m_ctx, &p, rgba.data()) != E8G_OK)
         throw std::runtime_error(std::string("e8g: ") + e8g_last_error(m_ctx));

@@ -1,16 +1,19 @@
 // Path-replay adjoint of the product estimator (E8G_MODE_MIS): gradients of a loss on the image
 // with respect to every material's albedo (3 channels) and GGX roughness.
 //
-// Each path is recomputed from its counter-based (Philox) stream twice, nothing is stored:
-//   pass 1: its radiance L (exactly the forward render's estimate for that path);
-//   pass 2: the same walk again, keeping L_before, the radiance gathered so far. The BSDF value
-//   f_j used for the continuation at vertex j multiplies every contribution gathered after it,
-//   i.e. L - L_before; the BSDF value of the light sample at vertex j multiplies that sample's
-//   contribution only. Sampling densities and MIS weights are held fixed (weights still sum to
-//   one, so the gradient estimate stays unbiased), and since f is linear in albedo and
-//   d ln f / d r follows from GGX's D and G, each vertex adds
-//       dL/d albedo_c += w_c (C_c / albedo_c)        dL/d r += (w . C) d ln f / d r
-//   with C the contribution it multiplies and w the upstream gradient of the path's pixel / spp.
+// Each path is recomputed from its counter-based (Philox) stream; nothing is stored between the
+// forward render and the adjoint. The BSDF value f_j used for the continuation at vertex j
+// multiplies every contribution gathered after it, i.e. L - L_j with L the path's radiance and
+// L_j the radiance gathered before that scatter; the BSDF value of the light sample at vertex j
+// multiplies that sample's contribution only. Sampling densities and MIS weights are held fixed
+// (weights still sum to one, so the gradient estimate stays unbiased), and since f is linear in
+// albedo and d ln f / d r follows from GGX's D and G, each vertex adds
+//     dL/d albedo_c += w_c (C_c / albedo_c)        dL/d r += (w . C) d ln f / d r
+// with C the contribution it multiplies and w the upstream gradient of the path's pixel / spp.
+// One walk does it: light-sample terms are added at once, and the first kScatterList scatters
+// are recorded as (material, d ln f / d r, L_j) and added when the walk ends and L is known.
+// A path with more scatters than that is walked a second time for the rest (the classic
+// two-pass replay), which only paths longer than kScatterList vertices pay.
 // Gradients are summed per block in shared memory and flushed with one atomic per material.
 // Materials whose parameters do not enter f linearly (mixtures, the fail-safe material) and the
 // Oren-Nayar sigma receive no gradient.
@@ -48,14 +51,25 @@ struct GradAcc {
     uint32_t nmat;
 };
 
-__device__ __forceinline__ void add_grad(GradAcc &g, DevScene const &S, int32_t mesh, float3 n, float3 o, float3 i,
-                                         float3 C, float3 w) {
+constexpr uint32_t kScatterList = 8;
+
+struct ScatterRec {
+    int32_t mat;  // -1: no gradient (other material types)
+    float dlog;   // d ln f / d r (cook_torr), else 0
+    float3 L;     // radiance gathered before the scatter
+};
+
+// Material index receiving gradients at a vertex of this mesh, or -1.
+__device__ __forceinline__ int32_t grad_mat(DevScene const &S, uint32_t nmat, int32_t mesh) {
     int32_t mi = __ldg(&S.mesh_mat[mesh]);
-    if (mi < 0 || static_cast<uint32_t>(mi) >= g.nmat)
-        return;
+    if (mi < 0 || static_cast<uint32_t>(mi) >= nmat)
+        return -1;
+    uint32_t t = S.mats[mi].type;
+    return (t == E8G_MAT_OREN_NAYAR || t == E8G_MAT_COOK_TORR) ? mi : -1;
+}
+
+__device__ __forceinline__ void add_grad_m(GradAcc &g, DevScene const &S, int32_t mi, float dlog, float3 C, float3 w) {
     const DevMaterial &m = S.mats[mi];
-    if (m.type != E8G_MAT_OREN_NAYAR && m.type != E8G_MAT_COOK_TORR)
-        return;
     if (m.albedo[0] > 0.0f)
         atomicAdd(&g.a[3 * mi], w.x * C.x / m.albedo[0]);
     if (m.albedo[1] > 0.0f)
@@ -63,14 +77,21 @@ __device__ __forceinline__ void add_grad(GradAcc &g, DevScene const &S, int32_t 
     if (m.albedo[2] > 0.0f)
         atomicAdd(&g.a[3 * mi + 2], w.z * C.z / m.albedo[2]);
     if (m.type == E8G_MAT_COOK_TORR)
-        atomicAdd(&g.r[mi], dot(w, C) * ct_dlog_dr(m, n, o, i));
+        atomicAdd(&g.r[mi], dot(w, C) * dlog);
 }
 
-// One replay of the MIS path of megakernel/oracle order. GRAD=false returns L; GRAD=true adds
-// the gradient contributions given the path's total L and upstream weight w.
-template <bool GRAD, int LAYOUT>
+__device__ __forceinline__ float grad_dlog(DevScene const &S, int32_t mi, float3 n, float3 o, float3 i) {
+    const DevMaterial &m = S.mats[mi];
+    return m.type == E8G_MAT_COOK_TORR ? ct_dlog_dr(m, n, o, i) : 0.0f;
+}
+
+// One walk of the MIS path in megakernel/oracle order.
+// FIRST: adds the light-sample terms, records the first kScatterList scatters in `rec` and
+// counts every scatter in *nscatter; returns L. !FIRST (second walk, L = Ltot known): adds the
+// terms of scatters kScatterList and later only.
+template <bool FIRST, int LAYOUT>
 __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const &f, uint32_t pixel, uint32_t sample,
-                         float3 Ltot, float3 w, GradAcc &g, uint32_t *stk) {
+                         float3 Ltot, float3 w, GradAcc &g, uint32_t *stk, ScatterRec *rec, uint32_t *nscatter) {
     RngPhilox rng;
     rng.seed(A.seed, pixel, sample);
     float3 p = xyz(f.p), n = xyz(f.n), o = neg(xyz(f.d));
@@ -80,6 +101,7 @@ __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const 
     if (l0 >= 0)
         L = light_radiance(S, l0, o, n);
     float3 beta = f3(1.0f, 1.0f, 1.0f);
+    uint32_t scat = 0;
     for (uint32_t depth = 0;; depth++) {
         if ((A.max_depth && depth >= A.max_depth) || depth >= kHardDepth)
             break;
@@ -108,8 +130,11 @@ __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const 
                     float wgt = power_heuristic(p_l, p_b);
                     float3 c = scale(mul(mul(beta, fv), light_rad(S, light)), cos_x * wgt / p_l);
                     L = add(L, c);
-                    if (GRAD)
-                        add_grad(g, S, mesh, n, o, wi, c, w);
+                    if (FIRST) {
+                        int32_t mi = grad_mat(S, g.nmat, mesh);
+                        if (mi >= 0)
+                            add_grad_m(g, S, mi, grad_dlog(S, mi, n, o, wi), c, w);
+                    }
                 }
             }
         }
@@ -121,8 +146,19 @@ __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const 
         if (cw <= 0.0f)
             break;
         float3 fv = bsdf_eval(S, m, n, o, i);
-        if (GRAD)
-            add_grad(g, S, mesh, n, o, i, sub(Ltot, L), w); // everything gathered after this scatter
+        if (FIRST) {
+            if (scat < kScatterList) {
+                int32_t mi = grad_mat(S, g.nmat, mesh);
+                rec[scat].mat = mi;
+                rec[scat].dlog = mi >= 0 ? grad_dlog(S, mi, n, o, i) : 0.0f;
+                rec[scat].L = L;
+            }
+        } else if (scat >= kScatterList) {
+            int32_t mi = grad_mat(S, g.nmat, mesh);
+            if (mi >= 0)
+                add_grad_m(g, S, mi, grad_dlog(S, mi, n, o, i), sub(Ltot, L), w); // gathered after this scatter
+        }
+        scat++;
         beta = mul(beta, scale(fv, cw / pdf));
         Hit h = trace_closest_l<LAYOUT, false>(S, p, i, stk, nullptr);
         if (h.tri == 0xFFFFFFFFu)
@@ -143,6 +179,8 @@ __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const 
         mesh = nv.mesh;
         o = neg(i);
     }
+    if (FIRST)
+        *nscatter = scat;
     return L;
 }
 
@@ -168,29 +206,23 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(DevScene S, RenderArgs A, Fi
             break;
         uint64_t idx = base + lane;
         if (idx < A.total_paths) {
-            uint32_t pixel, sample;
-            bool ok;
-            if (A.list_pixel) {
-                pixel = A.list_pixel[idx];
-                sample = A.list_sample[idx];
-                ok = true;
-            } else {
-                uint32_t s = static_cast<uint32_t>(idx / A.paths_per_sample);
-                uint32_t j = static_cast<uint32_t>(idx - static_cast<uint64_t>(s) * A.paths_per_sample);
-                uint32_t tile = j >> 5, wl = j & 31u;
-                uint32_t x = (tile % A.tiles_x) * 8 + (wl & 7u), y = (tile / A.tiles_x) * 4 + (wl >> 3);
-                ok = x < A.width && y < A.height;
-                pixel = y * A.width + x;
-                sample = A.sample_offset + s;
-            }
+            uint32_t pixel, sample, out;
+            bool ok = path_coords(A, idx, pixel, sample, out);
             if (ok) {
                 FirstHit f = fh[pixel];
                 if (__float_as_int(f.p.w) >= 0) {
                     float3 w = scale(f3(dl_dimage[3 * static_cast<size_t>(pixel)], dl_dimage[3 * static_cast<size_t>(pixel) + 1],
                                         dl_dimage[3 * static_cast<size_t>(pixel) + 2]),
                                      inv_spp);
-                    float3 Ltot = replay<false, LAYOUT>(S, A, f, pixel, sample, f3(0, 0, 0), w, g, stk);
-                    replay<true, LAYOUT>(S, A, f, pixel, sample, Ltot, w, g, stk);
+                    ScatterRec rec[kScatterList];
+                    uint32_t ns = 0;
+                    float3 Ltot = replay<true, LAYOUT>(S, A, f, pixel, sample, f3(0, 0, 0), w, g, stk, rec, &ns);
+                    uint32_t nl = ns < kScatterList ? ns : kScatterList;
+                    for (uint32_t j = 0; j < nl; j++)
+                        if (rec[j].mat >= 0)
+                            add_grad_m(g, S, rec[j].mat, rec[j].dlog, sub(Ltot, rec[j].L), w);
+                    if (ns > kScatterList)
+                        replay<false, LAYOUT>(S, A, f, pixel, sample, Ltot, w, g, stk, nullptr, nullptr);
                     if (path_rgb) {
                         path_rgb[3 * idx] = Ltot.x;
                         path_rgb[3 * idx + 1] = Ltot.y;

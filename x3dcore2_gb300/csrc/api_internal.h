@@ -39,7 +39,7 @@ struct e8g_ctx {
     // render scratch
     e8g::dev_buffer b_fh, b_accum, b_work, b_img, b_io0, b_io1, b_counts;
     // wavefront queues and adjoint state
-    e8g::dev_buffer b_wf, b_grad;
+    e8g::dev_buffer b_wf, b_grad, b_ff; // b_ff: per-sample images of the firefly clamp
     e8g_render_params fwd_params{};
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test

@@ -47,6 +47,8 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         uint32_t m = items[k].params.mode;
         if (m == E8G_MODE_REF_BDPT || m == E8G_MODE_BDPT_POWER)
             return fail(c, E8G_ERR_UNSUPPORTED, "batches run the unidirectional integrators");
+        if (items[k].params.firefly)
+            return fail(c, E8G_ERR_UNSUPPORTED, "batches do not run the firefly clamp");
     }
     cudaSetDevice(c->device);
     // host: pack, build, stage
@@ -59,6 +61,9 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     std::vector<packed_scene> packs(n);
     std::vector<RenderArgs> args(n);
     std::vector<uint64_t> path_prefix(n + 1, 0), pix_prefix(n + 1, 0);
+    uint32_t rng_kinds = 0;
+    for (uint32_t k = 0; k < n; k++)
+        rng_kinds |= 1u << items[k].params.rng;
     try {
         for (uint32_t k = 0; k < n; k++) {
             packed_scene &p = packs[k];
@@ -158,8 +163,8 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         return cuda_fail(c, e, "batch clear");
     cudaEventRecord(c->ev2, c->stream);
     launch_megakernel_batch(B, static_cast<FirstHit const *>(c->b_fh.ptr), static_cast<float4 *>(c->b_accum.ptr),
-                            static_cast<unsigned long long *>(c->b_work.ptr),
-                            persistent_grid(c, megakernel_batch_blocks_per_sm()), c->stream);
+                            static_cast<unsigned long long *>(c->b_work.ptr), rng_kinds,
+                            persistent_grid(c, megakernel_batch_blocks_per_sm(rng_kinds)), c->stream);
     cudaEventRecord(c->ev3, c->stream);
     launch_resolve_batch(B, total_pix, static_cast<float4 const *>(c->b_accum.ptr), static_cast<float *>(c->b_img.ptr),
                          c->stream);

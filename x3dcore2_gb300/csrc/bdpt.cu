@@ -135,6 +135,160 @@ __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, P
     return rad;
 }
 
+// ---- E8G_MODE_BDPT_POWER: bidirectional with power-heuristic MIS (product mode) ----
+// Camera subpath from the cached first hit, light subpath from an area-weighted emission sample
+// with a cosine direction, every (s, t >= 1) connection, weighted by the power heuristic over the
+// strategies that could produce the same path under the subpath caps. Per vertex: throughput and
+// the forward / reverse densities in area measure; a connection updates the four densities it
+// changes and restores them afterwards (Veach's recurrence).
+
+struct BV {
+    float3 p, n;
+    int32_t mesh;
+    float3 beta;
+    float fwd, rev;
+};
+
+__device__ __forceinline__ float to_area(float pdf_w, float3 from, float3 to, float3 n_to) {
+    float3 d = sub(to, from);
+    float d2 = dot(d, d);
+    if (d2 <= 0.0f)
+        return 0.0f;
+    float c = fabsf(dot(n_to, d)) / sqrtf(d2);
+    return pdf_w * c / d2;
+}
+
+__device__ __forceinline__ float vpdf(DevScene const &S, BV const &v, float3 wo, float3 wi) {
+    return bsdf_pdf(S, vert_mat(S, v.mesh), v.n, wo, wi);
+}
+
+template <class R>
+__device__ uint32_t bdp_walk(DevScene const &S, R &rng, BV *path, uint32_t len, uint32_t max_len, float3 wo,
+                             uint32_t *stk) {
+    while (len < max_len) {
+        BV &cur = path[len - 1];
+        const DevMaterial &m = vert_mat(S, cur.mesh);
+        float pdf;
+        float3 i = bsdf_sample_mis(S, m, rng, pdf, cur.n, wo);
+        if (!(pdf > 0.0f))
+            break;
+        float cw = dot(cur.n, i);
+        if (cw <= 0.0f)
+            break;
+        float3 f = bsdf_eval(S, m, cur.n, wo, i);
+        Hit h = trace_closest<false>(S, cur.p, i, stk, nullptr);
+        if (h.tri == 0xFFFFFFFFu)
+            break;
+        Vert nv = make_vert(S, h);
+        if (dot(nv.n, neg(i)) <= 0.0f)
+            break;
+        BV &nx = path[len];
+        nx.p = nv.p;
+        nx.n = nv.n;
+        nx.mesh = nv.mesh;
+        nx.beta = mul(cur.beta, scale(f, cw / pdf));
+        nx.fwd = to_area(pdf, cur.p, nx.p, nx.n);
+        nx.rev = 0.0f;
+        float prev_w = vpdf(S, cur, i, wo);
+        if (len >= 2)
+            path[len - 2].rev = to_area(prev_w, cur.p, path[len - 2].p, path[len - 2].n);
+        wo = neg(i);
+        len++;
+    }
+    return len;
+}
+
+__device__ float3 connect_power(DevScene const &S, BV *cam, uint32_t clen, BV *lp, uint32_t llen, uint32_t maxlen,
+                                float3 o0, int light, uint32_t *stk) {
+    float3 L = f3(0, 0, 0);
+    for (uint32_t t = 1; t <= clen; t++) {
+        for (uint32_t sl = 0; sl <= llen; sl++) {
+            BV &cv = cam[t - 1];
+            float3 wo_c = t >= 2 ? normalize(sub(cam[t - 2].p, cv.p)) : o0;
+            float3 contrib;
+            float save_c_rev = cv.rev, save_c2_rev = t >= 2 ? cam[t - 2].rev : 0.0f;
+            float save_l_rev = sl >= 1 ? lp[sl - 1].rev : 0.0f, save_l2_rev = sl >= 2 ? lp[sl - 2].rev : 0.0f;
+            if (sl == 0) {
+                int hl = __ldg(&S.mesh_light[cv.mesh]);
+                if (hl < 0)
+                    continue;
+                float3 le = light_radiance(S, hl, wo_c, cv.n);
+                if (vequals0(le))
+                    continue;
+                contrib = mul(cv.beta, le);
+                float pl = __ldg(&S.light_pnorm[hl]) / S.total_power;
+                cv.rev = pl * (1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]));
+                if (t >= 2) {
+                    float ew = fmaxf(dot(cv.n, wo_c), 0.0f) / kPi;
+                    cam[t - 2].rev = to_area(ew, cv.p, cam[t - 2].p, cam[t - 2].n);
+                }
+            } else {
+                BV &lv = lp[sl - 1];
+                float3 d = sub(lv.p, cv.p);
+                float d2 = dot(d, d);
+                if (d2 <= 0.0f)
+                    continue;
+                float dist = sqrtf(d2);
+                float3 dir = divs(d, dist);
+                float cos_c = dot(cv.n, dir);
+                float cos_l = dot(lv.n, neg(dir));
+                if (cos_c <= 0.0f || cos_l <= 0.0f)
+                    continue;
+                float3 fc = bsdf_eval(S, vert_mat(S, cv.mesh), cv.n, wo_c, dir);
+                if (vequals0(fc))
+                    continue;
+                float3 fl, wo_l = f3(0, 0, 0);
+                if (sl == 1) {
+                    fl = light_radiance(S, light, neg(dir), lv.n);
+                } else {
+                    wo_l = normalize(sub(lp[sl - 2].p, lv.p));
+                    fl = bsdf_eval(S, vert_mat(S, lv.mesh), lv.n, neg(dir), wo_l);
+                }
+                if (vequals0(fl))
+                    continue;
+                if (trace_any<false>(S, cv.p, dir, 1e-4f, dist - 1e-3f, stk, nullptr))
+                    continue;
+                float G = cos_c * cos_l / d2;
+                contrib = scale(mul(mul(mul(cv.beta, fc), fl), lv.beta), G);
+                float pc = vpdf(S, cv, wo_c, dir);
+                lv.rev = to_area(pc, cv.p, lv.p, lv.n);
+                if (sl == 1)
+                    cv.rev = to_area(cos_l / kPi, lv.p, cv.p, cv.n);
+                else
+                    cv.rev = to_area(vpdf(S, lv, wo_l, neg(dir)), lv.p, cv.p, cv.n);
+                if (t >= 2)
+                    cam[t - 2].rev = to_area(vpdf(S, cv, dir, wo_c), cv.p, cam[t - 2].p, cam[t - 2].n);
+                if (sl >= 2)
+                    lp[sl - 2].rev = to_area(vpdf(S, lv, neg(dir), wo_l), lv.p, lp[sl - 2].p, lp[sl - 2].n);
+            }
+            double sum = 0.0, ri = 1.0;
+            for (int i = static_cast<int>(t) - 1; i >= 1; i--) {
+                if (sl + t - static_cast<uint32_t>(i) > maxlen)
+                    break;
+                ri *= (cam[i].fwd > 0.0f) ? static_cast<double>(cam[i].rev) / cam[i].fwd : 0.0;
+                sum += ri * ri;
+            }
+            ri = 1.0;
+            for (int i = static_cast<int>(sl) - 1; i >= 0; i--) {
+                if (t + sl - static_cast<uint32_t>(i) > maxlen)
+                    break;
+                ri *= (lp[i].fwd > 0.0f) ? static_cast<double>(lp[i].rev) / lp[i].fwd : 0.0;
+                sum += ri * ri;
+            }
+            float wgt = static_cast<float>(1.0 / (1.0 + sum));
+            L = add(L, scale(contrib, wgt));
+            cv.rev = save_c_rev;
+            if (t >= 2)
+                cam[t - 2].rev = save_c2_rev;
+            if (sl >= 1)
+                lp[sl - 1].rev = save_l_rev;
+            if (sl >= 2)
+                lp[sl - 2].rev = save_l2_rev;
+        }
+    }
+    return L;
+}
+
 template <class R> __device__ __forceinline__ void seed_path(R &rng, RenderArgs const &A, uint64_t mix, uint32_t px, uint32_t s);
 template <> __device__ __forceinline__ void seed_path<RngMinstd>(RngMinstd &rng, RenderArgs const &, uint64_t mix,
                                                                 uint32_t px, uint32_t s) {
@@ -145,25 +299,6 @@ template <> __device__ __forceinline__ void seed_path<RngPhilox>(RngPhilox &rng,
     rng.seed(A.seed, px, s);
 }
 
-__device__ __forceinline__ bool coords(RenderArgs const &A, uint64_t idx, uint32_t &pixel, uint32_t &sample,
-                                       uint32_t &out) {
-    if (A.list_pixel) {
-        pixel = A.list_pixel[idx];
-        sample = A.list_sample[idx];
-        out = static_cast<uint32_t>(idx);
-        return true;
-    }
-    uint32_t s = static_cast<uint32_t>(idx / A.paths_per_sample);
-    uint32_t j = static_cast<uint32_t>(idx - static_cast<uint64_t>(s) * A.paths_per_sample);
-    uint32_t tile = j >> 5, w = j & 31u;
-    uint32_t x = (tile % A.tiles_x) * 8 + (w & 7u), y = (tile / A.tiles_x) * 4 + (w >> 3);
-    if (x >= A.width || y >= A.height)
-        return false;
-    pixel = y * A.width + x;
-    sample = A.sample_offset + s;
-    out = pixel;
-    return true;
-}
 
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
@@ -183,7 +318,7 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
             break;
         uint64_t idx = base + lane;
         uint32_t pixel, sample, out;
-        if (idx < A.total_paths && coords(A, idx, pixel, sample, out)) {
+        if (idx < A.total_paths && path_coords(A, idx, pixel, sample, out)) {
             R rng;
             seed_path(rng, A, mix, pixel, sample);
             FirstHit f = fh[pixel];
@@ -231,6 +366,83 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
     }
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
+                                                       float4 *accum, float *path_rgb, unsigned long long *work) {
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *stk = stk_all + threadIdx.x;
+    const uint64_t mix = splitmix64(A.seed);
+    const uint32_t lane = lane_id();
+    const uint32_t max_len = A.bdpt_max_len < kMaxSub ? A.bdpt_max_len : kMaxSub;
+    BV cam[kMaxSub], lp[kMaxSub];
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32ull);
+        base = __shfl_sync(~0u, base, 0);
+        if (base >= A.total_paths)
+            break;
+        uint64_t idx = base + lane;
+        uint32_t pixel, sample, out;
+        if (idx < A.total_paths && path_coords(A, idx, pixel, sample, out)) {
+            R rng;
+            seed_path(rng, A, mix, pixel, sample);
+            FirstHit f = fh[pixel];
+            int32_t mesh = __float_as_int(f.p.w);
+            float3 o0 = neg(xyz(f.d));
+            uint32_t clen = 0, llen = 0;
+            if (mesh >= 0 && max_len) {
+                cam[0].p = xyz(f.p);
+                cam[0].n = xyz(f.n);
+                cam[0].mesh = mesh;
+                cam[0].beta = f3(1.0f, 1.0f, 1.0f);
+                cam[0].fwd = 1.0f;
+                cam[0].rev = 0.0f;
+                clen = bdp_walk(S, rng, cam, 1, max_len, o0, stk);
+            }
+            float pmf;
+            int light = sample_light(S, rng, pmf);
+            uint32_t lmesh = __ldg(&S.light_mesh[light]);
+            Surf em = mesh_sample(S, lmesh, rng, true);
+            float3 w = cos_hemisphere(em.n, rng);
+            float pdf_w = dot(em.n, w) / kPi;
+            if (max_len) {
+                lp[0].p = em.p;
+                lp[0].n = em.n;
+                lp[0].mesh = static_cast<int32_t>(lmesh);
+                lp[0].fwd = pmf * em.area_dens;
+                lp[0].rev = 0.0f;
+                float ib = 1.0f / lp[0].fwd;
+                lp[0].beta = f3(ib, ib, ib);
+                llen = 1;
+                if (pdf_w > 0.0f && max_len > 1) {
+                    Hit h = trace_closest<false>(S, em.p, w, stk, nullptr);
+                    if (h.tri != 0xFFFFFFFFu) {
+                        Vert v0 = make_vert(S, h);
+                        if (dot(v0.n, neg(w)) > 0.0f) {
+                            lp[1].p = v0.p;
+                            lp[1].n = v0.n;
+                            lp[1].mesh = v0.mesh;
+                            lp[1].beta = scale(light_rad(S, light), dot(em.n, w) / (pdf_w * lp[0].fwd));
+                            lp[1].fwd = to_area(pdf_w, em.p, lp[1].p, lp[1].n);
+                            lp[1].rev = 0.0f;
+                            llen = bdp_walk(S, rng, lp, 2, max_len, neg(w), stk);
+                        }
+                    }
+                }
+            }
+            float3 L = clen ? connect_power(S, cam, clen, lp, llen, max_len, o0, light, stk) : f3(0, 0, 0);
+            if (path_rgb) {
+                path_rgb[3 * static_cast<size_t>(out)] = L.x;
+                path_rgb[3 * static_cast<size_t>(out) + 1] = L.y;
+                path_rgb[3 * static_cast<size_t>(out) + 2] = L.z;
+            } else {
+                atomicAdd(&accum[out], make_float4(L.x, L.y, L.z, 0.0f));
+            }
+        }
+    }
+}
+
 } // namespace
 
 int bdpt_blocks_per_sm() {
@@ -241,6 +453,13 @@ int bdpt_blocks_per_sm() {
 
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                  unsigned long long *work, int grid, cudaStream_t st) {
+    if (A.mode == E8G_MODE_BDPT_POWER) {
+        if (A.rng == E8G_RNG_MINSTD)
+            k_bdpt_power<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+        else
+            k_bdpt_power<RngPhilox><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+        return;
+    }
     if (A.rng == E8G_RNG_MINSTD)
         k_bdpt_ref<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
     else

@@ -62,7 +62,32 @@ struct RenderArgs {
     uint64_t total_paths;       // paths_per_sample * spp (or the explicit list length)
     const uint32_t *list_pixel; // explicit (pixel, sample) list, or null
     const uint32_t *list_sample;
+    uint32_t sample_major;      // image mode: per-path output at (sample - sample_offset) * W * H + pixel
 };
+
+// Map a path index to (pixel, sample) and its output slot: the list index (explicit lists), the
+// pixel (image accumulation) or sample * W * H + pixel (per-sample images). Consecutive path
+// indices cover 8x4 pixel tiles, one warp per tile, so a warp's first hits are neighbours.
+// Returns false for padding lanes outside the image.
+__device__ __forceinline__ bool path_coords(RenderArgs const &A, uint64_t idx, uint32_t &pixel, uint32_t &sample,
+                                            uint32_t &out) {
+    if (A.list_pixel) {
+        pixel = A.list_pixel[idx];
+        sample = A.list_sample[idx];
+        out = static_cast<uint32_t>(idx);
+        return true;
+    }
+    uint32_t s = static_cast<uint32_t>(idx / A.paths_per_sample);
+    uint32_t j = static_cast<uint32_t>(idx - static_cast<uint64_t>(s) * A.paths_per_sample);
+    uint32_t tile = j >> 5, w = j & 31u;
+    uint32_t x = (tile % A.tiles_x) * 8 + (w & 7u), y = (tile / A.tiles_x) * 4 + (w >> 3);
+    if (x >= A.width || y >= A.height)
+        return false;
+    pixel = y * A.width + x;
+    sample = A.sample_offset + s;
+    out = A.sample_major ? s * (A.width * A.height) + pixel : pixel;
+    return true;
+}
 
 // Per-pixel cached primary hit (compute_first_hit, pathtracer.cpp:456-472).
 struct FirstHit {

@@ -18,6 +18,8 @@ void launch_trace_any(DevScene const &S, float const *rays6, float const *tmin, 
 void launch_trace_closest_counted(DevScene const &S, float const *rays6, uint32_t n, float *hits5,
                                   unsigned long long *counters, cudaStream_t st);
 void launch_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rgba, cudaStream_t st);
+// Firefly clamp of K sample-major per-sample images (W*H rgb each), added to accum in sample order.
+void launch_firefly(float const *est, uint32_t K, uint32_t w, uint32_t h, float4 *accum, cudaStream_t st);
 
 // Megakernel integrator (one thread per path, persistent threads refilled warp-wide).
 // counters (when non-null): [0] rays, [1] nodes, [2] tris.
@@ -34,9 +36,10 @@ struct BatchDev {
     uint32_t n;
     uint64_t total_paths;
 };
+// rng_kinds: bit (1 << E8G_RNG_*) set for every stream kind some scene of the batch uses.
 void launch_megakernel_batch(BatchDev const &B, FirstHit const *fh_all, float4 *accum_all, unsigned long long *work,
-                             int grid, cudaStream_t st);
-int megakernel_batch_blocks_per_sm();
+                             uint32_t rng_kinds, int grid, cudaStream_t st);
+int megakernel_batch_blocks_per_sm(uint32_t rng_kinds);
 void launch_first_hits_batch(BatchDev const &B, DevScene const *h_scenes, RenderArgs const *h_args,
                              uint64_t const *h_pix_prefix, FirstHit *fh_all, cudaStream_t st);
 void launch_resolve_batch(BatchDev const &B, uint64_t total_pix, float4 const *accum_all, float *rgba_all,

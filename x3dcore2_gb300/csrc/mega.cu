@@ -26,27 +26,6 @@ struct PathState {
     uint32_t pixel, out; // out: pixel (image) or list index (per-path output)
 };
 
-// Map a path index to (pixel, sample); returns false for padding lanes outside the image.
-__device__ __forceinline__ bool path_coords(RenderArgs const &A, uint64_t idx, uint32_t &pixel, uint32_t &sample,
-                                            uint32_t &out) {
-    if (A.list_pixel) {
-        pixel = A.list_pixel[idx];
-        sample = A.list_sample[idx];
-        out = static_cast<uint32_t>(idx);
-        return true;
-    }
-    uint32_t s = static_cast<uint32_t>(idx / A.paths_per_sample);
-    uint32_t j = static_cast<uint32_t>(idx - static_cast<uint64_t>(s) * A.paths_per_sample);
-    uint32_t tile = j >> 5, w = j & 31u;
-    uint32_t tx = tile % A.tiles_x, ty = tile / A.tiles_x;
-    uint32_t x = tx * 8 + (w & 7u), y = ty * 4 + (w >> 3);
-    if (x >= A.width || y >= A.height)
-        return false;
-    pixel = y * A.width + x;
-    sample = A.sample_offset + s;
-    out = pixel;
-    return true;
-}
 
 template <class R> __device__ __forceinline__ void seed_rng(R &rng, RenderArgs const &A, uint64_t mix, uint32_t px, uint32_t s);
 template <> __device__ __forceinline__ void seed_rng<RngMinstd>(RngMinstd &rng, RenderArgs const &, uint64_t mix,
@@ -56,6 +35,23 @@ template <> __device__ __forceinline__ void seed_rng<RngMinstd>(RngMinstd &rng, 
 template <> __device__ __forceinline__ void seed_rng<RngPhilox>(RngPhilox &rng, RenderArgs const &A, uint64_t,
                                                                uint32_t px, uint32_t s) {
     rng.seed(A.seed, px, s);
+}
+
+// Either stream, chosen per path from its scene's RenderArgs: batches whose scenes mix the
+// reference's minstd streams and Philox.
+struct RngAny {
+    RngPhilox p;
+    RngMinstd m;
+    bool philox;
+    __device__ __forceinline__ float next() { return philox ? p.next() : m.next(); }
+};
+template <> __device__ __forceinline__ void seed_rng<RngAny>(RngAny &rng, RenderArgs const &A, uint64_t mix,
+                                                            uint32_t px, uint32_t s) {
+    rng.philox = A.rng == E8G_RNG_PHILOX;
+    if (rng.philox)
+        rng.p.seed(A.seed, px, s);
+    else
+        rng.m.seed(path_seed(mix, px, s));
 }
 
 __device__ __forceinline__ void emit(RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t out, float3 L) {
@@ -378,14 +374,25 @@ __global__ void __launch_bounds__(kBlock) k_mega_batch(BatchDev B, FirstHit cons
 
 } // namespace
 
+// rng_kinds: bit E8G_RNG_MINSTD / bit E8G_RNG_PHILOX set when some scene of the batch uses it.
 void launch_megakernel_batch(BatchDev const &B, FirstHit const *fh_all, float4 *accum_all, unsigned long long *work,
-                             int grid, cudaStream_t st) {
-    k_mega_batch<RngPhilox><<<grid, kBlock, 0, st>>>(B, fh_all, accum_all, work);
+                             uint32_t rng_kinds, int grid, cudaStream_t st) {
+    if (rng_kinds == (1u << E8G_RNG_PHILOX))
+        k_mega_batch<RngPhilox><<<grid, kBlock, 0, st>>>(B, fh_all, accum_all, work);
+    else if (rng_kinds == (1u << E8G_RNG_MINSTD))
+        k_mega_batch<RngMinstd><<<grid, kBlock, 0, st>>>(B, fh_all, accum_all, work);
+    else
+        k_mega_batch<RngAny><<<grid, kBlock, 0, st>>>(B, fh_all, accum_all, work);
 }
 
-int megakernel_batch_blocks_per_sm() {
+int megakernel_batch_blocks_per_sm(uint32_t rng_kinds) {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mega_batch<RngPhilox>, kBlock, 0);
+    if (rng_kinds == (1u << E8G_RNG_PHILOX))
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mega_batch<RngPhilox>, kBlock, 0);
+    else if (rng_kinds == (1u << E8G_RNG_MINSTD))
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mega_batch<RngMinstd>, kBlock, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mega_batch<RngAny>, kBlock, 0);
     return n > 0 ? n : 1;
 }
 

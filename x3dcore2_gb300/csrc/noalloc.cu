@@ -74,8 +74,8 @@ extern "C" e8g_status e8g_render_dev_noalloc(e8g_ctx *c, e8g_render_params const
     size_t npix = static_cast<size_t>(p->width) * p->height;
     if (npix > kNoallocPixels)
         return fail(c, E8G_ERR_INVALID_ARG, "e8g_render_dev_noalloc: image larger than E8G_NOALLOC_MAX_PIXELS (65536)");
-    if (p->mode == E8G_MODE_BDPT_POWER)
-        return fail(c, E8G_ERR_UNSUPPORTED, "mode not available");
+    if (p->firefly)
+        return fail(c, E8G_ERR_UNSUPPORTED, "e8g_render_dev_noalloc: the firefly clamp needs per-sample image buffers");
     cudaError_t e = cudaSetDevice(c->device);
     unsigned char *base = nullptr;
     if (e == cudaSuccess)
@@ -94,7 +94,7 @@ extern "C" e8g_status e8g_render_dev_noalloc(e8g_ctx *c, e8g_render_params const
         return cuda_fail(c, e, "no-alloc clear");
     launch_first_hits(c->dev, p->width, p->height, fh, st);
     RenderArgs A = make_args(p);
-    if (A.mode == E8G_MODE_REF_BDPT)
+    if (A.mode == E8G_MODE_REF_BDPT || A.mode == E8G_MODE_BDPT_POWER)
         launch_bdpt(c->dev, A, fh, accum, nullptr, work, persistent_grid(c, bdpt_blocks_per_sm()), st);
     else
         launch_megakernel(c->dev, A, fh, accum, nullptr, work, nullptr, persistent_grid(c, megakernel_blocks_per_sm()),

@@ -26,13 +26,45 @@ e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs con
         return cuda_fail(c, e, "work counter");
     auto *work = static_cast<unsigned long long *>(c->b_work.ptr);
     auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
-    if (A.mode == E8G_MODE_REF_BDPT) {
+    if (A.mode == E8G_MODE_REF_BDPT || A.mode == E8G_MODE_BDPT_POWER) {
         launch_bdpt(c->dev, A, fh, accum, path_rgb, work, persistent_grid(c, bdpt_blocks_per_sm()), c->stream);
     } else {
         int grid = persistent_grid(c, megakernel_blocks_per_sm());
         launch_megakernel(c->dev, A, fh, accum, path_rgb, work, d_counts, grid, c->stream);
     }
     c->launches++;
+    return E8G_OK;
+}
+
+// The firefly clamp compares each pixel with its neighbours within one sample of the whole image
+// (renderer.cpp:46-83), so samples are rendered in chunks of K per-sample images (sample-major
+// per-path output, at most 1 GiB), each chunk clamped and added to the accumulator in sample
+// order. The paths and their streams are those of the unclamped render.
+e8g_status run_firefly(e8g_ctx *c, e8g_render_params const *p, RenderArgs const &A, float4 *accum,
+                       unsigned long long *d_counts) {
+    size_t npix = static_cast<size_t>(p->width) * p->height;
+    size_t per_sample = npix * 3 * sizeof(float);
+    uint32_t K = static_cast<uint32_t>(std::max<size_t>(1, std::min<size_t>(p->spp, (size_t(1) << 30) / per_sample)));
+    cudaError_t e = c->b_ff.reserve(K * per_sample);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "firefly sample images");
+    float *est = static_cast<float *>(c->b_ff.ptr);
+    for (uint32_t s0 = 0; s0 < p->spp; s0 += K) {
+        uint32_t k = std::min(K, p->spp - s0);
+        RenderArgs B = A;
+        B.spp = k;
+        B.sample_offset = A.sample_offset + s0;
+        B.total_paths = static_cast<uint64_t>(A.paths_per_sample) * k;
+        B.sample_major = 1;
+        e = cudaMemsetAsync(est, 0, k * per_sample, c->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "firefly clear");
+        e8g_status s = run_integrator(c, p, B, nullptr, est, d_counts);
+        if (s != E8G_OK)
+            return s;
+        launch_firefly(est, k, p->width, p->height, accum, c->stream);
+        c->launches++;
+    }
     return E8G_OK;
 }
 
@@ -94,9 +126,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
 }
 
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts) {
-    if (p->mode == E8G_MODE_BDPT_POWER)
-        return fail(c, E8G_ERR_UNSUPPORTED, "power-heuristic BDPT is not available yet");
-    if (counts && p->mode == E8G_MODE_REF_BDPT)
+    if (counts && (p->mode == E8G_MODE_REF_BDPT || p->mode == E8G_MODE_BDPT_POWER))
         return fail(c, E8G_ERR_UNSUPPORTED, "traversal counters cover the unidirectional integrators");
     c->launches = 0;
     size_t npix = static_cast<size_t>(p->width) * p->height;
@@ -117,7 +147,10 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
         return cuda_fail(c, e, "render clear");
     RenderArgs A = make_args(p);
     cudaEventRecord(c->ev2, c->stream);
-    s = run_integrator(c, p, A, static_cast<float4 *>(c->b_accum.ptr), nullptr, d_counts);
+    if (p->firefly)
+        s = run_firefly(c, p, A, static_cast<float4 *>(c->b_accum.ptr), d_counts);
+    else
+        s = run_integrator(c, p, A, static_cast<float4 *>(c->b_accum.ptr), nullptr, d_counts);
     if (s != E8G_OK)
         return s;
     cudaEventRecord(c->ev3, c->stream);
@@ -149,8 +182,6 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
 
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,
                        uint32_t n, float *d_rgb) {
-    if (p->mode == E8G_MODE_BDPT_POWER)
-        return fail(c, E8G_ERR_UNSUPPORTED, "power-heuristic BDPT is not available yet");
     c->launches = 0;
     e8g_status s = first_hits(c, p->width, p->height);
     if (s != E8G_OK)

@@ -104,6 +104,51 @@ __global__ void k_resolve(float4 const *accum, uint32_t npix, float inv_spp, flo
     reinterpret_cast<float4 *>(rgba)[i] = make_float4(a.x * inv_spp, a.y * inv_spp, a.z * inv_spp, 1.0f);
 }
 
+// pt_image_renderer's firefly clamp (renderer.cpp:46-83) over K per-sample images est
+// (sample-major, W*H rgb each), accumulated per pixel in sample order like the reference's task
+// estimate: an interior pixel whose squared norm exceeds each of its 8 neighbours' by more than
+// 1.5 (renderer.h:118) has every channel capped at the neighbours' mean squared norm plus 1.5.
+__device__ __forceinline__ float sqnorm(float const *v) {
+    float r = 0.0f;
+    r += v[0] * v[0];
+    r += v[1] * v[1];
+    r += v[2] * v[2];
+    return r;
+}
+
+__global__ void k_firefly(float const *__restrict__ est, uint32_t K, uint32_t w, uint32_t h, float4 *accum) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t npix = w * h;
+    if (i >= npix)
+        return;
+    uint32_t x = i % w, y = i / w;
+    bool inner = x > 0 && x < w - 1 && y > 0 && y < h - 1;
+    const float diff = 1.5f;
+    float4 a = accum[i];
+    for (uint32_t k = 0; k < K; k++) {
+        float const *e = est + 3 * (static_cast<size_t>(k) * npix + i);
+        float v0 = e[0], v1 = e[1], v2 = e[2];
+        if (inner) {
+            size_t row = 3 * static_cast<size_t>(w);
+            float r00 = sqnorm(e - row - 3), r10 = sqnorm(e - row), r20 = sqnorm(e - row + 3);
+            float r01 = sqnorm(e - 3), r11 = sqnorm(e), r21 = sqnorm(e + 3);
+            float r02 = sqnorm(e + row - 3), r12 = sqnorm(e + row), r22 = sqnorm(e + row + 3);
+            bool ff = (r11 - r00) > diff && (r11 - r10) > diff && (r11 - r20) > diff && (r11 - r01) > diff &&
+                      (r11 - r21) > diff && (r11 - r02) > diff && (r11 - r12) > diff && (r11 - r22) > diff;
+            if (ff) {
+                float cap = 1.0f / 8.0f * (r00 + r10 + r20 + r01 + r21 + r02 + r12 + r22) + diff;
+                v0 = cap < v0 ? cap : v0;
+                v1 = cap < v1 ? cap : v1;
+                v2 = cap < v2 ? cap : v2;
+            }
+        }
+        a.x += v0;
+        a.y += v1;
+        a.z += v2;
+    }
+    accum[i] = a;
+}
+
 static inline int blocks(uint32_t n, int b) { return static_cast<int>((n + b - 1) / b); }
 
 void launch_first_hits(DevScene const &S, uint32_t w, uint32_t h, FirstHit *out, cudaStream_t st) {
@@ -128,6 +173,9 @@ void launch_trace_any(DevScene const &S, float const *rays6, float const *tmin, 
 }
 void launch_resolve(float4 const *accum, uint32_t npix, float inv_spp, float *rgba, cudaStream_t st) {
     k_resolve<<<blocks(npix, 256), 256, 0, st>>>(accum, npix, inv_spp, rgba);
+}
+void launch_firefly(float const *est, uint32_t K, uint32_t w, uint32_t h, float4 *accum, cudaStream_t st) {
+    k_firefly<<<blocks(w * h, 256), 256, 0, st>>>(est, K, w, h, accum);
 }
 
 } // namespace e8g

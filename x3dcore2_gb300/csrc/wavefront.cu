@@ -93,25 +93,6 @@ template <> struct RngSlot<RngPhilox> {
     }
 };
 
-__device__ __forceinline__ bool wf_coords(RenderArgs const &A, uint64_t idx, uint32_t &pixel, uint32_t &sample,
-                                          uint32_t &out) {
-    if (A.list_pixel) {
-        pixel = A.list_pixel[idx];
-        sample = A.list_sample[idx];
-        out = static_cast<uint32_t>(idx);
-        return true;
-    }
-    uint32_t s = static_cast<uint32_t>(idx / A.paths_per_sample);
-    uint32_t j = static_cast<uint32_t>(idx - static_cast<uint64_t>(s) * A.paths_per_sample);
-    uint32_t tile = j >> 5, w = j & 31u;
-    uint32_t x = (tile % A.tiles_x) * 8 + (w & 7u), y = (tile / A.tiles_x) * 4 + (w >> 3);
-    if (x >= A.width || y >= A.height)
-        return false;
-    pixel = y * A.width + x;
-    sample = A.sample_offset + s;
-    out = pixel;
-    return true;
-}
 
 template <class R>
 __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh, WfSlots W,
@@ -184,7 +165,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
             base = __shfl_sync(~0u, base, leader);
             if (want) {
                 uint64_t idx = base + __popc(mask & ((1u << lane_id()) - 1u));
-                if (idx < A.total_paths && wf_coords(A, idx, pixel, sample, out)) {
+                if (idx < A.total_paths && path_coords(A, idx, pixel, sample, out)) {
                     FirstHit f = fh[pixel];
                     int32_t m = __float_as_int(f.p.w);
                     if (m >= 0) {
