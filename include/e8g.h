@@ -110,19 +110,24 @@ typedef struct e8g_scene_desc {
     e8g_camera camera;
 } e8g_scene_desc;
 
+/* Build options of the SAH layout. e8g_default_bvh_opts gives values tuned for the GPU traversal
+ * (8, 32, 1, 1); the reference's own constants are 4, 20, 8, 1 (pathspace.cpp:121-124). The
+ * reference layout ignores them: it always builds the reference's tree. */
 typedef struct e8g_bvh_opts {
-    uint32_t max_leaf_prims; /* reference BVH_MAX_PRIMS = 4   pathspace.cpp:121 */
-    uint32_t num_bins;       /* reference BVH_BUCKET_COUNT = 20 pathspace.cpp:122 */
-    float tri_cost;          /* reference BVH_RAY_TRIANGLE_COST = 8 */
-    float node_cost;         /* reference BVH_RAY_BOX_COST = 1 */
+    uint32_t max_leaf_prims; /* largest leaf (reference BVH_MAX_PRIMS = 4) */
+    uint32_t num_bins;       /* SAH bins per axis, 2..64 (reference BVH_BUCKET_COUNT = 20) */
+    float tri_cost;          /* SAH triangle-test cost (reference BVH_RAY_TRIANGLE_COST = 8) */
+    float node_cost;         /* SAH box-test cost (reference BVH_RAY_BOX_COST = 1) */
     uint32_t num_threads;    /* host build threads, 0 = all */
     uint32_t layout;         /* E8G_BVH_SAH or E8G_BVH_REFERENCE */
 } e8g_bvh_opts;
 
 enum {
-    E8G_BVH_SAH = 0,      /* binned SAH over 3 axes, child pairs, ordered traversal (fast) */
-    E8G_BVH_REFERENCE = 1 /* the reference's own tree and visiting order (pathspace.cpp:121-456):
-                             hit identities match the reference bit for bit, ties included */
+    E8G_BVH_SAH = 0,       /* binned SAH over 3 axes, child pairs, ordered traversal */
+    E8G_BVH_REFERENCE = 1, /* the reference's own tree and visiting order (pathspace.cpp:121-456):
+                              hit identities match the reference bit for bit, ties included */
+    E8G_BVH_WIDE = 2       /* the SAH tree collapsed to eight-wide nodes with quantized child
+                              boxes (96 bytes per node), octant-ordered traversal: the fastest */
 };
 
 typedef struct e8g_bvh_stats {
@@ -132,8 +137,10 @@ typedef struct e8g_bvh_stats {
     uint32_t num_tris;
     double avg_leaf_depth;
     double build_ms;
-    uint64_t node_bytes;
+    uint64_t node_bytes;  /* bytes of the node array (32 per binary node, 96 per wide node) */
     uint64_t tri_bytes;
+    uint32_t layout;      /* the layout built (E8G_BVH_WIDE falls back to E8G_BVH_SAH when its
+                             tree would be deeper than the traversal stack) */
 } e8g_bvh_stats;
 
 /* ----------------------------------------------------------- traversal ---- */

@@ -17,7 +17,7 @@ def rel_mse(img, ref, eps=1e-2):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
 
 
-@pytest.mark.parametrize("layout", [abi.BVH_REFERENCE, abi.BVH_SAH])
+@pytest.mark.parametrize("layout", [abi.BVH_REFERENCE, abi.BVH_SAH, abi.BVH_WIDE])
 @pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT,
                                   abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER])
 def test_image_matches_oracle_same_streams(ctx, mode, layout):

@@ -38,11 +38,14 @@ def test_closest_hits_match_reference_golden_exactly(ctx, name):
     assert np.array_equal(g["t"][hit].view(np.uint32), d["hit_t"][hit].view(np.uint32))
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_WIDE])
 @pytest.mark.parametrize("name", FIXTURES)
-def test_closest_hits_match_reference_golden_sah(ctx, name):
-    """The fast SAH tree: same hits; ties on shared edges may resolve to the other triangle."""
+def test_closest_hits_match_reference_golden_sah(ctx, name, layout):
+    """The fast trees (SAH pairs, eight-wide): same hits; ties on shared edges may resolve to the
+    other triangle."""
     d = G.load(name)
-    ctx.upload(G.scene_from(d))
+    ctx.upload(G.scene_from(d), layout=layout)
+    assert ctx.bvh_stats()["layout"] == layout
     g = ctx.trace_closest(d["rays"])
     compare_hits(g, d["hit_mesh"], d["hit_tri"], d["hit_t"], min_match=1.0)
     hit = (d["hit_mesh"] >= 0) & (g["mesh"] == d["hit_mesh"])
@@ -67,7 +70,7 @@ def random_rays(n, lo, hi, seed):
     return ob.rays_array(o, dd)
 
 
-@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_REFERENCE])
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_REFERENCE, abi.BVH_WIDE])
 @pytest.mark.parametrize("kind,size", [("ico", 6), ("soup", 100_000), ("ico", 7)])
 def test_closest_and_any_hit_match_oracle_on_large_scenes(ctx, kind, size, layout):
     sc = (S.displaced_icosphere(level=size, seed=2, num_materials=64, width=64, height=36) if kind == "ico"

@@ -23,7 +23,7 @@ MODE_REF_UNI, MODE_REF_LT1, MODE_MIS, MODE_REF_BDPT, MODE_BDPT_POWER = 0, 1, 2, 
 MODE_REF_DIRECT, MODE_NORMAL, MODE_POSITION = 5, 6, 7
 INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT = 0, 1
 RNG_MINSTD, RNG_PHILOX = 0, 1
-BVH_SAH, BVH_REFERENCE = 0, 1
+BVH_SAH, BVH_REFERENCE, BVH_WIDE = 0, 1, 2
 # generators
 GEN_CORNELL, GEN_DISPLACED_ICO, GEN_SOUP, GEN_FURNACE = 0, 1, 2, 3
 
@@ -66,7 +66,7 @@ class BvhOpts(C.Structure):
 class BvhStats(C.Structure):
     _fields_ = [("num_nodes", C.c_uint32), ("num_leaves", C.c_uint32), ("max_depth", C.c_uint32),
                 ("num_tris", C.c_uint32), ("avg_leaf_depth", C.c_double), ("build_ms", C.c_double),
-                ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64)]
+                ("node_bytes", C.c_uint64), ("tri_bytes", C.c_uint64), ("layout", C.c_uint32)]
 
 
 class Ray(C.Structure):

@@ -60,6 +60,7 @@ void fill_dev_scene(e8g_ctx *c) {
     packed_scene &p = c->pack;
     S.nlo = static_cast<float4 const *>(c->b_nlo.ptr);
     S.nhi = static_cast<float4 const *>(c->b_nhi.ptr);
+    S.wnodes = static_cast<uint4 const *>(c->b_wide.ptr);
     S.tri = static_cast<float4 const *>(c->b_tri.ptr);
     S.tidx = static_cast<uint4 const *>(c->b_tidx.ptr);
     S.vpos = static_cast<float4 const *>(c->b_vpos.ptr);
@@ -167,9 +168,9 @@ char const *e8g_last_error(e8g_ctx const *ctx) { return ctx ? ctx->err.c_str() :
 void e8g_default_bvh_opts(e8g_bvh_opts *o) {
     if (!o)
         return;
-    o->max_leaf_prims = 4;
-    o->num_bins = 20;
-    o->tri_cost = 8.0f;
+    o->max_leaf_prims = 8;
+    o->num_bins = 32;
+    o->tri_cost = 1.0f;
     o->node_cost = 1.0f;
     o->num_threads = 0;
     o->layout = E8G_BVH_SAH;
@@ -317,7 +318,7 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
         bo.tri_cost = o->tri_cost;
         bo.node_cost = o->node_cost;
         bo.num_threads = o->num_threads;
-        if (o->layout > E8G_BVH_REFERENCE)
+        if (o->layout > E8G_BVH_WIDE)
             return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH layout");
         bo.layout = o->layout;
     }
@@ -336,6 +337,8 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
     if (e == cudaSuccess)
         e = upload(c->b_nhi, p.bvh.hi, c->stream);
     if (e == cudaSuccess)
+        e = upload(c->b_wide, p.wide, c->stream);
+    if (e == cudaSuccess)
         e = upload(c->b_tri, p.tri, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
@@ -347,7 +350,8 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
     c->bvh_stats.num_tris = p.nt;
     c->bvh_stats.avg_leaf_depth = p.bvh.avg_leaf_depth;
     c->bvh_stats.build_ms = p.build_ms;
-    c->bvh_stats.node_bytes = static_cast<uint64_t>(p.bvh.num_nodes) * 32;
+    c->bvh_stats.node_bytes = static_cast<uint64_t>(p.bvh.num_nodes) * (p.layout == 2 ? 4 * kWideWords : 32);
+    c->bvh_stats.layout = p.layout;
     c->bvh_stats.tri_bytes = static_cast<uint64_t>(p.nt) * 48;
     c->built = true;
     fill_dev_scene(c);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "layout.h"
+#include "wide_trav.h"
 
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -19,6 +20,7 @@ constexpr float kInvPi = 0.318309873342514038f; // 1.0f / static_cast<float>(M_P
 constexpr int kBlock = 128;                     // threads per block of the traversal kernels
 constexpr int kStack = 32;                      // per-thread (node, t) stack of the SAH layout (== kMaxTreeDepth)
 constexpr int kStackWords = 2 * kStack;          // shared words per thread: 64 node entries in reference order
+static_assert(2 * kWideStack <= kStackWords, "the eight-wide stack must fit the per-thread stack words");
 constexpr float kOneMinusUlp = 0.999999940395355225f; // nextafter(1.0f, 0.0f)
 // Safety stop for any path, whatever the policy (the C ABI rejects policies under which paths
 // could approach it: survival <= 0.95 from depth <= 64 leaves a 1e-21 chance of reaching it).
@@ -29,6 +31,7 @@ constexpr uint32_t kHardDepth = 1024;
 struct DevScene {
     const float4 *nlo;      // node min xyz | link
     const float4 *nhi;      // node max xyz | count
+    const uint4 *wnodes;    // eight-wide layout: 6 uint4 per node (bvh_wide.h)
     const float4 *tri;      // 3 float4 per BVH position: (v0 | global tri id), (v1 - v0), (v2 - v0)
     const uint4 *tidx;      // per global triangle: global vertex indices, mesh
     const float4 *vpos;     // per vertex
@@ -44,7 +47,8 @@ struct DevScene {
     const float *light_cum;    // basic_light_sources::commit CDF (lightsources.cpp:45-52)
     const float *light_pnorm;  // |power| per light
     uint32_t nmat, nl, nm, nnodes, ntris;
-    uint32_t layout; // 0: SAH child pairs (ordered traversal), 1: the reference's tree and order
+    uint32_t layout; // 0: SAH child pairs (ordered traversal), 1: the reference's tree and order,
+                     // 2: eight-wide quantized nodes
     float total_power;
     float bmin[3], bmax[3]; // if_path_space::aabb() for the position tracer
     DevCamera cam;
@@ -207,12 +211,6 @@ __host__ __device__ __forceinline__ uint32_t path_seed(uint64_t seed_mix, uint32
 
 // ----------------------------------------------------------------- traversal ----
 
-struct Hit {
-    float t;
-    uint32_t tri; // global triangle index; 0xFFFFFFFF = miss
-    float b1, b2;
-};
-
 struct TraceCounters {
     uint32_t nodes, tris;
 };
@@ -233,27 +231,7 @@ __device__ __forceinline__ bool slab(float4 lo, float4 hi, float3 o, float3 inv,
 // ray::intersect (tensor.h:688-725) on a triangle stored as (v0, v1 - v0, v2 - v0).
 __device__ __forceinline__ bool tri_test(float3 o, float3 d, float4 a, float4 b, float4 c, float tmin,
                                          float tmax, float &t0, float &b1o, float &b2o) {
-    float3 va = xyz(b), vb = xyz(c);
-    float3 vc = sub(o, xyz(a));
-    float3 e2 = cross(d, vb);
-    float det = dot(va, e2);
-    if (det == 0.0f)
-        return false;
-    float inv = __frcp_rn(det);
-    float b1 = dot(vc, e2) * inv;
-    if (b1 < 0.0f || b1 > 1.0f)
-        return false;
-    float3 e1 = cross(vc, va);
-    float b2 = dot(d, e1) * inv;
-    if (b2 < 0.0f || b1 + b2 > 1.0f)
-        return false;
-    float t = dot(vb, e1) * inv;
-    if (t < tmin || t > tmax)
-        return false;
-    t0 = t;
-    b1o = b1;
-    b2o = b2;
-    return true;
+    return hd_tri_test(o, d, a, b, c, tmin, tmax, t0, b1o, b2o);
 }
 
 // Closest hit over [1e-4, 1000] with the reference's strict `t0 < t` (pathspace.cpp:330-413):
@@ -476,7 +454,18 @@ __device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d,
     return false;
 }
 
-// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336); LAYOUT 0 = SAH, 1 = reference tree.
+// Eight-wide layout through the shared traversal (wide_trav.h).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ Hit trace_wide(const DevScene &S, float3 o, float3 d, float tmin, float tmax, uint32_t *stk,
+                                          TraceCounters *cnt) {
+    WideView W{S.wnodes, S.tri, S.nnodes};
+    Hit h;
+    wide_trace<ANY>(W, o, d, tmin, tmax, h, stk, kBlock, COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr);
+    return h;
+}
+
+// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336); LAYOUT 0 = SAH pairs, 1 = reference
+// tree, 2 = eight-wide.
 template <int LAYOUT, bool COUNT>
 __device__ __forceinline__ Hit trace_closest_l(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
     if (LAYOUT == 1) {
@@ -487,6 +476,8 @@ __device__ __forceinline__ Hit trace_closest_l(const DevScene &S, float3 o, floa
         trace_ref<false, COUNT>(S, o, d, 1e-4f, 1000.0f, h, stk, cnt);
         return h;
     }
+    if (LAYOUT == 2)
+        return trace_wide<false, COUNT>(S, o, d, 1e-4f, 1000.0f, stk, cnt);
     return trace_closest_sah<COUNT>(S, o, d, stk, cnt);
 }
 
@@ -498,33 +489,30 @@ __device__ __forceinline__ bool trace_any_l(const DevScene &S, float3 o, float3 
         h.t = INFINITY;
         return trace_ref<true, COUNT>(S, o, d, tmin, tmax, h, stk, cnt);
     }
+    if (LAYOUT == 2)
+        return trace_wide<true, COUNT>(S, o, d, tmin, tmax, stk, cnt).tri != 0xFFFFFFFFu;
     return trace_any_sah<COUNT>(S, o, d, tmin, tmax, stk, cnt);
 }
 
 // Closest hit in the scene's layout, chosen at run time (kernels off the hot path).
 template <bool COUNT>
 __device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
-    if (S.layout == 1) {
-        Hit h;
-        h.t = INFINITY;
-        h.tri = 0xFFFFFFFFu;
-        h.b1 = h.b2 = 0.0f;
-        trace_ref<false, COUNT>(S, o, d, 1e-4f, 1000.0f, h, stk, cnt);
-        return h;
-    }
-    return trace_closest_sah<COUNT>(S, o, d, stk, cnt);
+    if (S.layout == 1)
+        return trace_closest_l<1, COUNT>(S, o, d, stk, cnt);
+    if (S.layout == 2)
+        return trace_closest_l<2, COUNT>(S, o, d, stk, cnt);
+    return trace_closest_l<0, COUNT>(S, o, d, stk, cnt);
 }
 
-// Any hit on [tmin, tmax] in either layout.
+// Any hit on [tmin, tmax] in the scene's layout.
 template <bool COUNT>
 __device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d, float tmin, float tmax, uint32_t *stk,
                                           TraceCounters *cnt) {
-    if (S.layout == 1) {
-        Hit h;
-        h.t = INFINITY;
-        return trace_ref<true, COUNT>(S, o, d, tmin, tmax, h, stk, cnt);
-    }
-    return trace_any_sah<COUNT>(S, o, d, tmin, tmax, stk, cnt);
+    if (S.layout == 1)
+        return trace_any_l<1, COUNT>(S, o, d, tmin, tmax, stk, cnt);
+    if (S.layout == 2)
+        return trace_any_l<2, COUNT>(S, o, d, tmin, tmax, stk, cnt);
+    return trace_any_l<0, COUNT>(S, o, d, tmin, tmax, stk, cnt);
 }
 
 // ---- resumable traversal (SAH layout): one node per call ----

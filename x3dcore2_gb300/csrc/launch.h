@@ -26,8 +26,15 @@ void launch_firefly(float const *est, uint32_t K, uint32_t w, uint32_t h, float4
 void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                        unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
 int megakernel_blocks_per_sm();
+// The same for one tree layout (mega_l0.cu: SAH pairs, mega_l1.cu: reference, mega_l2.cu: wide).
+void launch_mega_l0(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+void launch_mega_l1(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+void launch_mega_l2(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
 
-// Many scenes, one persistent launch (SAH layout, Philox streams).
+// Many scenes, one persistent launch (SAH-pair or eight-wide trees, any stream kind).
 struct BatchDev {
     DevScene const *scenes;      // per scene
     RenderArgs const *args;      // per scene
@@ -45,7 +52,7 @@ void launch_first_hits_batch(BatchDev const &B, DevScene const *h_scenes, Render
 void launch_resolve_batch(BatchDev const &B, uint64_t total_pix, float4 const *accum_all, float *rgba_all,
                           cudaStream_t st);
 
-// Bidirectional path tracing (reference uniform weights), one thread per path.
+// Bidirectional path tracing (uniform or power-heuristic weights), one thread per path.
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                  unsigned long long *work, int grid, cudaStream_t st);
 int bdpt_blocks_per_sm();

@@ -1,0 +1,11 @@
+// Megakernel instantiations for the reference tree (layout 1).
+#include "mega.cuh"
+
+namespace e8g {
+
+void launch_mega_l1(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st) {
+    launch_layout<1>(S, A, fh, accum, path_rgb, work, counters, grid, st);
+}
+
+} // namespace e8g

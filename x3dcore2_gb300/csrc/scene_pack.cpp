@@ -145,8 +145,36 @@ void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
     for (uint32_t t = 0; t < s.nt; t++)
         for (int k = 0; k < 3; k++)
             t3[3 * static_cast<size_t>(t) + k] = s.tidx[4 * static_cast<size_t>(t) + k];
-    s.bvh = o.layout == 1 ? build_bvh_reference(p3.data(), t3.data(), s.nt) : build_bvh(p3.data(), t3.data(), s.nt, o);
-    s.layout = o.layout;
+    s.wide.clear();
+    if (o.layout == 1) {
+        s.bvh = build_bvh_reference(p3.data(), t3.data(), s.nt);
+        s.layout = 1;
+    } else if (o.layout == 2) {
+        flat_bvh bin = build_bvh(p3.data(), t3.data(), s.nt, o);
+        // the grid of the quantized boxes is sized for coordinates up to the scene's and the
+        // camera's largest magnitude
+        float max_abs = 0.0f;
+        for (float v : p3)
+            max_abs = std::max(max_abs, std::fabs(v));
+        for (int k = 0; k < 3; k++)
+            max_abs = std::max(max_abs, std::fabs(s.cam.origin[k]));
+        wide_bvh w = collapse_wide(bin, p3.data(), t3.data(), max_abs);
+        if (w.ok) {
+            s.bvh = flat_bvh{};
+            s.bvh.num_nodes = w.num_nodes;
+            s.bvh.num_leaves = w.num_leaves;
+            s.bvh.max_depth = w.max_depth;
+            s.bvh.tri_order = std::move(w.tri_order);
+            s.wide = std::move(w.nodes);
+            s.layout = 2;
+        } else { // deeper than the traversal stack: keep the binary tree
+            s.bvh = std::move(bin);
+            s.layout = 0;
+        }
+    } else {
+        s.bvh = build_bvh(p3.data(), t3.data(), s.nt, o);
+        s.layout = 0;
+    }
     s.tri.assign(12 * static_cast<size_t>(s.nt), 0.0f);
     for (uint32_t k = 0; k < s.nt; k++) {
         uint32_t t = s.bvh.tri_order[k];

@@ -3,6 +3,7 @@
 
 #include "../../include/e8g.h"
 #include "bvh.h"
+#include "bvh_wide.h"
 #include "layout.h"
 
 #include <cstdint>
@@ -26,8 +27,10 @@ struct packed_scene {
     float total_power = 0;
     float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
     DevCamera cam{};
-    // BVH (after build)
+    // BVH (after build). Layout 2 keeps the eight-wide nodes in `wide` and only the triangle
+    // order and counts in `bvh`.
     flat_bvh bvh;
+    std::vector<uint32_t> wide;
     std::vector<float> tri;         // 12 floats per BVH position
     double build_ms = 0;
     uint32_t layout = 0;

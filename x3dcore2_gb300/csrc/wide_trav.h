@@ -1,0 +1,257 @@
+// Traversal of the eight-wide quantized BVH (layout in bvh_wide.h), written once for the device
+// kernels and for the host-side checker (tests/cpp/wide_check.cpp), which runs the same code
+// against brute force on the CPU.
+//
+// One node visit loads the 96-byte record, tests the eight child boxes against [tmin, cull],
+// tests the triangles of every hit leaf slot at once, descends into the first hit interior child
+// in the ray's octant order and keeps the other hit interior children as one stack entry
+// (child base, interior mask, remaining hit mask). The stack therefore grows by at most one entry
+// per level, and the builder keeps the tree at most kWideMaxDepth levels deep.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector_types.h>
+
+#if defined(__CUDACC__)
+#define E8G_HD __host__ __device__ __forceinline__
+#else
+#define E8G_HD inline
+#endif
+
+namespace e8g {
+
+struct Hit {
+    float t;
+    uint32_t tri; // triangle record position (traversal) or global triangle index; 0xFFFFFFFF = miss
+    float b1, b2;
+};
+
+E8G_HD float hd_u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+E8G_HD uint32_t hd_f2u(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+E8G_HD int hd_ffs(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+    return __ffs(static_cast<int>(v));
+#else
+    return __builtin_ffs(static_cast<int>(v));
+#endif
+}
+E8G_HD int hd_popc(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+    return __popc(v);
+#else
+    return __builtin_popcount(v);
+#endif
+}
+E8G_HD float hd_fma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fmaf(a, b, c);
+#endif
+}
+E8G_HD float hd_rcp(float x) {
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
+E8G_HD uint4 hd_ld(uint4 const *p) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+E8G_HD float4 hd_ld(float4 const *p) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
+// ray::intersect (tensor.h:688-725) on a triangle stored as (v0, v1 - v0, v2 - v0), in the
+// reference's operation order; callers compile it without FMA contraction.
+E8G_HD bool hd_tri_test(float3 o, float3 d, float4 a, float4 b, float4 c, float tmin, float tmax, float &t0,
+                        float &b1o, float &b2o) {
+    float vax = b.x, vay = b.y, vaz = b.z; // va = v1 - v0
+    float vbx = c.x, vby = c.y, vbz = c.z; // vb = v2 - v0
+    float vcx = o.x - a.x, vcy = o.y - a.y, vcz = o.z - a.z;
+    // e2 = d x vb
+    float e2x = d.y * vbz - d.z * vby, e2y = d.z * vbx - d.x * vbz, e2z = d.x * vby - d.y * vbx;
+    float det = vax * e2x + vay * e2y + vaz * e2z;
+    if (det == 0.0f)
+        return false;
+    float inv = hd_rcp(det);
+    float b1 = (vcx * e2x + vcy * e2y + vcz * e2z) * inv;
+    if (b1 < 0.0f || b1 > 1.0f)
+        return false;
+    // e1 = vc x va
+    float e1x = vcy * vaz - vcz * vay, e1y = vcz * vax - vcx * vaz, e1z = vcx * vay - vcy * vax;
+    float b2 = (d.x * e1x + d.y * e1y + d.z * e1z) * inv;
+    if (b2 < 0.0f || b1 + b2 > 1.0f)
+        return false;
+    float t = (vbx * e1x + vby * e1y + vbz * e1z) * inv;
+    if (t < tmin || t > tmax)
+        return false;
+    t0 = t;
+    b1o = b1;
+    b2o = b2;
+    return true;
+}
+
+struct WideView {
+    uint4 const *nodes;  // 6 per node
+    float4 const *tri;   // 3 per triangle record: (v0 | global id), (v1 - v0), (v2 - v0)
+    uint32_t nnodes;
+};
+
+constexpr int kWideStack = 32; // entries; each takes two words, `stride` apart, in stk[0..63]
+
+// Byte s&3 of word w as a float (exact: 2^23 + q - 2^23).
+E8G_HD float hd_qf(uint32_t w, uint32_t s) {
+    return hd_u2f(0x4B000000u | ((w >> (8u * (s & 3u))) & 0xFFu)) - 8388608.0f;
+}
+
+// ANY: returns at the first triangle with t in [tmin, tmax]. Otherwise fills h with the closest
+// hit (h.tri = record position, h.t = infinity on a miss). stk holds 2 * kWideStack words,
+// `stride` apart. The counters, when given, add one per node visited and per triangle tested.
+template <bool ANY>
+E8G_HD bool wide_trace(WideView const &W, float3 o, float3 d, float tmin, float tmax, Hit &h, uint32_t *stk,
+                       int stride, uint32_t *cnt_nodes, uint32_t *cnt_tris) {
+    h.t = INFINITY;
+    h.tri = 0xFFFFFFFFu;
+    h.b1 = h.b2 = 0.0f;
+    if (W.nnodes == 0)
+        return false;
+    // Box tests use direction components at least 1e-30 in magnitude: an exactly parallel ray
+    // would turn the factored plane distance q * (step / d) + (p - o) / d into 0 * inf or
+    // inf - inf. The nudged ray moves less than 1e-27 off its line over t <= 1000, and boxes are
+    // inflated far beyond that, so no box a triangle hit lies in is culled; triangle tests use d.
+    float ix = 1.0f / (fabsf(d.x) < 1e-30f ? copysignf(1e-30f, d.x) : d.x);
+    float iy = 1.0f / (fabsf(d.y) < 1e-30f ? copysignf(1e-30f, d.y) : d.y);
+    float iz = 1.0f / (fabsf(d.z) < 1e-30f ? copysignf(1e-30f, d.z) : d.z);
+    uint32_t oct = (ix < 0.0f ? 1u : 0u) | (iy < 0.0f ? 2u : 0u) | (iz < 0.0f ? 4u : 0u);
+    float cull = tmax;
+    uint32_t node = 0;
+    int sp = 0;
+    for (uint32_t guard = 0; guard <= W.nnodes; guard++) {
+        uint4 const *np = W.nodes + 6 * static_cast<size_t>(node);
+        uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
+              n5 = hd_ld(np + 5);
+        if (cnt_nodes)
+            (*cnt_nodes)++;
+        float sx = hd_u2f((n0.w & 0xFFu) << 23) * ix;
+        float sy = hd_u2f(((n0.w >> 8) & 0xFFu) << 23) * iy;
+        float sz = hd_u2f(((n0.w >> 16) & 0xFFu) << 23) * iz;
+        float ox = (hd_u2f(n0.x) - o.x) * ix, oy = (hd_u2f(n0.y) - o.y) * iy, oz = (hd_u2f(n0.z) - o.z) * iz;
+        uint32_t imask = n0.w >> 24;
+        uint32_t counts = n5.x;
+        // near / far planes per axis follow the ray's direction signs
+        uint32_t nx0 = (oct & 1u) ? n3.z : n2.x, nx1 = (oct & 1u) ? n3.w : n2.y;
+        uint32_t fx0 = (oct & 1u) ? n2.x : n3.z, fx1 = (oct & 1u) ? n2.y : n3.w;
+        uint32_t ny0 = (oct & 2u) ? n4.x : n2.z, ny1 = (oct & 2u) ? n4.y : n2.w;
+        uint32_t fy0 = (oct & 2u) ? n2.z : n4.x, fy1 = (oct & 2u) ? n2.w : n4.y;
+        uint32_t nz0 = (oct & 4u) ? n4.z : n3.x, nz1 = (oct & 4u) ? n4.w : n3.y;
+        uint32_t fz0 = (oct & 4u) ? n3.x : n4.z, fz1 = (oct & 4u) ? n3.y : n4.w;
+        uint32_t hit_int = 0, hit_leaf = 0;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+        for (uint32_t s = 0; s < 8; s++) {
+            bool inner = (imask >> s) & 1u;
+            if (!inner && ((counts >> (4u * s)) & 0xFu) == 0u)
+                continue;
+            bool hi4 = s >= 4;
+            float tnx = hd_fma(hd_qf(hi4 ? nx1 : nx0, s), sx, ox), tfx = hd_fma(hd_qf(hi4 ? fx1 : fx0, s), sx, ox);
+            float tny = hd_fma(hd_qf(hi4 ? ny1 : ny0, s), sy, oy), tfy = hd_fma(hd_qf(hi4 ? fy1 : fy0, s), sy, oy);
+            float tnz = hd_fma(hd_qf(hi4 ? nz1 : nz0, s), sz, oz), tfz = hd_fma(hd_qf(hi4 ? fz1 : fz0, s), sz, oz);
+            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+            float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+            if (tn <= tf) {
+                if (inner)
+                    hit_int |= 1u << (s ^ oct);
+                else
+                    hit_leaf |= 1u << s;
+            }
+        }
+        // triangles of the hit leaf slots
+        while (hit_leaf) {
+            uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
+            hit_leaf &= hit_leaf - 1u;
+            uint32_t meta = (s < 4 ? n1.z : n1.w) >> (8u * (s & 3u)) & 0xFFu;
+            uint32_t k0 = n1.y + meta, k1 = k0 + ((counts >> (4u * s)) & 0xFu);
+            for (uint32_t k = k0; k < k1; k++) {
+                float4 a = hd_ld(W.tri + 3 * static_cast<size_t>(k));
+                float4 b = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 1);
+                float4 c = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 2);
+                if (cnt_tris)
+                    (*cnt_tris)++;
+                float t0, b1, b2;
+                if (hd_tri_test(o, d, a, b, c, tmin, ANY ? tmax : cull, t0, b1, b2)) {
+                    if (ANY) {
+                        h.t = t0;
+                        h.tri = hd_f2u(a.w);
+                        return true;
+                    }
+                    if (t0 < h.t) {
+                        h.t = t0;
+                        h.tri = hd_f2u(a.w);
+                        h.b1 = b1;
+                        h.b2 = b2;
+                        cull = t0;
+                    }
+                }
+            }
+        }
+        // next node: the first hit interior child in octant order, the rest on the stack
+        if (hit_int) {
+            uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
+            hit_int &= hit_int - 1u;
+            uint32_t s = k ^ oct;
+            uint32_t base = n1.x;
+            if (hit_int && sp < kWideStack) {
+                stk[sp * stride] = base;
+                stk[(kWideStack + sp) * stride] = imask << 8 | hit_int;
+                sp++;
+            }
+            node = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
+            continue;
+        }
+        if (sp == 0)
+            break;
+        uint32_t base = stk[(sp - 1) * stride];
+        uint32_t info = stk[(kWideStack + sp - 1) * stride];
+        uint32_t m = info & 0xFFu, im = info >> 8;
+        uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
+        m &= m - 1u;
+        if (m)
+            stk[(kWideStack + sp - 1) * stride] = im << 8 | m;
+        else
+            sp--;
+        uint32_t s = k ^ oct;
+        node = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
+    }
+    return !ANY ? h.tri != 0xFFFFFFFFu : false;
+}
+
+} // namespace e8g
