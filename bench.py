@@ -250,6 +250,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--res", default=None, help="WxH override, e.g. 480x270 (profiling a smaller launch)")
     ap.add_argument("--spp", type=int, default=None, help="spp override (profiling)")
+    ap.add_argument("--layout", default=None, choices=["sah", "wide", "reference"],
+                    help="BVH layout (default: the library's default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 64-scene batch and adjoint legs")
     args = ap.parse_args()
@@ -278,7 +280,10 @@ def main():
         spp = args.spp
     ctx = Context(local)
     t0 = time.time()
-    ctx.upload(scene)
+    if args.layout:
+        ctx.upload(scene, layout={"sah": abi.BVH_SAH, "wide": abi.BVH_WIDE, "reference": abi.BVH_REFERENCE}[args.layout])
+    else:
+        ctx.upload(scene)
     commit_s = time.time() - t0
     bvh = ctx.bvh_stats()
     p = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5,
@@ -359,7 +364,8 @@ def main():
 
     peak, peak_kind = read_peaks()
     mean_kernel_ms = mega_kernel_ms
-    alg_bytes = 32 * counts["nodes"] + 48 * counts["tris"]
+    node_bytes = bvh["node_bytes"] // max(bvh["num_nodes"], 1)  # 32 (binary node) or 96 (wide node)
+    alg_bytes = node_bytes * counts["nodes"] + 48 * counts["tris"]
     achieved = alg_bytes / (mean_kernel_ms / 1000.0) / 1e9
     traffic = TRAFFIC_BYTES_PER_PATH * paths_per_step if TRAFFIC_BYTES_PER_PATH else None
 
@@ -370,7 +376,8 @@ def main():
         "config": dict(WORKLOAD, integrator=best, l2="flushed between steps (256 MB write)",
                        integrators={k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in r.items()}
                                     for k, r in results.items()}, wavefront_tune=tune,
-                       small=args.small, bvh_nodes=bvh["num_nodes"], bvh_build_ms=bvh["build_ms"],
+                       small=args.small, bvh_layout=["sah", "reference", "wide"][bvh["layout"]],
+                       bvh_nodes=bvh["num_nodes"], bvh_build_ms=bvh["build_ms"],
                        commit_s=round(commit_s, 3)),
         "e2e": {"value": e2e_value, "unit": "paths/s", "ms_per_step": statistics.mean(e2e_ms),
                 "h2d_bytes_per_step": C.sizeof(abi.RenderParams),

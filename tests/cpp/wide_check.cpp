@@ -94,9 +94,8 @@ int main(int argc, char **argv) {
                 bf.tri = t;
             }
         }
-        Hit h;
         uint32_t cn = 0, ct = 0;
-        wide_trace<false>(W, org, dir, 1e-4f, 1000.0f, h, stk, 1, &cn, &ct);
+        Hit h = wide_trace(W, org, dir, 1e-4f, 1000.0f, false, stk, 1, &cn, &ct);
         visits += cn;
         tested += ct;
         if (bf.tri != 0xFFFFFFFFu)
@@ -121,8 +120,7 @@ int main(int argc, char **argv) {
             float t0, b1, bb2;
             bfa = hd_tri_test(org, dir, grec[3 * t], grec[3 * t + 1], grec[3 * t + 2], 1e-4f, tmax, t0, b1, bb2);
         }
-        Hit ha;
-        bool wa = wide_trace<true>(W, org, dir, 1e-4f, tmax, ha, stk, 1, nullptr, nullptr);
+        bool wa = wide_trace(W, org, dir, 1e-4f, tmax, true, stk, 1, nullptr, nullptr).tri != 0xFFFFFFFFu;
         if (wa != bfa)
             bad_any++;
     }

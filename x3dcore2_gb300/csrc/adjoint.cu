@@ -126,7 +126,7 @@ __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const 
             if (!vequals0(fv)) {
                 float p_l = pmf * ls.area_dens * r2 / cos_l;
                 float p_b = bsdf_pdf(S, m, n, o, wi);
-                if (!trace_any_l<LAYOUT, false>(S, p, wi, 1e-4f, dist - 1e-3f, stk, nullptr)) {
+                if (trace_l<LAYOUT, false>(S, p, wi, 1e-4f, dist - 1e-3f, true, stk, nullptr).tri == 0xFFFFFFFFu) {
                     float wgt = power_heuristic(p_l, p_b);
                     float3 c = scale(mul(mul(beta, fv), light_rad(S, light)), cos_x * wgt / p_l);
                     L = add(L, c);
@@ -160,7 +160,7 @@ __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const 
         }
         scat++;
         beta = mul(beta, scale(fv, cw / pdf));
-        Hit h = trace_closest_l<LAYOUT, false>(S, p, i, stk, nullptr);
+        Hit h = trace_l<LAYOUT, false>(S, p, i, 1e-4f, 1000.0f, false, stk, nullptr);
         if (h.tri == 0xFFFFFFFFu)
             break;
         Vert nv = make_vert(S, h);

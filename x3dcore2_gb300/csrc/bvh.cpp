@@ -1,7 +1,7 @@
-// Binned-SAH BVH builder (host). Same cost model and defaults as the reference's builder
-// (pathspace.cpp:121-260: node cost 1, triangle cost 8, 20 buckets, leaves of at most 4), but
-// bins over all three axes of the centroid bounds, builds large subtrees on several threads,
-// caps the depth at kMaxTreeDepth and writes the GPU layout directly.
+// Binned-SAH BVH builder (host). The reference's cost model (pathspace.cpp:121-260: box cost +
+// triangle cost x area-weighted counts, leaf size cap), with its constants as options, but bins
+// over all three axes of the centroid bounds, builds large subtrees on several threads, caps the
+// depth at kMaxTreeDepth and writes the GPU layout directly.
 #include "bvh.h"
 
 #include <algorithm>

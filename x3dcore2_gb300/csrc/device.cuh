@@ -234,12 +234,14 @@ __device__ __forceinline__ bool tri_test(float3 o, float3 d, float4 a, float4 b,
     return hd_tri_test(o, d, a, b, c, tmin, tmax, t0, b1o, b2o);
 }
 
-// Closest hit over [1e-4, 1000] with the reference's strict `t0 < t` (pathspace.cpp:330-413):
+// SAH child-pair tree. Closest hit (any = false) with the reference's strict `t0 < t`
+// (pathspace.cpp:330-413) or any hit (has_intersect, pathspace.cpp:415-456) on [tmin, tmax]:
 // ordered child visits, far children and their entry distances kept on a per-thread stack in
-// shared memory (stack entries of one thread are kBlock words apart, so lanes never conflict).
+// shared memory (stack entries of one thread are kBlock words apart, so lanes never conflict);
+// the closest-hit query culls boxes beyond its best hit.
 template <bool COUNT>
-__device__ __forceinline__ Hit trace_closest_sah(const DevScene &S, float3 o, float3 d, uint32_t *stk,
-                                                 TraceCounters *cnt) {
+__device__ __forceinline__ Hit trace_sah(const DevScene &S, float3 o, float3 d, float tmin, float tmax, bool any,
+                                         uint32_t *stk, TraceCounters *cnt) {
     uint32_t *sn = stk;
     float *st = reinterpret_cast<float *>(stk + kStack * kBlock);
     Hit h;
@@ -248,7 +250,6 @@ __device__ __forceinline__ Hit trace_closest_sah(const DevScene &S, float3 o, fl
     h.b1 = h.b2 = 0.0f;
     if (S.nnodes == 0)
         return h;
-    const float tmin = 1e-4f, tmax = 1000.0f;
     float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     float cull = tmax;
     uint32_t link = __float_as_uint(__ldg(&S.nlo[0].w));
@@ -265,10 +266,8 @@ __device__ __forceinline__ Hit trace_closest_sah(const DevScene &S, float3 o, fl
             bool hit1 = slab(l1, h1, o, inv, tmin, cull, tn1);
             if (hit0 && hit1) {
                 bool swap = tn1 < tn0;
-                uint32_t far_node = swap ? link : link + 1;
-                float far_t = swap ? tn0 : tn1;
-                sn[sp * kBlock] = far_node;
-                st[sp * kBlock] = far_t;
+                sn[sp * kBlock] = swap ? link : link + 1;
+                st[sp * kBlock] = swap ? tn0 : tn1;
                 sp++;
                 float4 nl = swap ? l1 : l0, nh = swap ? h1 : h0;
                 link = __float_as_uint(nl.w);
@@ -290,6 +289,8 @@ __device__ __forceinline__ Hit trace_closest_sah(const DevScene &S, float3 o, fl
                     h.tri = __float_as_uint(a.w);
                     h.b1 = b1;
                     h.b2 = b2;
+                    if (any)
+                        return h;
                     cull = fminf(t0, tmax);
                 }
             }
@@ -312,58 +313,6 @@ __device__ __forceinline__ Hit trace_closest_sah(const DevScene &S, float3 o, fl
     }
     return h;
 }
-
-// Any hit with t in [tmin, tmax] (has_intersect, pathspace.cpp:415-456).
-template <bool COUNT>
-__device__ __forceinline__ bool trace_any_sah(const DevScene &S, float3 o, float3 d, float tmin, float tmax,
-                                              uint32_t *sn, TraceCounters *cnt) {
-    if (S.nnodes == 0)
-        return false;
-    float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
-    uint32_t link = __float_as_uint(__ldg(&S.nlo[0].w));
-    uint32_t count = __float_as_uint(__ldg(&S.nhi[0].w));
-    int sp = 0;
-    while (true) {
-        if (count == 0) {
-            float4 l0 = __ldg(&S.nlo[link]), h0 = __ldg(&S.nhi[link]);
-            float4 l1 = __ldg(&S.nlo[link + 1]), h1 = __ldg(&S.nhi[link + 1]);
-            if (COUNT)
-                cnt->nodes += 2;
-            float tn0, tn1;
-            bool hit0 = slab(l0, h0, o, inv, tmin, tmax, tn0);
-            bool hit1 = slab(l1, h1, o, inv, tmin, tmax, tn1);
-            if (hit0 && hit1) {
-                bool swap = tn1 < tn0;
-                sn[sp * kBlock] = swap ? link : link + 1;
-                sp++;
-                float4 nl = swap ? l1 : l0, nh = swap ? h1 : h0;
-                link = __float_as_uint(nl.w);
-                count = __float_as_uint(nh.w);
-                continue;
-            } else if (hit0 || hit1) {
-                link = __float_as_uint(hit0 ? l0.w : l1.w);
-                count = __float_as_uint(hit0 ? h0.w : h1.w);
-                continue;
-            }
-        } else {
-            for (uint32_t k = link; k < link + count; k++) {
-                float4 a = __ldg(&S.tri[3 * k]), b = __ldg(&S.tri[3 * k + 1]), c = __ldg(&S.tri[3 * k + 2]);
-                if (COUNT)
-                    cnt->tris++;
-                float t0, b1, b2;
-                if (tri_test(o, d, a, b, c, tmin, tmax, t0, b1, b2))
-                    return true;
-            }
-        }
-        if (sp == 0)
-            return false;
-        sp--;
-        uint32_t node = sn[sp * kBlock];
-        link = __float_as_uint(__ldg(&S.nlo[node].w));
-        count = __float_as_uint(__ldg(&S.nhi[node].w));
-    }
-}
-
 
 // ---- the reference's tree, visited in the reference's order ----
 // bvh_path_space_layout::intersect / has_intersect (pathspace.cpp:330-456): depth-first with an
@@ -410,9 +359,9 @@ __device__ __forceinline__ bool ref_slab(float4 lo, float4 hi, float3 o, float3 
     return !(tmin > tmax);
 }
 
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d, float tmin, float tmax, Hit &h,
-                                          uint32_t *stk, TraceCounters *cnt) {
+template <bool COUNT>
+__device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d, float tmin, float tmax, bool any,
+                                          Hit &h, uint32_t *stk, TraceCounters *cnt) {
     if (S.nnodes == 0)
         return false;
     float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
@@ -431,8 +380,11 @@ __device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d,
                     cnt->tris++;
                 float t0, b1, b2;
                 if (tri_test(o, d, a, b, c, tmin, tmax, t0, b1, b2)) {
-                    if (ANY)
+                    if (any) {
+                        h.t = t0;
+                        h.tri = __float_as_uint(a.w);
                         return true;
+                    }
                     if (t0 < h.t) {
                         h.t = t0;
                         h.tri = __float_as_uint(a.w);
@@ -454,54 +406,37 @@ __device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d,
     return false;
 }
 
-// Eight-wide layout through the shared traversal (wide_trav.h).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ Hit trace_wide(const DevScene &S, float3 o, float3 d, float tmin, float tmax, uint32_t *stk,
-                                          TraceCounters *cnt) {
-    WideView W{S.wnodes, S.tri, S.nnodes};
-    Hit h;
-    wide_trace<ANY>(W, o, d, tmin, tmax, h, stk, kBlock, COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr);
-    return h;
-}
-
-// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336); LAYOUT 0 = SAH pairs, 1 = reference
-// tree, 2 = eight-wide.
+// One query in a given layout: closest hit (any = false) or any hit (any = true) on [tmin, tmax].
+// Kernels on the hot path call this from a single site, so each holds one inlined traversal.
 template <int LAYOUT, bool COUNT>
-__device__ __forceinline__ Hit trace_closest_l(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
+__device__ __forceinline__ Hit trace_l(const DevScene &S, float3 o, float3 d, float tmin, float tmax, bool any,
+                                       uint32_t *stk, TraceCounters *cnt) {
     if (LAYOUT == 1) {
         Hit h;
         h.t = INFINITY;
         h.tri = 0xFFFFFFFFu;
         h.b1 = h.b2 = 0.0f;
-        trace_ref<false, COUNT>(S, o, d, 1e-4f, 1000.0f, h, stk, cnt);
+        trace_ref<COUNT>(S, o, d, tmin, tmax, any, h, stk, cnt);
         return h;
     }
-    if (LAYOUT == 2)
-        return trace_wide<false, COUNT>(S, o, d, 1e-4f, 1000.0f, stk, cnt);
-    return trace_closest_sah<COUNT>(S, o, d, stk, cnt);
-}
-
-template <int LAYOUT, bool COUNT>
-__device__ __forceinline__ bool trace_any_l(const DevScene &S, float3 o, float3 d, float tmin, float tmax,
-                                            uint32_t *stk, TraceCounters *cnt) {
-    if (LAYOUT == 1) {
-        Hit h;
-        h.t = INFINITY;
-        return trace_ref<true, COUNT>(S, o, d, tmin, tmax, h, stk, cnt);
+    if (LAYOUT == 2) {
+        WideView W{S.wnodes, S.tri, S.nnodes};
+        return wide_trace(W, o, d, tmin, tmax, any, stk, kBlock, COUNT ? &cnt->nodes : nullptr,
+                          COUNT ? &cnt->tris : nullptr);
     }
-    if (LAYOUT == 2)
-        return trace_wide<true, COUNT>(S, o, d, tmin, tmax, stk, cnt).tri != 0xFFFFFFFFu;
-    return trace_any_sah<COUNT>(S, o, d, tmin, tmax, stk, cnt);
+    return trace_sah<COUNT>(S, o, d, tmin, tmax, any, stk, cnt);
 }
 
-// Closest hit in the scene's layout, chosen at run time (kernels off the hot path).
+// Closest hit on [1e-4, 1000] (pathspace.cpp:335-336) in the scene's layout, chosen at run time
+// (kernels off the hot path; the eight-wide traversal is called out of line).
 template <bool COUNT>
 __device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3 d, uint32_t *stk, TraceCounters *cnt) {
     if (S.layout == 1)
-        return trace_closest_l<1, COUNT>(S, o, d, stk, cnt);
+        return trace_l<1, COUNT>(S, o, d, 1e-4f, 1000.0f, false, stk, cnt);
     if (S.layout == 2)
-        return trace_closest_l<2, COUNT>(S, o, d, stk, cnt);
-    return trace_closest_l<0, COUNT>(S, o, d, stk, cnt);
+        return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes}, o, d, 1e-4f, 1000.0f, false, stk, kBlock,
+                               COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr);
+    return trace_l<0, COUNT>(S, o, d, 1e-4f, 1000.0f, false, stk, cnt);
 }
 
 // Any hit on [tmin, tmax] in the scene's layout.
@@ -509,10 +444,12 @@ template <bool COUNT>
 __device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d, float tmin, float tmax, uint32_t *stk,
                                           TraceCounters *cnt) {
     if (S.layout == 1)
-        return trace_any_l<1, COUNT>(S, o, d, tmin, tmax, stk, cnt);
+        return trace_l<1, COUNT>(S, o, d, tmin, tmax, true, stk, cnt).tri != 0xFFFFFFFFu;
     if (S.layout == 2)
-        return trace_any_l<2, COUNT>(S, o, d, tmin, tmax, stk, cnt);
-    return trace_any_l<0, COUNT>(S, o, d, tmin, tmax, stk, cnt);
+        return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes}, o, d, tmin, tmax, true, stk, kBlock,
+                               COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr)
+                   .tri != 0xFFFFFFFFu;
+    return trace_l<0, COUNT>(S, o, d, tmin, tmax, true, stk, cnt).tri != 0xFFFFFFFFu;
 }
 
 // ---- resumable traversal (SAH layout): one node per call ----

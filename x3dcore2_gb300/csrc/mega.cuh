@@ -69,28 +69,6 @@ __device__ __forceinline__ void emit(RenderArgs const &A, float4 *accum, float *
     }
 }
 
-// transport_direct_illum with one light sample (pathtracer.cpp:152-242).
-template <class R, bool COUNT, int LAYOUT>
-__device__ __forceinline__ float3 ref_direct(DevScene const &S, R &rng, const DevMaterial &m, float3 p, float3 n,
-                                             float3 o, uint32_t *sn, TraceCounters *cnt, uint32_t &rays) {
-    float pmf;
-    int light = sample_light(S, rng, pmf);
-    Surf s = mesh_sample(S, __ldg(&S.light_mesh[light]), rng, false);
-    s.area_dens *= pmf;
-    float3 l = sub(p, s.p);
-    float3 illum = light_eval(S, light, l, s.n, n);
-    float3 c = f3(0, 0, 0);
-    if (!vequals0(illum)) {
-        float dist = norm(l);
-        float3 i = divs(neg(l), dist);
-        if (COUNT)
-            rays++;
-        if (!trace_any_l<LAYOUT, COUNT>(S, p, i, 1e-4f, dist - 1e-3f, sn, cnt))
-            c = mul(illum, bsdf_eval(S, m, n, o, i));
-    }
-    return divs(divs(c, s.area_dens), 1.0f);
-}
-
 // Starts a path at its cached first hit. Returns false when the path is already complete
 // (no valid first hit, or a tracer without random walk, whose value it emits itself).
 template <class R>
@@ -131,49 +109,51 @@ __device__ __forceinline__ bool mega_start(DevScene const &S, RenderArgs const &
 }
 
 // One vertex of a path: returns true when the path is finished.
+// The vertex first draws everything it needs in the reference's order (Russian roulette, the
+// light sample, the BSDF sample), then traces its two rays, the shadow ray and the extension
+// ray, through one traversal call site, so the kernel holds a single inlined traversal.
 template <class R, bool COUNT, int LAYOUT>
 __device__ __forceinline__ bool mega_step(DevScene const &S, RenderArgs const &A, PathState &ps, R &rng, uint32_t *sn,
                                           TraceCounters *cnt, uint32_t &rays) {
-    bool finish = false;
     const DevMaterial &m = vert_mat(S, ps.mesh);
-    if (A.mode == E8G_MODE_REF_DIRECT) {
-        float3 r = ref_direct<R, COUNT, LAYOUT>(S, rng, m, ps.p, ps.n, ps.o, sn, cnt, rays);
-        int32_t light = __ldg(&S.mesh_light[ps.mesh]);
-        if (light >= 0)
-            r = add(r, light_projected(S, light, ps.o, ps.n));
-        ps.L = r;
-        return true;
-    }
-    if ((A.max_depth && ps.depth >= A.max_depth) || ps.depth >= kHardDepth)
-        return true;
-    float surv = A.rr_prob;
-    if (ps.depth >= A.rr_start) {
-        if (rng.next() >= surv)
+    const bool ref_nee = A.mode == E8G_MODE_REF_DIRECT || A.mode == E8G_MODE_REF_LT1;
+    float3 bl = ps.beta;
+    if (A.mode != E8G_MODE_REF_DIRECT) {
+        if ((A.max_depth && ps.depth >= A.max_depth) || ps.depth >= kHardDepth)
             return true;
+        float surv = A.rr_prob;
+        if (ps.depth >= A.rr_start) {
+            if (rng.next() >= surv)
+                return true;
+        }
+        if (A.mode == E8G_MODE_MIS) {
+            if (ps.depth >= A.rr_start)
+                ps.beta = divs(ps.beta, surv);
+            bl = ps.beta;
+        } else {
+            bl = divs(ps.beta, ps.depth >= A.rr_start ? surv : 1.0f);
+        }
     }
-    float3 bl;
-    if (A.mode == E8G_MODE_MIS) {
-        if (ps.depth >= A.rr_start)
-            ps.beta = divs(ps.beta, surv);
-        bl = ps.beta;
-    } else {
-        bl = divs(ps.beta, ps.depth >= A.rr_start ? surv : 1.0f);
-    }
-    float pdf;
-    float3 i;
-    if (A.mode == E8G_MODE_REF_LT1) {
-        ps.L = add(ps.L, mul(bl, ref_direct<R, COUNT, LAYOUT>(S, rng, m, ps.p, ps.n, ps.o, sn, cnt, rays)));
-        i = bsdf_sample_ref(S, m, rng, pdf, ps.n, ps.o);
-        if (pdf == 0.0f)
-            finish = true;
-    } else if (A.mode == E8G_MODE_REF_UNI) {
-        int32_t light = __ldg(&S.mesh_light[ps.mesh]);
-        if (light >= 0)
-            ps.L = add(ps.L, mul(bl, light_radiance(S, light, ps.o, ps.n)));
-        i = bsdf_sample_ref(S, m, rng, pdf, ps.n, ps.o);
-        if (pdf == 0.0f)
-            finish = true;
-    } else { // E8G_MODE_MIS
+    // --- next-event estimation: the shadow query and what it adds when unoccluded
+    bool shadow = false;
+    float3 sh_d = f3(0, 0, 1), sh_vis = f3(0, 0, 0), sh_occ = f3(0, 0, 0);
+    float sh_tmax = 0.0f;
+    if (ref_nee) { // transport_direct_illum with one light sample (pathtracer.cpp:152-242)
+        float pmf;
+        int light = sample_light(S, rng, pmf);
+        Surf ls = mesh_sample(S, __ldg(&S.light_mesh[light]), rng, false);
+        ls.area_dens *= pmf;
+        float3 l = sub(ps.p, ls.p);
+        float3 illum = light_eval(S, light, l, ls.n, ps.n);
+        sh_occ = divs(divs(f3(0, 0, 0), ls.area_dens), 1.0f);
+        if (!vequals0(illum)) {
+            float dist = norm(l);
+            sh_d = divs(neg(l), dist);
+            sh_tmax = dist - 1e-3f;
+            sh_vis = divs(divs(mul(illum, bsdf_eval(S, m, ps.n, ps.o, sh_d)), ls.area_dens), 1.0f);
+            shadow = true;
+        }
+    } else if (A.mode == E8G_MODE_MIS) {
         float pmf;
         int light = sample_light(S, rng, pmf);
         Surf ls = mesh_sample(S, __ldg(&S.light_mesh[light]), rng, true);
@@ -189,33 +169,67 @@ __device__ __forceinline__ bool mega_step(DevScene const &S, RenderArgs const &A
             if (!vequals0(f)) {
                 float p_l = pmf * ls.area_dens * r2 / cos_l;
                 float p_b = bsdf_pdf(S, m, ps.n, ps.o, wi);
-                if (COUNT)
-                    rays++;
-                if (!trace_any_l<LAYOUT, COUNT>(S, ps.p, wi, 1e-4f, dist - 1e-3f, sn, cnt)) {
-                    float w = power_heuristic(p_l, p_b);
-                    ps.L = add(ps.L, scale(mul(mul(ps.beta, f), light_rad(S, light)), cos_x * w / p_l));
-                }
+                float w = power_heuristic(p_l, p_b);
+                sh_vis = scale(mul(mul(ps.beta, f), light_rad(S, light)), cos_x * w / p_l);
+                sh_d = wi;
+                sh_tmax = dist - 1e-3f;
+                shadow = true;
             }
         }
+    } else if (A.mode == E8G_MODE_REF_UNI) { // emission at every vertex (pathtracer.cpp:543-547)
+        int32_t light = __ldg(&S.mesh_light[ps.mesh]);
+        if (light >= 0)
+            ps.L = add(ps.L, mul(bl, light_radiance(S, light, ps.o, ps.n)));
+    }
+    // --- the BSDF sample: the extension query
+    bool extend = false;
+    float pdf = 0.0f;
+    float3 i = f3(0, 0, 1);
+    if (A.mode == E8G_MODE_REF_LT1 || A.mode == E8G_MODE_REF_UNI) {
+        i = bsdf_sample_ref(S, m, rng, pdf, ps.n, ps.o);
+        extend = pdf != 0.0f;
+    } else if (A.mode == E8G_MODE_MIS) {
         i = bsdf_sample_mis(S, m, rng, pdf, ps.n, ps.o);
-        if (!(pdf > 0.0f))
-            finish = true;
+        if (pdf > 0.0f) {
+            float cw = dot(ps.n, i);
+            if (cw > 0.0f) {
+                float3 f = bsdf_eval(S, m, ps.n, ps.o, i);
+                ps.beta = mul(ps.beta, scale(f, cw / pdf));
+                extend = true;
+            }
+        }
     }
-    if (finish)
-        return true;
-    float3 f;
-    float cw;
-    if (A.mode == E8G_MODE_MIS) {
-        cw = dot(ps.n, i);
-        if (cw <= 0.0f)
+    // --- trace: shadow ray (q = 0) then extension ray (q = 1), one call site
+    bool visible = false;
+    Hit h;
+    h.tri = 0xFFFFFFFFu;
+    h.t = INFINITY;
+    h.b1 = h.b2 = 0.0f;
+#pragma unroll 1
+    for (uint32_t q = shadow ? 0u : 1u; q < (extend ? 2u : 1u); q++) {
+        bool any = q == 0;
+        if (COUNT)
+            rays++;
+        Hit r = trace_l<LAYOUT, COUNT>(S, ps.p, any ? sh_d : i, 1e-4f, any ? sh_tmax : 1000.0f, any, sn, cnt);
+        if (any)
+            visible = r.tri == 0xFFFFFFFFu;
+        else
+            h = r;
+    }
+    if (ref_nee) {
+        float3 r = shadow && visible ? sh_vis : sh_occ;
+        if (A.mode == E8G_MODE_REF_DIRECT) {
+            int32_t light = __ldg(&S.mesh_light[ps.mesh]);
+            if (light >= 0)
+                r = add(r, light_projected(S, light, ps.o, ps.n));
+            ps.L = r;
             return true;
-        f = bsdf_eval(S, m, ps.n, ps.o, i);
-        ps.beta = mul(ps.beta, scale(f, cw / pdf));
+        }
+        ps.L = add(ps.L, mul(bl, r));
+    } else if (shadow && visible) {
+        ps.L = add(ps.L, sh_vis);
     }
-    if (COUNT)
-        rays++;
-    Hit h = trace_closest_l<LAYOUT, COUNT>(S, ps.p, i, sn, cnt);
-    if (h.tri == 0xFFFFFFFFu)
+    if (!extend || h.tri == 0xFFFFFFFFu)
         return true;
     Vert nv = make_vert(S, h);
     if (dot(nv.n, neg(i)) <= 0.0f)
@@ -231,8 +245,8 @@ __device__ __forceinline__ bool mega_step(DevScene const &S, RenderArgs const &A
             ps.L = add(ps.L, scale(mul(ps.beta, light_rad(S, hl)), w));
         }
     } else {
-        f = bsdf_eval(S, m, ps.n, ps.o, i);
-        cw = dot(ps.n, i);
+        float3 f = bsdf_eval(S, m, ps.n, ps.o, i);
+        float cw = dot(ps.n, i);
         ps.beta = divs(scale(mul(bl, f), cw), pdf);
     }
     ps.p = nv.p;

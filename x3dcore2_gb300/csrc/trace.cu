@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kBlock) k_first_hits_batch(BatchDev B, uint64_
     uint32_t px = static_cast<uint32_t>(i - B.pix_prefix[lo]);
     float3 o, d;
     camera_ray(S.cam, px % A.width, px / A.width, A.width, A.height, o, d);
-    Hit hit = trace_closest_l<0, false>(S, o, d, stk + threadIdx.x, nullptr);
+    Hit hit = trace_closest<false>(S, o, d, stk + threadIdx.x, nullptr); // the scene's own layout
     FirstHit f;
     f.d = make_float4(d.x, d.y, d.z, 0.0f);
     int32_t mesh = -1, light = -1;

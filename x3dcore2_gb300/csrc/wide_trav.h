@@ -16,8 +16,11 @@
 
 #if defined(__CUDACC__)
 #define E8G_HD __host__ __device__ __forceinline__
+// Out of line: for kernels with many traversal call sites (keeps them within the instruction cache)
+#define E8G_HD_CALL static __host__ __device__ __noinline__
 #else
 #define E8G_HD inline
+#define E8G_HD_CALL inline
 #endif
 
 namespace e8g {
@@ -132,17 +135,18 @@ E8G_HD float hd_qf(uint32_t w, uint32_t s) {
     return hd_u2f(0x4B000000u | ((w >> (8u * (s & 3u))) & 0xFFu)) - 8388608.0f;
 }
 
-// ANY: returns at the first triangle with t in [tmin, tmax]. Otherwise fills h with the closest
-// hit (h.tri = record position, h.t = infinity on a miss). stk holds 2 * kWideStack words,
-// `stride` apart. The counters, when given, add one per node visited and per triangle tested.
-template <bool ANY>
-E8G_HD bool wide_trace(WideView const &W, float3 o, float3 d, float tmin, float tmax, Hit &h, uint32_t *stk,
-                       int stride, uint32_t *cnt_nodes, uint32_t *cnt_tris) {
+// any: returns at the first triangle with t in [tmin, tmax] (h.tri != miss). Otherwise returns
+// the closest hit (h.tri = global triangle id, h.t = infinity on a miss). stk holds
+// 2 * kWideStack words, `stride` apart. The counters, when given, add one per node visited and
+// one per triangle tested.
+E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bool any, uint32_t *stk, int stride,
+                      uint32_t *cnt_nodes, uint32_t *cnt_tris) {
+    Hit h;
     h.t = INFINITY;
     h.tri = 0xFFFFFFFFu;
     h.b1 = h.b2 = 0.0f;
     if (W.nnodes == 0)
-        return false;
+        return h;
     // Box tests use direction components at least 1e-30 in magnitude: an exactly parallel ray
     // would turn the factored plane distance q * (step / d) + (p - o) / d into 0 * inf or
     // inf - inf. The nudged ray moves less than 1e-27 off its line over t <= 1000, and boxes are
@@ -156,8 +160,8 @@ E8G_HD bool wide_trace(WideView const &W, float3 o, float3 d, float tmin, float 
     int sp = 0;
     for (uint32_t guard = 0; guard <= W.nnodes; guard++) {
         uint4 const *np = W.nodes + 6 * static_cast<size_t>(node);
-        uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
-              n5 = hd_ld(np + 5);
+        uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4);
+        uint32_t counts = hd_ld(np + 5).x;
         if (cnt_nodes)
             (*cnt_nodes)++;
         float sx = hd_u2f((n0.w & 0xFFu) << 23) * ix;
@@ -165,33 +169,37 @@ E8G_HD bool wide_trace(WideView const &W, float3 o, float3 d, float tmin, float 
         float sz = hd_u2f(((n0.w >> 16) & 0xFFu) << 23) * iz;
         float ox = (hd_u2f(n0.x) - o.x) * ix, oy = (hd_u2f(n0.y) - o.y) * iy, oz = (hd_u2f(n0.z) - o.z) * iz;
         uint32_t imask = n0.w >> 24;
-        uint32_t counts = n5.x;
-        // near / far planes per axis follow the ray's direction signs
-        uint32_t nx0 = (oct & 1u) ? n3.z : n2.x, nx1 = (oct & 1u) ? n3.w : n2.y;
-        uint32_t fx0 = (oct & 1u) ? n2.x : n3.z, fx1 = (oct & 1u) ? n2.y : n3.w;
-        uint32_t ny0 = (oct & 2u) ? n4.x : n2.z, ny1 = (oct & 2u) ? n4.y : n2.w;
-        uint32_t fy0 = (oct & 2u) ? n2.z : n4.x, fy1 = (oct & 2u) ? n2.w : n4.y;
-        uint32_t nz0 = (oct & 4u) ? n4.z : n3.x, nz1 = (oct & 4u) ? n4.w : n3.y;
-        uint32_t fz0 = (oct & 4u) ? n3.x : n4.z, fz1 = (oct & 4u) ? n3.y : n4.w;
         uint32_t hit_int = 0, hit_leaf = 0;
+        // slots 0-3 then 4-7; near / far planes per axis follow the ray's direction signs
+#if defined(__CUDA_ARCH__)
+#pragma unroll 1
+#endif
+        for (uint32_t half = 0; half < 2; half++) {
+            uint32_t lx = half ? n2.y : n2.x, hx = half ? n3.w : n3.z;
+            uint32_t ly = half ? n2.w : n2.z, hy = half ? n4.y : n4.x;
+            uint32_t lz = half ? n3.y : n3.x, hz = half ? n4.w : n4.z;
+            uint32_t wnx = (oct & 1u) ? hx : lx, wfx = (oct & 1u) ? lx : hx;
+            uint32_t wny = (oct & 2u) ? hy : ly, wfy = (oct & 2u) ? ly : hy;
+            uint32_t wnz = (oct & 4u) ? hz : lz, wfz = (oct & 4u) ? lz : hz;
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-        for (uint32_t s = 0; s < 8; s++) {
-            bool inner = (imask >> s) & 1u;
-            if (!inner && ((counts >> (4u * s)) & 0xFu) == 0u)
-                continue;
-            bool hi4 = s >= 4;
-            float tnx = hd_fma(hd_qf(hi4 ? nx1 : nx0, s), sx, ox), tfx = hd_fma(hd_qf(hi4 ? fx1 : fx0, s), sx, ox);
-            float tny = hd_fma(hd_qf(hi4 ? ny1 : ny0, s), sy, oy), tfy = hd_fma(hd_qf(hi4 ? fy1 : fy0, s), sy, oy);
-            float tnz = hd_fma(hd_qf(hi4 ? nz1 : nz0, s), sz, oz), tfz = hd_fma(hd_qf(hi4 ? fz1 : fz0, s), sz, oz);
-            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-            float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
-            if (tn <= tf) {
-                if (inner)
-                    hit_int |= 1u << (s ^ oct);
-                else
-                    hit_leaf |= 1u << s;
+            for (uint32_t j = 0; j < 4; j++) {
+                uint32_t s = 4 * half + j;
+                bool inner = (imask >> s) & 1u;
+                if (!inner && ((counts >> (4u * s)) & 0xFu) == 0u)
+                    continue;
+                float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
+                float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
+                float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
+                float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+                float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+                if (tn <= tf) {
+                    if (inner)
+                        hit_int |= 1u << (s ^ oct);
+                    else
+                        hit_leaf |= 1u << s;
+                }
             }
         }
         // triangles of the hit leaf slots
@@ -207,11 +215,11 @@ E8G_HD bool wide_trace(WideView const &W, float3 o, float3 d, float tmin, float 
                 if (cnt_tris)
                     (*cnt_tris)++;
                 float t0, b1, b2;
-                if (hd_tri_test(o, d, a, b, c, tmin, ANY ? tmax : cull, t0, b1, b2)) {
-                    if (ANY) {
+                if (hd_tri_test(o, d, a, b, c, tmin, any ? tmax : cull, t0, b1, b2)) {
+                    if (any) {
                         h.t = t0;
                         h.tri = hd_f2u(a.w);
-                        return true;
+                        return h;
                     }
                     if (t0 < h.t) {
                         h.t = t0;
@@ -251,7 +259,13 @@ E8G_HD bool wide_trace(WideView const &W, float3 o, float3 d, float tmin, float 
         uint32_t s = k ^ oct;
         node = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
     }
-    return !ANY ? h.tri != 0xFFFFFFFFu : false;
+    return h;
+}
+
+// The same as one out-of-line function, for kernels that trace from many call sites.
+E8G_HD_CALL Hit wide_trace_call(WideView W, float3 o, float3 d, float tmin, float tmax, bool any, uint32_t *stk,
+                                int stride, uint32_t *cnt_nodes, uint32_t *cnt_tris) {
+    return wide_trace(W, o, d, tmin, tmax, any, stk, stride, cnt_nodes, cnt_tris);
 }
 
 } // namespace e8g
