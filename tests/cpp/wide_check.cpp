@@ -76,6 +76,17 @@ int main(int argc, char **argv) {
                               lo[2] + (hi[2] - lo[2]) * (1.2f * U(rng) - 0.1f));
         }
         float dx = 2 * U(rng) - 1, dy = 2 * U(rng) - 1, dz = 2 * U(rng) - 1;
+        if (r % 8 == 7 && nt) { // a grazing ray: from a point of a triangle, along its plane
+            uint32_t t = static_cast<uint32_t>(U(rng) * nt) % nt;
+            float const *v0 = &pos[3 * tris[3 * t]], *v1 = &pos[3 * tris[3 * t + 1]], *v2 = &pos[3 * tris[3 * t + 2]];
+            float u = U(rng), v = U(rng) * (1 - u), a = U(rng) - 0.5f, b = U(rng) - 0.5f;
+            org = make_float3(v0[0] + u * (v1[0] - v0[0]) + v * (v2[0] - v0[0]),
+                              v0[1] + u * (v1[1] - v0[1]) + v * (v2[1] - v0[1]),
+                              v0[2] + u * (v1[2] - v0[2]) + v * (v2[2] - v0[2]));
+            dx = a * (v1[0] - v0[0]) + b * (v2[0] - v0[0]);
+            dy = a * (v1[1] - v0[1]) + b * (v2[1] - v0[1]);
+            dz = a * (v1[2] - v0[2]) + b * (v2[2] - v0[2]);
+        }
         if (r % 16 == 5)
             dx = dy = 0.0f; // axis-aligned rays
         if (r % 16 == 9)

@@ -1,6 +1,6 @@
 """The eight-wide quantized BVH on the CPU: tests/cpp/wide_check.cpp builds the binary SAH tree
 and its eight-wide collapse with the library's own builder sources, then traces random rays
-(from inside and around the scene, from vertices, exactly axis-parallel) through the same
+(from inside and around the scene, from vertices, along triangle planes, exactly axis-parallel) through the same
 traversal code the kernels run (csrc/wide_trav.h, compiled for the host) and through brute force
 over every triangle. Closest hits must have the brute-force distance bit for bit (and the same
 triangle, or one at exactly that distance); any-hit answers must agree."""
@@ -62,7 +62,7 @@ SCENES = {
 def test_wide_traversal_matches_brute_force(checker, tmp_path, name):
     path = tmp_path / (name + ".bin")
     dump(SCENES[name](), path)
-    r = subprocess.run([str(checker), str(path), "4000", "11"], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([str(checker), str(path), "8000", "11"], capture_output=True, text=True, timeout=600)
     res = json.loads(r.stdout)
     assert r.returncode == 0, res
     assert res["ok"] == 1 and res["bad_t"] == 0 and res["bad_tri"] == 0 and res["bad_any"] == 0

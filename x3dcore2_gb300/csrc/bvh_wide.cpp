@@ -194,16 +194,26 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
         uint32_t words[kWideWords] = {0};
         uint32_t ebytes[3];
         double step[3];
+        // The grid starts one step below the children's union and 253 steps cover it, so no
+        // child box is clamped to the grid's ends and every quantized plane lies at least one
+        // step outside the (already inflated) child box: the slack absorbs the rounding of the
+        // traversal's plane arithmetic.
+        float org[3];
         for (int a = 0; a < 3; a++) {
             double ext = static_cast<double>(u.hi[a]) - static_cast<double>(u.lo[a]);
-            double want = std::max(ext / 253.0, step_min);
+            double want = std::max(ext / 251.0, step_min);
             int e = static_cast<int>(std::ceil(std::log2(want)));
             e = std::max(-126, std::min(127, e));
             if (std::ldexp(1.0, e) < want && e < 127)
                 e++;
             step[a] = std::ldexp(1.0, e);
             ebytes[a] = static_cast<uint32_t>(e + 127);
-            std::memcpy(&words[a], &u.lo[a], 4);
+            double lo = static_cast<double>(u.lo[a]) - step[a];
+            float f = static_cast<float>(lo);
+            if (static_cast<double>(f) > lo)
+                f = std::nextafter(f, -INFINITY);
+            org[a] = f;
+            std::memcpy(&words[a], &f, 4);
         }
         uint32_t imask = 0, n_int = 0;
         for (int s = 0; s < 8; s++)
@@ -217,15 +227,15 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
         words[4] = child_base;
         words[5] = tri_base;
         uint8_t meta[8] = {0}, qb[6][8] = {{0}};
-        uint32_t counts = 0, rank = 0;
+        uint32_t counts = 0, rank = 0, leaves = 0;
         for (int s = 0; s < 8; s++) {
             int i = child_in[s];
             if (i < 0)
                 continue;
             item const &c = ch[i];
             for (int a = 0; a < 3; a++) {
-                double lo = std::floor((static_cast<double>(c.b.lo[a]) - u.lo[a]) / step[a]) - 1.0;
-                double hi = std::ceil((static_cast<double>(c.b.hi[a]) - u.lo[a]) / step[a]) + 1.0;
+                double lo = std::floor((static_cast<double>(c.b.lo[a]) - org[a]) / step[a]) - 1.0;
+                double hi = std::ceil((static_cast<double>(c.b.hi[a]) - org[a]) / step[a]) + 1.0;
                 qb[a][s] = static_cast<uint8_t>(std::max(0.0, std::min(255.0, lo)));
                 qb[3 + a][s] = static_cast<uint8_t>(std::max(0.0, std::min(255.0, hi)));
             }
@@ -235,6 +245,7 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
             } else {
                 meta[s] = static_cast<uint8_t>(w.tri_order.size() - tri_base);
                 counts |= c.count << (4 * s);
+                leaves |= 1u << s;
                 for (uint32_t k = c.start; k < c.start + c.count; k++)
                     w.tri_order.push_back(b.tri_order[k]);
                 w.num_leaves++;
@@ -243,6 +254,7 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
         std::memcpy(&words[6], meta, 8);
         std::memcpy(&words[8], qb, 48);
         words[20] = counts;
+        words[21] = leaves;
         std::memcpy(&w.nodes[static_cast<size_t>(jb.node) * kWideWords], words, sizeof(words));
     }
     w.ok = w.max_depth <= kWideMaxDepth;

@@ -11,7 +11,8 @@
 //   w[8..19] quantized boxes: lo_x[8], lo_y[8], lo_z[8], hi_x[8], hi_y[8], hi_z[8] (bytes);
 //            a child box is p + q * step, rounded outwards by at least one step
 //   w[20]    leaf triangle counts, 4 bits per slot (0: interior or empty slot)
-//   w[21..23] unused
+//   w[21]    leaf mask (bit s: slot s is a leaf with at least one triangle)
+//   w[22..23] unused
 // Child slots are assigned per node so that, for a ray whose direction has sign octant o
 // (bit a set when d[a] < 0), visiting slots in the order k ^ o for k = 0..7 goes roughly front
 // to back (the ordering of Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs

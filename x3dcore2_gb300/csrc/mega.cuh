@@ -136,8 +136,8 @@ __device__ __forceinline__ bool mega_step(DevScene const &S, RenderArgs const &A
     }
     // --- next-event estimation: the shadow query and what it adds when unoccluded
     bool shadow = false;
-    float3 sh_d = f3(0, 0, 1), sh_vis = f3(0, 0, 0), sh_occ = f3(0, 0, 0);
-    float sh_tmax = 0.0f;
+    float3 sh_d = f3(0, 0, 1), sh_vis = f3(0, 0, 0);
+    float sh_tmax = 0.0f, sh_ad = 1.0f; // sh_ad: the light sample's area density (reference NEE)
     if (ref_nee) { // transport_direct_illum with one light sample (pathtracer.cpp:152-242)
         float pmf;
         int light = sample_light(S, rng, pmf);
@@ -145,7 +145,7 @@ __device__ __forceinline__ bool mega_step(DevScene const &S, RenderArgs const &A
         ls.area_dens *= pmf;
         float3 l = sub(ps.p, ls.p);
         float3 illum = light_eval(S, light, l, ls.n, ps.n);
-        sh_occ = divs(divs(f3(0, 0, 0), ls.area_dens), 1.0f);
+        sh_ad = ls.area_dens;
         if (!vequals0(illum)) {
             float dist = norm(l);
             sh_d = divs(neg(l), dist);
@@ -217,7 +217,7 @@ __device__ __forceinline__ bool mega_step(DevScene const &S, RenderArgs const &A
             h = r;
     }
     if (ref_nee) {
-        float3 r = shadow && visible ? sh_vis : sh_occ;
+        float3 r = shadow && visible ? sh_vis : divs(divs(f3(0, 0, 0), sh_ad), 1.0f);
         if (A.mode == E8G_MODE_REF_DIRECT) {
             int32_t light = __ldg(&S.mesh_light[ps.mesh]);
             if (light >= 0)

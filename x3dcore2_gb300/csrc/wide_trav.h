@@ -130,9 +130,24 @@ struct WideView {
 
 constexpr int kWideStack = 32; // entries; each takes two words, `stride` apart, in stk[0..63]
 
-// Byte s&3 of word w as a float (exact: 2^23 + q - 2^23).
-E8G_HD float hd_qf(uint32_t w, uint32_t s) {
-    return hd_u2f(0x4B000000u | ((w >> (8u * (s & 3u))) & 0xFFu)) - 8388608.0f;
+// Byte j of word w as the float 1 + q * 2^-15 (exact), placed into the mantissa with one byte
+// permute: result bytes (0x00, q, 0x80, 0x3F).
+E8G_HD float hd_qf(uint32_t w, uint32_t j) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (j << 4)));
+#else
+    return hd_u2f(0x3F800000u | ((w >> (8u * j)) & 0xFFu) << 8);
+#endif
+}
+
+// The permutation bit s -> bit s ^ oct of an eight-bit mask.
+E8G_HD uint32_t hd_xor_perm(uint32_t m, uint32_t oct) {
+    uint32_t a = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    m = (oct & 1u) ? a : m;
+    uint32_t b = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    m = (oct & 2u) ? b : m;
+    uint32_t c = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+    return (oct & 4u) ? c : m;
 }
 
 // any: returns at the first triangle with t in [tmin, tmax] (h.tri != miss). Otherwise returns
@@ -160,16 +175,21 @@ E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bo
     int sp = 0;
     for (uint32_t guard = 0; guard <= W.nnodes; guard++) {
         uint4 const *np = W.nodes + 6 * static_cast<size_t>(node);
-        uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4);
-        uint32_t counts = hd_ld(np + 5).x;
+        uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
+              n5 = hd_ld(np + 5);
+        uint32_t counts = n5.x, leaves = n5.y;
         if (cnt_nodes)
             (*cnt_nodes)++;
-        float sx = hd_u2f((n0.w & 0xFFu) << 23) * ix;
-        float sy = hd_u2f(((n0.w >> 8) & 0xFFu) << 23) * iy;
-        float sz = hd_u2f(((n0.w >> 16) & 0xFFu) << 23) * iz;
-        float ox = (hd_u2f(n0.x) - o.x) * ix, oy = (hd_u2f(n0.y) - o.y) * iy, oz = (hd_u2f(n0.z) - o.z) * iz;
+        // plane of byte q on axis a: p + q * step = (p - 2^15 step) + (1 + q 2^-15) * 2^15 step, so
+        // t = (1 + q 2^-15) * S + O with S = 2^15 step / d and O = (p - 2^15 step - o) / d
+        float gx = hd_u2f((n0.w & 0xFFu) << 23) * 32768.0f;
+        float gy = hd_u2f(((n0.w >> 8) & 0xFFu) << 23) * 32768.0f;
+        float gz = hd_u2f(((n0.w >> 16) & 0xFFu) << 23) * 32768.0f;
+        float sx = gx * ix, sy = gy * iy, sz = gz * iz;
+        float ox = (hd_u2f(n0.x) - gx - o.x) * ix, oy = (hd_u2f(n0.y) - gy - o.y) * iy,
+              oz = (hd_u2f(n0.z) - gz - o.z) * iz;
         uint32_t imask = n0.w >> 24;
-        uint32_t hit_int = 0, hit_leaf = 0;
+        uint32_t hits = 0;
         // slots 0-3 then 4-7; near / far planes per axis follow the ray's direction signs
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
@@ -185,23 +205,16 @@ E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bo
 #pragma unroll
 #endif
             for (uint32_t j = 0; j < 4; j++) {
-                uint32_t s = 4 * half + j;
-                bool inner = (imask >> s) & 1u;
-                if (!inner && ((counts >> (4u * s)) & 0xFu) == 0u)
-                    continue;
                 float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
                 float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
                 float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
                 float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
                 float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
-                if (tn <= tf) {
-                    if (inner)
-                        hit_int |= 1u << (s ^ oct);
-                    else
-                        hit_leaf |= 1u << s;
-                }
+                hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
             }
         }
+        uint32_t hit_leaf = hits & leaves;
+        uint32_t hit_int = hd_xor_perm(hits & imask, oct);
         // triangles of the hit leaf slots
         while (hit_leaf) {
             uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
