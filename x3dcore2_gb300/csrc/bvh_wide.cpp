@@ -160,7 +160,9 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
         for (int i = 0; i < n; i++)
             u.grow(ch[i].b);
         // slot assignment: child i goes to slot s with the smallest projection of its centre
-        // offset onto octant s's direction, greedily over all (child, slot) pairs
+        // offset onto octant s's direction, greedily over all (child, slot) pairs; a node with
+        // at most four children uses slots 0-3 only (ordered by the x and y signs), so the
+        // traversal tests one half of the slots
         int slot_of[8], child_in[8];
         for (int i = 0; i < 8; i++)
             slot_of[i] = child_in[i] = -1;
@@ -180,7 +182,7 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
             for (int i = 0; i < n; i++) {
                 if (slot_of[i] >= 0)
                     continue;
-                for (int s = 0; s < 8; s++)
+                for (int s = 0; s < (n <= 4 ? 4 : 8); s++)
                     if (child_in[s] < 0 && (bi < 0 || cost[i][s] < bc)) {
                         bi = i;
                         bs = s;

@@ -140,6 +140,27 @@ E8G_HD float hd_qf(uint32_t w, uint32_t j) {
 #endif
 }
 
+// max / min of three floats (one instruction on sm_100 and later; NaN operands are dropped like
+// fmaxf / fminf do).
+E8G_HD float hd_max3(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+E8G_HD float hd_min3(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+
 // The permutation bit s -> bit s ^ oct of an eight-bit mask.
 E8G_HD uint32_t hd_xor_perm(uint32_t m, uint32_t oct) {
     uint32_t a = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
@@ -190,11 +211,13 @@ E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bo
               oz = (hd_u2f(n0.z) - gz - o.z) * iz;
         uint32_t imask = n0.w >> 24;
         uint32_t hits = 0;
-        // slots 0-3 then 4-7; near / far planes per axis follow the ray's direction signs
+        // slots 0-3 then 4-7 (nodes with at most four children use slots 0-3 only); near / far
+        // planes per axis follow the ray's direction signs
+        uint32_t halves = ((imask | leaves) & 0xF0u) ? 2u : 1u;
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
-        for (uint32_t half = 0; half < 2; half++) {
+        for (uint32_t half = 0; half < halves; half++) {
             uint32_t lx = half ? n2.y : n2.x, hx = half ? n3.w : n3.z;
             uint32_t ly = half ? n2.w : n2.z, hy = half ? n4.y : n4.x;
             uint32_t lz = half ? n3.y : n3.x, hz = half ? n4.w : n4.z;
@@ -208,8 +231,8 @@ E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bo
                 float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
                 float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
                 float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
-                float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-                float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+                float tn = fmaxf(hd_max3(tnx, tny, tnz), tmin);
+                float tf = fminf(hd_min3(tfx, tfy, tfz), cull);
                 hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
             }
         }
