@@ -32,10 +32,12 @@ METRIC = "paths/s at fixed relMSE, plain vs wavefront-batched; adjoint/forward t
 WORKLOAD = dict(workload="displaced_icosphere_l8_1080p_64spp", triangles=1310730, width=1920,
                 height=1080, spp=64, max_depth=8, rr_start=3, materials=512, lights=4,
                 estimator="nee+bsdf power-heuristic MIS", rng="philox4x32-10")
-# DRAM traffic per path of the megakernel, from the ncu capture summarised in
-# profiles/megakernel_icosphere_l8.md (dram__bytes_read.sum + dram__bytes_write.sum divided by
-# the paths of the captured launch); None until a capture exists.
-TRAFFIC_BYTES_PER_PATH = None
+# DRAM traffic per path of the megakernel on the SAH-pair tree, from the ncu capture summarised in
+# profiles/megakernel_icosphere_l8.md: dram__bytes_read.sum + dram__bytes_write.sum of one launch
+# on a 480x270, 8-spp frame of the same scene (212.6 MB + 12.5 MB over 1,036,800 paths), scaled
+# to the full launch by its path count.
+TRAFFIC_BYTES_PER_PATH = 217.1
+INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
 
 
 def read_peaks():
@@ -147,6 +149,44 @@ def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
                                            f"(oracle), {threads} threads, {total_s:.1f} s render, BVH build {build_s:.1f} s")
 
 
+def quality_leg(ctx, p, img64, results):
+    """relMSE of the timed frame against a 4096-spp reference of the same estimator rendered with
+    independent streams (epsilon 1e-2 in the denominator). relMSE falls as 1/spp, so the spp that
+    reaches relMSE 1e-3 and each integrator's time to get there follow from the paths/s: every
+    integrator renders the same paths, so they reach it with the same spp."""
+    import ctypes as C
+    import numpy as np
+    from x3dcore2_gb300 import abi
+    q = abi.RenderParams.from_buffer_copy(p)
+    q.spp, q.seed, q.sample_offset = 4096, 4242, 0
+    q.integrator = abi.INTEGRATOR_MEGAKERNEL
+    ref = ctx.render(q)[..., :3].astype(np.float64)
+    img = img64[..., :3].astype(np.float64)
+    rel = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+    spp_needed = p.spp * rel / 1e-3
+    paths_needed = spp_needed * p.width * p.height
+    return {"reference_spp": 4096, "relmse": rel, "relmse_spp": p.spp, "spp_for_relmse_1e-3": spp_needed,
+            "seconds_to_relmse_1e-3": {k: paths_needed / r["paths_per_s"] for k, r in results.items()}}
+
+
+def bdpt_leg(ctx):
+    """Bidirectional MIS on the benchmark scene (still uploaded) at 1280x720, subpaths of at most 6
+    vertices, 32 spp: power-heuristic weights (E8G_MODE_BDPT_POWER) and the reference's uniform
+    weights (E8G_MODE_REF_BDPT)."""
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300.core import default_params
+    out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6}
+    for name, mode in (("power", abi.MODE_BDPT_POWER), ("uniform", abi.MODE_REF_BDPT)):
+        p = default_params(mode, 1280, 720, 32, seed=1, bdpt_max_len=6)
+        ctx.render(p)
+        ms = []
+        for _ in range(2):
+            ctx.render(p)
+            ms.append(ctx.stats()["kernel_ms"])
+        out[name] = {"kernel_ms": statistics.mean(ms), "paths_per_s": 1280 * 720 * 32 / (statistics.mean(ms) / 1000.0)}
+    return out
+
+
 def batch_leg(ctx, seed=1):
     """64 independent scenes in one persistent launch: seeded random soups in an enclosing box,
     triangles log-uniform in [1k, 500k], resolution from {128, 256, 512, 1024}^2, spp from
@@ -244,7 +284,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="e8g")
-    ap.add_argument("--integrator", default="both", choices=["megakernel", "wavefront", "both"])
+    ap.add_argument("--integrator", default="all", choices=["plain", "megakernel", "wavefront", "all"],
+                    help="plain: one thread per path (the baseline kernel); all: time the three")
     ap.add_argument("--small", action="store_true", help="reduced scene for quick checks (not a bench line)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -270,7 +311,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    integrators = ["megakernel", "wavefront"] if args.integrator == "both" else [args.integrator]
+    integrators = ["plain", "megakernel", "wavefront"] if args.integrator == "all" else [args.integrator]
     scene, w, h, spp = make_scene(args.small)
     if args.res:
         w, h = (int(x) for x in args.res.lower().split("x"))
@@ -312,7 +353,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     for integ in integrators:
-        p.integrator = abi.INTEGRATOR_WAVEFRONT if integ == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+        p.integrator = INTEGRATORS[integ]
         for _ in range(args.warmup):
             ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
         barrier()
@@ -343,7 +384,8 @@ def main():
     value = results[best]["paths_per_s"]
     ms_per_step = results[best]["ms_per_step"]
     launches = results[best]["launches"]
-    p.integrator = abi.INTEGRATOR_WAVEFRONT if best == "wavefront" else abi.INTEGRATOR_MEGAKERNEL
+    p.integrator = INTEGRATORS[best]
+    img64 = d_img.cpu().numpy()  # the last timed frame (every integrator renders the same paths)
 
     # traversal counts for the roofline: instrumented run of the megakernel (same paths, same rays)
     pc = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
@@ -367,7 +409,7 @@ def main():
     node_bytes = bvh["node_bytes"] // max(bvh["num_nodes"], 1)  # 32 (binary node) or 96 (wide node)
     alg_bytes = node_bytes * counts["nodes"] + 48 * counts["tris"]
     achieved = alg_bytes / (mean_kernel_ms / 1000.0) / 1e9
-    traffic = TRAFFIC_BYTES_PER_PATH * paths_per_step if TRAFFIC_BYTES_PER_PATH else None
+    traffic = TRAFFIC_BYTES_PER_PATH * paths_per_step if TRAFFIC_BYTES_PER_PATH and bvh["layout"] == 0 else None
 
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
@@ -392,6 +434,8 @@ def main():
         "clocks": clk,
     }
     if rank == 0 and not args.no_extras and world == 1:
+        line["quality"] = quality_leg(ctx, p, img64, results)
+        line["bdpt"] = bdpt_leg(ctx)
         line["batch"] = batch_leg(ctx)
         line["adjoint"] = adjoint_leg(ctx)
     if rank == 0 and not args.no_cpu_baseline and world == 1:

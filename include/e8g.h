@@ -173,7 +173,11 @@ enum {
     E8G_MODE_POSITION = 7     /* position_tracer              pathtracer.cpp:474-490 */
 };
 
-enum { E8G_INTEGRATOR_MEGAKERNEL = 0, E8G_INTEGRATOR_WAVEFRONT = 1 };
+enum {
+    E8G_INTEGRATOR_MEGAKERNEL = 0, /* persistent threads; a lane whose path ends takes the next one */
+    E8G_INTEGRATOR_WAVEFRONT = 1,  /* queues of path slots, bounce loop as a CUDA graph (E8G_MODE_MIS) */
+    E8G_INTEGRATOR_PLAIN = 2       /* one thread per path for its whole length: the baseline kernel */
+};
 
 enum {
     E8G_RNG_MINSTD = 0, /* the reference's std::minstd_rand0 stream, one stream per path */

@@ -93,6 +93,32 @@ def test_zero_spp_renders_black(ctx):
     assert np.all(img[..., :3] == 0)
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_WIDE])
+@pytest.mark.parametrize("mode", [abi.MODE_MIS, abi.MODE_REF_LT1, abi.MODE_REF_UNI])
+def test_plain_image_equals_megakernel(ctx, mode, layout):
+    """The baseline one-thread-per-path kernel and the persistent megakernel run the same paths
+    on the same streams: equal images up to the order of float accumulation."""
+    sc = S.displaced_icosphere(level=5, seed=3, num_materials=32, width=96, height=54)
+    ctx.upload(sc, layout=layout)
+    p = default_params(mode, 96, 54, 8, seed=4, max_depth=8 if mode == abi.MODE_MIS else 0, rr_start=3)
+    mk = ctx.render(p)
+    p.integrator = abi.INTEGRATOR_PLAIN
+    pl = ctx.render(p)
+    close = np.abs(pl - mk) <= np.maximum(1e-4 * np.abs(mk), 1e-5)
+    assert close.mean() >= 0.999, close.mean()
+
+
+def test_converged_mis_agrees_with_reference_estimator(ctx):
+    """Check (c) on the Cornell box of the first benchmark configuration at 256x256: the product
+    estimator (NEE + BSDF sampling, power heuristic) and the reference's unidirect_lt1 estimator,
+    both at 4096 spp with independent streams and the reference's unbounded Russian-roulette
+    policy, agree within relMSE 1e-3 (epsilon 1e-2 in the denominator)."""
+    ctx.upload(S.cornell(256, 256))
+    a = ctx.render(default_params(abi.MODE_MIS, 256, 256, 4096, seed=21))[..., :3]
+    b = ctx.render(default_params(abi.MODE_REF_LT1, 256, 256, 4096, seed=22))[..., :3]
+    assert rel_mse(a, b) < 1e-3, rel_mse(a, b)
+
+
 @pytest.mark.parametrize("capacity_small", [False, True])
 def test_wavefront_image_equals_megakernel(ctx, capacity_small):
     """Same estimator, same streams: the wavefront image equals the megakernel image up to the

@@ -110,7 +110,7 @@ e8g_status validate_params(e8g_ctx *c, e8g_render_params const *p) {
         return fail(c, E8G_ERR_INVALID_ARG, "unknown mode");
     if (p->rng > E8G_RNG_PHILOX)
         return fail(c, E8G_ERR_INVALID_ARG, "unknown rng");
-    if (p->integrator > E8G_INTEGRATOR_WAVEFRONT)
+    if (p->integrator > E8G_INTEGRATOR_PLAIN)
         return fail(c, E8G_ERR_INVALID_ARG, "unknown integrator");
     if (!(p->rr_prob > 0.0f) || p->rr_prob > 1.0f)
         return fail(c, E8G_ERR_INVALID_ARG, "rr_prob must be in (0, 1]");

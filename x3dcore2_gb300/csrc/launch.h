@@ -23,16 +23,18 @@ void launch_firefly(float const *est, uint32_t K, uint32_t w, uint32_t h, float4
 
 // Megakernel integrator (one thread per path, persistent threads refilled warp-wide).
 // counters (when non-null): [0] rays, [1] nodes, [2] tris.
+// plain: the baseline one-thread-per-path kernel instead (E8G_INTEGRATOR_PLAIN; not with counters).
 void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                       unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+                       unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st,
+                       bool plain = false);
 int megakernel_blocks_per_sm();
 // The same for one tree layout (mega_l0.cu: SAH pairs, mega_l1.cu: reference, mega_l2.cu: wide).
 void launch_mega_l0(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+                    unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
 void launch_mega_l1(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+                    unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
 void launch_mega_l2(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st);
+                    unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
 
 // Many scenes, one persistent launch (SAH-pair or eight-wide trees, any stream kind).
 struct BatchDev {

@@ -29,13 +29,13 @@ int megakernel_batch_blocks_per_sm(uint32_t rng_kinds) {
 
 
 void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                       unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st) {
+                       unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st, bool plain) {
     if (S.layout == 1)
-        launch_mega_l1(S, A, fh, accum, path_rgb, work, counters, grid, st);
+        launch_mega_l1(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
     else if (S.layout == 2)
-        launch_mega_l2(S, A, fh, accum, path_rgb, work, counters, grid, st);
+        launch_mega_l2(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
     else
-        launch_mega_l0(S, A, fh, accum, path_rgb, work, counters, grid, st);
+        launch_mega_l0(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
 }
 
 } // namespace e8g

@@ -333,6 +333,28 @@ __global__ void __launch_bounds__(kBlock, kMegaBlocksPerSm) k_mega(DevScene S, R
     }
 }
 
+// The baseline per-path kernel (E8G_INTEGRATOR_PLAIN): one thread per path index, the thread
+// walks its path to the end; a warp runs as long as its longest path and no lane is refilled.
+template <class R, int LAYOUT>
+__global__ void __launch_bounds__(kBlock, kMegaBlocksPerSm) k_plain(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
+                                                                   float4 *accum, float *path_rgb) {
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *sn = stk_all + threadIdx.x;
+    uint64_t idx = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x;
+    uint32_t pixel, sample, out;
+    if (idx >= A.total_paths || !path_coords(A, idx, pixel, sample, out))
+        return;
+    TraceCounters cnt{0, 0};
+    uint32_t rays = 0;
+    PathState ps;
+    R rng;
+    if (!mega_start(S, A, splitmix64(A.seed), fh[pixel], pixel, sample, out, ps, rng, accum, path_rgb))
+        return;
+    while (!mega_step<R, false, LAYOUT>(S, A, ps, rng, sn, &cnt, rays)) {
+    }
+    emit(A, accum, path_rgb, ps.out, mega_final(S, A, ps, fh));
+}
+
 // Many scenes in one persistent launch: the path index runs over the concatenation of every
 // scene's paths; a lane that takes a path looks up its scene (binary search over the path
 // prefix) and keeps that scene's record for the path's lifetime.
@@ -402,8 +424,19 @@ __global__ void __launch_bounds__(kBlock, kMegaBlocksPerSm) k_mega_batch(BatchDe
 
 template <int LAYOUT>
 inline void launch_layout(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                          unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st) {
+                          unsigned long long *work, unsigned long long *counters, int grid, bool plain,
+                          cudaStream_t st) {
     bool minstd = A.rng == E8G_RNG_MINSTD;
+    if (plain && !counters) {
+        unsigned blocks = static_cast<unsigned>((A.total_paths + kBlock - 1) / kBlock);
+        if (blocks == 0)
+            return;
+        if (minstd)
+            k_plain<RngMinstd, LAYOUT><<<blocks, kBlock, 0, st>>>(S, A, fh, accum, path_rgb);
+        else
+            k_plain<RngPhilox, LAYOUT><<<blocks, kBlock, 0, st>>>(S, A, fh, accum, path_rgb);
+        return;
+    }
     if (counters) {
         if (minstd)
             k_mega<RngMinstd, true, LAYOUT><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);

@@ -4,8 +4,8 @@
 namespace e8g {
 
 void launch_mega_l0(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                    unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st) {
-    launch_layout<0>(S, A, fh, accum, path_rgb, work, counters, grid, st);
+                    unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st) {
+    launch_layout<0>(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
 }
 
 int megakernel_blocks_per_sm() {

@@ -98,7 +98,7 @@ extern "C" e8g_status e8g_render_dev_noalloc(e8g_ctx *c, e8g_render_params const
         launch_bdpt(c->dev, A, fh, accum, nullptr, work, persistent_grid(c, bdpt_blocks_per_sm()), st);
     else
         launch_megakernel(c->dev, A, fh, accum, nullptr, work, nullptr, persistent_grid(c, megakernel_blocks_per_sm()),
-                          st);
+                          st, p->integrator == E8G_INTEGRATOR_PLAIN);
     launch_resolve(accum, static_cast<uint32_t>(npix), p->spp ? 1.0f / static_cast<float>(p->spp) : 0.0f,
                    d_rgba_out, st);
     e = cudaGetLastError();

@@ -30,7 +30,8 @@ e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs con
         launch_bdpt(c->dev, A, fh, accum, path_rgb, work, persistent_grid(c, bdpt_blocks_per_sm()), c->stream);
     } else {
         int grid = persistent_grid(c, megakernel_blocks_per_sm());
-        launch_megakernel(c->dev, A, fh, accum, path_rgb, work, d_counts, grid, c->stream);
+        launch_megakernel(c->dev, A, fh, accum, path_rgb, work, d_counts, grid, c->stream,
+                          p->integrator == E8G_INTEGRATOR_PLAIN);
     }
     c->launches++;
     return E8G_OK;
