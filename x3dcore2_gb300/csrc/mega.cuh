@@ -411,9 +411,7 @@ __global__ void __launch_bounds__(kBlock, kMegaBlocksPerSm) k_mega_batch(BatchDe
             continue;
         DevScene const &S = B.scenes[sid];
         RenderArgs const &A = B.args[sid];
-        bool ended = S.layout == 2 ? mega_step<R, false, 2>(S, A, ps, rng, sn, &cnt, rays)
-                                   : mega_step<R, false, 0>(S, A, ps, rng, sn, &cnt, rays);
-        if (ended) {
+        if (mega_step<R, false, 0>(S, A, ps, rng, sn, &cnt, rays)) { // batch scenes use the SAH pairs
             emit(A, accum_all + B.pix_prefix[sid], nullptr, ps.out, mega_final(S, A, ps, fh_all + B.pix_prefix[sid]));
             active = false;
         }
