@@ -106,13 +106,14 @@ def test_render_paths_rejects_bad_pixels(ctx):
         ctx.render_paths(p, np.array([64 * 48], np.uint32), np.zeros(1, np.uint32))
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_WIDE])
 @pytest.mark.parametrize("rng", [abi.RNG_PHILOX, abi.RNG_MINSTD])
-def test_wavefront_paths_match_oracle(ctx, rng):
+def test_wavefront_paths_match_oracle(ctx, rng, layout):
     """The wavefront integrator draws in the megakernel's order: per-path MIS radiance equals the
-    oracle's (and so the megakernel's)."""
+    oracle's (and so the megakernel's), with either fast tree under the dynamic-fetch kernels."""
     d = G.load("ico.npz")
     sc = G.scene_from(d)
-    ctx.upload(sc)
+    ctx.upload(sc, layout=layout)
     osc = ob.OracleScene(sc)
     w, h = int(d["width"]), int(d["height"])
     px = np.random.default_rng(9).integers(0, w * h, 3000).astype(np.uint32)

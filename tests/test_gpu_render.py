@@ -119,13 +119,14 @@ def test_converged_mis_agrees_with_reference_estimator(ctx):
     assert rel_mse(a, b) < 1e-3, rel_mse(a, b)
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_WIDE])
 @pytest.mark.parametrize("capacity_small", [False, True])
-def test_wavefront_image_equals_megakernel(ctx, capacity_small):
+def test_wavefront_image_equals_megakernel(ctx, capacity_small, layout):
     """Same estimator, same streams: the wavefront image equals the megakernel image up to the
     order of float accumulation; with few slots the queues refill many times."""
     import ctypes as C
     sc = S.displaced_icosphere(level=5, seed=3, num_materials=32, width=96, height=54)
-    ctx.upload(sc)
+    ctx.upload(sc, layout=layout)
     p = default_params(abi.MODE_MIS, 96, 54, 16, seed=2, max_depth=8, rr_start=3)
     mk = ctx.render(p)
     if capacity_small:

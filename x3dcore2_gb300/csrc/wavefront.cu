@@ -292,8 +292,9 @@ __global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Cou
 
 // Persistent trace kernel with per-lane dynamic fetch: a lane whose ray is finished takes the
 // next queue entry; lanes are refilled together (one atomic) once at least `threshold` of them
-// are idle, or when none is busy.
-template <bool ANY>
+// are idle, or when none is busy. WIDE: the eight-wide tree (one node visit per step), else the
+// SAH child pairs.
+template <bool ANY, bool WIDE>
 __global__ void __launch_bounds__(kBlock) k_wf_trace_dyn(DevScene S, RenderArgs A, WfSlots W, Counters *cnt,
                                                          float4 *accum, float *path_rgb, uint32_t threshold) {
     __shared__ uint32_t stk_all[kStackWords * kBlock];
@@ -302,9 +303,11 @@ __global__ void __launch_bounds__(kBlock) k_wf_trace_dyn(DevScene S, RenderArgs 
     uint32_t *head = ANY ? &cnt->shadow_head : &cnt->ext_head;
     const uint32_t lane = lane_id();
     constexpr uint32_t kNone = 0xFFFFFFFFu;
+    const WideView WV{S.wnodes, S.tri, S.nnodes};
     uint32_t q = kNone;
     bool exhausted = false;
     TravState T;
+    WideTrav TW;
     while (true) {
         bool idle = q == kNone && !exhausted;
         uint32_t im = __ballot_sync(~0u, idle);
@@ -319,13 +322,23 @@ __global__ void __launch_bounds__(kBlock) k_wf_trace_dyn(DevScene S, RenderArgs 
                 uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
                 if (qq < n) {
                     q = qq;
+                    float3 ro, rd;
+                    float tmax;
                     if (ANY) {
                         float4 so = W.sh_o[q], sd = W.sh_d[q];
-                        trav_begin(S, T, xyz(so), xyz(sd), 1e-4f, sd.w);
+                        ro = xyz(so);
+                        rd = xyz(sd);
+                        tmax = sd.w;
                     } else {
                         uint32_t s = W.ext_slot[q];
-                        trav_begin(S, T, xyz(W.p_mesh[s]), neg(xyz(W.o[s])), 1e-4f, 1000.0f);
+                        ro = xyz(W.p_mesh[s]);
+                        rd = neg(xyz(W.o[s]));
+                        tmax = 1000.0f;
                     }
+                    if (WIDE)
+                        wide_begin(TW, ro, rd, 1e-4f, tmax, ANY);
+                    else
+                        trav_begin(S, T, ro, rd, 1e-4f, tmax);
                 } else {
                     exhausted = true;
                 }
@@ -337,12 +350,17 @@ __global__ void __launch_bounds__(kBlock) k_wf_trace_dyn(DevScene S, RenderArgs 
                 break;
             continue;
         }
-        if (q != kNone && trav_step<ANY>(S, T, stk)) {
+        if (q == kNone)
+            continue;
+        bool done = WIDE ? wide_step(WV, TW, stk, kBlock, nullptr, nullptr) : trav_step<ANY>(S, T, stk);
+        if (done) {
             if (ANY) {
-                if (!T.found)
+                bool occluded = WIDE ? TW.h.tri != 0xFFFFFFFFu : T.found;
+                if (!occluded)
                     emit_to(A, accum, path_rgb, __float_as_uint(W.sh_o[q].w), xyz(W.sh_c[q]));
             } else {
-                W.hit[W.ext_slot[q]] = make_float4(T.best.t, __uint_as_float(T.best.tri), T.best.b1, T.best.b2);
+                Hit b = WIDE ? TW.h : T.best;
+                W.hit[W.ext_slot[q]] = make_float4(b.t, __uint_as_float(b.tri), b.b1, b.b2);
             }
             q = kNone;
         }
@@ -406,10 +424,13 @@ int wf_trace_blocks_per_sm() {
     int a = 0, b = 0, c = 0, d = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_trace_dyn<true>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_wf_trace_dyn<false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_trace_dyn<true, false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_wf_trace_dyn<false, false>, kBlock, 0);
+    int e = 0, f = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e, k_wf_trace_dyn<true, true>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_wf_trace_dyn<false, true>, kBlock, 0);
     int n = a;
-    for (int x : {b, c, d})
+    for (int x : {b, c, d, e, f})
         n = x < n ? x : n;
     return n > 0 ? n : 1;
 }
@@ -424,8 +445,11 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
     else
         k_wf_shade<RngPhilox><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
     if (threshold > 0 && S.layout == 0) {
-        k_wf_trace_dyn<true><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
-        k_wf_trace_dyn<false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_dyn<true, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_dyn<false, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+    } else if (threshold > 0 && S.layout == 2) {
+        k_wf_trace_dyn<true, true><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_dyn<false, true><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
     } else {
         k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
         k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);

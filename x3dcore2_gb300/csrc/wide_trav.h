@@ -171,131 +171,158 @@ E8G_HD uint32_t hd_xor_perm(uint32_t m, uint32_t oct) {
     return (oct & 4u) ? c : m;
 }
 
-// any: returns at the first triangle with t in [tmin, tmax] (h.tri != miss). Otherwise returns
-// the closest hit (h.tri = global triangle id, h.t = infinity on a miss). stk holds
-// 2 * kWideStack words, `stride` apart. The counters, when given, add one per node visited and
-// one per triangle tested.
-E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bool any, uint32_t *stk, int stride,
-                      uint32_t *cnt_nodes, uint32_t *cnt_tris) {
-    Hit h;
-    h.t = INFINITY;
-    h.tri = 0xFFFFFFFFu;
-    h.b1 = h.b2 = 0.0f;
-    if (W.nnodes == 0)
-        return h;
+// Resumable traversal state of one ray: wide_begin, then wide_step until it returns true. A
+// persistent trace kernel can give a lane a new ray as soon as its ray is done.
+struct WideTrav {
+    float3 o, d;     // ray (triangle tests use d as given)
+    float ix, iy, iz; // reciprocal direction of the box tests
+    float tmin, cull; // any: cull stays tmax; closest: the best hit so far
+    uint32_t oct;    // direction sign octant
+    uint32_t node;   // the node to visit next
+    int sp;          // stack entries in use
+    bool any;
+    Hit h;           // any: the occluder found; closest: the best hit (global triangle id)
+};
+
+E8G_HD void wide_begin(WideTrav &T, float3 o, float3 d, float tmin, float tmax, bool any) {
+    T.o = o;
+    T.d = d;
     // Box tests use direction components at least 1e-30 in magnitude: an exactly parallel ray
     // would turn the factored plane distance q * (step / d) + (p - o) / d into 0 * inf or
     // inf - inf. The nudged ray moves less than 1e-27 off its line over t <= 1000, and boxes are
     // inflated far beyond that, so no box a triangle hit lies in is culled; triangle tests use d.
-    float ix = 1.0f / (fabsf(d.x) < 1e-30f ? copysignf(1e-30f, d.x) : d.x);
-    float iy = 1.0f / (fabsf(d.y) < 1e-30f ? copysignf(1e-30f, d.y) : d.y);
-    float iz = 1.0f / (fabsf(d.z) < 1e-30f ? copysignf(1e-30f, d.z) : d.z);
-    uint32_t oct = (ix < 0.0f ? 1u : 0u) | (iy < 0.0f ? 2u : 0u) | (iz < 0.0f ? 4u : 0u);
-    float cull = tmax;
-    uint32_t node = 0;
-    int sp = 0;
-    for (uint32_t guard = 0; guard <= W.nnodes; guard++) {
-        uint4 const *np = W.nodes + 6 * static_cast<size_t>(node);
-        uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
-              n5 = hd_ld(np + 5);
-        uint32_t counts = n5.x, leaves = n5.y;
-        if (cnt_nodes)
-            (*cnt_nodes)++;
-        // plane of byte q on axis a: p + q * step = (p - 2^15 step) + (1 + q 2^-15) * 2^15 step, so
-        // t = (1 + q 2^-15) * S + O with S = 2^15 step / d and O = (p - 2^15 step - o) / d
-        float gx = hd_u2f((n0.w & 0xFFu) << 23) * 32768.0f;
-        float gy = hd_u2f(((n0.w >> 8) & 0xFFu) << 23) * 32768.0f;
-        float gz = hd_u2f(((n0.w >> 16) & 0xFFu) << 23) * 32768.0f;
-        float sx = gx * ix, sy = gy * iy, sz = gz * iz;
-        float ox = (hd_u2f(n0.x) - gx - o.x) * ix, oy = (hd_u2f(n0.y) - gy - o.y) * iy,
-              oz = (hd_u2f(n0.z) - gz - o.z) * iz;
-        uint32_t imask = n0.w >> 24;
-        uint32_t hits = 0;
-        // slots 0-3 then 4-7 (nodes with at most four children use slots 0-3 only); near / far
-        // planes per axis follow the ray's direction signs
-        uint32_t halves = ((imask | leaves) & 0xF0u) ? 2u : 1u;
+    T.ix = 1.0f / (fabsf(d.x) < 1e-30f ? copysignf(1e-30f, d.x) : d.x);
+    T.iy = 1.0f / (fabsf(d.y) < 1e-30f ? copysignf(1e-30f, d.y) : d.y);
+    T.iz = 1.0f / (fabsf(d.z) < 1e-30f ? copysignf(1e-30f, d.z) : d.z);
+    T.oct = (T.ix < 0.0f ? 1u : 0u) | (T.iy < 0.0f ? 2u : 0u) | (T.iz < 0.0f ? 4u : 0u);
+    T.tmin = tmin;
+    T.cull = tmax;
+    T.node = 0;
+    T.sp = 0;
+    T.any = any;
+    T.h.t = INFINITY;
+    T.h.tri = 0xFFFFFFFFu;
+    T.h.b1 = T.h.b2 = 0.0f;
+}
+
+// Visits T.node: tests its eight child boxes, the triangles of every hit leaf slot, and moves
+// T.node to the next node (the first hit interior child in octant order; the rest go on the
+// stack as one entry). Returns true when the ray is finished (stack empty, or an any-hit found).
+E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride, uint32_t *cnt_nodes,
+                      uint32_t *cnt_tris) {
+    uint4 const *np = W.nodes + 6 * static_cast<size_t>(T.node);
+    uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
+          n5 = hd_ld(np + 5);
+    uint32_t counts = n5.x, leaves = n5.y;
+    if (cnt_nodes)
+        (*cnt_nodes)++;
+    const uint32_t oct = T.oct;
+    // plane of byte q on axis a: p + q * step = (p - 2^15 step) + (1 + q 2^-15) * 2^15 step, so
+    // t = (1 + q 2^-15) * S + O with S = 2^15 step / d and O = (p - 2^15 step - o) / d
+    float gx = hd_u2f((n0.w & 0xFFu) << 23) * 32768.0f;
+    float gy = hd_u2f(((n0.w >> 8) & 0xFFu) << 23) * 32768.0f;
+    float gz = hd_u2f(((n0.w >> 16) & 0xFFu) << 23) * 32768.0f;
+    float sx = gx * T.ix, sy = gy * T.iy, sz = gz * T.iz;
+    float ox = (hd_u2f(n0.x) - gx - T.o.x) * T.ix, oy = (hd_u2f(n0.y) - gy - T.o.y) * T.iy,
+          oz = (hd_u2f(n0.z) - gz - T.o.z) * T.iz;
+    uint32_t imask = n0.w >> 24;
+    uint32_t hits = 0;
+    // slots 0-3 then 4-7 (nodes with at most four children use slots 0-3 only); near / far
+    // planes per axis follow the ray's direction signs
+    uint32_t halves = ((imask | leaves) & 0xF0u) ? 2u : 1u;
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
-        for (uint32_t half = 0; half < halves; half++) {
-            uint32_t lx = half ? n2.y : n2.x, hx = half ? n3.w : n3.z;
-            uint32_t ly = half ? n2.w : n2.z, hy = half ? n4.y : n4.x;
-            uint32_t lz = half ? n3.y : n3.x, hz = half ? n4.w : n4.z;
-            uint32_t wnx = (oct & 1u) ? hx : lx, wfx = (oct & 1u) ? lx : hx;
-            uint32_t wny = (oct & 2u) ? hy : ly, wfy = (oct & 2u) ? ly : hy;
-            uint32_t wnz = (oct & 4u) ? hz : lz, wfz = (oct & 4u) ? lz : hz;
+    for (uint32_t half = 0; half < halves; half++) {
+        uint32_t lx = half ? n2.y : n2.x, hx = half ? n3.w : n3.z;
+        uint32_t ly = half ? n2.w : n2.z, hy = half ? n4.y : n4.x;
+        uint32_t lz = half ? n3.y : n3.x, hz = half ? n4.w : n4.z;
+        uint32_t wnx = (oct & 1u) ? hx : lx, wfx = (oct & 1u) ? lx : hx;
+        uint32_t wny = (oct & 2u) ? hy : ly, wfy = (oct & 2u) ? ly : hy;
+        uint32_t wnz = (oct & 4u) ? hz : lz, wfz = (oct & 4u) ? lz : hz;
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-            for (uint32_t j = 0; j < 4; j++) {
-                float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
-                float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
-                float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
-                float tn = fmaxf(hd_max3(tnx, tny, tnz), tmin);
-                float tf = fminf(hd_min3(tfx, tfy, tfz), cull);
-                hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
-            }
+        for (uint32_t j = 0; j < 4; j++) {
+            float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
+            float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
+            float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
+            float tn = fmaxf(hd_max3(tnx, tny, tnz), T.tmin);
+            float tf = fminf(hd_min3(tfx, tfy, tfz), T.cull);
+            hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
         }
-        uint32_t hit_leaf = hits & leaves;
-        uint32_t hit_int = hd_xor_perm(hits & imask, oct);
-        // triangles of the hit leaf slots
-        while (hit_leaf) {
-            uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
-            hit_leaf &= hit_leaf - 1u;
-            uint32_t meta = (s < 4 ? n1.z : n1.w) >> (8u * (s & 3u)) & 0xFFu;
-            uint32_t k0 = n1.y + meta, k1 = k0 + ((counts >> (4u * s)) & 0xFu);
-            for (uint32_t k = k0; k < k1; k++) {
-                float4 a = hd_ld(W.tri + 3 * static_cast<size_t>(k));
-                float4 b = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 1);
-                float4 c = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 2);
-                if (cnt_tris)
-                    (*cnt_tris)++;
-                float t0, b1, b2;
-                if (hd_tri_test(o, d, a, b, c, tmin, any ? tmax : cull, t0, b1, b2)) {
-                    if (any) {
-                        h.t = t0;
-                        h.tri = hd_f2u(a.w);
-                        return h;
-                    }
-                    if (t0 < h.t) {
-                        h.t = t0;
-                        h.tri = hd_f2u(a.w);
-                        h.b1 = b1;
-                        h.b2 = b2;
-                        cull = t0;
-                    }
-                }
-            }
-        }
-        // next node: the first hit interior child in octant order, the rest on the stack
-        if (hit_int) {
-            uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
-            hit_int &= hit_int - 1u;
-            uint32_t s = k ^ oct;
-            uint32_t base = n1.x;
-            if (hit_int && sp < kWideStack) {
-                stk[sp * stride] = base;
-                stk[(kWideStack + sp) * stride] = imask << 8 | hit_int;
-                sp++;
-            }
-            node = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
-            continue;
-        }
-        if (sp == 0)
-            break;
-        uint32_t base = stk[(sp - 1) * stride];
-        uint32_t info = stk[(kWideStack + sp - 1) * stride];
-        uint32_t m = info & 0xFFu, im = info >> 8;
-        uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
-        m &= m - 1u;
-        if (m)
-            stk[(kWideStack + sp - 1) * stride] = im << 8 | m;
-        else
-            sp--;
-        uint32_t s = k ^ oct;
-        node = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
     }
-    return h;
+    uint32_t hit_leaf = hits & leaves;
+    uint32_t hit_int = hd_xor_perm(hits & imask, oct);
+    // triangles of the hit leaf slots
+    while (hit_leaf) {
+        uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
+        hit_leaf &= hit_leaf - 1u;
+        uint32_t meta = (s < 4 ? n1.z : n1.w) >> (8u * (s & 3u)) & 0xFFu;
+        uint32_t k0 = n1.y + meta, k1 = k0 + ((counts >> (4u * s)) & 0xFu);
+        for (uint32_t k = k0; k < k1; k++) {
+            float4 a = hd_ld(W.tri + 3 * static_cast<size_t>(k));
+            float4 b = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 1);
+            float4 c = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 2);
+            if (cnt_tris)
+                (*cnt_tris)++;
+            float t0, b1, b2;
+            if (hd_tri_test(T.o, T.d, a, b, c, T.tmin, T.cull, t0, b1, b2) && t0 < T.h.t) {
+                T.h.t = t0;
+                T.h.tri = hd_f2u(a.w);
+                T.h.b1 = b1;
+                T.h.b2 = b2;
+                if (T.any)
+                    return true;
+                T.cull = t0;
+            }
+        }
+    }
+    // next node: the first hit interior child in octant order, the rest on the stack
+    if (hit_int) {
+        uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
+        hit_int &= hit_int - 1u;
+        uint32_t s = k ^ oct;
+        uint32_t base = n1.x;
+        if (hit_int && T.sp < kWideStack) {
+            stk[T.sp * stride] = base;
+            stk[(kWideStack + T.sp) * stride] = imask << 8 | hit_int;
+            T.sp++;
+        }
+        T.node = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
+        return false;
+    }
+    if (T.sp == 0)
+        return true;
+    uint32_t base = stk[(T.sp - 1) * stride];
+    uint32_t info = stk[(kWideStack + T.sp - 1) * stride];
+    uint32_t m = info & 0xFFu, im = info >> 8;
+    uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
+    m &= m - 1u;
+    if (m)
+        stk[(kWideStack + T.sp - 1) * stride] = im << 8 | m;
+    else
+        T.sp--;
+    uint32_t s = k ^ oct;
+    T.node = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
+    return false;
+}
+
+// any: returns at the first triangle with t in [tmin, tmax] (h.tri != miss). Otherwise returns
+// the closest hit (h.tri = global triangle id, h.t = infinity on a miss). stk holds
+// 2 * kWideStack words, `stride` apart. The counters, when given, add one per node visited and
+// one per triangle tested. Each node is visited at most once, so the loop ends within nnodes
+// steps.
+E8G_HD Hit wide_trace(WideView W, float3 o, float3 d, float tmin, float tmax, bool any, uint32_t *stk, int stride,
+                      uint32_t *cnt_nodes, uint32_t *cnt_tris) {
+    WideTrav T;
+    wide_begin(T, o, d, tmin, tmax, any);
+    if (W.nnodes == 0)
+        return T.h;
+    for (uint32_t guard = 0; guard <= W.nnodes; guard++)
+        if (wide_step(W, T, stk, stride, cnt_nodes, cnt_tris))
+            break;
+    return T.h;
 }
 
 // The same as one out-of-line function, for kernels that trace from many call sites.
