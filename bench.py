@@ -32,11 +32,11 @@ METRIC = "paths/s at fixed relMSE, plain vs wavefront-batched; adjoint/forward t
 WORKLOAD = dict(workload="displaced_icosphere_l8_1080p_64spp", triangles=1310730, width=1920,
                 height=1080, spp=64, max_depth=8, rr_start=3, materials=512, lights=4,
                 estimator="nee+bsdf power-heuristic MIS", rng="philox4x32-10")
-# DRAM traffic per path of the megakernel on the SAH-pair tree, from the ncu capture summarised in
-# profiles/megakernel_icosphere_l8.md: dram__bytes_read.sum + dram__bytes_write.sum of one launch
-# on a 480x270, 8-spp frame of the same scene (212.6 MB + 12.5 MB over 1,036,800 paths), scaled
-# to the full launch by its path count.
-TRAFFIC_BYTES_PER_PATH = 217.1
+# DRAM traffic per path of a (tree, integrator) combination, from the ncu captures summarised in
+# profiles/: dram__bytes_read.sum + dram__bytes_write.sum over one frame of a 480x270, 8-spp
+# render of the same scene divided by its 1,036,800 paths, scaled to the full frame by its path
+# count. SAH pairs + megakernel: 212.6 MB + 12.5 MB (profiles/megakernel_icosphere_l8.md).
+TRAFFIC_BYTES_PER_PATH = {("sah", "megakernel"): 217.1}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
 
 
@@ -166,7 +166,8 @@ def quality_leg(ctx, p, img64, results):
     spp_needed = p.spp * rel / 1e-3
     paths_needed = spp_needed * p.width * p.height
     return {"reference_spp": 4096, "relmse": rel, "relmse_spp": p.spp, "spp_for_relmse_1e-3": spp_needed,
-            "seconds_to_relmse_1e-3": {k: paths_needed / r["paths_per_s"] for k, r in results.items()}}
+            "seconds_to_relmse_1e-3": {f"{k[0]}/{k[1]}": paths_needed / r["paths_per_s"]
+                                       for k, r in results.items()}}
 
 
 def bdpt_leg(ctx):
@@ -294,7 +295,8 @@ def main():
     ap.add_argument("--layout", default=None, choices=["sah", "wide", "reference"],
                     help="BVH layout (default: the library's default)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the 64-scene batch and adjoint legs")
+    ap.add_argument("--no-extras", action="store_true", help="skip the quality, BDPT, batch and adjoint legs")
+    ap.add_argument("--no-tune", action="store_true", help="wavefront with the library defaults (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -320,13 +322,9 @@ def main():
     if args.spp:
         spp = args.spp
     ctx = Context(local)
-    t0 = time.time()
-    if args.layout:
-        ctx.upload(scene, layout={"sah": abi.BVH_SAH, "wide": abi.BVH_WIDE, "reference": abi.BVH_REFERENCE}[args.layout])
-    else:
-        ctx.upload(scene)
-    commit_s = time.time() - t0
-    bvh = ctx.bvh_stats()
+    LAYOUTS = {"sah": abi.BVH_SAH, "wide": abi.BVH_WIDE, "reference": abi.BVH_REFERENCE}
+    layouts = [args.layout] if args.layout else ["sah", "wide"]
+    ctx.upload(scene, build=False)
     p = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5,
                        sample_offset=rank * spp)
     stream = torch.cuda.current_stream()
@@ -340,58 +338,74 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    tune = None
-    if "wavefront" in integrators:
+    def build(lay):
+        t0 = time.time()
+        ctx.build_bvh(layout=LAYOUTS[lay])
+        return time.time() - t0
+
+    def tune_wavefront():
         r = abi.TuneResult()
         pw = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
         abi.check(lib.e8g_wavefront_tune(ctx.h, C.byref(pw), C.byref(r)), ctx.h, "e8g_wavefront_tune")
-        tune = {"capacity": r.capacity, "bounces_per_graph": r.bounces_per_graph, "threshold": r.threshold,
+        return {"capacity": r.capacity, "bounces_per_graph": r.bounces_per_graph, "threshold": r.threshold,
                 "candidates": [[r.cand_capacity[i], r.cand_bounces[i], r.cand_threshold[i], round(r.cand_ms[i], 3)]
                                for i in range(r.num_candidates)]}
 
-    results = {}
+    results, tunes, trees = {}, {}, {}
     clocks = ClockSampler(local)
     clocks.start()
-    for integ in integrators:
-        p.integrator = INTEGRATORS[integ]
-        for _ in range(args.warmup):
-            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
-        barrier()
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        kernel_ms, launches = [], 0
-        for k in range(args.steps):
-            flush.zero_()  # L2 flush between timed steps (outside the event pair)
-            starts[k].record(stream)
-            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
-            ends[k].record(stream)
-            st = ctx.stats()
-            kernel_ms.append(st["kernel_ms"])
-            launches += st["launches"]
-        barrier()
-        total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-        if world > 1:
-            t = torch.tensor([total_ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(t.item())
-        results[integ] = dict(ms_per_step=total_ms / args.steps, kernel_ms=statistics.mean(kernel_ms),
-                              launches=launches)
+    for lay in layouts:
+        commit_s = build(lay)
+        st = ctx.bvh_stats()
+        trees[lay] = {"nodes": st["num_nodes"], "node_bytes": st["node_bytes"], "depth": st["max_depth"],
+                      "build_s": round(commit_s, 3)}
+        if "wavefront" in integrators and not args.no_tune:
+            tunes[lay] = tune_wavefront()
+        for integ in integrators:
+            p.integrator = INTEGRATORS[integ]
+            for _ in range(args.warmup):
+                ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+            barrier()
+            starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+            ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+            kernel_ms, launches = [], 0
+            for k in range(args.steps):
+                flush.zero_()  # L2 flush between timed steps (outside the event pair)
+                starts[k].record(stream)
+                ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+                ends[k].record(stream)
+                st = ctx.stats()
+                kernel_ms.append(st["kernel_ms"])
+                launches += st["launches"]
+            barrier()
+            total_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends))
+            if world > 1:
+                t = torch.tensor([total_ms], device="cuda")
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                total_ms = float(t.item())
+            results[(lay, integ)] = dict(ms_per_step=total_ms / args.steps, kernel_ms=statistics.mean(kernel_ms),
+                                         launches=launches)
     clk = clocks.stop()
     paths_per_step = w * h * spp
     for r in results.values():
         r["paths_per_s"] = paths_per_step * world / (r["ms_per_step"] / 1000.0)
     best = max(results, key=lambda k: results[k]["paths_per_s"])
+    best_lay, best_integ = best
     value = results[best]["paths_per_s"]
     ms_per_step = results[best]["ms_per_step"]
     launches = results[best]["launches"]
-    p.integrator = INTEGRATORS[best]
-    img64 = d_img.cpu().numpy()  # the last timed frame (every integrator renders the same paths)
+    img64 = d_img.cpu().numpy()  # the last timed frame (every combination renders the same paths)
+    if best_lay != layouts[-1]:  # back to the best tree (and its wavefront tuning)
+        build(best_lay)
+        if best_integ == "wavefront" and not args.no_tune:
+            tunes[best_lay] = tune_wavefront()
+    bvh = ctx.bvh_stats()
+    p.integrator = INTEGRATORS[best_integ]
 
-    # traversal counts for the roofline: instrumented run of the megakernel (same paths, same rays)
+    # traversal counts for the roofline: instrumented megakernel run on the same tree (the same
+    # paths, rays and node visits as every integrator)
     pc = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
     counts = ctx.count_traversal(pc)
-    roof_integ = "megakernel" if "megakernel" in results else best
-    mega_kernel_ms = results[roof_integ]["kernel_ms"]
 
     # end to end through the public call: host buffer, image read back every step
     e2e_ms = []
@@ -405,29 +419,34 @@ def main():
     e2e_value = paths_per_step * world / (statistics.mean(e2e_ms) / 1000.0)
 
     peak, peak_kind = read_peaks()
-    mean_kernel_ms = mega_kernel_ms
+    mean_kernel_ms = results[best]["kernel_ms"]
     node_bytes = bvh["node_bytes"] // max(bvh["num_nodes"], 1)  # 32 (binary node) or 96 (wide node)
     alg_bytes = node_bytes * counts["nodes"] + 48 * counts["tris"]
     achieved = alg_bytes / (mean_kernel_ms / 1000.0) / 1e9
-    traffic = TRAFFIC_BYTES_PER_PATH * paths_per_step if TRAFFIC_BYTES_PER_PATH and bvh["layout"] == 0 else None
+    per_path = TRAFFIC_BYTES_PER_PATH.get(best)
+    traffic = per_path * paths_per_step if per_path else None
+    roof_kernel = {"plain": "k_plain (baseline per-path kernel)", "megakernel": "k_mega (megakernel)",
+                   "wavefront": "wavefront kernels (whole bounce loop: shade + trace)"}[best_integ]
+    commit_s = trees[best_lay]["build_s"]
 
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": dict(WORKLOAD, integrator=best, l2="flushed between steps (256 MB write)",
-                       integrators={k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in r.items()}
-                                    for k, r in results.items()}, wavefront_tune=tune,
-                       small=args.small, bvh_layout=["sah", "reference", "wide"][bvh["layout"]],
-                       bvh_nodes=bvh["num_nodes"], bvh_build_ms=bvh["build_ms"],
+        "config": dict(WORKLOAD, integrator=best_integ, bvh_layout=best_lay,
+                       l2="flushed between steps (256 MB write)",
+                       integrators={f"{k[0]}/{k[1]}": {kk: (round(vv, 4) if isinstance(vv, float) else vv)
+                                                       for kk, vv in r.items()} for k, r in results.items()},
+                       trees=trees, wavefront_tune={k: {kk: v for kk, v in t.items() if kk != "candidates"}
+                                                    for k, t in tunes.items()},
+                       small=args.small, bvh_nodes=bvh["num_nodes"], bvh_build_ms=bvh["build_ms"],
                        commit_s=round(commit_s, 3)),
         "e2e": {"value": e2e_value, "unit": "paths/s", "ms_per_step": statistics.mean(e2e_ms),
                 "h2d_bytes_per_step": C.sizeof(abi.RenderParams),
                 "d2h_bytes_per_step": w * h * 16},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "k_mega (megakernel)" if roof_integ == "megakernel" else
-                               "wavefront kernels (sum over one frame)", "kernel_ms": mean_kernel_ms,
+                     "kernel": roof_kernel, "kernel_ms": mean_kernel_ms, "node_bytes": node_bytes,
                      "algorithmic_bytes": alg_bytes, "rays": counts["rays"], "nodes": counts["nodes"],
                      "tris": counts["tris"], "rays_per_s": counts["rays"] / (mean_kernel_ms / 1000.0)},
         "gpu_launches": launches,

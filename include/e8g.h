@@ -257,19 +257,21 @@ e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *
                           void *stream);
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
 
-/* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity,
- * bounces-per-graph and warp refill threshold (the number of idle lanes at which a trace kernel
- * hands its idle lanes new rays) on a short render of `params` (at most 2 spp), and keeps the
- * fastest for this context. Without it: 2^21 slots, 8 bounces per graph, threshold 16. */
+/* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity
+ * {2^20, 2^21, 2^22}, bounces per graph {2, 4, 8} and warp refill threshold {0, 4, 8, 12, 16, 24}
+ * (the number of idle lanes at which a trace kernel hands its idle lanes new rays; 0 = one ray
+ * per thread) on a short render of `params` (at most 2 spp), and keeps the fastest for this
+ * context and its current tree. Without it: 2^21 slots, 4 bounces per graph, threshold 16. */
+#define E8G_TUNE_MAX_CANDIDATES 64
 typedef struct e8g_tune_result {
     uint32_t capacity;          /* chosen number of path slots */
     uint32_t bounces_per_graph; /* chosen bounces captured in one CUDA graph */
     uint32_t threshold;         /* chosen warp refill threshold of the trace kernels (0 = off) */
     uint32_t num_candidates;
-    uint32_t cand_capacity[16];
-    uint32_t cand_bounces[16];
-    uint32_t cand_threshold[16];
-    double cand_ms[16];
+    uint32_t cand_capacity[E8G_TUNE_MAX_CANDIDATES];
+    uint32_t cand_bounces[E8G_TUNE_MAX_CANDIDATES];
+    uint32_t cand_threshold[E8G_TUNE_MAX_CANDIDATES];
+    double cand_ms[E8G_TUNE_MAX_CANDIDATES];
 } e8g_tune_result;
 e8g_status e8g_wavefront_tune(e8g_ctx *ctx, const e8g_render_params *params, e8g_tune_result *result);
 

@@ -99,9 +99,9 @@ class BatchItem(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("capacity", C.c_uint32), ("bounces_per_graph", C.c_uint32), ("threshold", C.c_uint32),
-                ("num_candidates", C.c_uint32), ("cand_capacity", C.c_uint32 * 16),
-                ("cand_bounces", C.c_uint32 * 16), ("cand_threshold", C.c_uint32 * 16),
-                ("cand_ms", C.c_double * 16)]
+                ("num_candidates", C.c_uint32), ("cand_capacity", C.c_uint32 * 64),
+                ("cand_bounces", C.c_uint32 * 64), ("cand_threshold", C.c_uint32 * 64),
+                ("cand_ms", C.c_double * 64)]
 
 
 class GenOpts(C.Structure):

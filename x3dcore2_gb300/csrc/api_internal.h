@@ -43,7 +43,7 @@ struct e8g_ctx {
     e8g_render_params fwd_params{};
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
-    uint32_t wf_capacity = 1u << 21, wf_bounces = 8, wf_threshold = 16;
+    uint32_t wf_capacity = 1u << 21, wf_bounces = 4, wf_threshold = 16;
     void *host_pinned = nullptr;
 
     std::vector<e8g::dev_buffer *> all_buffers() {

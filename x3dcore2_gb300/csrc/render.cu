@@ -224,9 +224,9 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     cudaError_t e = c->b_img.reserve(bytes);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "image buffer");
-    const uint32_t caps[] = {1u << 21, 1u << 22};
-    const uint32_t bnc[] = {4, 8};
-    const uint32_t thr[] = {0, 8, 16, 24};
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
+    const uint32_t bnc[] = {2, 4, 8};
+    const uint32_t thr[] = {0, 4, 8, 12, 16, 24};
     e8g_tune_result r{};
     double best = 1e300;
     for (uint32_t cap : caps)
@@ -242,7 +242,7 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                     return s;
                 ms = std::min(ms, c->stats.kernel_ms);
             }
-            if (r.num_candidates < 16) {
+            if (r.num_candidates < E8G_TUNE_MAX_CANDIDATES) {
                 r.cand_capacity[r.num_candidates] = cap;
                 r.cand_bounces[r.num_candidates] = b;
                 r.cand_threshold[r.num_candidates] = th;
