@@ -28,7 +28,7 @@ namespace e8g {
 
 constexpr uint32_t kWideWords = 24;     // 32-bit words per node
 constexpr uint32_t kWideMaxLeaf = 15;   // triangles per leaf slot (4-bit count)
-constexpr uint32_t kWideMaxDepth = 32;  // traversal stack entries; deeper trees are rejected
+constexpr uint32_t kWideMaxDepth = 16;  // traversal stack entries; deeper trees are rejected
 
 struct wide_bvh {
     std::vector<uint32_t> nodes;     // kWideWords per node, node 0 is the root

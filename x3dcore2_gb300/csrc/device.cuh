@@ -21,6 +21,7 @@ constexpr int kBlock = 128;                     // threads per block of the trav
 constexpr int kStack = 32;                      // per-thread (node, t) stack of the SAH layout (== kMaxTreeDepth)
 constexpr int kStackWords = 2 * kStack;          // shared words per thread: 64 node entries in reference order
 static_assert(2 * kWideStack <= kStackWords, "the eight-wide stack must fit the per-thread stack words");
+static_assert(kWideStack >= 16, "bvh_wide.h kWideMaxDepth needs 16 stack entries");
 constexpr float kOneMinusUlp = 0.999999940395355225f; // nextafter(1.0f, 0.0f)
 // Safety stop for any path, whatever the policy (the C ABI rejects policies under which paths
 // could approach it: survival <= 0.95 from depth <= 64 leaves a 1e-21 chance of reaching it).

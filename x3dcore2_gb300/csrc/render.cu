@@ -83,7 +83,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront init");
     int shade_grid = static_cast<int>(std::min<uint64_t>((Q + 255) / 256, static_cast<uint64_t>(c->num_sms) * 8));
-    int trace_grid = persistent_grid(c, wf_trace_blocks_per_sm());
+    int trace_grid = persistent_grid(c, wf_trace_blocks_per_sm(c->dev.layout, threshold));
     auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
     // capture `bounces` bounces once, replay until no slot is busy and no path is left
     cudaGraph_t graph = nullptr;

@@ -294,10 +294,15 @@ __global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Cou
 // next queue entry; lanes are refilled together (one atomic) once at least `threshold` of them
 // are idle, or when none is busy. WIDE: the eight-wide tree (one node visit per step), else the
 // SAH child pairs.
+// The wide tree's stack takes 2 * kWideStack words per thread (16 KB per block), so its kernels
+// fit eight blocks per SM when they are held to 64 registers.
+constexpr int kWfWideBlocks = 8;
+
 template <bool ANY, bool WIDE>
-__global__ void __launch_bounds__(kBlock) k_wf_trace_dyn(DevScene S, RenderArgs A, WfSlots W, Counters *cnt,
-                                                         float4 *accum, float *path_rgb, uint32_t threshold) {
-    __shared__ uint32_t stk_all[kStackWords * kBlock];
+__global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
+    k_wf_trace_dyn(DevScene S, RenderArgs A, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
+                   uint32_t threshold) {
+    __shared__ uint32_t stk_all[(WIDE ? 2 * kWideStack : kStackWords) * kBlock];
     uint32_t *stk = stk_all + threadIdx.x;
     const uint32_t n = ANY ? cnt->shadow_n : cnt->ext_n;
     uint32_t *head = ANY ? &cnt->shadow_head : &cnt->ext_head;
@@ -420,18 +425,20 @@ size_t wf_total_bytes(uint32_t capacity) {
     return total;
 }
 
-int wf_trace_blocks_per_sm() {
-    int a = 0, b = 0, c = 0, d = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_wf_trace_dyn<true, false>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d, k_wf_trace_dyn<false, false>, kBlock, 0);
-    int e = 0, f = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e, k_wf_trace_dyn<true, true>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_wf_trace_dyn<false, true>, kBlock, 0);
-    int n = a;
-    for (int x : {b, c, d, e, f})
-        n = x < n ? x : n;
+// Resident blocks per SM of the trace kernels a bounce launches for this tree and threshold.
+int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
+    int a = 0, b = 0;
+    if (threshold > 0 && layout == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_dyn<true, false>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_trace_dyn<false, false>, kBlock, 0);
+    } else if (threshold > 0 && layout == 2) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_dyn<true, true>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_trace_dyn<false, true>, kBlock, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
+    }
+    int n = a < b ? a : b;
     return n > 0 ? n : 1;
 }
 

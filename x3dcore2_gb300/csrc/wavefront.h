@@ -17,7 +17,7 @@ struct WfSlots {
 size_t wf_total_bytes(uint32_t capacity);
 WfSlots wf_carve(void *base, uint32_t capacity);
 cudaError_t wf_init(WfSlots const &W, cudaStream_t st);
-int wf_trace_blocks_per_sm();
+int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold);
 // threshold > 0: trace kernels refill idle lanes with new rays during traversal once that many
 // lanes of a warp are idle; 0: one ray per thread.
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,

@@ -128,7 +128,8 @@ struct WideView {
     uint32_t nnodes;
 };
 
-constexpr int kWideStack = 32; // entries; each takes two words, `stride` apart, in stk[0..63]
+constexpr int kWideStack = 16; // stack entries (the builder keeps the tree at most 16 levels deep);
+                               // entry i takes words 2i and 2i + 1 of stk, `stride` apart
 
 // Byte j of word w as the float 1 + q * 2^-15 (exact), placed into the mantissa with one byte
 // permute: result bytes (0x00, q, 0x80, 0x3F).
@@ -285,8 +286,8 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
         uint32_t s = k ^ oct;
         uint32_t base = n1.x;
         if (hit_int && T.sp < kWideStack) {
-            stk[T.sp * stride] = base;
-            stk[(kWideStack + T.sp) * stride] = imask << 8 | hit_int;
+            stk[2 * T.sp * stride] = base;
+            stk[(2 * T.sp + 1) * stride] = imask << 8 | hit_int;
             T.sp++;
         }
         T.node = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
@@ -294,13 +295,13 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
     }
     if (T.sp == 0)
         return true;
-    uint32_t base = stk[(T.sp - 1) * stride];
-    uint32_t info = stk[(kWideStack + T.sp - 1) * stride];
+    uint32_t base = stk[2 * (T.sp - 1) * stride];
+    uint32_t info = stk[(2 * (T.sp - 1) + 1) * stride];
     uint32_t m = info & 0xFFu, im = info >> 8;
     uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
     m &= m - 1u;
     if (m)
-        stk[(kWideStack + T.sp - 1) * stride] = im << 8 | m;
+        stk[(2 * (T.sp - 1) + 1) * stride] = im << 8 | m;
     else
         T.sp--;
     uint32_t s = k ^ oct;
