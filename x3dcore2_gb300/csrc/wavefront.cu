@@ -243,8 +243,10 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
             W.sh_c[sq] = make_float4(sh_c.x, sh_c.y, sh_c.z, 0.0f);
         }
         uint32_t eq = warp_append(&cnt->ext_n, push_ext);
-        if (push_ext)
-            W.ext_slot[eq] = s;
+        if (push_ext) {
+            W.ext_o[eq] = make_float4(p.x, p.y, p.z, __uint_as_float(s));
+            W.ext_d[eq] = make_float4(-o.x, -o.y, -o.z, 0.0f);
+        }
         if (in) {
             W.state[s] = state;
             if (state != kEmpty) {
@@ -282,11 +284,9 @@ __global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Cou
     __shared__ uint32_t stk[kStackWords * kBlock];
     uint32_t n = cnt->ext_n;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        uint32_t s = W.ext_slot[q];
-        float3 p = xyz(W.p_mesh[s]);
-        float3 d = neg(xyz(W.o[s]));
-        Hit h = trace_closest<false>(S, p, d, stk + threadIdx.x, nullptr);
-        W.hit[s] = make_float4(h.t, __uint_as_float(h.tri), h.b1, h.b2);
+        float4 eo = W.ext_o[q];
+        Hit h = trace_closest<false>(S, xyz(eo), xyz(W.ext_d[q]), stk + threadIdx.x, nullptr);
+        W.hit[__float_as_uint(eo.w)] = make_float4(h.t, __uint_as_float(h.tri), h.b1, h.b2);
     }
 }
 
@@ -335,9 +335,8 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
                         rd = xyz(sd);
                         tmax = sd.w;
                     } else {
-                        uint32_t s = W.ext_slot[q];
-                        ro = xyz(W.p_mesh[s]);
-                        rd = neg(xyz(W.o[s]));
+                        ro = xyz(W.ext_o[q]);
+                        rd = xyz(W.ext_d[q]);
                         tmax = 1000.0f;
                     }
                     if (WIDE)
@@ -365,7 +364,7 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
                     emit_to(A, accum, path_rgb, __float_as_uint(W.sh_o[q].w), xyz(W.sh_c[q]));
             } else {
                 Hit b = WIDE ? TW.h : T.best;
-                W.hit[W.ext_slot[q]] = make_float4(b.t, __uint_as_float(b.tri), b.b1, b.b2);
+                W.hit[__float_as_uint(W.ext_o[q].w)] = make_float4(b.t, __uint_as_float(b.tri), b.b1, b.b2);
             }
             q = kNone;
         }
@@ -382,19 +381,15 @@ __global__ void k_wf_reset(Counters *cnt) {
 
 } // namespace
 
-size_t wf_bytes_per_slot() {
-    // state, pixel, sample, out, rng (5 x 4) + beta_pdf, p_mesh, n_depth, o, hit (5 x 16)
-    // + shadow queue entry (3 x 16) + extension queue entry (4)
-    return 20 + 80 + 48 + 4;
-}
-
-WfSlots wf_carve(void *base, uint32_t capacity) {
+// Lays the slot arrays and queues out from `base` (each array 256-byte aligned) and returns
+// the bytes used in *total; with a null base it only measures (all pointers null).
+static WfSlots carve(char *base, uint32_t capacity, size_t *total) {
     WfSlots W{};
     W.capacity = capacity;
-    char *p = static_cast<char *>(base);
+    size_t off = 0;
     auto take = [&](size_t bytes) {
-        char *r = p;
-        p += (bytes + 255) & ~static_cast<size_t>(255);
+        char *r = base ? base + off : nullptr;
+        off += (bytes + 255) & ~static_cast<size_t>(255);
         return r;
     };
     size_t Q = capacity;
@@ -411,17 +406,21 @@ WfSlots wf_carve(void *base, uint32_t capacity) {
     W.sh_o = reinterpret_cast<float4 *>(take(Q * 16));
     W.sh_d = reinterpret_cast<float4 *>(take(Q * 16));
     W.sh_c = reinterpret_cast<float4 *>(take(Q * 16));
-    W.ext_slot = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.ext_o = reinterpret_cast<float4 *>(take(Q * 16));
+    W.ext_d = reinterpret_cast<float4 *>(take(Q * 16));
     W.counters = take(sizeof(Counters));
+    *total = off;
     return W;
 }
 
+WfSlots wf_carve(void *base, uint32_t capacity) {
+    size_t total = 0;
+    return carve(static_cast<char *>(base), capacity, &total);
+}
+
 size_t wf_total_bytes(uint32_t capacity) {
-    size_t Q = capacity, total = 0;
-    size_t sizes[] = {Q * 4, Q * 4, Q * 4, Q * 4, Q * 4, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 16, Q * 4,
-                      sizeof(Counters)};
-    for (size_t s : sizes)
-        total += (s + 255) & ~static_cast<size_t>(255);
+    size_t total = 0;
+    carve(nullptr, capacity, &total);
     return total;
 }
 

@@ -10,7 +10,7 @@ struct WfSlots {
     uint32_t *state, *pixel, *sample, *out, *rng;
     float4 *beta_pdf, *p_mesh, *n_depth, *o, *hit;
     float4 *sh_o, *sh_d, *sh_c; // shadow queue: origin | out, direction | tmax, contribution
-    uint32_t *ext_slot;         // extension queue: slot indices
+    float4 *ext_o, *ext_d;      // extension queue: origin | slot, direction
     void *counters;
 };
 
