@@ -141,6 +141,16 @@ E8G_HD float hd_qf(uint32_t w, uint32_t j) {
 #endif
 }
 
+// Brings the 96-byte node at p into L1 ahead of its use (no-op on the host).
+E8G_HD void hd_prefetch_node(uint4 const *p) {
+#if defined(__CUDA_ARCH__)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 5));
+#else
+    (void)p;
+#endif
+}
+
 // max / min of three floats (one instruction on sm_100 and later; NaN operands are dropped like
 // fmaxf / fminf do).
 E8G_HD float hd_max3(float a, float b, float c) {
@@ -255,6 +265,38 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
     }
     uint32_t hit_leaf = hits & leaves;
     uint32_t hit_int = hd_xor_perm(hits & imask, oct);
+    // the next node first (the first hit interior child in octant order, the rest on the stack,
+    // else the stack's top), prefetched so that its load overlaps this node's triangle tests
+    bool more = true;
+    uint32_t next = 0;
+    if (hit_int) {
+        uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
+        hit_int &= hit_int - 1u;
+        uint32_t s = k ^ oct;
+        uint32_t base = n1.x;
+        if (hit_int && T.sp < kWideStack) {
+            stk[2 * T.sp * stride] = base;
+            stk[(2 * T.sp + 1) * stride] = imask << 8 | hit_int;
+            T.sp++;
+        }
+        next = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
+    } else if (T.sp > 0) {
+        uint32_t base = stk[2 * (T.sp - 1) * stride];
+        uint32_t info = stk[(2 * (T.sp - 1) + 1) * stride];
+        uint32_t m = info & 0xFFu, im = info >> 8;
+        uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
+        m &= m - 1u;
+        if (m)
+            stk[(2 * (T.sp - 1) + 1) * stride] = im << 8 | m;
+        else
+            T.sp--;
+        uint32_t s = k ^ oct;
+        next = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
+    } else {
+        more = false;
+    }
+    if (more)
+        hd_prefetch_node(W.nodes + 6 * static_cast<size_t>(next));
     // triangles of the hit leaf slots
     while (hit_leaf) {
         uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
@@ -279,34 +321,8 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
             }
         }
     }
-    // next node: the first hit interior child in octant order, the rest on the stack
-    if (hit_int) {
-        uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
-        hit_int &= hit_int - 1u;
-        uint32_t s = k ^ oct;
-        uint32_t base = n1.x;
-        if (hit_int && T.sp < kWideStack) {
-            stk[2 * T.sp * stride] = base;
-            stk[(2 * T.sp + 1) * stride] = imask << 8 | hit_int;
-            T.sp++;
-        }
-        T.node = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
-        return false;
-    }
-    if (T.sp == 0)
-        return true;
-    uint32_t base = stk[2 * (T.sp - 1) * stride];
-    uint32_t info = stk[(2 * (T.sp - 1) + 1) * stride];
-    uint32_t m = info & 0xFFu, im = info >> 8;
-    uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
-    m &= m - 1u;
-    if (m)
-        stk[(2 * (T.sp - 1) + 1) * stride] = im << 8 | m;
-    else
-        T.sp--;
-    uint32_t s = k ^ oct;
-    T.node = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
-    return false;
+    T.node = next;
+    return !more;
 }
 
 // any: returns at the first triangle with t in [tmin, tmax] (h.tri != miss). Otherwise returns
