@@ -113,7 +113,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
             e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess)
             break;
-        c->launches += 4 * bounces;
+        c->launches += (c->dev.layout == 2 && threshold > 0 ? 3 : 4) * bounces; // reset, shade, trace(s)
         if (host->busy == 0 && host->next_path >= A.total_paths)
             break;
     }

@@ -371,6 +371,67 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
     }
 }
 
+// Both queues of a bounce in one launch on the eight-wide tree: queue positions below ext_n are
+// extension rays (closest hit), the rest shadow rays (any hit), so a bounce has one kernel tail
+// instead of two. Same per-lane dynamic fetch as k_wf_trace_dyn.
+__global__ void __launch_bounds__(kBlock, kWfWideBlocks)
+    k_wf_trace_wide_both(DevScene S, RenderArgs A, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
+                         uint32_t threshold) {
+    __shared__ uint32_t stk_all[2 * kWideStack * kBlock];
+    uint32_t *stk = stk_all + threadIdx.x;
+    const uint32_t n_ext = cnt->ext_n, n = n_ext + cnt->shadow_n;
+    uint32_t *head = &cnt->ext_head;
+    const uint32_t lane = lane_id();
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    const WideView WV{S.wnodes, S.tri, S.nnodes};
+    uint32_t q = kNone;
+    bool exhausted = false;
+    WideTrav T;
+    while (true) {
+        bool idle = q == kNone && !exhausted;
+        uint32_t im = __ballot_sync(~0u, idle);
+        uint32_t busy = __ballot_sync(~0u, q != kNone);
+        if (im && (__popc(im) >= threshold || busy == 0)) {
+            int leader = __ffs(im) - 1;
+            uint32_t base = 0;
+            if (static_cast<int>(lane) == leader)
+                base = atomicAdd(head, static_cast<uint32_t>(__popc(im)));
+            base = __shfl_sync(~0u, base, leader);
+            if (idle) {
+                uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
+                if (qq < n) {
+                    q = qq;
+                    if (q < n_ext) {
+                        wide_begin(T, xyz(W.ext_o[q]), xyz(W.ext_d[q]), 1e-4f, 1000.0f, false);
+                    } else {
+                        float4 sd = W.sh_d[q - n_ext];
+                        wide_begin(T, xyz(W.sh_o[q - n_ext]), xyz(sd), 1e-4f, sd.w, true);
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+            busy = __ballot_sync(~0u, q != kNone);
+        }
+        if (busy == 0) {
+            if (__ballot_sync(~0u, !exhausted) == 0)
+                break;
+            continue;
+        }
+        if (q == kNone)
+            continue;
+        if (wide_step(WV, T, stk, kBlock, nullptr, nullptr)) {
+            if (q < n_ext) {
+                W.hit[__float_as_uint(W.ext_o[q].w)] = make_float4(T.h.t, __uint_as_float(T.h.tri), T.h.b1, T.h.b2);
+            } else if (T.h.tri == 0xFFFFFFFFu) {
+                uint32_t sq = q - n_ext;
+                emit_to(A, accum, path_rgb, __float_as_uint(W.sh_o[sq].w), xyz(W.sh_c[sq]));
+            }
+            q = kNone;
+        }
+    }
+}
+
 __global__ void k_wf_reset(Counters *cnt) {
     cnt->shadow_n = 0;
     cnt->ext_n = 0;
@@ -431,8 +492,8 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_dyn<true, false>, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_trace_dyn<false, false>, kBlock, 0);
     } else if (threshold > 0 && layout == 2) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_dyn<true, true>, kBlock, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_trace_dyn<false, true>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_wide_both, kBlock, 0);
+        b = a;
     } else {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
@@ -454,8 +515,7 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
         k_wf_trace_dyn<true, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
         k_wf_trace_dyn<false, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
     } else if (threshold > 0 && S.layout == 2) {
-        k_wf_trace_dyn<true, true><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
-        k_wf_trace_dyn<false, true><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_wide_both<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
     } else {
         k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
         k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);

@@ -141,16 +141,6 @@ E8G_HD float hd_qf(uint32_t w, uint32_t j) {
 #endif
 }
 
-// Brings the 96-byte node at p into L1 ahead of its use (no-op on the host).
-E8G_HD void hd_prefetch_node(uint4 const *p) {
-#if defined(__CUDA_ARCH__)
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 5));
-#else
-    (void)p;
-#endif
-}
-
 // max / min of three floats (one instruction on sm_100 and later; NaN operands are dropped like
 // fmaxf / fminf do).
 E8G_HD float hd_max3(float a, float b, float c) {
@@ -265,8 +255,8 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
     }
     uint32_t hit_leaf = hits & leaves;
     uint32_t hit_int = hd_xor_perm(hits & imask, oct);
-    // the next node first (the first hit interior child in octant order, the rest on the stack,
-    // else the stack's top), prefetched so that its load overlaps this node's triangle tests
+    // the next node: the first hit interior child in octant order (the rest go on the stack),
+    // else the stack's top
     bool more = true;
     uint32_t next = 0;
     if (hit_int) {
@@ -295,8 +285,6 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
     } else {
         more = false;
     }
-    if (more)
-        hd_prefetch_node(W.nodes + 6 * static_cast<size_t>(next));
     // triangles of the hit leaf slots
     while (hit_leaf) {
         uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
