@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
         }
         // refill empty slots, one atomic per warp
         bool want = in && state == kEmpty;
+        bool refilled = false;
         uint32_t mask = __ballot_sync(~0u, want);
         if (mask) {
             int leader = __ffs(mask) - 1;
@@ -180,6 +181,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
                         if (light >= 0)
                             emit_to(A, accum, path_rgb, out, light_radiance(S, light, o, n));
                         state = kAtVertex;
+                        refilled = true;
                     }
                 }
             }
@@ -250,9 +252,11 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
         if (in) {
             W.state[s] = state;
             if (state != kEmpty) {
-                W.pixel[s] = pixel;
-                W.sample[s] = sample;
-                W.out[s] = out;
+                if (refilled) { // a path keeps its pixel, sample and output slot
+                    W.pixel[s] = pixel;
+                    W.sample[s] = sample;
+                    W.out[s] = out;
+                }
                 W.beta_pdf[s] = make_float4(beta.x, beta.y, beta.z, last_pdf);
                 W.p_mesh[s] = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
                 W.n_depth[s] = make_float4(n.x, n.y, n.z, __uint_as_float(depth));
