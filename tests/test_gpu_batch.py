@@ -56,3 +56,26 @@ def test_batch_mixes_stream_kinds(ctx):
         ref = ctx.render(p)
         close = np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-5)
         assert close.mean() >= 0.999, close.mean()
+
+
+def test_batch_wavefront_equals_separate_renders(ctx):
+    """The many-scene wavefront (eight-wide trees, slots shared by every scene, one graph-captured
+    bounce loop): each scene's image equals its separate wavefront render on the same tree, for
+    scenes of different sizes, resolutions, sample counts and depth policies."""
+    rng = np.random.default_rng(8)
+    scenes, params = [], []
+    for k in range(7):
+        ntri = int(np.exp(rng.uniform(np.log(1000), np.log(60000))))
+        w, h = [(32, 32), (48, 40), (64, 64), (40, 24)][k % 4]
+        sc = S.soup(ntri, seed=20 + k, width=w, height=h, roughness_lo=0.02, roughness_hi=1.0)
+        p = default_params(abi.MODE_MIS, w, h, [4, 16, 8][k % 3], seed=k + 5, max_depth=int(rng.integers(4, 11)),
+                           rr_start=3, integrator=abi.INTEGRATOR_WAVEFRONT)
+        scenes.append(sc)
+        params.append(p)
+    imgs, st = render_batch(ctx, scenes, params)
+    assert st["launches"] >= 5  # first hits, reset + shade + trace per bounce, resolve
+    for sc, p, img in zip(scenes, params, imgs):
+        ctx.upload(sc, layout=abi.BVH_WIDE)
+        ref = ctx.render(p)
+        close = np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-5)
+        assert close.mean() >= 0.999, close.mean()

@@ -39,7 +39,7 @@ struct e8g_ctx {
     // render scratch
     e8g::dev_buffer b_fh, b_accum, b_work, b_img, b_io0, b_io1, b_counts;
     // wavefront queues and adjoint state
-    e8g::dev_buffer b_wf, b_grad, b_ff; // b_ff: per-sample images of the firefly clamp
+    e8g::dev_buffer b_wf, b_grad, b_ff, b_batch; // b_ff: firefly per-sample images; b_batch: staged batch scenes
     e8g_render_params fwd_params{};
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
@@ -49,7 +49,7 @@ struct e8g_ctx {
     std::vector<e8g::dev_buffer *> all_buffers() {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
-                &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff};
+                &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch};
     }
 };
 
@@ -68,7 +68,8 @@ void fill_dev_scene(e8g_ctx *c);
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts);
 // Wavefront integrator over the image or a path list (E8G_MODE_MIS).
 e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
-                         uint32_t bounces, uint32_t threshold);
+                         uint32_t bounces, uint32_t threshold, BatchDev const *B = nullptr,
+                         FirstHit const *fh_all = nullptr);
 
 // Per-path radiance for device lists of pixels and samples into d_rgb (3 floats per path).
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,

@@ -1,10 +1,12 @@
-// e8g_batch_render: many independent scenes rendered by one persistent megakernel launch.
+// e8g_batch_render: many independent scenes rendered together.
 //
-// Every scene is packed and its SAH BVH built on the host (scenes are independent; the build
-// runs scene by scene), then all scenes go to the device in one allocation: per-scene arrays at
-// 256-byte aligned offsets, one DevScene record and one RenderArgs record per scene. One
-// batched first-hit kernel, one persistent k_mega_batch over the concatenated path ranges and
-// one batched resolve render the whole batch.
+// Every scene is packed and its tree built on the host (scene by scene), then all scenes go to
+// the device in one allocation: per-scene arrays at 256-byte aligned offsets, one DevScene record
+// and one RenderArgs record per scene. One batched first-hit kernel, the integrator over the
+// concatenated path ranges and one batched resolve render the whole batch. The integrator is the
+// many-scene wavefront on eight-wide trees (slots shared by all scenes, the bounce loop one CUDA
+// graph) when every item asks for E8G_INTEGRATOR_WAVEFRONT with E8G_MODE_MIS and one stream kind,
+// else the persistent megakernel on SAH-pair trees (k_mega_batch).
 #include "api_internal.h"
 
 #include <algorithm>
@@ -50,11 +52,15 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         if (items[k].params.firefly)
             return fail(c, E8G_ERR_UNSUPPORTED, "batches do not run the firefly clamp");
     }
+    bool use_wf = true;
+    for (uint32_t k = 0; k < n; k++)
+        use_wf = use_wf && items[k].params.integrator == E8G_INTEGRATOR_WAVEFRONT &&
+                 items[k].params.mode == E8G_MODE_MIS && items[k].params.rng == items[0].params.rng;
     cudaSetDevice(c->device);
     // host: pack, build, stage
     staged st;
     struct offs {
-        size_t nlo, nhi, tri, tidx, vpos, vnrm, mesh_mat, mesh_light, mesh_toff, mesh_area, tri_cum, mats, light_mesh,
+        size_t nlo, nhi, wide, tri, tidx, vpos, vnrm, mesh_mat, mesh_light, mesh_toff, mesh_area, tri_cum, mats, light_mesh,
             light_rad, light_cum, light_pnorm;
     };
     std::vector<offs> off(n);
@@ -65,13 +71,25 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     for (uint32_t k = 0; k < n; k++)
         rng_kinds |= 1u << items[k].params.rng;
     try {
+        for (uint32_t k = 0; k < n; k++)
+            pack_scene(*items[k].scene, packs[k]);
+        bvh_build_opts bo;
+        bo.layout = use_wf ? 2u : 0u;
+        for (uint32_t k = 0; k < n; k++)
+            build_scene_bvh(packs[k], bo);
+        for (uint32_t k = 0; k < n && use_wf; k++)
+            if (packs[k].layout != 2) { // a tree too deep for the wide stack: SAH pairs for all
+                use_wf = false;
+                bo.layout = 0;
+                for (uint32_t j = 0; j < n; j++)
+                    build_scene_bvh(packs[j], bo);
+            }
         for (uint32_t k = 0; k < n; k++) {
             packed_scene &p = packs[k];
-            pack_scene(*items[k].scene, p);
-            build_scene_bvh(p, bvh_build_opts());
             offs &o = off[k];
             o.nlo = st.put(p.bvh.lo);
             o.nhi = st.put(p.bvh.hi);
+            o.wide = st.put(p.wide);
             o.tri = st.put(p.tri);
             o.tidx = st.put(p.tidx);
             o.vpos = st.put(p.vpos);
@@ -99,7 +117,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     size_t scene_rec = (st.bytes.size() + 255) & ~static_cast<size_t>(255);
     st.bytes.resize(scene_rec + n * sizeof(DevScene));
     uint64_t total_pix = pix_prefix[n];
-    cudaError_t e = c->b_wf.reserve(st.bytes.size());
+    cudaError_t e = c->b_batch.reserve(st.bytes.size());
     if (e == cudaSuccess)
         e = c->b_fh.reserve(total_pix * sizeof(FirstHit));
     if (e == cudaSuccess)
@@ -108,13 +126,14 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         e = c->b_img.reserve(total_pix * 4 * sizeof(float));
     if (e != cudaSuccess)
         return cuda_fail(c, e, "batch buffers");
-    unsigned char *base = static_cast<unsigned char *>(c->b_wf.ptr);
+    unsigned char *base = static_cast<unsigned char *>(c->b_batch.ptr);
     for (uint32_t k = 0; k < n; k++) { // device records point into the one allocation
         packed_scene &p = packs[k];
         offs &o = off[k];
         DevScene S{};
         S.nlo = reinterpret_cast<float4 const *>(base + o.nlo);
         S.nhi = reinterpret_cast<float4 const *>(base + o.nhi);
+        S.wnodes = reinterpret_cast<uint4 const *>(base + o.wide);
         S.tri = reinterpret_cast<float4 const *>(base + o.tri);
         S.tidx = reinterpret_cast<uint4 const *>(base + o.tidx);
         S.vpos = reinterpret_cast<float4 const *>(base + o.vpos);
@@ -134,7 +153,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         S.nm = p.nm;
         S.nnodes = p.bvh.num_nodes;
         S.ntris = p.nt;
-        S.layout = 0;
+        S.layout = p.layout;
         S.total_power = p.total_power;
         for (int i = 0; i < 3; i++) {
             S.bmin[i] = p.bmin[i];
@@ -162,9 +181,18 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     if (e != cudaSuccess)
         return cuda_fail(c, e, "batch clear");
     cudaEventRecord(c->ev2, c->stream);
-    launch_megakernel_batch(B, static_cast<FirstHit const *>(c->b_fh.ptr), static_cast<float4 *>(c->b_accum.ptr),
-                            static_cast<unsigned long long *>(c->b_work.ptr), rng_kinds,
-                            persistent_grid(c, megakernel_batch_blocks_per_sm(rng_kinds)), c->stream);
+    c->launches = 0;
+    if (use_wf) {
+        e8g_status s = run_wavefront(c, args[0], static_cast<float4 *>(c->b_accum.ptr), nullptr, c->wf_capacity,
+                                     c->wf_bounces, c->wf_threshold, &B, static_cast<FirstHit const *>(c->b_fh.ptr));
+        if (s != E8G_OK)
+            return s;
+    } else {
+        launch_megakernel_batch(B, static_cast<FirstHit const *>(c->b_fh.ptr), static_cast<float4 *>(c->b_accum.ptr),
+                                static_cast<unsigned long long *>(c->b_work.ptr), rng_kinds,
+                                persistent_grid(c, megakernel_batch_blocks_per_sm(rng_kinds)), c->stream);
+        c->launches = 1;
+    }
     cudaEventRecord(c->ev3, c->stream);
     launch_resolve_batch(B, total_pix, static_cast<float4 const *>(c->b_accum.ptr), static_cast<float *>(c->b_img.ptr),
                          c->stream);
@@ -187,7 +215,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     for (uint32_t k = 0; k < n; k++)
         paths += static_cast<uint64_t>(items[k].params.width) * items[k].params.height * items[k].params.spp;
     c->stats.paths = paths;
-    c->stats.launches = 3;
+    c->stats.launches = c->launches + 2; // first hits, integrator, resolve
     if (stats)
         *stats = c->stats;
     return E8G_OK;

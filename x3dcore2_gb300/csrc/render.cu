@@ -72,8 +72,12 @@ e8g_status run_firefly(e8g_ctx *c, e8g_render_params const *p, RenderArgs const 
 } // namespace
 
 e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
-                         uint32_t bounces, uint32_t threshold) {
-    uint64_t want = std::max<uint64_t>(A.total_paths, 1024);
+                         uint32_t bounces, uint32_t threshold, BatchDev const *B, FirstHit const *fh_all) {
+    uint64_t total = B ? B->total_paths : A.total_paths;
+    uint32_t layout = B ? 2u : c->dev.layout;
+    if (B && threshold == 0)
+        threshold = 16; // the many-scene form always traces with dynamic fetch
+    uint64_t want = std::max<uint64_t>(total, 1024);
     uint32_t Q = static_cast<uint32_t>(std::min<uint64_t>(capacity, (want + 255) / 256 * 256));
     cudaError_t e = c->b_wf.reserve(wf_total_bytes(Q));
     if (e != cudaSuccess)
@@ -83,8 +87,8 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront init");
     int shade_grid = static_cast<int>(std::min<uint64_t>((Q + 255) / 256, static_cast<uint64_t>(c->num_sms) * 8));
-    int trace_grid = persistent_grid(c, wf_trace_blocks_per_sm(c->dev.layout, threshold));
-    auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
+    int trace_grid = persistent_grid(c, wf_trace_blocks_per_sm(layout, threshold));
+    auto const *fh = B ? fh_all : static_cast<FirstHit const *>(c->b_fh.ptr);
     // capture `bounces` bounces once, replay until no slot is busy and no path is left
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -92,7 +96,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront capture");
     for (uint32_t k = 0; k < bounces; k++)
-        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, threshold, c->stream);
+        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, threshold, total, B, c->stream);
     e = cudaStreamEndCapture(c->stream, &graph);
     if (e == cudaSuccess)
         e = cudaGraphInstantiate(&exec, graph, 0);
@@ -103,7 +107,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     }
     auto *host = static_cast<WfCounters *>(c->host_pinned);
     // every path needs at most kHardDepth + 2 bounces; slots refill continuously
-    uint64_t max_replays = ((A.total_paths + Q - 1) / Q + 1) * (kHardDepth + 2) / bounces + 16;
+    uint64_t max_replays = ((total + Q - 1) / Q + 1) * (kHardDepth + 2) / bounces + 16;
     uint64_t r = 0;
     for (; r < max_replays; r++) {
         e = cudaGraphLaunch(exec, c->stream);
@@ -113,8 +117,8 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
             e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess)
             break;
-        c->launches += (c->dev.layout == 2 && threshold > 0 ? 3 : 4) * bounces; // reset, shade, trace(s)
-        if (host->busy == 0 && host->next_path >= A.total_paths)
+        c->launches += (layout == 2 && threshold > 0 ? 3 : 4) * bounces; // reset, shade, trace(s)
+        if (host->busy == 0 && host->next_path >= total)
             break;
     }
     cudaGraphExecDestroy(exec);
@@ -219,7 +223,7 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
         return fail(c, E8G_ERR_INVALID_ARG, "the wavefront integrator runs E8G_MODE_MIS");
     e8g_render_params p = *params;
     p.integrator = E8G_INTEGRATOR_WAVEFRONT;
-    p.spp = std::max<uint32_t>(1, std::min<uint32_t>(p.spp, 2));
+    p.spp = std::max<uint32_t>(1, std::min<uint32_t>(p.spp, 8)); // long enough for slots to refill steadily
     size_t bytes = static_cast<size_t>(p.width) * p.height * 4 * sizeof(float);
     cudaError_t e = c->b_img.reserve(bytes);
     if (e != cudaSuccess)

@@ -94,22 +94,46 @@ template <> struct RngSlot<RngPhilox> {
 };
 
 
-template <class R>
-__global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh, WfSlots W,
-                                                  Counters *cnt, float4 *accum, float *path_rgb) {
-    const uint64_t mix = splitmix64(A.seed);
+// The scene table of a many-scene wavefront: MULTI kernels look a path's scene and render
+// arguments up by its scene index; single-scene kernels use their parameters.
+template <bool MULTI>
+__device__ __forceinline__ DevScene const &scene_of(DevScene const &S0, BatchDev const &B, uint32_t sid) {
+    if constexpr (MULTI)
+        return B.scenes[sid];
+    else
+        return S0;
+}
+template <bool MULTI>
+__device__ __forceinline__ RenderArgs const &args_of(RenderArgs const &A0, BatchDev const &B, uint32_t sid) {
+    if constexpr (MULTI)
+        return B.args[sid];
+    else
+        return A0;
+}
+
+// Shading of every slot. MULTI: paths of many scenes share the slots; a slot keeps its path's
+// scene index, `out` is the path's pixel in the concatenated accumulator and first hits are
+// indexed the same way.
+template <class R, bool MULTI>
+__global__ void __launch_bounds__(256)
+    k_wf_shade(const __grid_constant__ DevScene S0, const __grid_constant__ RenderArgs A0, BatchDev B,
+               FirstHit const *__restrict__ fh, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
+               uint64_t total_paths) {
+    const uint64_t mix0 = MULTI ? 0 : splitmix64(A0.seed);
     uint32_t busy_local = 0;
     for (uint32_t s0 = blockIdx.x * blockDim.x; s0 < W.capacity; s0 += gridDim.x * blockDim.x) {
         uint32_t s = s0 + threadIdx.x;
         bool in = s < W.capacity;
         uint32_t state = in ? W.state[s] : kEmpty;
-        uint32_t pixel = 0, sample = 0, out = 0;
+        uint32_t sid = 0, pixel = 0, sample = 0, out = 0;
         float3 beta = f3(0, 0, 0), p = f3(0, 0, 0), n = f3(0, 0, 0), o = f3(0, 0, 0);
         int32_t mesh = 0;
         uint32_t depth = 0;
         float last_pdf = 0.0f;
         R rng;
         if (state != kEmpty) {
+            if (MULTI)
+                sid = W.sid[s];
             pixel = W.pixel[s];
             sample = W.sample[s];
             out = W.out[s];
@@ -123,9 +147,10 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
             n = xyz(nd);
             depth = __float_as_uint(nd.w);
             o = xyz(W.o[s]);
-            rng = RngSlot<R>::load(A, pixel, sample, W.rng[s]);
+            rng = RngSlot<R>::load(args_of<MULTI>(A0, B, sid), pixel, sample, W.rng[s]);
         }
         if (state == kWaitHit) { // complete the extension ray shot last bounce
+            DevScene const &S = scene_of<MULTI>(S0, B, sid);
             float4 hv = W.hit[s];
             Hit h;
             h.t = hv.x;
@@ -144,7 +169,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
                         float inv_area = 1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]);
                         float p_l = pl * inv_area * (nv.t * nv.t) / cos_l2;
                         float w = power_heuristic(last_pdf, p_l);
-                        emit_to(A, accum, path_rgb, out, scale(mul(beta, light_rad(S, hl)), w));
+                        emit_to(A0, accum, path_rgb, out, scale(mul(beta, light_rad(S, hl)), w));
                     }
                     p = nv.p;
                     n = nv.n;
@@ -166,20 +191,38 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
             base = __shfl_sync(~0u, base, leader);
             if (want) {
                 uint64_t idx = base + __popc(mask & ((1u << lane_id()) - 1u));
-                if (idx < A.total_paths && path_coords(A, idx, pixel, sample, out)) {
-                    FirstHit f = fh[pixel];
+                uint32_t nsid = 0;
+                uint64_t local = idx, pbase = 0;
+                if (MULTI && idx < total_paths) { // the scene whose path range holds idx
+                    uint32_t lo = 0, hi = B.n;
+                    while (hi - lo > 1) {
+                        uint32_t mi = (lo + hi) >> 1;
+                        if (B.path_prefix[mi] <= idx)
+                            lo = mi;
+                        else
+                            hi = mi;
+                    }
+                    nsid = lo;
+                    local = idx - B.path_prefix[lo];
+                    pbase = B.pix_prefix[lo];
+                }
+                RenderArgs const &A = args_of<MULTI>(A0, B, nsid);
+                if (idx < total_paths && path_coords(A, local, pixel, sample, out)) {
+                    FirstHit f = fh[pbase + pixel];
                     int32_t m = __float_as_int(f.p.w);
                     if (m >= 0) {
+                        sid = nsid;
+                        out += static_cast<uint32_t>(pbase);
                         p = xyz(f.p);
                         n = xyz(f.n);
                         o = neg(xyz(f.d));
                         mesh = m;
                         depth = 0;
                         beta = f3(1.0f, 1.0f, 1.0f);
-                        rng = RngSlot<R>::fresh(A, mix, pixel, sample);
+                        rng = RngSlot<R>::fresh(A, MULTI ? splitmix64(A.seed) : mix0, pixel, sample);
                         int32_t light = __float_as_int(f.n.w);
                         if (light >= 0)
-                            emit_to(A, accum, path_rgb, out, light_radiance(S, light, o, n));
+                            emit_to(A, accum, path_rgb, out, light_radiance(scene_of<MULTI>(S0, B, sid), light, o, n));
                         state = kAtVertex;
                         refilled = true;
                     }
@@ -191,6 +234,8 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
         float3 sh_dir = f3(0, 0, 0), sh_c = f3(0, 0, 0);
         float sh_tmax = 0.0f;
         if (state == kAtVertex) {
+            DevScene const &S = scene_of<MULTI>(S0, B, sid);
+            RenderArgs const &A = args_of<MULTI>(A0, B, sid);
             state = kEmpty;
             bool go = !((A.max_depth && depth >= A.max_depth) || depth >= kHardDepth);
             if (go && depth >= A.rr_start) {
@@ -242,20 +287,22 @@ __global__ void __launch_bounds__(256) k_wf_shade(DevScene S, RenderArgs A, Firs
         if (push_shadow) {
             W.sh_o[sq] = make_float4(p.x, p.y, p.z, __uint_as_float(out));
             W.sh_d[sq] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, sh_tmax);
-            W.sh_c[sq] = make_float4(sh_c.x, sh_c.y, sh_c.z, 0.0f);
+            W.sh_c[sq] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(sid));
         }
         uint32_t eq = warp_append(&cnt->ext_n, push_ext);
         if (push_ext) {
             W.ext_o[eq] = make_float4(p.x, p.y, p.z, __uint_as_float(s));
-            W.ext_d[eq] = make_float4(-o.x, -o.y, -o.z, 0.0f);
+            W.ext_d[eq] = make_float4(-o.x, -o.y, -o.z, __uint_as_float(sid));
         }
         if (in) {
             W.state[s] = state;
             if (state != kEmpty) {
-                if (refilled) { // a path keeps its pixel, sample and output slot
+                if (refilled) { // a path keeps its pixel, sample, output slot and scene
                     W.pixel[s] = pixel;
                     W.sample[s] = sample;
                     W.out[s] = out;
+                    if (MULTI)
+                        W.sid[s] = sid;
                 }
                 W.beta_pdf[s] = make_float4(beta.x, beta.y, beta.z, last_pdf);
                 W.p_mesh[s] = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
@@ -377,17 +424,19 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
 
 // Both queues of a bounce in one launch on the eight-wide tree: queue positions below ext_n are
 // extension rays (closest hit), the rest shadow rays (any hit), so a bounce has one kernel tail
-// instead of two. Same per-lane dynamic fetch as k_wf_trace_dyn.
+// instead of two. Same per-lane dynamic fetch as k_wf_trace_dyn. MULTI: each ray carries its
+// scene index (w of its direction or of its contribution) and traces that scene's tree.
+template <bool MULTI>
 __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
-    k_wf_trace_wide_both(DevScene S, RenderArgs A, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
-                         uint32_t threshold) {
+    k_wf_trace_wide_both(const __grid_constant__ DevScene S0, RenderArgs A, BatchDev B, WfSlots W, Counters *cnt,
+                         float4 *accum, float *path_rgb, uint32_t threshold) {
     __shared__ uint32_t stk_all[2 * kWideStack * kBlock];
     uint32_t *stk = stk_all + threadIdx.x;
     const uint32_t n_ext = cnt->ext_n, n = n_ext + cnt->shadow_n;
     uint32_t *head = &cnt->ext_head;
     const uint32_t lane = lane_id();
     constexpr uint32_t kNone = 0xFFFFFFFFu;
-    const WideView WV{S.wnodes, S.tri, S.nnodes};
+    WideView WV{S0.wnodes, S0.tri, S0.nnodes};
     uint32_t q = kNone;
     bool exhausted = false;
     WideTrav T;
@@ -405,11 +454,19 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
                 uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
                 if (qq < n) {
                     q = qq;
+                    uint32_t sid;
                     if (q < n_ext) {
-                        wide_begin(T, xyz(W.ext_o[q]), xyz(W.ext_d[q]), 1e-4f, 1000.0f, false);
+                        float4 ed = W.ext_d[q];
+                        sid = __float_as_uint(ed.w);
+                        wide_begin(T, xyz(W.ext_o[q]), xyz(ed), 1e-4f, 1000.0f, false);
                     } else {
                         float4 sd = W.sh_d[q - n_ext];
+                        sid = MULTI ? __float_as_uint(W.sh_c[q - n_ext].w) : 0;
                         wide_begin(T, xyz(W.sh_o[q - n_ext]), xyz(sd), 1e-4f, sd.w, true);
+                    }
+                    if (MULTI) {
+                        DevScene const &S = B.scenes[sid];
+                        WV = WideView{S.wnodes, S.tri, S.nnodes};
                     }
                 } else {
                     exhausted = true;
@@ -463,6 +520,7 @@ static WfSlots carve(char *base, uint32_t capacity, size_t *total) {
     W.sample = reinterpret_cast<uint32_t *>(take(Q * 4));
     W.out = reinterpret_cast<uint32_t *>(take(Q * 4));
     W.rng = reinterpret_cast<uint32_t *>(take(Q * 4));
+    W.sid = reinterpret_cast<uint32_t *>(take(Q * 4));
     W.beta_pdf = reinterpret_cast<float4 *>(take(Q * 16));
     W.p_mesh = reinterpret_cast<float4 *>(take(Q * 16));
     W.n_depth = reinterpret_cast<float4 *>(take(Q * 16));
@@ -496,8 +554,8 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_dyn<true, false>, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_trace_dyn<false, false>, kBlock, 0);
     } else if (threshold > 0 && layout == 2) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_wide_both, kBlock, 0);
-        b = a;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_trace_wide_both<false>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_trace_wide_both<true>, kBlock, 0);
     } else {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_wf_extend, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wf_shadow, kBlock, 0);
@@ -506,20 +564,31 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
     return n > 0 ? n : 1;
 }
 
-// One bounce: reset queue lengths, shade, shadow, extend.
+// One bounce: reset queue lengths, shade, then the trace kernel(s). B (or null): the scene table
+// of a many-scene wavefront (eight-wide trees, dynamic fetch).
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
-                       float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, cudaStream_t st) {
+                       float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, uint64_t total_paths,
+                       BatchDev const *B, cudaStream_t st) {
     auto *cnt = reinterpret_cast<Counters *>(W.counters);
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
+    if (B) {
+        if (A.rng == E8G_RNG_MINSTD)
+            k_wf_shade<RngMinstd, true><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr, total_paths);
+        else
+            k_wf_shade<RngPhilox, true><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr, total_paths);
+        k_wf_trace_wide_both<true><<<trace_grid, kBlock, 0, st>>>(S, A, *B, W, cnt, accum, nullptr, threshold);
+        return;
+    }
+    BatchDev none{};
     if (A.rng == E8G_RNG_MINSTD)
-        k_wf_shade<RngMinstd><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
+        k_wf_shade<RngMinstd, false><<<shade_grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
     else
-        k_wf_shade<RngPhilox><<<shade_grid, 256, 0, st>>>(S, A, fh, W, cnt, accum, path_rgb);
+        k_wf_shade<RngPhilox, false><<<shade_grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
     if (threshold > 0 && S.layout == 0) {
         k_wf_trace_dyn<true, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
         k_wf_trace_dyn<false, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
     } else if (threshold > 0 && S.layout == 2) {
-        k_wf_trace_wide_both<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_wide_both<false><<<trace_grid, kBlock, 0, st>>>(S, A, none, W, cnt, accum, path_rgb, threshold);
     } else {
         k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
         k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);

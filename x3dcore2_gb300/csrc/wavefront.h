@@ -2,12 +2,13 @@
 #pragma once
 
 #include "device.cuh"
+#include "launch.h"
 
 namespace e8g {
 
 struct WfSlots {
     uint32_t capacity;
-    uint32_t *state, *pixel, *sample, *out, *rng;
+    uint32_t *state, *pixel, *sample, *out, *rng, *sid; // sid: scene index (many-scene wavefront)
     float4 *beta_pdf, *p_mesh, *n_depth, *o, *hit;
     float4 *sh_o, *sh_d, *sh_c; // shadow queue: origin | out, direction | tmax, contribution
     float4 *ext_o, *ext_d;      // extension queue: origin | slot, direction
@@ -20,8 +21,10 @@ cudaError_t wf_init(WfSlots const &W, cudaStream_t st);
 int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold);
 // threshold > 0: trace kernels refill idle lanes with new rays during traversal once that many
 // lanes of a warp are idle; 0: one ray per thread.
+// B: the scene table of a many-scene wavefront (eight-wide trees, threshold > 0), or null.
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
-                       float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, cudaStream_t st);
+                       float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, uint64_t total_paths,
+                       BatchDev const *B, cudaStream_t st);
 uint32_t *wf_busy_ptr(WfSlots const &W);
 unsigned long long *wf_next_ptr(WfSlots const &W);
 
