@@ -308,7 +308,12 @@ e8g_status e8g_backward(e8g_ctx *ctx, const float *dl_dimage, float *d_albedo, f
 /* Overwrite material parameters of the uploaded scene without re-uploading geometry. */
 e8g_status e8g_set_materials(e8g_ctx *ctx, const e8g_material *materials, uint32_t n);
 
-/* Render many independent scenes in one persistent launch (wavefront, batched). */
+/* Render many independent scenes together; each item has its own scene, parameters and output.
+ * When every item asks for E8G_INTEGRATOR_WAVEFRONT with E8G_MODE_MIS and the same stream kind,
+ * the scenes get eight-wide trees and share the wavefront's path slots (one graph-captured
+ * bounce loop over all scenes, with the context's wavefront settings); otherwise one persistent
+ * megakernel launch runs every path on SAH-pair trees. Unidirectional modes only; no firefly
+ * clamp. The scenes stay independent of the context's uploaded scene. */
 e8g_status e8g_batch_render(e8g_ctx *ctx, const e8g_batch_item *items, uint32_t n,
                             e8g_render_stats *stats);
 
