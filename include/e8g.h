@@ -170,7 +170,8 @@ enum {
     E8G_MODE_BDPT_POWER = 4,  /* bidirectional, power-heuristic MIS (new) */
     E8G_MODE_REF_DIRECT = 5,  /* direct_path_tracer           pathtracer.cpp:508-526 */
     E8G_MODE_NORMAL = 6,      /* normal_tracer                pathtracer.cpp:492-506 */
-    E8G_MODE_POSITION = 7     /* position_tracer              pathtracer.cpp:474-490 */
+    E8G_MODE_POSITION = 7,    /* position_tracer              pathtracer.cpp:474-490 */
+    E8G_MODE_REF_LT2 = 8      /* bidirect_lt2_path_tracer     pathtracer.cpp:655-752 */
 };
 
 enum {
@@ -202,8 +203,9 @@ typedef struct e8g_render_params {
     uint32_t sample_offset; /* first sample index (progressive rendering) */
 } e8g_render_params;
 
-/* Fill p with the reference's defaults for a mode: rr_start 2, rr_prob 0.5, unlimited depth,
- * bdpt_max_len 8, minstd stream for reference modes and Philox otherwise. */
+/* Fill p with the reference's defaults for a mode: rr_start 2 (1 for E8G_MODE_REF_LT2, the
+ * reference's mutate_depth of that tracer), rr_prob 0.5, unlimited depth, bdpt_max_len 8, minstd
+ * stream for reference modes and Philox otherwise. */
 void e8g_default_params(e8g_render_params *p, uint32_t mode, uint32_t width, uint32_t height,
                         uint32_t spp);
 

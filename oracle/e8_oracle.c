@@ -1288,6 +1288,75 @@ static v3 lt1_rec(octx *c, v3 o, const overt *vert, unsigned depth) {
     return vdivs(vadd(direct, vdivs(multi, (float)1u)), ps);
 }
 
+/* ---- bidirect_lt2_path_tracer, pathtracer.cpp:655-752 ---- */
+
+/* join_with_light_paths, pathtracer.cpp:655-699: one light sample (transport_direct_illum)
+ * plus a one-vertex light path (emission sample, the light ray's hit) joined to poi; the light
+ * ray's miss drops both terms (:667-668). */
+static v3 lt2_join(octx *c, v3 o, const overt *poi, unsigned cam_path_len) {
+    const o_scene *s = c->s;
+    v3 p1 = transport_direct_illum(c, o, poi);
+    float pmf;
+    int light = sample_light(s, c->rng, &pmf);
+    osurf em = mesh_sample(s, s->lights[light].mesh, c->rng, 0); /* area_light::sample_emssion, light.cpp:26-32 */
+    v3 w = cos_hemisphere(em.n, c->rng);
+    float sa_dens = vdot(em.n, w) / PI_F;
+    oray lr = mkray(em.p, w);
+    overt term = intersect(s, &lr);
+    if (!term.valid)
+        return V0;
+    v3 light_illum = vdivs(light_projected_radiance(s, light, w, em.n), pmf * em.area_dens * sa_dens);
+    v3 tray = vneg(w);
+    v3 join = vsub(poi->vertex, term.vertex);
+    float distance = vnorm(join);
+    join = vdivs(join, distance);
+    oray jr = mkray(term.vertex, join);
+    float cos_w2 = vdot(term.normal, tray);
+    float cos_wo = vdot(term.normal, join);
+    float cos_wi = vdot(poi->normal, vneg(join));
+    if (cos_wo > 0.0f && cos_wi > 0.0f && cos_w2 > 0.0f && !has_intersect(s, &jr, 1e-4f, distance - 1e-3f)) {
+        v3 f2 = vscale(vmul(light_illum, bsdf_eval(s, vert_mat(s, &term), term.normal, join, tray)), cos_w2);
+        v3 p2 = vscale(vmul(vdivs(vscale(f2, cos_wo), distance * distance),
+                            bsdf_eval(s, vert_mat(s, poi), poi->normal, o, vneg(join))),
+                       cos_wi);
+        if (cam_path_len == 0)
+            return vadd(p1, vscale(p2, 0.5f));
+        return vscale(vadd(p1, p2), 0.5f);
+    }
+    return p1;
+}
+
+/* bidirect_lt2_path_tracer::sample_indirect_illum, pathtracer.cpp:701-729: Russian roulette
+ * from mutate_depth = 1 (the policy's rr_start), no back-face test on the continuation's hit,
+ * and a continuation leaving below the surface (cos_w < 0, tested after the recursion) zeroes
+ * the whole vertex. */
+static v3 lt2_rec(octx *c, v3 o, const overt *vert, unsigned depth) {
+    const o_scene *s = c->s;
+    if (c->pol->max_depth && depth >= c->pol->max_depth)
+        return V0;
+    float ps = c->pol->rr_prob;
+    if (depth >= c->pol->rr_start) {
+        if (draw(c->rng) >= ps)
+            return V0;
+    } else {
+        ps = 1;
+    }
+    v3 bidirect = lt2_join(c, o, vert, depth);
+    float pdf;
+    v3 i = bsdf_sample(s, vert_mat(s, vert), c->rng, &pdf, vert->normal, o);
+    oray r = mkray(vert->vertex, i);
+    overt nv = intersect(s, &r);
+    v3 rr = V0;
+    if (nv.valid) {
+        v3 ind = lt2_rec(c, vneg(i), &nv, depth + 1);
+        float cos_w = vdot(vert->normal, i);
+        if (cos_w < 0.0f)
+            return V0;
+        rr = vdivs(vscale(vmul(ind, bsdf_eval(s, vert_mat(s, vert), vert->normal, o, i)), cos_w), pdf);
+    }
+    return vdivs(vadd(bidirect, rr), ps);
+}
+
 /* ---- bidirectional (bidirect_mis_path_tracer), pathtracer.cpp:12-137, :247-452, :754-803 ---- */
 
 typedef struct opathlet {
@@ -1811,6 +1880,14 @@ static v3 path_radiance(const o_scene *s, uint32_t mode, const o_policy *pol, or
     }
     case E8G_MODE_REF_BDPT:
         return bdpt_path(&c, &f->ray, &f->hit, f->light);
+    case E8G_MODE_REF_LT2: { /* bidirect_lt2_path_tracer::sample, :731-752 */
+        if (!f->hit.valid)
+            return V0;
+        v3 p = lt2_rec(&c, vneg(f->ray.v), &f->hit, 0);
+        if (f->light >= 0)
+            return vadd(p, light_projected_radiance(s, f->light, vneg(f->ray.v), f->hit.normal));
+        return p;
+    }
     case E8G_MODE_MIS:
         return mis_path(&c, &f->ray, &f->hit, f->light);
     case E8G_MODE_BDPT_POWER:

@@ -73,6 +73,8 @@ e8::pathtracer_factory::pt_type tracer_type(uint32_t mode) {
         return e8::pathtracer_factory::normal;
     case E8G_MODE_POSITION:
         return e8::pathtracer_factory::position;
+    case E8G_MODE_REF_LT2:
+        return e8::pathtracer_factory::bidirect_lt2;
     default:
         return e8::pathtracer_factory::unidirect_lt1;
     }

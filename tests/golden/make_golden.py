@@ -22,7 +22,8 @@ from x3dcore2_gb300 import abi, scene as S  # noqa: E402
 import oracle_bind as ob  # noqa: E402
 
 MODES = {"uni": abi.MODE_REF_UNI, "lt1": abi.MODE_REF_LT1, "bdpt": abi.MODE_REF_BDPT,
-         "direct": abi.MODE_REF_DIRECT, "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION}
+         "direct": abi.MODE_REF_DIRECT, "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION,
+         "lt2": abi.MODE_REF_LT2}
 
 
 def scene_arrays(sc):
@@ -133,12 +134,12 @@ def main(only=()):
         "bsdf": bsdf_fixture,
         "cornell": lambda: paths_fixture("cornell.npz", S.cornell(64, 48), 64, 48, 512, 7, all_modes),
         "furnace": lambda: paths_fixture("furnace.npz", S.furnace(), 32, 32, 256, 11,
-                                         ["uni", "lt1", "bdpt", "direct"]),
+                                         ["uni", "lt1", "bdpt", "direct", "lt2"]),
         "ico": lambda: paths_fixture("ico.npz", S.displaced_icosphere(level=3, seed=5, num_materials=16,
                                                                       width=48, height=27),
-                                     48, 27, 384, 3, ["uni", "lt1", "bdpt", "direct"]),
+                                     48, 27, 384, 3, ["uni", "lt1", "bdpt", "direct", "lt2"]),
         "soup": lambda: paths_fixture("soup.npz", S.soup(3000, seed=2, width=40, height=40), 40, 40, 256, 9,
-                                      ["lt1", "bdpt", "direct"]),
+                                      ["lt1", "bdpt", "direct", "lt2"]),
         "renderer": renderer_fixture,  # reads cornell.npz, so it runs after it
     }
     for name, fn in jobs.items():

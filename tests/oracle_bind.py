@@ -28,6 +28,12 @@ class OPolicy(C.Structure):
 
 
 REF_POLICY = OPolicy(0, 2, 0.5, 8)
+LT2_POLICY = OPolicy(0, 1, 0.5, 8)  # bidirect_lt2: Russian roulette from depth 1 (pathtracer.cpp:705)
+
+
+def ref_policy(mode):
+    """The reference's own policy for a tracer mode (what e8g_default_params sets)."""
+    return LT2_POLICY if mode == abi.MODE_REF_LT2 else REF_POLICY
 
 _P = C.c_void_p
 _U = C.c_uint32
@@ -162,8 +168,9 @@ class OracleScene:
         self.lib.o_trace_closest_counts(self.h, ptr(rays), len(rays), C.byref(nodes), C.byref(tris))
         return nodes.value, tris.value
 
-    def render_paths(self, mode, w, h, pixels, seeds, policy=REF_POLICY, rng=abi.RNG_MINSTD,
+    def render_paths(self, mode, w, h, pixels, seeds, policy=None, rng=abi.RNG_MINSTD,
                      seed=0, threads=8):
+        policy = ref_policy(mode) if policy is None else policy
         pixels = np.ascontiguousarray(pixels, np.uint32)
         seeds = np.ascontiguousarray(seeds, np.uint32)
         out = np.zeros((len(pixels), 3), dtype=np.float32)
@@ -171,16 +178,18 @@ class OracleScene:
                                 ptr(seeds), len(pixels), ptr(out), threads)
         return out
 
-    def render(self, mode, w, h, spp, seed=1, policy=REF_POLICY, rng=abi.RNG_MINSTD, offset=0,
+    def render(self, mode, w, h, spp, seed=1, policy=None, rng=abi.RNG_MINSTD, offset=0,
                crop=None, threads=8):
+        policy = ref_policy(mode) if policy is None else policy
         x0, y0, x1, y1 = crop if crop else (0, 0, w, h)
         out = np.zeros(((y1 - y0) * (x1 - x0), 4), dtype=np.float32)
         self.lib.o_render(self.h, mode, rng, seed, C.byref(policy), w, h, spp, offset, x0, y0, x1,
                           y1, ptr(out), threads)
         return out.reshape(y1 - y0, x1 - x0, 4)
 
-    def render_task(self, mode, w, h, spp, firefly=False, task_seed=33, policy=REF_POLICY):
+    def render_task(self, mode, w, h, spp, firefly=False, task_seed=33, policy=None):
         """pt_image_renderer::render with one task: the reference's own sequential stream."""
+        policy = ref_policy(mode) if policy is None else policy
         out = np.zeros((w * h, 4), dtype=np.float32)
         self.lib.o_render_task(self.h, mode, C.byref(policy), w, h, spp, int(firefly), task_seed, ptr(out))
         return out.reshape(h, w, 4)

@@ -13,7 +13,7 @@ from x3dcore2_gb300.core import default_params
 pytestmark = pytest.mark.gpu
 
 MODES = {"uni": abi.MODE_REF_UNI, "lt1": abi.MODE_REF_LT1, "direct": abi.MODE_REF_DIRECT,
-         "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION, "bdpt": abi.MODE_REF_BDPT}
+         "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION, "bdpt": abi.MODE_REF_BDPT, "lt2": abi.MODE_REF_LT2}
 RTOL = 1e-4
 
 

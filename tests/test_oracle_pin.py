@@ -16,7 +16,7 @@ from x3dcore2_gb300 import scene as S
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
 MODES = {"uni": abi.MODE_REF_UNI, "lt1": abi.MODE_REF_LT1, "bdpt": abi.MODE_REF_BDPT,
-         "direct": abi.MODE_REF_DIRECT, "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION}
+         "direct": abi.MODE_REF_DIRECT, "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION, "lt2": abi.MODE_REF_LT2}
 FIXTURES = ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz"]
 
 
@@ -148,7 +148,7 @@ def test_oracle_matches_live_reference(reference, seed):
     assert np.array_equal(osc.trace_any(rr, tmin, tmax), rsc.trace_any(rr, tmin, tmax))
     px = rng.integers(0, 1200, 300).astype(np.uint32)
     seeds = rng.integers(0, 2**31 - 1, 300).astype(np.uint32)
-    for mode in (abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_REF_BDPT, abi.MODE_REF_DIRECT):
+    for mode in (abi.MODE_REF_UNI, abi.MODE_REF_LT1, abi.MODE_REF_BDPT, abi.MODE_REF_DIRECT, abi.MODE_REF_LT2):
         a = osc.render_paths(mode, 40, 30, px, seeds)
         b = rsc.render_paths(mode, 40, 30, px, seeds)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), mode

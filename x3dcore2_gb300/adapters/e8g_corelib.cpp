@@ -195,6 +195,9 @@ gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space cons
     case e8::pathtracer_factory::bidirect_mis:
         mode = E8G_MODE_REF_BDPT;
         break;
+    case e8::pathtracer_factory::bidirect_lt2:
+        mode = E8G_MODE_REF_LT2;
+        break;
     case e8::pathtracer_factory::direct:
         mode = E8G_MODE_REF_DIRECT;
         break;

@@ -106,7 +106,7 @@ e8g_status validate_params(e8g_ctx *c, e8g_render_params const *p) {
         return fail(c, E8G_ERR_INVALID_ARG, "image must be at least 2x2 (pinhole_camera divides by w-1, h-1)");
     if (static_cast<uint64_t>(p->width) * p->height > (1ull << 28))
         return fail(c, E8G_ERR_INVALID_ARG, "image too large");
-    if (p->mode > E8G_MODE_POSITION)
+    if (p->mode > E8G_MODE_REF_LT2)
         return fail(c, E8G_ERR_INVALID_ARG, "unknown mode");
     if (p->rng > E8G_RNG_PHILOX)
         return fail(c, E8G_ERR_INVALID_ARG, "unknown rng");
@@ -188,7 +188,7 @@ void e8g_default_params(e8g_render_params *p, uint32_t mode, uint32_t width, uin
     p->spp = spp;
     p->seed = 1;
     p->max_depth = 0;
-    p->rr_start = 2;
+    p->rr_start = mode == E8G_MODE_REF_LT2 ? 1 : 2; // bidirect_lt2's mutate_depth (pathtracer.cpp:705)
     p->rr_prob = 0.5f;
     p->bdpt_max_len = 8;
 }

@@ -47,7 +47,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         if (!items[k].rgba_out)
             return fail(c, E8G_ERR_INVALID_ARG, "batch item has no output");
         uint32_t m = items[k].params.mode;
-        if (m == E8G_MODE_REF_BDPT || m == E8G_MODE_BDPT_POWER)
+        if (m == E8G_MODE_REF_BDPT || m == E8G_MODE_BDPT_POWER || m == E8G_MODE_REF_LT2)
             return fail(c, E8G_ERR_UNSUPPORTED, "batches run the unidirectional integrators");
         if (items[k].params.firefly)
             return fail(c, E8G_ERR_UNSUPPORTED, "batches do not run the firefly clamp");

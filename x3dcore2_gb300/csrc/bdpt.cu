@@ -451,6 +451,126 @@ int bdpt_blocks_per_sm() {
     return n > 0 ? n : 1;
 }
 
+// ---- bidirect_lt2_path_tracer (pathtracer.cpp:655-752) ----
+
+// join_with_light_paths (pathtracer.cpp:655-699): one light sample (transport_direct_illum)
+// plus a one-vertex light path joined to tv; a light ray that misses drops both terms.
+template <class R>
+__device__ __forceinline__ float3 lt2_join(DevScene const &S, R &rng, PV const &tv, uint32_t cam_len, uint32_t *stk) {
+    float pmf;
+    int light = sample_light(S, rng, pmf);
+    Surf ls = mesh_sample(S, __ldg(&S.light_mesh[light]), rng, false);
+    ls.area_dens *= pmf;
+    float3 p1 = divs(add(f3(0, 0, 0), divs(illum_source(S, light, ls.p, ls.n, tv, stk), ls.area_dens)), 1.0f);
+    float pmf2;
+    int light2 = sample_light(S, rng, pmf2);
+    Surf em = mesh_sample(S, __ldg(&S.light_mesh[light2]), rng, false); // area_light::sample_emssion
+    float3 w = cos_hemisphere(em.n, rng);
+    float sa_dens = dot(em.n, w) / kPi;
+    Hit lh = trace_closest<false>(S, em.p, w, stk, nullptr);
+    if (lh.tri == 0xFFFFFFFFu)
+        return f3(0, 0, 0);
+    float3 illum = divs(light_projected(S, light2, w, em.n), pmf2 * em.area_dens * sa_dens);
+    Vert term = make_vert(S, lh);
+    float3 tray = neg(w);
+    float3 join = sub(tv.p, term.p);
+    float dist = norm(join);
+    join = divs(join, dist);
+    float cos_w2 = dot(term.n, tray);
+    float cos_wo = dot(term.n, join);
+    float cos_wi = dot(tv.n, neg(join));
+    if (cos_wo > 0.0f && cos_wi > 0.0f && cos_w2 > 0.0f &&
+        !trace_any<false>(S, term.p, join, 1e-4f, dist - 1e-3f, stk, nullptr)) {
+        float3 f2 = scale(mul(illum, bsdf_eval(S, vert_mat(S, term.mesh), term.n, join, tray)), cos_w2);
+        float3 p2 = scale(mul(divs(scale(f2, cos_wo), dist * dist), bsdf_eval(S, vert_mat(S, tv.mesh), tv.n, tv.v, neg(join))),
+                          cos_wi);
+        return cam_len == 0 ? add(p1, scale(p2, 0.5f)) : scale(add(p1, p2), 0.5f);
+    }
+    return p1;
+}
+
+// One thread per path. The reference recurses, value(v) = (join(v) + g(v) value(next)) / survive
+// with g = f cos / pdf (sample_indirect_illum, :701-729); the kernel walks forwards with the
+// throughput beta and adds beta / survive x join(v) at each vertex. Russian roulette from depth
+// rr_start (the reference's mutate_depth = 1, e8g_default_params' value for this mode); a
+// continuation whose ray hits nothing keeps the vertex's join term, one that leaves below the
+// surface drops it and ends the path; the continuation's hit is not tested for back faces.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_lt2(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
+                                                float4 *accum, float *path_rgb, unsigned long long *work) {
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *stk = stk_all + threadIdx.x;
+    const uint64_t mix = splitmix64(A.seed);
+    const uint32_t lane = lane_id();
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32ull);
+        base = __shfl_sync(~0u, base, 0);
+        if (base >= A.total_paths)
+            break;
+        uint64_t idx = base + lane;
+        uint32_t pixel, sample, out;
+        if (idx < A.total_paths && path_coords(A, idx, pixel, sample, out)) {
+            R rng;
+            seed_path(rng, A, mix, pixel, sample);
+            FirstHit f = fh[pixel];
+            float3 L = f3(0, 0, 0);
+            int32_t fmesh = __float_as_int(f.p.w);
+            if (fmesh >= 0) {
+                PV tv;
+                tv.v = neg(xyz(f.d));
+                tv.p = xyz(f.p);
+                tv.n = xyz(f.n);
+                tv.mesh = fmesh;
+                tv.light = -1;
+                tv.dens = 1.0f;
+                float3 beta = f3(1.0f, 1.0f, 1.0f);
+                for (uint32_t depth = 0; depth < kHardDepth; depth++) {
+                    if (A.max_depth && depth >= A.max_depth)
+                        break;
+                    float surv = 1.0f;
+                    if (depth >= A.rr_start) {
+                        if (rng.next() >= A.rr_prob)
+                            break;
+                        surv = A.rr_prob;
+                    }
+                    float3 bid = lt2_join(S, rng, tv, depth, stk);
+                    float pdf;
+                    float3 i = bsdf_sample_ref(S, vert_mat(S, tv.mesh), rng, pdf, tv.n, tv.v);
+                    Hit h = trace_closest<false>(S, tv.p, i, stk, nullptr);
+                    float3 bl = divs(beta, surv);
+                    if (h.tri == 0xFFFFFFFFu) {
+                        L = add(L, mul(bl, bid));
+                        break;
+                    }
+                    float cw = dot(tv.n, i);
+                    if (cw < 0.0f)
+                        break;
+                    L = add(L, mul(bl, bid));
+                    float3 fv = bsdf_eval(S, vert_mat(S, tv.mesh), tv.n, tv.v, i);
+                    beta = divs(scale(mul(bl, fv), cw), pdf);
+                    Vert nv = make_vert(S, h);
+                    tv.v = neg(i);
+                    tv.p = nv.p;
+                    tv.n = nv.n;
+                    tv.mesh = nv.mesh;
+                }
+                int32_t fl = __float_as_int(f.n.w);
+                if (fl >= 0)
+                    L = add(L, light_projected(S, fl, neg(xyz(f.d)), xyz(f.n)));
+            }
+            if (path_rgb) {
+                path_rgb[3 * static_cast<size_t>(out)] = L.x;
+                path_rgb[3 * static_cast<size_t>(out) + 1] = L.y;
+                path_rgb[3 * static_cast<size_t>(out) + 2] = L.z;
+            } else {
+                atomicAdd(&accum[out], make_float4(L.x, L.y, L.z, 0.0f));
+            }
+        }
+    }
+}
+
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                  unsigned long long *work, int grid, cudaStream_t st) {
     if (A.mode == E8G_MODE_BDPT_POWER) {
@@ -458,6 +578,13 @@ void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, flo
             k_bdpt_power<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
         else
             k_bdpt_power<RngPhilox><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+        return;
+    }
+    if (A.mode == E8G_MODE_REF_LT2) {
+        if (A.rng == E8G_RNG_MINSTD)
+            k_lt2<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+        else
+            k_lt2<RngPhilox><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
         return;
     }
     if (A.rng == E8G_RNG_MINSTD)

@@ -94,7 +94,7 @@ extern "C" e8g_status e8g_render_dev_noalloc(e8g_ctx *c, e8g_render_params const
         return cuda_fail(c, e, "no-alloc clear");
     launch_first_hits(c->dev, p->width, p->height, fh, st);
     RenderArgs A = make_args(p);
-    if (A.mode == E8G_MODE_REF_BDPT || A.mode == E8G_MODE_BDPT_POWER)
+    if (A.mode == E8G_MODE_REF_BDPT || A.mode == E8G_MODE_BDPT_POWER || A.mode == E8G_MODE_REF_LT2)
         launch_bdpt(c->dev, A, fh, accum, nullptr, work, persistent_grid(c, bdpt_blocks_per_sm()), st);
     else
         launch_megakernel(c->dev, A, fh, accum, nullptr, work, nullptr, persistent_grid(c, megakernel_blocks_per_sm()),
