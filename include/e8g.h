@@ -232,6 +232,20 @@ typedef struct e8g_batch_item {
     float *rgba_out; /* host, width*height*4 */
 } e8g_batch_item;
 
+/* ------------------------------------------------------- compositing ---- */
+
+/* Tone mapping of a float RGBA image to 8-bit pixels (if_compositor::commit,
+ * compositor.cpp:29-98): clamp_compositor clamps every channel to [0, 1]; aces_compositor
+ * multiplies RGB by the exposure and applies the ACES filmic curve, alpha unchanged. Both then
+ * write pow(clamp(c, 0, 1), 1 / 2.2) * 255 truncated (alpha: a * 255 truncated). */
+enum { E8G_TONEMAP_CLAMP = 0, E8G_TONEMAP_ACES = 1 };
+typedef struct e8g_composite_params {
+    uint32_t tonemap;       /* E8G_TONEMAP_* */
+    uint32_t auto_exposure; /* ACES: exposure = exp(mean log(luminance + 1e-3)) over the pixels not
+                               all-zero (aces_compositor::exposure, compositor.cpp:87-98) */
+    float exposure;         /* ACES without auto exposure */
+} e8g_composite_params;
+
 /* ----------------------------------------------------------- functions ---- */
 
 e8g_status e8g_create(e8g_ctx **ctx, const e8g_device_opts *opts);
@@ -309,6 +323,14 @@ e8g_status e8g_forward(e8g_ctx *ctx, const e8g_render_params *params, float *rgb
 e8g_status e8g_backward(e8g_ctx *ctx, const float *dl_dimage, float *d_albedo, float *d_roughness);
 /* Overwrite material parameters of the uploaded scene without re-uploading geometry. */
 e8g_status e8g_set_materials(e8g_ctx *ctx, const e8g_material *materials, uint32_t n);
+
+/* Composite a float RGBA image (width*height*4) into 8-bit RGBA pixels (width*height*4 bytes).
+ * _dev: device buffers on `stream` (the caller synchronises); the host form copies in and out.
+ * Replaces aces_compositor / clamp_compositor::commit into an if_frame (compositor.cpp:49-69). */
+e8g_status e8g_composite(e8g_ctx *ctx, const float *rgba, uint32_t width, uint32_t height,
+                         const e8g_composite_params *params, uint8_t *pixels_out);
+e8g_status e8g_composite_dev(e8g_ctx *ctx, const float *d_rgba, uint32_t width, uint32_t height,
+                             const e8g_composite_params *params, uint8_t *d_pixels_out, void *stream);
 
 /* Render many independent scenes together; each item has its own scene, parameters and output.
  * When every item asks for E8G_INTEGRATOR_WAVEFRONT with E8G_MODE_MIS and the same stream kind,

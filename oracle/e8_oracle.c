@@ -2130,6 +2130,68 @@ void o_render_task(const o_scene *s, uint32_t mode, const o_policy *pol, uint32_
     free(acc);
 }
 
+/* ---- compositors, compositor.cpp:29-98 ---- */
+
+/* if_compositor::pixel_of (compositor.cpp:29-38): CLAMP to [0, 1], pow 1/2.2, * 255 truncated;
+ * alpha * 255 truncated without a clamp. */
+static unsigned char comp_channel(float c) {
+    float x = c < 0.0f ? 0.0f : (c > 1.0f ? 1.0f : c);
+    return (unsigned char)(powf(x, 1.0f / 2.2f) * 255.0f);
+}
+
+/* vec == 0.0f with the reference's epsilon: every component within 1e-5 (tensor.h:14-16, :123-128) */
+static int comp_is_zero(const float *c) {
+    for (int k = 0; k < 4; k++)
+        if (!(fabsf(c[k] - 0.0f) <= 1e-5f))
+            return 0;
+    return 1;
+}
+
+/* aces_compositor::exposure (compositor.cpp:87-98): exp of the mean log(luminance + 1e-3) over
+ * the pixels that are not all-zero, summed in float in pixel order. */
+static float comp_exposure(const float *rgba, size_t npix) {
+    unsigned n = 0;
+    float sum = 0;
+    for (size_t i = 0; i < npix; i++) {
+        const float *c = rgba + 4 * i;
+        if (!comp_is_zero(c)) {
+            float lum = c[0] * 0.299f + c[1] * 0.587f + c[2] * 0.114f; /* luminance, :83-85 */
+            sum += logf(lum + 1e-3f);
+            n++;
+        }
+    }
+    sum /= n;
+    return expf(sum);
+}
+
+void o_composite(const float *rgba, uint32_t w, uint32_t h, uint32_t tonemap, int auto_exposure, float exposure,
+                 unsigned char *out) {
+    size_t npix = (size_t)w * h;
+    float e = exposure;
+    if (tonemap == E8G_TONEMAP_ACES && auto_exposure)
+        e = comp_exposure(rgba, npix);
+    for (size_t i = 0; i < npix; i++) {
+        const float *c = rgba + 4 * i;
+        float v[4];
+        if (tonemap == E8G_TONEMAP_ACES) { /* aces_tonemap, :71-81 */
+            const float A = 2.51f, B = 0.03f, C = 2.43f, D = 0.59f, E = 0.14f;
+            for (int k = 0; k < 3; k++) {
+                float x = c[k] * e;
+                v[k] = x * (x * A + B) / (x * (x * C + D) + E);
+            }
+            v[3] = c[3];
+        } else { /* clamp_compositor::commit, :47-53: at_least(0).at_most(1) */
+            for (int k = 0; k < 4; k++) {
+                float x = 0.0f > c[k] ? 0.0f : c[k]; /* at_least, tensor.h:277-282 */
+                v[k] = 1.0f < x ? 1.0f : x;          /* at_most, tensor.h:284-289 */
+            }
+        }
+        for (int k = 0; k < 3; k++)
+            out[4 * i + k] = comp_channel(v[k]);
+        out[4 * i + 3] = (unsigned char)(v[3] * 255.0f);
+    }
+}
+
 /* ------------------------------------------------- FP64 adjoint reference -- */
 /* Double-precision restatement of the product estimator (mis_path above) and of the path-replay
  * gradient the GPU computes: same draws and discrete decisions (light, triangle, Russian

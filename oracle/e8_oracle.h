@@ -80,6 +80,11 @@ void o_firefly_add(const float *est, uint32_t w, uint32_t h, float *acc);
 void o_render_task(const o_scene *s, uint32_t mode, const o_policy *pol, uint32_t w, uint32_t h, uint32_t spp,
                    int firefly, uint32_t task_seed, float *rgba_out);
 
+/* The reference's compositors (compositor.cpp:29-98) on a float RGBA image: tonemap
+ * E8G_TONEMAP_CLAMP or E8G_TONEMAP_ACES (auto exposure or the given one); 8-bit RGBA out. */
+void o_composite(const float *rgba, uint32_t w, uint32_t h, uint32_t tonemap, int auto_exposure, float exposure,
+                 unsigned char *out);
+
 /* Seed of the per-path minstd stream; the same function as e8g_path_seed. */
 uint32_t o_path_seed(uint64_t seed, uint32_t pixel, uint32_t sample);
 /* First n draws of the minstd stream with this seed (tensor.h:987-1001 + libstdc++

@@ -41,6 +41,11 @@ template <class Base> struct open_space : public Base {
     }
 };
 
+struct mem_frame : public e8::if_frame {
+    mem_frame(unsigned w, unsigned h) { back().resize(w, h); }
+    void commit() override {}
+};
+
 struct mem_compositor : public e8::if_compositor {
     mem_compositor(unsigned w, unsigned h) : e8::if_compositor(w, h) {}
     void commit(e8::if_frame *) const override {}
@@ -335,5 +340,30 @@ uint32_t r_uv_sphere(float r, uint32_t res, int flip, float *pos_out, float *nrm
 
 uint32_t r_bvh_num_nodes(r_scene const *s) { return s->bvh->num_nodes(); }
 uint32_t r_bvh_max_depth(r_scene const *s) { return s->bvh->max_depth(); }
+
+// aces_compositor / clamp_compositor::commit (compositor.cpp:49-69) into a memory frame.
+void r_composite(float const *rgba, uint32_t w, uint32_t h, uint32_t tonemap, int auto_exposure, float exposure,
+                 uint8_t *out) {
+    std::unique_ptr<e8::if_compositor> comp;
+    if (tonemap == E8G_TONEMAP_ACES) {
+        auto a = std::make_unique<e8::aces_compositor>(w, h);
+        a->enable_auto_exposure(auto_exposure != 0);
+        a->exposure(exposure);
+        comp = std::move(a);
+    } else {
+        comp = std::make_unique<e8::clamp_compositor>(w, h);
+    }
+    for (uint32_t j = 0; j < h; j++)
+        for (uint32_t i = 0; i < w; i++) {
+            float const *c = &rgba[4 * (static_cast<size_t>(j) * w + i)];
+            (*comp)(i, j) = e8::rgba_color({c[0], c[1], c[2], c[3]});
+        }
+    mem_frame frame(w, h);
+    comp->commit(&frame);
+    for (uint32_t j = 0; j < h; j++)
+        for (uint32_t i = 0; i < w; i++)
+            for (int k = 0; k < 4; k++)
+                out[4 * (static_cast<size_t>(j) * w + i) + k] = frame(i, j)(k);
+}
 
 } // extern "C"

@@ -125,6 +125,23 @@ def renderer_fixture():
     print("renderer.npz")
 
 
+def composite_fixture():
+    """The reference's compositors (compositor.cpp:29-98) on a seeded float image with negative,
+    all-zero and above-one values: clamp and ACES, auto exposure and a fixed one."""
+    rng = np.random.default_rng(3)
+    img = np.abs(rng.lognormal(-1.0, 1.2, (37, 53, 4))).astype(np.float32)
+    img[..., 3] = rng.uniform(0.0, 1.2, (37, 53)).astype(np.float32)
+    img[0, 0] = 0.0
+    img[1, 1, :3] = -0.3
+    ref = ob.reference()
+    out = {"image": img}
+    for tm, tname in ((abi.TONEMAP_CLAMP, "clamp"), (abi.TONEMAP_ACES, "aces")):
+        for auto in (True, False):
+            out[f"{tname}_{'auto' if auto else 'fixed'}"] = ob.composite(img, tm, auto, 0.8, lib=ref)
+    np.savez_compressed(os.path.join(HERE, "composite.npz"), **out)
+    print("composite.npz")
+
+
 def main(only=()):
     subprocess.run(["make", "-s", "-C", ob.ORACLE_DIR, "all", "ref"], check=True)
     all_modes = list(MODES)
@@ -141,6 +158,7 @@ def main(only=()):
         "soup": lambda: paths_fixture("soup.npz", S.soup(3000, seed=2, width=40, height=40), 40, 40, 256, 9,
                                       ["lt1", "bdpt", "direct", "lt2"]),
         "renderer": renderer_fixture,  # reads cornell.npz, so it runs after it
+        "composite": composite_fixture,
     }
     for name, fn in jobs.items():
         if not only or name in only:

@@ -66,6 +66,7 @@ def oracle():
                                 _U, _U, _U, _P, C.c_int]),
             "o_path_seed": (_U, [C.c_uint64, _U, _U]),
             "o_firefly_add": (None, [_P, _U, _U, _P]),
+            "o_composite": (None, [_P, _U, _U, _U, C.c_int, C.c_float, _P]),
             "o_render_task": (None, [_P, _U, C.POINTER(OPolicy), _U, _U, _U, C.c_int, _U, _P]),
             "o_minstd_draws": (None, [_U, _U, _P]),
             "o_philox_draws": (None, [C.c_uint64, _U, _U, _U, _P]),
@@ -101,6 +102,7 @@ def reference(timing=False):
             "r_camera_rays": (None, [_P, _U, _U, _P]),
             "r_render_paths": (None, [_P, _U, _U, _U, _P, _P, _U, _P]),
             "r_render": (C.c_double, [_P, _U, _U, _U, _U, _U, _P, _P, C.c_int]),
+            "r_composite": (None, [_P, _U, _U, _U, C.c_int, C.c_float, _P]),
             "r_bsdf_eval": (None, [_P, C.c_int32, _P, _P, _P, _P]),
             "r_bsdf_sample": (None, [_P, C.c_int32, _U, _P, _P, _U, _P, _P]),
             "r_minstd_draws": (None, [_U, _U, _P]),
@@ -218,6 +220,18 @@ def firefly_add(est, acc):
     est = np.ascontiguousarray(est, np.float32)
     assert acc.dtype == np.float32 and acc.flags.c_contiguous and acc.shape == est.shape
     oracle().o_firefly_add(ptr(est), est.shape[1], est.shape[0], ptr(acc))
+
+
+def composite(rgba, tonemap, auto_exposure=True, exposure=1.0, lib=None):
+    """The compositors on a float (h, w, 4) image: the oracle's restatement, or the compiled
+    reference when lib is the reference library."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    h, w = rgba.shape[:2]
+    out = np.zeros((h, w, 4), np.uint8)
+    fn = (lib or oracle())
+    f = fn.r_composite if lib is not None else fn.o_composite
+    f(ptr(rgba), w, h, tonemap, int(auto_exposure), exposure, ptr(out))
+    return out
 
 
 class RefScene:

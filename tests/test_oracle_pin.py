@@ -197,3 +197,22 @@ def test_renderer_matches_live_reference(reference, mode):
         a = osc.render_task(mode, 24, 20, 3, firefly=ff)
         b, _, taken = rsc.render(mode, 24, 20, 3, 1, firefly=ff)
         assert taken == 3 and np.array_equal(a.view(np.uint32), b.view(np.uint32)), ff
+
+
+def test_compositor_matches_reference_golden(oracle):
+    """clamp_compositor and aces_compositor (compositor.cpp:29-98), auto and fixed exposure: the
+    oracle's restatement reproduces the reference's 8-bit frame exactly."""
+    d = G.load("composite.npz")
+    for tm, tname in ((abi.TONEMAP_CLAMP, "clamp"), (abi.TONEMAP_ACES, "aces")):
+        for auto in (True, False):
+            got = ob.composite(d["image"], tm, auto, 0.8)
+            assert np.array_equal(got, d[f"{tname}_{'auto' if auto else 'fixed'}"]), (tname, auto)
+
+
+def test_compositor_matches_live_reference(reference):
+    rng = np.random.default_rng(11)
+    img = rng.gamma(0.7, 1.5, (64, 48, 4)).astype(np.float32)
+    img[::7, ::5] = 0.0
+    for tm in (abi.TONEMAP_CLAMP, abi.TONEMAP_ACES):
+        for auto in (True, False):
+            assert np.array_equal(ob.composite(img, tm, auto, 1.7), ob.composite(img, tm, auto, 1.7, lib=reference))

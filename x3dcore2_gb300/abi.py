@@ -24,6 +24,8 @@ MODE_REF_DIRECT, MODE_NORMAL, MODE_POSITION, MODE_REF_LT2 = 5, 6, 7, 8
 INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT, INTEGRATOR_PLAIN = 0, 1, 2
 RNG_MINSTD, RNG_PHILOX = 0, 1
 BVH_SAH, BVH_REFERENCE, BVH_WIDE = 0, 1, 2
+# compositing
+TONEMAP_CLAMP, TONEMAP_ACES = 0, 1
 # generators
 GEN_CORNELL, GEN_DISPLACED_ICO, GEN_SOUP, GEN_FURNACE = 0, 1, 2, 3
 
@@ -116,6 +118,10 @@ _U32 = C.c_uint32
 _ST = C.c_int
 
 # name -> (restype, argtypes); every symbol include/e8g.h declares
+class CompositeParams(C.Structure):
+    _fields_ = [("tonemap", C.c_uint32), ("auto_exposure", C.c_uint32), ("exposure", C.c_float)]
+
+
 SIGNATURES = {
     "e8g_create": (_ST, [C.POINTER(_P), _P]),
     "e8g_destroy": (_ST, [_P]),
@@ -133,6 +139,8 @@ SIGNATURES = {
     "e8g_render_dev": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_render_dev_noalloc": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
+    "e8g_composite": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P]),
+    "e8g_composite_dev": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P, _P]),
     "e8g_count_traversal": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(RenderStats)]),
     "e8g_wavefront_tune": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(TuneResult)]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),

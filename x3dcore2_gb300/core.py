@@ -121,6 +121,15 @@ class Context:
                                               len(pixels), _ptr(out)), "e8g_render_paths")
         return out
 
+    def composite(self, rgba, tonemap=abi.TONEMAP_ACES, auto_exposure=True, exposure=1.0):
+        """e8g_composite: the reference's compositors on a float (h, w, 4) image -> uint8 RGBA."""
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        h, w = rgba.shape[:2]
+        out = np.zeros((h, w, 4), np.uint8)
+        cp = abi.CompositeParams(tonemap, int(auto_exposure), exposure)
+        self._check(self.lib.e8g_composite(self.h, _ptr(rgba), w, h, C.byref(cp), _ptr(out)), "e8g_composite")
+        return out
+
     def stats(self):
         s = abi.RenderStats()
         self._check(self.lib.e8g_get_render_stats(self.h, C.byref(s)), "e8g_get_render_stats")
