@@ -271,6 +271,14 @@ e8g_status e8g_render(e8g_ctx *ctx, const e8g_render_params *params, float *rgba
 /* Same, writing a device buffer; the caller synchronises. */
 e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
                           void *stream);
+/* Progressive rendering on the device: adds params->spp samples per call to the context's
+ * accumulator, continuing the sample sequence (sample indices params->sample_offset + samples
+ * already accumulated), and writes the running mean to d_rgba_out. The accumulator restarts
+ * when reset is nonzero, when the image size changes, and after any other render of the
+ * context or a scene or material change (those reuse or invalidate it). Four calls of 16 spp
+ * give the image of one 64-spp render. No firefly clamp. */
+e8g_status e8g_render_progressive(e8g_ctx *ctx, const e8g_render_params *params, int reset, float *d_rgba_out,
+                                  void *stream);
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
 
 /* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity

@@ -198,3 +198,26 @@ def test_lt2_furnace_equals_oracle(ctx):
     g, o = float(img[..., :3].sum(axis=-1).mean()), float(ref[..., :3].sum(axis=-1).mean())
     assert abs(g - o) <= 1e-3 * o, (g, o)
     assert 8.5 < o < 9.6
+
+
+def test_progressive_accumulation_equals_one_render(ctx):
+    """e8g_render_progressive: four calls of 4 spp continue the sample sequence in the device
+    accumulator and give the image of one 16-spp render; reset starts over; a plain render in
+    between ends the sequence."""
+    import torch
+    ctx.upload(S.cornell(64, 48))
+    p = default_params(abi.MODE_MIS, 64, 48, 4, seed=7)
+    d = torch.empty((48, 64, 4), dtype=torch.float32, device="cuda")
+    for k in range(4):
+        ctx.render_progressive(p, d.data_ptr(), reset=(k == 0))
+    torch.cuda.synchronize()
+    prog = d.cpu().numpy()
+    one = ctx.render(default_params(abi.MODE_MIS, 64, 48, 16, seed=7))
+    close = np.abs(prog - one) <= np.maximum(1e-5 * np.abs(one), 1e-6)
+    assert close.mean() >= 0.999, close.mean()
+    # after a plain render the next progressive call starts a new sequence at sample 0
+    ctx.render_progressive(p, d.data_ptr())
+    torch.cuda.synchronize()
+    first = d.cpu().numpy()
+    four = ctx.render(p)
+    assert np.allclose(first, four, rtol=1e-5, atol=1e-6)

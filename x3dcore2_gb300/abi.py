@@ -139,6 +139,7 @@ SIGNATURES = {
     "e8g_render_dev": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_render_dev_noalloc": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
+    "e8g_render_progressive": (_ST, [_P, C.POINTER(RenderParams), C.c_int, _P, _P]),
     "e8g_composite": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P]),
     "e8g_composite_dev": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P, _P]),
     "e8g_count_traversal": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(RenderStats)]),

@@ -113,6 +113,11 @@ class Context:
         self._check(self.lib.e8g_render_dev(self.h, C.byref(params), _P(d_out_ptr), _P(stream)),
                     "e8g_render_dev")
 
+    def render_progressive(self, params, d_out_ptr, reset=False, stream=None):
+        """e8g_render_progressive: params.spp more samples into the running mean at d_out_ptr."""
+        self._check(self.lib.e8g_render_progressive(self.h, C.byref(params), int(reset), _P(d_out_ptr), _P(stream)),
+                    "e8g_render_progressive")
+
     def render_paths(self, params, pixels, samples):
         pixels = np.ascontiguousarray(pixels, np.uint32)
         samples = np.ascontiguousarray(np.broadcast_to(samples, pixels.shape), np.uint32)

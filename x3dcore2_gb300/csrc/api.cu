@@ -300,6 +300,7 @@ e8g_status e8g_scene_upload(e8g_ctx *c, e8g_scene_desc const *d) {
         return cuda_fail(c, e, "scene upload");
     c->uploaded = true;
     c->built = false;
+    c->prog_spp = 0;
     fill_dev_scene(c);
     return E8G_OK;
 }
@@ -354,6 +355,7 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
     c->bvh_stats.layout = p.layout;
     c->bvh_stats.tri_bytes = static_cast<uint64_t>(p.nt) * 48;
     c->built = true;
+    c->prog_spp = 0;
     fill_dev_scene(c);
     return E8G_OK;
 }
@@ -469,6 +471,38 @@ e8g_status e8g_render_dev(e8g_ctx *c, e8g_render_params const *p, float *d_rgba,
     s = render_image(c, p, d_rgba, nullptr);
     c->stream = saved;
     return s;
+}
+
+e8g_status e8g_render_progressive(e8g_ctx *c, e8g_render_params const *p, int reset, float *d_rgba, void *stream) {
+    e8g_status s = check_ready(c);
+    if (s != E8G_OK)
+        return s;
+    s = validate_params(c, p);
+    if (s != E8G_OK)
+        return s;
+    if (!d_rgba)
+        return fail(c, E8G_ERR_INVALID_ARG, "NULL output");
+    if (p->firefly)
+        return fail(c, E8G_ERR_UNSUPPORTED, "progressive rendering does not run the firefly clamp");
+    cudaSetDevice(c->device);
+    if (reset || c->prog_w != p->width || c->prog_h != p->height)
+        c->prog_spp = 0;
+    e8g_render_params q = *p;
+    q.sample_offset = static_cast<uint32_t>(p->sample_offset + c->prog_spp); // continue the sample sequence
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+    cudaStream_t saved = c->stream;
+    c->stream = st;
+    s = render_image(c, &q, d_rgba, nullptr, c->prog_spp);
+    c->stream = saved;
+    if (s != E8G_OK) {
+        c->prog_spp = 0;
+        return s;
+    }
+    c->prog_w = p->width;
+    c->prog_h = p->height;
+    c->prog_spp += p->spp;
+    c->stats.paths = static_cast<uint64_t>(p->width) * p->height * p->spp;
+    return E8G_OK;
 }
 
 e8g_status e8g_render(e8g_ctx *c, e8g_render_params const *p, float *rgba_out) {

@@ -45,6 +45,9 @@ struct e8g_ctx {
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
     uint32_t wf_capacity = 1u << 21, wf_bounces = 4, wf_threshold = 16;
     void *host_pinned = nullptr;
+    // progressive rendering: samples in the accumulator, and the image they belong to
+    uint64_t prog_spp = 0;
+    uint32_t prog_w = 0, prog_h = 0;
 
     std::vector<e8g::dev_buffer *> all_buffers() {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
@@ -65,7 +68,8 @@ int persistent_grid(e8g_ctx *c, int blocks_per_sm);
 void fill_dev_scene(e8g_ctx *c);
 
 // Renders an image into d_rgba (device). counts (host, 3 values) requests the instrumented run.
-e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts);
+e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts,
+                        uint64_t prior_spp = 0);
 // Wavefront integrator over the image or a path list (E8G_MODE_MIS).
 e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
                          uint32_t bounces, uint32_t threshold, BatchDev const *B = nullptr,

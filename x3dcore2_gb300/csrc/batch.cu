@@ -57,6 +57,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         use_wf = use_wf && items[k].params.integrator == E8G_INTEGRATOR_WAVEFRONT &&
                  items[k].params.mode == E8G_MODE_MIS && items[k].params.rng == items[0].params.rng;
     cudaSetDevice(c->device);
+    c->prog_spp = 0; // the batch reuses the accumulator
     // host: pack, build, stage
     staged st;
     struct offs {

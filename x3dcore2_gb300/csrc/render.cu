@@ -130,7 +130,8 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     return E8G_OK;
 }
 
-e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts) {
+e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts,
+                        uint64_t prior_spp) {
     if (counts && (p->mode == E8G_MODE_REF_BDPT || p->mode == E8G_MODE_BDPT_POWER || p->mode == E8G_MODE_REF_LT2))
         return fail(c, E8G_ERR_UNSUPPORTED, "traversal counters cover the unidirectional integrators");
     c->launches = 0;
@@ -145,7 +146,10 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
     e8g_status s = first_hits(c, p->width, p->height);
     if (s != E8G_OK)
         return s;
-    e = cudaMemsetAsync(c->b_accum.ptr, 0, npix * sizeof(float4), c->stream);
+    if (prior_spp == 0) { // else the accumulator already holds prior_spp samples of these pixels
+        c->prog_spp = 0;  // a fresh accumulator ends any progressive sequence
+        e = cudaMemsetAsync(c->b_accum.ptr, 0, npix * sizeof(float4), c->stream);
+    }
     if (e == cudaSuccess && d_counts)
         e = cudaMemsetAsync(d_counts, 0, 64, c->stream);
     if (e != cudaSuccess)
@@ -159,8 +163,9 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
     if (s != E8G_OK)
         return s;
     cudaEventRecord(c->ev3, c->stream);
+    uint64_t total_spp = prior_spp + p->spp;
     launch_resolve(static_cast<float4 const *>(c->b_accum.ptr), static_cast<uint32_t>(npix),
-                   p->spp ? 1.0f / static_cast<float>(p->spp) : 0.0f, d_rgba, c->stream);
+                   total_spp ? 1.0f / static_cast<float>(total_spp) : 0.0f, d_rgba, c->stream);
     c->launches++;
     cudaEventRecord(c->ev1, c->stream);
     e = cudaGetLastError();
@@ -363,6 +368,7 @@ e8g_status e8g_set_materials(e8g_ctx *c, e8g_material const *m, uint32_t n) {
     }
     cudaSetDevice(c->device);
     pack_materials(m, n, c->pack.mats);
+    c->prog_spp = 0;
     c->materials.assign(m, m + n);
     cudaError_t e = cudaMemcpyAsync(c->b_mats.ptr, c->pack.mats.data(), c->pack.mats.size() * sizeof(DevMaterial),
                                     cudaMemcpyHostToDevice, c->stream);
