@@ -121,7 +121,8 @@ def make_scene(small):
 def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
     """Times the reference's CPU tracer (unidirect_lt1, the reference's direct-lighting
     integrator) on a centred crop of the same frame: the reference itself when it is compiled
-    here, else the oracle's restatement. Returns (paths/s, kind, sample description)."""
+    here, else the oracle's restatement. Returns (paths/s, kind, sample description, seconds of
+    the restated reference BVH build (its commit) or None)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import numpy as np
     import oracle_bind as ob
@@ -133,7 +134,8 @@ def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
         rs = ob.RefScene(scene, timing=True)
         spp = threads
         img, secs, taken = rs.render(abi.MODE_REF_LT1, cw, ch, spp, threads)
-        return cw * ch * taken / secs, "reference", f"{cw}x{ch} frame, {taken} spp, unidirect_lt1, {threads} threads"
+        return (cw * ch * taken / secs, "reference", f"{cw}x{ch} frame, {taken} spp, unidirect_lt1, {threads} threads",
+                None)
     t0 = time.time()
     osc = ob.OracleScene(scene)
     build_s = time.time() - t0
@@ -147,8 +149,9 @@ def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
         spp *= 2
         if dt * 2 + total_s > budget_s * 1.5:
             break
-    return total_paths / total_s, "port", (f"{cw}x{ch} crop of the {width}x{height} frame, unidirect_lt1 restated "
-                                           f"(oracle), {threads} threads, {total_s:.1f} s render, BVH build {build_s:.1f} s")
+    return (total_paths / total_s, "port", (f"{cw}x{ch} crop of the {width}x{height} frame, unidirect_lt1 restated "
+                                            f"(oracle), {threads} threads, {total_s:.1f} s render, BVH build {build_s:.1f} s"),
+            build_s)
 
 
 def quality_leg(ctx, p, img64, results):
@@ -250,6 +253,98 @@ def adjoint_leg(ctx):
             bwd.append(b)
     return {"triangles": sc.num_tris, "materials": 256, "forward_ms": statistics.mean(fwd),
             "backward_ms": statistics.mean(bwd), "ratio": statistics.mean(bwd) / statistics.mean(fwd)}
+
+
+def update_leg(ctx, scene):
+    """Incremental commit on the benchmark scene (the 1.3 M-triangle displaced icosphere): the
+    big mesh rotated on the device (trimesh::transform) and the tree refitted, against a full host
+    rebuild; new host vertices of that mesh uploaded (dirty-only) and refitted; and the frame rate
+    after a refit and after a rebuild (a refitted tree traverses slower as geometry moves)."""
+    import numpy as np
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300.core import default_params
+    big = int(np.argmax(np.diff(scene.toff)))
+    v0, v1 = int(scene.voff[big]), int(scene.voff[big + 1])
+    c, s = np.cos(0.2), np.sin(0.2)
+    rot = np.array([[c, 0, s, 0], [0, 1, 0, 0], [-s, 0, c, 0], [0, 0, 0, 1]], np.float32)
+    p = default_params(abi.MODE_MIS, 1920, 1080, 4, seed=3, max_depth=8, rr_start=3)
+    nt, nv = scene.num_tris, len(scene.pos)
+    out = {"triangles": nt, "vertices": nv, "mesh_vertices": v1 - v0}
+    moved = (scene.pos[v0:v1] * np.float32(1.001)).astype(np.float32)
+    for name, lay in (("sah", abi.BVH_SAH), ("wide", abi.BVH_WIDE)):
+        ctx.upload(scene, layout=lay)
+        st0 = ctx.bvh_stats()
+        nn = st0["num_nodes"]
+        xf_wall, refit_dev = [], []
+        for k in range(6):
+            t0 = time.perf_counter()
+            ctx.transform_mesh(big, rot if k % 2 == 0 else np.eye(4, dtype=np.float32))
+            st = ctx.commit(abi.COMMIT_REFIT)
+            if k >= 2:
+                xf_wall.append((time.perf_counter() - t0) * 1e3)
+                refit_dev.append(st["build_ms"])
+        up_wall = []
+        for k in range(4):
+            t0 = time.perf_counter()
+            ctx.update_mesh(big, moved if k % 2 == 0 else scene.pos[v0:v1])
+            ctx.commit(abi.COMMIT_REFIT)
+            if k >= 1:
+                up_wall.append((time.perf_counter() - t0) * 1e3)
+        ctx.transform_mesh(big, rot)
+        ctx.commit(abi.COMMIT_REFIT)
+        fr_refit = []
+        for k in range(3):
+            ctx.render(p)
+            fr_refit.append(ctx.stats()["ms"])
+        t0 = time.perf_counter()
+        ctx.commit(abi.COMMIT_REBUILD)
+        rebuild_wall = (time.perf_counter() - t0) * 1e3
+        fr_rebuild = []
+        for k in range(3):
+            ctx.render(p)
+            fr_rebuild.append(ctx.stats()["ms"])
+        refit_ms = statistics.median(refit_dev)
+        if lay == abi.BVH_SAH:  # per refit: triangle records, leaf walks, node boxes, vertex reduction
+            alg = nt * (16 + 48 + 48) + nt * (4 + 16 + 48) + nn * 64 + (nn // 2) * 64 + nv * 16
+        else:
+            alg = nt * (16 + 48 + 48) + nt * (4 + 16 + 48) + nn * (96 + 32 + 8 * 32) + nv * 16
+        paths = p.width * p.height * p.spp
+        out[name] = {
+            "nodes": nn, "host_build_ms": st0["build_ms"], "rebuild_commit_ms": rebuild_wall,
+            "refit_device_ms": refit_ms, "transform_commit_wall_ms": statistics.median(xf_wall),
+            "update_commit_wall_ms": statistics.median(up_wall),
+            "refit_algorithmic_bytes": alg, "refit_gbs": alg / (refit_ms * 1e-3) / 1e9,
+            "paths_per_s_after_refit": paths / (statistics.median(fr_refit) * 1e-3),
+            "paths_per_s_after_rebuild": paths / (statistics.median(fr_rebuild) * 1e-3),
+        }
+    ctx.upload(scene)
+    return out
+
+
+def obj_leg():
+    """OBJ ingest: a displaced icosphere of level 7 (327,680 triangles) written as OBJ text with
+    v/vt/vn/f lines and read back with the reference loader's rules (e8g_obj_parse)."""
+    import numpy as np
+    from x3dcore2_gb300 import scene as S
+    sc = S.displaced_icosphere(level=7, seed=5, num_materials=4, width=64, height=64)
+    big = int(np.argmax(np.diff(sc.toff)))
+    pos = sc.pos[sc.voff[big]:sc.voff[big + 1]]
+    nrm = sc.nrm[sc.voff[big]:sc.voff[big + 1]]
+    tri = sc.tris[sc.toff[big]:sc.toff[big + 1]].astype(np.int64) + 1
+    lines = ["v %.6f %.6f %.6f" % tuple(v) for v in pos.tolist()]
+    lines += ["vn %.6f %.6f %.6f" % tuple(v) for v in nrm.tolist()]
+    lines.append("vt 0 0")
+    lines += ["f %d/1/%d %d/1/%d %d/1/%d" % (a, a, b, b, c, c) for a, b, c in tri.tolist()]
+    text = ("\n".join(lines) + "\n").encode()
+    ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        m = S.load_obj(text=text)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    assert len(m.tris) == len(tri)
+    best = min(ms)
+    return {"triangles": len(tri), "vertices": len(pos), "bytes": len(text), "ms": best,
+            "mb_per_s": len(text) / (best * 1e-3) / 1e6, "threads": 1}
 
 
 def run_reference_arm(args):
@@ -465,8 +560,14 @@ def main():
         line["bdpt"] = bdpt_leg(ctx)
         line["batch"] = batch_leg(ctx)
         line["adjoint"] = adjoint_leg(ctx)
+        line["update"] = update_leg(ctx, scene)
+        line["obj_ingest"] = obj_leg()
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        v, kind, sample = cpu_sample(scene, w, h, args.cpu_budget, os.cpu_count() or 1, timing_ref=False)
+        v, kind, sample, ref_build_s = cpu_sample(scene, w, h, args.cpu_budget, os.cpu_count() or 1, timing_ref=False)
+        if "update" in line and ref_build_s is not None:
+            # the reference rebuilds its whole tree on every commit (pathspace.cpp:292-328)
+            line["update"]["reference_commit_ms"] = {"value": ref_build_s * 1e3, "kind": kind, "threads": 1,
+                                                     "note": "the reference's tree build restated (oracle), one thread"}
         line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": os.cpu_count() or 1, "kind": kind,
                                 "sample": sample}
     if rank == 0:

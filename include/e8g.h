@@ -20,6 +20,11 @@
  *   e8g_render_paths    if_path_tracer::sample (one ray per call, as the reference's own
  *                       furnace test drives it)              corelib/src/pathtracer.h:59-63,
  *                                                            corelib/test/tst_pathtracer/tst_pathtracer.cpp:58-86
+ *   e8g_scene_update_mesh / e8g_scene_transform_mesh / e8g_scene_commit
+ *                       objdb::push_updates + actuator commit  corelib/src/objdb.cpp:59-87,
+ *                       trimesh::transform                     corelib/src/geometry.cpp:76-87
+ *   e8g_composite       aces_compositor / clamp_compositor     corelib/src/compositor.cpp:29-98
+ *   e8g_obj_load        wavefront_obj::load_geometry           corelib/src/resource.cpp:137-255
  *   e8g_forward / e8g_backward, e8g_batch_render: no counterpart in the reference (new).
  */
 #ifndef E8G_H
@@ -256,6 +261,11 @@ const char *e8g_version(void);
 e8g_status e8g_scene_upload(e8g_ctx *ctx, const e8g_scene_desc *desc);
 e8g_status e8g_scene_build_bvh(e8g_ctx *ctx, const e8g_bvh_opts *opts);
 e8g_status e8g_bvh_get_stats(const e8g_ctx *ctx, e8g_bvh_stats *stats);
+/* Copies the device tree to host memory: nodes_out receives stats.node_bytes (SAH pairs and the
+ * reference layout: num_nodes float4 (min xyz | link) followed by num_nodes float4
+ * (max xyz | count); eight-wide: num_nodes records of 96 bytes), tris_out stats.tri_bytes (per
+ * triangle position: v0 | triangle id, v1 - v0, v2 - v0 as three float4). Either may be NULL. */
+e8g_status e8g_bvh_read(e8g_ctx *ctx, void *nodes_out, void *tris_out);
 void e8g_default_bvh_opts(e8g_bvh_opts *opts);
 
 e8g_status e8g_camera_rays(e8g_ctx *ctx, uint32_t width, uint32_t height, e8g_ray *rays_out);
@@ -348,6 +358,75 @@ e8g_status e8g_composite_dev(e8g_ctx *ctx, const float *d_rgba, uint32_t width, 
  * clamp. The scenes stay independent of the context's uploaded scene. */
 e8g_status e8g_batch_render(e8g_ctx *ctx, const e8g_batch_item *items, uint32_t n,
                             e8g_render_stats *stats);
+
+/* ------------------------------------------------- incremental updates ---- */
+
+/* Scene changes between renders without a new e8g_scene_upload: the counterpart of
+ * objdb::push_updates (objdb.cpp:59-87), which unloads and reloads every dirty object through its
+ * actuator and then commits (bvh_path_space_layout::commit rebuilds the whole tree). Here only the
+ * changed meshes travel to the device, and e8g_scene_commit brings the tree up to date on the
+ * device. Meshes keep their vertex and triangle counts; a different topology needs an upload.
+ * After any of these calls renders and traces fail with E8G_ERR_NOT_BUILT until the next
+ * e8g_scene_commit (or e8g_scene_build_bvh). */
+
+/* Replaces the vertex positions (3 floats per vertex of the mesh) and, unless normals is NULL,
+ * the normals of mesh `mesh`: the mesh's new blueprint. Its area, the light powers and the light
+ * CDF are recomputed as e8g_scene_upload computes them (trimesh::update, geometry.cpp:105-124;
+ * basic_light_sources::commit, lightsources.cpp:45-52), so update + commit renders what an upload
+ * of the changed scene renders. */
+e8g_status e8g_scene_update_mesh(e8g_ctx *ctx, uint32_t mesh, const float *positions, const float *normals);
+
+/* trimesh::transform (geometry.cpp:76-87) of mesh `mesh` on the device, from its blueprint (the
+ * vertices of the last upload or e8g_scene_update_mesh; transforms do not compound). m is the 4x4
+ * matrix, row-major (m[4*i + j] = row i, column j). Positions become (m * (v, 1)).cart(); normals
+ * become (~(m ^ -1) * (n, 1)).cart() with the reference's cofactor inverse, a w divide included
+ * (flags 0), or the inverse transpose applied to (n, 0) (flags E8G_XFORM_NORMALS_AS_DIRECTIONS).
+ * The mesh keeps its blueprint area for light sampling, as the reference's transformed copy does
+ * (transform calls update_aabb only). |det m| <= 1e-5 is E8G_ERR_INVALID_ARG, the reference's
+ * "matrix not invertible" (tensor.h:511-540). */
+enum { E8G_XFORM_REFERENCE = 0, E8G_XFORM_NORMALS_AS_DIRECTIONS = 1 };
+e8g_status e8g_scene_transform_mesh(e8g_ctx *ctx, uint32_t mesh, const float m[16], uint32_t flags);
+
+/* Replaces the camera (camera_container::load after pinhole_camera::transform, camera.cpp:63-71).
+ * The tree is unaffected: no commit needed. */
+e8g_status e8g_scene_set_camera(e8g_ctx *ctx, const e8g_camera *camera);
+
+/* Reads back a mesh's current world-space vertices (3 floats per vertex each; either may be NULL). */
+e8g_status e8g_scene_get_mesh(e8g_ctx *ctx, uint32_t mesh, float *positions, float *normals);
+
+/* Brings the tree up to date with the changed meshes.
+ * E8G_COMMIT_REFIT keeps the tree's topology and recomputes, on the device, every triangle record
+ * and every box bottom-up (one pass; a refit of an unchanged scene writes exactly the bytes of the
+ * build). The tree's quality degrades as geometry moves far from where it was built; rebuild then.
+ * E8G_COMMIT_REBUILD builds a new tree on the host with the last build options.
+ * The reference layout (E8G_BVH_REFERENCE) always rebuilds, as the reference does on every commit,
+ * so its hit identities stay the reference's. stats (may be NULL) receives the tree's statistics;
+ * its build_ms is the commit's time. */
+enum { E8G_COMMIT_REFIT = 0, E8G_COMMIT_REBUILD = 1 };
+e8g_status e8g_scene_commit(e8g_ctx *ctx, uint32_t mode, e8g_bvh_stats *stats);
+
+/* ------------------------------------------------------------- OBJ ingest ---- */
+
+/* One triangle mesh read from a Wavefront OBJ file with the reference's rules
+ * (wavefront_obj::load_geometry, resource.cpp:137-255): "v", "vn", "vt" and triangular "f a/b/c"
+ * lines, matched as the reference's regular expressions match them (other lines are ignored;
+ * polygons with more corners are errors); per vertex, the normal and texcoord of the last face
+ * corner naming it, zero when none does. A file whose faces omit a texcoord or normal index,
+ * which the reference reads out of bounds, is refused. Host memory owned by the library. */
+typedef struct e8g_host_mesh e8g_host_mesh;
+typedef struct e8g_mesh_data {
+    uint32_t num_vertices;
+    uint32_t num_triangles;
+    const float *positions;    /* 3 * num_vertices */
+    const float *normals;      /* 3 * num_vertices */
+    const float *texcoords;    /* 2 * num_vertices */
+    const uint32_t *triangles; /* 3 * num_triangles, 0-based */
+} e8g_mesh_data;
+/* err (may be NULL) receives a message of at most err_len bytes on failure. */
+e8g_status e8g_obj_load(const char *path, e8g_host_mesh **out, char *err, size_t err_len);
+e8g_status e8g_obj_parse(const char *text, size_t len, e8g_host_mesh **out, char *err, size_t err_len);
+e8g_status e8g_host_mesh_data(const e8g_host_mesh *mesh, e8g_mesh_data *data);
+void e8g_host_mesh_free(e8g_host_mesh *mesh);
 
 /* Host-side scene generators (no GPU needed): fill a scene owned by the library. */
 typedef struct e8g_host_scene e8g_host_scene;

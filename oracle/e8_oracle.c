@@ -2441,3 +2441,78 @@ void o_path_gradient_f64(const o_scene *s, uint64_t seed, const o_policy *pol, u
     rgb_out[1] = Ltot.y;
     rgb_out[2] = Ltot.z;
 }
+
+/* ------------------------------------------------------------- transform -- */
+/* trimesh::transform, geometry.cpp:76-87, on mat<4,4> of tensor.h. */
+
+/* mat::det(next_row, curr_col, removed_col), tensor.h:451-473: Laplace expansion along column
+ * `col` (1-based) over the rows left in the linked list next[] (1-based, 5 ends it), the next
+ * column skipping `removed`. */
+static float mat4_minor(const float a[4][4], unsigned next[5], unsigned col, unsigned removed) {
+    unsigned row = next[0];
+    if (next[row] == 5)
+        return a[row - 1][col - 1];
+    float d = 0.0f;
+    unsigned i = 0, prev = 0;
+    while (row != 5) {
+        next[prev] = next[row];
+        float m = mat4_minor(a, next, col + 1 == removed ? col + 2 : col + 1, removed);
+        next[prev] = row;
+        float x = a[row - 1][col - 1];
+        d += (i & 1 ? -x : x) * m;
+        prev = row;
+        row = next[row];
+        i++;
+    }
+    return d;
+}
+
+/* mat::operator^(-1) (tensor.h:511-540) through adjugate (:483-504) and det(adj) (:475-481),
+ * transposed (operator~, :551-559). */
+static int mat4_normal_matrix(const float a[4][4], float out[4][4]) {
+    unsigned next[5] = {1, 2, 3, 4, 5};
+    float adj[4][4];
+    for (unsigned j = 1; j <= 4; j++)
+        for (unsigned i = 1; i <= 4; i++) {
+            next[i - 1] = i + 1;
+            float m = mat4_minor(a, next, j == 1 ? 2 : 1, j);
+            next[i - 1] = i;
+            adj[j - 1][i - 1] = ((i + j) & 1) ? -m : m;
+        }
+    float d = 0;
+    for (unsigned i = 0; i < 4; i++)
+        d += a[i][0] * adj[0][i];
+    if (fabsf(d - 0.0f) <= 1e-5f)
+        return 0;
+    float k = 1.0f / d;
+    for (unsigned i = 0; i < 4; i++)
+        for (unsigned j = 0; j < 4; j++)
+            out[j][i] = k * adj[i][j];
+    return 1;
+}
+
+/* (m * (x, y, z, w)).cart(): mat * vec (tensor.h:425-433) then vec::cart (:261-268). */
+static void mat4_apply_cart(const float a[4][4], const float *x, float w, float *out) {
+    float h[4] = {x[0], x[1], x[2], w}, v[4] = {0, 0, 0, 0};
+    for (unsigned j = 0; j < 4; j++)
+        for (unsigned i = 0; i < 4; i++)
+            v[i] = v[i] + a[i][j] * h[j];
+    float inv_w = 1.0f / v[3];
+    for (unsigned i = 0; i < 3; i++)
+        out[i] = inv_w * v[i];
+}
+
+int o_transform_mesh(const float m[16], const float *pos, const float *nrm, uint32_t n, float *pos_out,
+                     float *nrm_out) {
+    float a[4][4], nm[4][4];
+    for (unsigned i = 0; i < 4; i++)
+        for (unsigned j = 0; j < 4; j++)
+            a[i][j] = m[4 * i + j];
+    if (!mat4_normal_matrix(a, nm))
+        return 0;
+    for (uint32_t v = 0; v < n; v++)
+        mat4_apply_cart(a, &pos[3 * (size_t)v], 1.0f, &pos_out[3 * (size_t)v]);
+    for (uint32_t v = 0; v < n; v++)
+        mat4_apply_cart(nm, &nrm[3 * (size_t)v], 1.0f, &nrm_out[3 * (size_t)v]);
+    return 1;
+}

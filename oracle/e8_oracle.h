@@ -86,6 +86,13 @@ void o_composite(const float *rgba, uint32_t w, uint32_t h, uint32_t tonemap, in
                  unsigned char *out);
 
 /* Seed of the per-path minstd stream; the same function as e8g_path_seed. */
+/* trimesh::transform (geometry.cpp:76-87) of n vertices by the row-major 4x4 matrix m:
+ * positions (m * (p, 1)).cart(), normals (~(m ^ -1) * (n, 1)).cart() with mat::operator^(-1)'s
+ * cofactor inverse (tensor.h:451-540). Returns 0 when |det m| <= 1e-5 (the reference throws
+ * "matrix not invertible"), 1 otherwise. */
+int o_transform_mesh(const float m[16], const float *pos, const float *nrm, uint32_t n, float *pos_out,
+                     float *nrm_out);
+
 uint32_t o_path_seed(uint64_t seed, uint32_t pixel, uint32_t sample);
 /* First n draws of the minstd stream with this seed (tensor.h:987-1001 + libstdc++
  * generate_canonical<float>). */

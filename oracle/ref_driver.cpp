@@ -24,6 +24,7 @@
 #include "pathtracer.h"
 #include "pathtracerfact.h"
 #include "renderer.h"
+#include "resource.h"
 
 #include <chrono>
 #include <complex>
@@ -336,6 +337,81 @@ uint32_t r_uv_sphere(float r, uint32_t res, int flip, float *pos_out, float *nrm
                 tris_out[3 * i + k] = t[i](k);
     }
     return static_cast<uint32_t>(t.size());
+}
+
+// trimesh::transform (geometry.cpp:76-87) of a mesh given as vertex and normal arrays; returns 0
+// when the reference throws (a singular matrix).
+int r_transform_mesh(float const m[16], float const *pos, float const *nrm, uint32_t n, float *pos_out,
+                     float *nrm_out) {
+    e8::trimesh mesh("xform");
+    std::vector<e8util::vec3> verts, norms;
+    for (uint32_t v = 0; v < n; v++) {
+        verts.push_back(e8util::vec3{pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]});
+        norms.push_back(e8util::vec3{nrm[3 * v], nrm[3 * v + 1], nrm[3 * v + 2]});
+    }
+    mesh.vertices(verts);
+    mesh.normals(norms);
+    e8util::mat44 t;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            t(i, j) = m[4 * i + j];
+    std::unique_ptr<e8::if_geometry> out;
+    try {
+        out = mesh.transform(t);
+    } catch (std::string const &) {
+        return 0;
+    }
+    auto const &tv = out->vertices();
+    auto const &tn = out->normals();
+    for (uint32_t v = 0; v < n; v++)
+        for (int k = 0; k < 3; k++) {
+            pos_out[3 * v + k] = tv[v](k);
+            nrm_out[3 * v + k] = tn[v](k);
+        }
+    return 1;
+}
+
+// wavefront_obj::load_geometry (resource.cpp:137-255) of the file at `path`. Returns 1 and fills
+// the counts (and the arrays when pos is not NULL: 3 floats per vertex for positions and normals,
+// 2 for texcoords, 3 indices per triangle), or 0 when the reference throws (err receives the
+// message).
+int r_obj_load(char const *path, uint32_t *nv, uint32_t *nt, float *pos, float *nrm, float *uv, uint32_t *tris,
+               char *err, uint32_t err_len) {
+    std::string msg;
+    try {
+        std::shared_ptr<e8::if_geometry> g = e8util::wavefront_obj(path).load_geometry();
+        if (!g) {
+            msg = "cannot open";
+        } else {
+            auto const &v = g->vertices();
+            auto const &n = g->normals();
+            auto const &t = g->texcoords();
+            auto const &f = g->triangles();
+            *nv = static_cast<uint32_t>(v.size());
+            *nt = static_cast<uint32_t>(f.size());
+            if (pos) {
+                for (size_t i = 0; i < v.size(); i++) {
+                    for (int k = 0; k < 3; k++) {
+                        pos[3 * i + k] = v[i](k);
+                        nrm[3 * i + k] = n[i](k);
+                    }
+                    uv[2 * i] = t[i](0);
+                    uv[2 * i + 1] = t[i](1);
+                }
+                for (size_t i = 0; i < f.size(); i++)
+                    for (int k = 0; k < 3; k++)
+                        tris[3 * i + k] = f[i](k);
+            }
+            return 1;
+        }
+    } catch (std::string const &e) {
+        msg = e;
+    } catch (std::exception const &e) {
+        msg = e.what();
+    }
+    if (err && err_len)
+        std::snprintf(err, err_len, "%s", msg.c_str());
+    return 0;
 }
 
 uint32_t r_bvh_num_nodes(r_scene const *s) { return s->bvh->num_nodes(); }

@@ -142,6 +142,73 @@ def composite_fixture():
     print("composite.npz")
 
 
+def transform_matrices():
+    """Row-major 4x4 matrices for trimesh::transform: identity, a rigid motion, scale with shear,
+    a projective matrix (w != 1) and one whose |det| <= 1e-5 (the reference throws)."""
+    rng = np.random.default_rng(21)
+    c, s = np.cos(0.7), np.sin(0.7)
+    rigid = np.array([[c, 0, s, 0.3], [0, 1, 0, -1.2], [-s, 0, c, 2.5], [0, 0, 0, 1]])
+    shear = np.array([[1.7, 0.4, 0.0, -0.5], [0.1, 0.6, 0.3, 0.2], [0.0, -0.2, 2.2, 1.1], [0, 0, 0, 1]])
+    proj = np.eye(4) + rng.normal(0, 0.2, (4, 4))
+    tiny = np.diag([0.02, 0.02, 0.02, 1.0])
+    return np.stack([np.eye(4), rigid, shear, proj, tiny]).astype(np.float32)
+
+
+def transform_fixture():
+    """trimesh::transform (geometry.cpp:76-87) by the compiled reference: positions and normals."""
+    rng = np.random.default_rng(22)
+    pos = rng.uniform(-3, 3, (64, 3)).astype(np.float32)
+    nrm = rng.normal(0, 1, (64, 3))
+    nrm = (nrm / np.linalg.norm(nrm, axis=1, keepdims=True)).astype(np.float32)
+    mats = transform_matrices()
+    ref = ob.reference()
+    out = {"pos": pos, "nrm": nrm, "mats": mats, "ok": np.zeros(len(mats), np.int32),
+           "pos_out": np.zeros((len(mats), 64, 3), np.float32), "nrm_out": np.zeros((len(mats), 64, 3), np.float32)}
+    for k, m in enumerate(mats):
+        r = ob.transform_mesh(m, pos, nrm, lib=ref)
+        if r is not None:
+            out["ok"][k] = 1
+            out["pos_out"][k], out["nrm_out"][k] = r
+    np.savez_compressed(os.path.join(HERE, "transform.npz"), **out)
+    print("transform.npz")
+
+
+def obj_fixture():
+    """wavefront_obj::load_geometry (resource.cpp:137-255) by the compiled reference on the
+    hand-written cases of obj_cases.py and 64 seeded random files: vertex, normal, texcoord and
+    triangle arrays, or a failure flag where the reference throws."""
+    import tempfile
+    import obj_cases as OC
+    names = list(OC.CASES)
+    texts = [OC.CASES[n] for n in names]
+    rng = np.random.default_rng(31)
+    for k in range(64):
+        names.append(f"random{k}")
+        texts.append(OC.random_obj(rng))
+    ref = ob.reference()
+    ok = np.zeros(len(texts), np.int32)
+    nv = np.zeros(len(texts), np.int64)
+    nt = np.zeros(len(texts), np.int64)
+    arrays = {"pos": [], "nrm": [], "uv": [], "tris": []}
+    with tempfile.TemporaryDirectory() as d:
+        for i, t in enumerate(texts):
+            path = os.path.join(d, f"case{i}.obj")
+            with open(path, "wb") as f:
+                f.write(t.encode())
+            r = ob.ref_obj_load(path, ref)
+            if isinstance(r, dict):
+                ok[i] = 1
+                nv[i], nt[i] = len(r["pos"]), len(r["tris"])
+                for k in arrays:
+                    arrays[k].append(r[k].reshape(-1))
+    data, off = OC.pack_texts(texts)
+    out = {"names": np.array(names), "text": data, "text_off": off, "ok": ok, "nv": nv, "nt": nt}
+    for k, v in arrays.items():
+        out[k] = np.concatenate(v) if v else np.zeros(0)
+    np.savez_compressed(os.path.join(HERE, "obj.npz"), **out)
+    print("obj.npz", int(ok.sum()), "of", len(ok), "load")
+
+
 def main(only=()):
     subprocess.run(["make", "-s", "-C", ob.ORACLE_DIR, "all", "ref"], check=True)
     all_modes = list(MODES)
@@ -159,6 +226,8 @@ def main(only=()):
                                       ["lt1", "bdpt", "direct", "lt2"]),
         "renderer": renderer_fixture,  # reads cornell.npz, so it runs after it
         "composite": composite_fixture,
+        "transform": transform_fixture,
+        "obj": obj_fixture,
     }
     for name, fn in jobs.items():
         if not only or name in only:

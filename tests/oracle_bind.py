@@ -67,6 +67,7 @@ def oracle():
             "o_path_seed": (_U, [C.c_uint64, _U, _U]),
             "o_firefly_add": (None, [_P, _U, _U, _P]),
             "o_composite": (None, [_P, _U, _U, _U, C.c_int, C.c_float, _P]),
+            "o_transform_mesh": (C.c_int, [_P, _P, _P, _U, _P, _P]),
             "o_render_task": (None, [_P, _U, C.POINTER(OPolicy), _U, _U, _U, C.c_int, _U, _P]),
             "o_minstd_draws": (None, [_U, _U, _P]),
             "o_philox_draws": (None, [C.c_uint64, _U, _U, _U, _P]),
@@ -103,6 +104,8 @@ def reference(timing=False):
             "r_render_paths": (None, [_P, _U, _U, _U, _P, _P, _U, _P]),
             "r_render": (C.c_double, [_P, _U, _U, _U, _U, _U, _P, _P, C.c_int]),
             "r_composite": (None, [_P, _U, _U, _U, C.c_int, C.c_float, _P]),
+            "r_transform_mesh": (C.c_int, [_P, _P, _P, _U, _P, _P]),
+            "r_obj_load": (C.c_int, [C.c_char_p, _P, _P, _P, _P, _P, _P, C.c_char_p, _U]),
             "r_bsdf_eval": (None, [_P, C.c_int32, _P, _P, _P, _P]),
             "r_bsdf_sample": (None, [_P, C.c_int32, _U, _P, _P, _U, _P, _P]),
             "r_minstd_draws": (None, [_U, _U, _P]),
@@ -232,6 +235,38 @@ def composite(rgba, tonemap, auto_exposure=True, exposure=1.0, lib=None):
     f = fn.r_composite if lib is not None else fn.o_composite
     f(ptr(rgba), w, h, tonemap, int(auto_exposure), exposure, ptr(out))
     return out
+
+
+def transform_mesh(m, pos, nrm, lib=None):
+    """trimesh::transform of (n, 3) vertex and normal arrays by the row-major 4x4 matrix m: the
+    oracle's restatement, or the compiled reference when lib is the reference library. Returns
+    (positions, normals), or None where the reference throws (singular matrix)."""
+    m = np.ascontiguousarray(m, np.float32).reshape(16)
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    po = np.zeros_like(pos)
+    no = np.zeros_like(nrm)
+    f = lib.r_transform_mesh if lib is not None else oracle().o_transform_mesh
+    if not f(ptr(m), ptr(pos), ptr(nrm), len(pos), ptr(po), ptr(no)):
+        return None
+    return po, no
+
+
+def ref_obj_load(path, lib):
+    """wavefront_obj::load_geometry of the compiled reference: dict(pos, nrm, uv, tris), or the
+    message of the exception it throws (a str)."""
+    nv, nt = C.c_uint32(0), C.c_uint32(0)
+    err = C.create_string_buffer(512)
+    p = str(path).encode()
+    if not lib.r_obj_load(p, C.byref(nv), C.byref(nt), None, None, None, None, err, len(err)):
+        return err.value.decode(errors="replace")
+    pos = np.zeros((nv.value, 3), np.float32)
+    nrm = np.zeros((nv.value, 3), np.float32)
+    uv = np.zeros((nv.value, 2), np.float32)
+    tris = np.zeros((nt.value, 3), np.uint32)
+    ok = lib.r_obj_load(p, C.byref(nv), C.byref(nt), ptr(pos), ptr(nrm), ptr(uv), ptr(tris), err, len(err))
+    assert ok
+    return dict(pos=pos, nrm=nrm, uv=uv, tris=tris)
 
 
 class RefScene:

@@ -216,3 +216,34 @@ def test_compositor_matches_live_reference(reference):
     for tm in (abi.TONEMAP_CLAMP, abi.TONEMAP_ACES):
         for auto in (True, False):
             assert np.array_equal(ob.composite(img, tm, auto, 1.7), ob.composite(img, tm, auto, 1.7, lib=reference))
+
+
+def test_transform_matches_reference_golden(oracle):
+    """trimesh::transform (geometry.cpp:76-87): positions (m (p, 1)).cart() and normals through
+    the reference's cofactor inverse with its w divide; a matrix with |det| <= 1e-5 is refused
+    as the reference's "matrix not invertible"."""
+    d = G.load("transform.npz")
+    for k, m in enumerate(d["mats"]):
+        r = ob.transform_mesh(m, d["pos"], d["nrm"])
+        if not d["ok"][k]:
+            assert r is None, k
+            continue
+        assert r is not None, k
+        assert np.array_equal(r[0].view(np.uint32), d["pos_out"][k].view(np.uint32)), k
+        assert np.array_equal(r[1].view(np.uint32), d["nrm_out"][k].view(np.uint32)), k
+
+
+def test_transform_matches_live_reference(reference):
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(-10, 10, (200, 3)).astype(np.float32)
+    nrm = rng.normal(0, 1, (200, 3)).astype(np.float32)
+    for k in range(20):
+        m = (np.eye(4) * rng.uniform(0.3, 3.0) + rng.normal(0, 0.5, (4, 4))).astype(np.float32)
+        if k % 2 == 0:
+            m[3] = (0, 0, 0, 1)  # affine
+        a = ob.transform_mesh(m, pos, nrm)
+        b = ob.transform_mesh(m, pos, nrm, lib=reference)
+        assert (a is None) == (b is None)
+        if a is not None:
+            assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32)), k
+            assert np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32)), k

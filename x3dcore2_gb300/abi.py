@@ -26,6 +26,8 @@ RNG_MINSTD, RNG_PHILOX = 0, 1
 BVH_SAH, BVH_REFERENCE, BVH_WIDE = 0, 1, 2
 # compositing
 TONEMAP_CLAMP, TONEMAP_ACES = 0, 1
+XFORM_REFERENCE, XFORM_NORMALS_AS_DIRECTIONS = 0, 1
+COMMIT_REFIT, COMMIT_REBUILD = 0, 1
 # generators
 GEN_CORNELL, GEN_DISPLACED_ICO, GEN_SOUP, GEN_FURNACE = 0, 1, 2, 3
 
@@ -118,6 +120,12 @@ _U32 = C.c_uint32
 _ST = C.c_int
 
 # name -> (restype, argtypes); every symbol include/e8g.h declares
+class MeshData(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("num_triangles", C.c_uint32),
+                ("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+                ("texcoords", C.POINTER(C.c_float)), ("triangles", C.POINTER(C.c_uint32))]
+
+
 class CompositeParams(C.Structure):
     _fields_ = [("tonemap", C.c_uint32), ("auto_exposure", C.c_uint32), ("exposure", C.c_float)]
 
@@ -131,6 +139,7 @@ SIGNATURES = {
     "e8g_scene_build_bvh": (_ST, [_P, C.POINTER(BvhOpts)]),
     "e8g_bvh_get_stats": (_ST, [_P, C.POINTER(BvhStats)]),
     "e8g_default_bvh_opts": (None, [C.POINTER(BvhOpts)]),
+    "e8g_bvh_read": (_ST, [_P, _P, _P]),
     "e8g_camera_rays": (_ST, [_P, _U32, _U32, _P]),
     "e8g_trace_closest": (_ST, [_P, _P, _U32, _P]),
     "e8g_trace_any": (_ST, [_P, _P, _P, _P, _U32, _P]),
@@ -151,6 +160,15 @@ SIGNATURES = {
     "e8g_batch_render": (_ST, [_P, C.POINTER(BatchItem), _U32, C.POINTER(RenderStats)]),
     "e8g_default_params": (None, [C.POINTER(RenderParams), _U32, _U32, _U32, _U32]),
     "e8g_path_seed": (_U32, [C.c_uint64, _U32, _U32]),
+    "e8g_scene_update_mesh": (_ST, [_P, _U32, _P, _P]),
+    "e8g_scene_transform_mesh": (_ST, [_P, _U32, _P, _U32]),
+    "e8g_scene_set_camera": (_ST, [_P, C.POINTER(Camera)]),
+    "e8g_scene_get_mesh": (_ST, [_P, _U32, _P, _P]),
+    "e8g_scene_commit": (_ST, [_P, _U32, C.POINTER(BvhStats)]),
+    "e8g_obj_load": (_ST, [C.c_char_p, C.POINTER(_P), C.c_char_p, C.c_size_t]),
+    "e8g_obj_parse": (_ST, [C.c_char_p, C.c_size_t, C.POINTER(_P), C.c_char_p, C.c_size_t]),
+    "e8g_host_mesh_data": (_ST, [_P, C.POINTER(MeshData)]),
+    "e8g_host_mesh_free": (None, [_P]),
     "e8g_gen_scene": (_ST, [C.POINTER(GenOpts), C.POINTER(_P)]),
     "e8g_host_scene_desc": (_ST, [_P, C.POINTER(SceneDesc)]),
     "e8g_host_scene_free": (None, [_P]),

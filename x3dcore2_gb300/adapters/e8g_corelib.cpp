@@ -1,5 +1,7 @@
 #include "e8g_corelib.h"
 
+#include <cstring>
+
 #include <stdexcept>
 
 namespace e8g_corelib {
@@ -174,6 +176,62 @@ gpu_image_renderer::~gpu_image_renderer() {
         e8g_destroy(m_ctx);
 }
 
+namespace {
+
+template <class T> bool same_bytes(std::vector<T> const &a, std::vector<T> const &b) {
+    return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0);
+}
+
+bool same_structure(scene_storage const &a, scene_storage const &b) {
+    return same_bytes(a.geo.voff, b.geo.voff) && same_bytes(a.geo.toff, b.geo.toff) &&
+           same_bytes(a.geo.tris, b.geo.tris) && same_bytes(a.mesh_mat, b.mesh_mat) &&
+           a.geo.geo_ids == b.geo.geo_ids && same_bytes(a.lights, b.lights) && a.mats.size() == b.mats.size();
+}
+
+} // namespace
+
+void gpu_image_renderer::commit_scene(scene_storage &next) {
+    auto check = [this](e8g_status st) {
+        if (st != E8G_OK)
+            throw std::runtime_error(std::string("e8g: ") + e8g_last_error(m_ctx));
+    };
+    if (!m_have_scene || !same_structure(m_scene, next)) {
+        e8g_bvh_opts bo;
+        e8g_default_bvh_opts(&bo);
+        check(e8g_scene_upload(m_ctx, &next.desc));
+        check(e8g_scene_build_bvh(m_ctx, &bo));
+    } else {
+        bool moved = false;
+        for (uint32_t m = 0; m + 1 < next.geo.voff.size(); m++) {
+            size_t b = 3 * static_cast<size_t>(next.geo.voff[m]), n = 3 * static_cast<size_t>(next.geo.voff[m + 1]) - b;
+            bool pos_same = std::memcmp(&next.geo.pos[b], &m_scene.geo.pos[b], n * sizeof(float)) == 0;
+            bool nrm_same = std::memcmp(&next.geo.nrm[b], &m_scene.geo.nrm[b], n * sizeof(float)) == 0;
+            if (n && (!pos_same || !nrm_same)) {
+                check(e8g_scene_update_mesh(m_ctx, m, &next.geo.pos[b], &next.geo.nrm[b]));
+                moved = true;
+            }
+        }
+        if (std::memcmp(&next.desc.camera, &m_scene.desc.camera, sizeof(e8g_camera)) != 0)
+            check(e8g_scene_set_camera(m_ctx, &next.desc.camera));
+        if (!same_bytes(next.mats, m_scene.mats))
+            check(e8g_set_materials(m_ctx, next.mats.data(), static_cast<uint32_t>(next.mats.size())));
+        if (moved)
+            check(e8g_scene_commit(m_ctx, E8G_COMMIT_REFIT, nullptr));
+    }
+    m_scene = std::move(next);
+    // the description points into the storage's own vectors
+    scene_storage &s = m_scene;
+    s.desc.mesh_vert_offset = s.geo.voff.data();
+    s.desc.mesh_tri_offset = s.geo.toff.data();
+    s.desc.mesh_material = s.mesh_mat.data();
+    s.desc.positions = s.geo.pos.data();
+    s.desc.normals = s.geo.nrm.data();
+    s.desc.triangles = s.geo.tris.data();
+    s.desc.materials = s.mats.data();
+    s.desc.lights = s.lights.data();
+    m_have_scene = true;
+}
+
 e8::pt_image_renderer::numerical_stats
 gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space const &path_space,
                            e8::if_material_container const &mats, e8::if_light_sources const &light_sources,
@@ -182,11 +240,9 @@ gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space cons
     auto const &mc = dynamic_cast<gpu_material_container const &>(mats);
     auto const &ls = dynamic_cast<gpu_light_sources const &>(light_sources);
     auto const &pc = dynamic_cast<gpu_pinhole_camera const &>(cam);
-    pack_scene(ps, mc, ls, pc, m_scene);
-    e8g_bvh_opts bo;
-    e8g_default_bvh_opts(&bo);
-    if (e8g_scene_upload(m_ctx, &m_scene.desc) != E8G_OK || e8g_scene_build_bvh(m_ctx, &bo) != E8G_OK)
-        throw std::runtime_error(std::string("e8g: ") + e8g_last_error(m_ctx));
+    scene_storage next;
+    pack_scene(ps, mc, ls, pc, next);
+    commit_scene(next);
     uint32_t mode = E8G_MODE_REF_LT1;
     switch (m_type) {
     case e8::pathtracer_factory::unidirect:

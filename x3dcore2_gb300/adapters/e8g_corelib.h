@@ -126,9 +126,16 @@ class gpu_image_renderer {
                                                    unsigned num_samps, bool firefly_filter);
 
   private:
+    // Brings the context's scene up to date with `next`: a full upload and build when the scene's
+    // structure changed (meshes, triangles, lights), otherwise only the meshes whose vertices
+    // changed are uploaded and the tree is refitted (objdb::push_updates, objdb.cpp:59-87, followed
+    // by the path space's commit), and camera and materials are replaced when they changed.
+    void commit_scene(scene_storage &next);
+
     e8::pathtracer_factory::pt_type m_type;
     e8g_ctx *m_ctx = nullptr;
     scene_storage m_scene;
+    bool m_have_scene = false;
     uint64_t m_frame = 0;
 };
 

@@ -79,6 +79,47 @@ class Context:
         self._check(self.lib.e8g_bvh_get_stats(self.h, C.byref(s)), "e8g_bvh_get_stats")
         return {k: getattr(s, k) for k, _ in abi.BvhStats._fields_}
 
+    def bvh_read(self):
+        """The device tree as (node bytes, triangle records (n, 12) float32)."""
+        st = self.bvh_stats()
+        nodes = np.zeros(st["node_bytes"], np.uint8)
+        tris = np.zeros((st["num_tris"], 12), np.float32)
+        self._check(self.lib.e8g_bvh_read(self.h, _ptr(nodes), _ptr(tris)), "e8g_bvh_read")
+        return nodes, tris
+
+    # ---- incremental updates ------------------------------------------------------------
+    def mesh_vertex_count(self, mesh):
+        d = self.scene.desc
+        return d.mesh_vert_offset[mesh + 1] - d.mesh_vert_offset[mesh]
+
+    def update_mesh(self, mesh, positions, normals=None):
+        """New blueprint vertices (and normals) of one mesh; needs commit() before rendering."""
+        n = self.mesh_vertex_count(mesh)
+        pos = np.ascontiguousarray(positions, np.float32).reshape(n, 3)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(n, 3)
+        self._check(self.lib.e8g_scene_update_mesh(self.h, mesh, _ptr(pos), None if nrm is None else _ptr(nrm)),
+                    "e8g_scene_update_mesh")
+
+    def transform_mesh(self, mesh, matrix, flags=abi.XFORM_REFERENCE):
+        """trimesh::transform of one mesh's blueprint by a 4x4 matrix (row-major), on the device."""
+        m = np.ascontiguousarray(matrix, np.float32).reshape(16)
+        self._check(self.lib.e8g_scene_transform_mesh(self.h, mesh, _ptr(m), flags), "e8g_scene_transform_mesh")
+
+    def set_camera(self, camera):
+        self._check(self.lib.e8g_scene_set_camera(self.h, C.byref(camera)), "e8g_scene_set_camera")
+
+    def get_mesh(self, mesh):
+        n = self.mesh_vertex_count(mesh)
+        pos = np.zeros((n, 3), np.float32)
+        nrm = np.zeros((n, 3), np.float32)
+        self._check(self.lib.e8g_scene_get_mesh(self.h, mesh, _ptr(pos), _ptr(nrm)), "e8g_scene_get_mesh")
+        return pos, nrm
+
+    def commit(self, mode=abi.COMMIT_REFIT):
+        s = abi.BvhStats()
+        self._check(self.lib.e8g_scene_commit(self.h, mode, C.byref(s)), "e8g_scene_commit")
+        return {k: getattr(s, k) for k, _ in abi.BvhStats._fields_}
+
     # ---- traversal ----------------------------------------------------------------------
     def camera_rays(self, w, h):
         out = np.empty((w * h, 6), np.float32)

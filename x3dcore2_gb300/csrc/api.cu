@@ -5,6 +5,7 @@
 #include "api_internal.h"
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -96,6 +97,8 @@ e8g_status check_ready(e8g_ctx *c) {
         return fail(c, E8G_ERR_NO_SCENE, "no scene uploaded");
     if (!c->built)
         return fail(c, E8G_ERR_NOT_BUILT, "BVH not built (call e8g_scene_build_bvh)");
+    if (c->dirty)
+        return fail(c, E8G_ERR_NOT_BUILT, "the scene changed since the last commit (call e8g_scene_commit)");
     return E8G_OK;
 }
 
@@ -156,6 +159,88 @@ e8g_status first_hits(e8g_ctx *c, uint32_t w, uint32_t h) {
 }
 
 int persistent_grid(e8g_ctx *c, int blocks_per_sm) { return c->num_sms * std::max(1, blocks_per_sm); }
+
+} // namespace e8g
+
+namespace e8g {
+
+e8g_status sync_host_vertices(e8g_ctx *c) {
+    if (!c->host_stale)
+        return E8G_OK;
+    packed_scene &p = c->pack;
+    cudaError_t e = cudaMemcpyAsync(p.vpos.data(), c->b_vpos.ptr, p.vpos.size() * sizeof(float),
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p.vnrm.data(), c->b_vnrm.ptr, p.vnrm.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                            c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "vertex read-back");
+    c->host_stale = false;
+    return E8G_OK;
+}
+
+e8g_status build_tree(e8g_ctx *c) {
+    cudaSetDevice(c->device);
+    e8g_status st = sync_host_vertices(c);
+    if (st != E8G_OK)
+        return st;
+    packed_scene &p = c->pack;
+    try {
+        build_scene_bvh(p, c->bvh_opts);
+    } catch (std::bad_alloc const &) {
+        return fail(c, E8G_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+    }
+    if (p.layout == E8G_BVH_REFERENCE && p.bvh.max_depth > kMaxRefTreeDepth) {
+        c->built = false;
+        return fail(c, E8G_ERR_UNSUPPORTED, "reference BVH deeper than the traversal stack (63 levels)");
+    }
+    cudaError_t e = upload(c->b_nlo, p.bvh.lo, c->stream);
+    if (e == cudaSuccess)
+        e = upload(c->b_nhi, p.bvh.hi, c->stream);
+    if (e == cudaSuccess)
+        e = upload(c->b_wide, p.wide, c->stream);
+    if (e == cudaSuccess)
+        e = upload(c->b_tri, p.tri, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "BVH upload");
+    // the vertex box (if_path_space::aabb) follows the vertices the tree was built from
+    for (uint32_t v = 0; v < p.nv; v++)
+        for (int k = 0; k < 3; k++) {
+            float x = p.vpos[4 * static_cast<size_t>(v) + k];
+            if (v == 0) {
+                p.bmin[k] = p.bmax[k] = x;
+            } else {
+                p.bmin[k] = x < p.bmin[k] ? x : p.bmin[k];
+                p.bmax[k] = p.bmax[k] < x ? x : p.bmax[k];
+            }
+        }
+    float max_abs = 0.0f;
+    for (uint32_t v = 0; v < p.nv; v++)
+        for (int k = 0; k < 3; k++)
+            max_abs = std::max(max_abs, std::fabs(p.vpos[4 * static_cast<size_t>(v) + k]));
+    for (int k = 0; k < 3; k++)
+        max_abs = std::max(max_abs, std::fabs(p.cam.origin[k]));
+    c->tree_max_abs = max_abs;
+    c->bvh_stats.num_nodes = p.bvh.num_nodes;
+    c->bvh_stats.num_leaves = p.bvh.num_leaves;
+    c->bvh_stats.max_depth = p.bvh.max_depth;
+    c->bvh_stats.num_tris = p.nt;
+    c->bvh_stats.avg_leaf_depth = p.bvh.avg_leaf_depth;
+    c->bvh_stats.build_ms = p.build_ms;
+    c->bvh_stats.node_bytes = static_cast<uint64_t>(p.bvh.num_nodes) * (p.layout == 2 ? 4 * kWideWords : 32);
+    c->bvh_stats.layout = p.layout;
+    c->bvh_stats.tri_bytes = static_cast<uint64_t>(p.nt) * 48;
+    c->built = true;
+    c->dirty = false;
+    c->refit_ready = false;
+    c->prog_spp = 0;
+    fill_dev_scene(c);
+    return E8G_OK;
+}
 
 } // namespace e8g
 
@@ -300,6 +385,11 @@ e8g_status e8g_scene_upload(e8g_ctx *c, e8g_scene_desc const *d) {
         return cuda_fail(c, e, "scene upload");
     c->uploaded = true;
     c->built = false;
+    c->dirty = false;
+    c->host_stale = false;
+    c->refit_ready = false;
+    c->b_vpos0.release();
+    c->b_vnrm0.release();
     c->prog_spp = 0;
     fill_dev_scene(c);
     return E8G_OK;
@@ -323,41 +413,33 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
             return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH layout");
         bo.layout = o->layout;
     }
+    c->bvh_opts = bo;
+    return build_tree(c);
+}
+
+e8g_status e8g_bvh_read(e8g_ctx *c, void *nodes_out, void *tris_out) {
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    if (!c->built)
+        return fail(c, E8G_ERR_NOT_BUILT, "BVH not built");
     cudaSetDevice(c->device);
-    try {
-        build_scene_bvh(c->pack, bo);
-    } catch (std::bad_alloc const &) {
-        return fail(c, E8G_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+    packed_scene const &p = c->pack;
+    size_t nn = p.bvh.num_nodes;
+    cudaError_t e = cudaSuccess;
+    if (nodes_out && p.layout == E8G_BVH_WIDE) {
+        e = cudaMemcpyAsync(nodes_out, c->b_wide.ptr, nn * 4 * kWideWords, cudaMemcpyDeviceToHost, c->stream);
+    } else if (nodes_out && nn) {
+        e = cudaMemcpyAsync(nodes_out, c->b_nlo.ptr, nn * 16, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(static_cast<char *>(nodes_out) + nn * 16, c->b_nhi.ptr, nn * 16,
+                                cudaMemcpyDeviceToHost, c->stream);
     }
-    packed_scene &p = c->pack;
-    if (p.layout == E8G_BVH_REFERENCE && p.bvh.max_depth > kMaxRefTreeDepth) {
-        c->built = false;
-        return fail(c, E8G_ERR_UNSUPPORTED, "reference BVH deeper than the traversal stack (63 levels)");
-    }
-    cudaError_t e = upload(c->b_nlo, p.bvh.lo, c->stream);
-    if (e == cudaSuccess)
-        e = upload(c->b_nhi, p.bvh.hi, c->stream);
-    if (e == cudaSuccess)
-        e = upload(c->b_wide, p.wide, c->stream);
-    if (e == cudaSuccess)
-        e = upload(c->b_tri, p.tri, c->stream);
+    if (e == cudaSuccess && tris_out && p.nt)
+        e = cudaMemcpyAsync(tris_out, c->b_tri.ptr, static_cast<size_t>(p.nt) * 48, cudaMemcpyDeviceToHost,
+                            c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess)
-        return cuda_fail(c, e, "BVH upload");
-    c->bvh_stats.num_nodes = p.bvh.num_nodes;
-    c->bvh_stats.num_leaves = p.bvh.num_leaves;
-    c->bvh_stats.max_depth = p.bvh.max_depth;
-    c->bvh_stats.num_tris = p.nt;
-    c->bvh_stats.avg_leaf_depth = p.bvh.avg_leaf_depth;
-    c->bvh_stats.build_ms = p.build_ms;
-    c->bvh_stats.node_bytes = static_cast<uint64_t>(p.bvh.num_nodes) * (p.layout == 2 ? 4 * kWideWords : 32);
-    c->bvh_stats.layout = p.layout;
-    c->bvh_stats.tri_bytes = static_cast<uint64_t>(p.nt) * 48;
-    c->built = true;
-    c->prog_spp = 0;
-    fill_dev_scene(c);
-    return E8G_OK;
+    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "tree read-back");
 }
 
 e8g_status e8g_bvh_get_stats(e8g_ctx const *c, e8g_bvh_stats *s) {

@@ -4,6 +4,7 @@
 #include "../../include/e8g.h"
 #include "host_scene.h"
 #include "launch.h"
+#include "refit.h"
 #include "scene_pack.h"
 
 #include <string>
@@ -48,11 +49,21 @@ struct e8g_ctx {
     // progressive rendering: samples in the accumulator, and the image they belong to
     uint64_t prog_spp = 0;
     uint32_t prog_w = 0, prog_h = 0;
+    // incremental updates: the build options of the last build, meshes changed since the last
+    // commit (dirty), host vertex copies behind the device's (host_stale: after device transforms),
+    // parent links of the current tree computed (refit_ready), the blueprint vertices transforms
+    // start from (b_vpos0 / b_vnrm0, made at the first transform), and the largest |coordinate|
+    // the eight-wide grid was sized for
+    e8g::bvh_build_opts bvh_opts{};
+    bool dirty = false, host_stale = false, refit_ready = false;
+    float tree_max_abs = 0;
+    e8g::dev_buffer b_refit, b_vpos0, b_vnrm0;
 
     std::vector<e8g::dev_buffer *> all_buffers() {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
-                &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch};
+                &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch,
+                &b_refit, &b_vpos0, &b_vnrm0};
     }
 };
 
@@ -66,6 +77,10 @@ RenderArgs make_args(e8g_render_params const *p);
 e8g_status first_hits(e8g_ctx *c, uint32_t w, uint32_t h);
 int persistent_grid(e8g_ctx *c, int blocks_per_sm);
 void fill_dev_scene(e8g_ctx *c);
+// Builds the tree on the host with c->bvh_opts and uploads it (e8g_scene_build_bvh, commit rebuild).
+e8g_status build_tree(e8g_ctx *c);
+// Copies the device's vertices back into the host pack when device transforms left it behind.
+e8g_status sync_host_vertices(e8g_ctx *c);
 
 // Renders an image into d_rgba (device). counts (host, 3 values) requests the instrumented run.
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts,

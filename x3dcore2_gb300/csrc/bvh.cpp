@@ -3,6 +3,7 @@
 // over all three axes of the centroid bounds, builds large subtrees on several threads, caps the
 // depth at kMaxTreeDepth and writes the GPU layout directly.
 #include "bvh.h"
+#include "bvh_boxes.h"
 
 #include <algorithm>
 #include <atomic>
@@ -156,9 +157,6 @@ struct builder {
     }
 };
 
-inline float inflate_down(float v, float eps) { return v - (std::fabs(v) * 1.0e-6f + eps); }
-inline float inflate_up(float v, float eps) { return v + (std::fabs(v) * 1.0e-6f + eps); }
-
 } // namespace
 
 flat_bvh build_bvh(float const *pos, uint32_t const *tris, uint32_t num_tris, bvh_build_opts const &o) {
@@ -189,10 +187,8 @@ flat_bvh build_bvh(float const *pos, uint32_t const *tris, uint32_t num_tris, bv
     // Flatten depth first; the two children of an interior node take adjacent slots.
     out.lo.assign(4 * static_cast<size_t>(n_tmp), 0.0f);
     out.hi.assign(4 * static_cast<size_t>(n_tmp), 0.0f);
-    float diag = 0;
-    for (int a = 0; a < 3; a++)
-        diag = std::max(diag, scene.hi[a] - scene.lo[a]);
-    float eps = diag * 1.0e-6f;
+    float eps = scene_eps(scene.lo, scene.hi);
+    out.eps = eps;
     uint32_t next_slot = 1;
     uint64_t leaf_depth_sum = 0;
     struct item {
@@ -206,8 +202,8 @@ flat_bvh build_bvh(float const *pos, uint32_t const *tris, uint32_t num_tris, bv
         float *lo = &out.lo[4 * static_cast<size_t>(it.slot)];
         float *hi = &out.hi[4 * static_cast<size_t>(it.slot)];
         for (int a = 0; a < 3; a++) {
-            lo[a] = inflate_down(t.b.lo[a], eps);
-            hi[a] = inflate_up(t.b.hi[a], eps);
+            lo[a] = inflate_lo(t.b.lo[a], eps);
+            hi[a] = inflate_hi(t.b.hi[a], eps);
         }
         uint32_t link, count;
         if (t.child[0] < 0) {

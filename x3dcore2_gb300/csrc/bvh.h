@@ -35,6 +35,7 @@ struct flat_bvh {
     uint32_t num_leaves = 0;
     uint32_t max_depth = 0;
     double avg_leaf_depth = 0;
+    float eps = 0; // boxes are the exact unions pushed out by |v| * 1e-6 + eps (bvh_boxes.h)
 };
 
 // tris: 3 global vertex indices per triangle; pos: 3 floats per vertex.

@@ -6,6 +6,7 @@
 // position into halves with their own boxes. Wide nodes are laid out breadth first so that each
 // node's interior children are contiguous.
 #include "bvh_wide.h"
+#include "bvh_boxes.h"
 
 #include <algorithm>
 #include <cmath>
@@ -85,8 +86,8 @@ struct collapser {
             }
         }
         for (int a = 0; a < 3; a++) {
-            it.b.lo[a] -= std::fabs(it.b.lo[a]) * 1.0e-6f + eps;
-            it.b.hi[a] += std::fabs(it.b.hi[a]) * 1.0e-6f + eps;
+            it.b.lo[a] = inflate_lo(it.b.lo[a], eps);
+            it.b.hi[a] = inflate_hi(it.b.hi[a], eps);
         }
         return it;
     }
@@ -110,13 +111,10 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
     wide_bvh w;
     if (b.num_nodes == 0)
         return w;
-    float diag = 0;
-    for (int a = 0; a < 3; a++)
-        diag = std::max(diag, b.hi[a] - b.lo[a]);
-    collapser cl{b, pos, tris, diag * 1.0e-6f};
-    // Smallest grid step: 2^-18 of the largest coordinate, far above the rounding of the
-    // slab arithmetic, so one step of outward rounding keeps every box conservative.
-    double step_min = std::max(static_cast<double>(max_abs) * std::ldexp(1.0, -18), std::ldexp(1.0, -100));
+    // split leaves get boxes pushed out like the binary tree's, so every slot box is the exact
+    // union of its triangles pushed out by the same eps (what the device refit recomputes)
+    collapser cl{b, pos, tris, b.eps};
+    double step_min = wide_step_min(max_abs);
 
     struct job {
         item it;
@@ -156,13 +154,13 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
             ch[0] = jb.it; // a root that is a small leaf
             n = 1;
         }
-        wbox u;
-        for (int i = 0; i < n; i++)
-            u.grow(ch[i].b);
         // slot assignment: child i goes to slot s with the smallest projection of its centre
         // offset onto octant s's direction, greedily over all (child, slot) pairs; a node with
         // at most four children uses slots 0-3 only (ordered by the x and y signs), so the
         // traversal tests one half of the slots
+        wbox u;
+        for (int i = 0; i < n; i++)
+            u.grow(ch[i].b);
         int slot_of[8], child_in[8];
         for (int i = 0; i < 8; i++)
             slot_of[i] = child_in[i] = -1;
@@ -192,31 +190,20 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
             slot_of[bi] = bs;
             child_in[bs] = bi;
         }
-        // quantization grid
+        // quantization grid and child boxes
         uint32_t words[kWideWords] = {0};
-        uint32_t ebytes[3];
-        double step[3];
-        // The grid starts one step below the children's union and 253 steps cover it, so no
-        // child box is clamped to the grid's ends and every quantized plane lies at least one
-        // step outside the (already inflated) child box: the slack absorbs the rounding of the
-        // traversal's plane arithmetic.
-        float org[3];
-        for (int a = 0; a < 3; a++) {
-            double ext = static_cast<double>(u.hi[a]) - static_cast<double>(u.lo[a]);
-            double want = std::max(ext / 251.0, step_min);
-            int e = static_cast<int>(std::ceil(std::log2(want)));
-            e = std::max(-126, std::min(127, e));
-            if (std::ldexp(1.0, e) < want && e < 127)
-                e++;
-            step[a] = std::ldexp(1.0, e);
-            ebytes[a] = static_cast<uint32_t>(e + 127);
-            double lo = static_cast<double>(u.lo[a]) - step[a];
-            float f = static_cast<float>(lo);
-            if (static_cast<double>(f) > lo)
-                f = std::nextafter(f, -INFINITY);
-            org[a] = f;
-            std::memcpy(&words[a], &f, 4);
+        float slo[8][3] = {{0}}, shi[8][3] = {{0}};
+        uint32_t present = 0;
+        for (int s = 0; s < 8; s++) {
+            if (child_in[s] < 0)
+                continue;
+            present |= 1u << s;
+            for (int a = 0; a < 3; a++) {
+                slo[s][a] = ch[child_in[s]].b.lo[a];
+                shi[s][a] = ch[child_in[s]].b.hi[a];
+            }
         }
+        wide_quantize(slo, shi, present, step_min, words);
         uint32_t imask = 0, n_int = 0;
         for (int s = 0; s < 8; s++)
             if (child_in[s] >= 0 && collapser::openable(ch[child_in[s]]))
@@ -225,22 +212,16 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
         w.num_nodes += n_int;
         w.nodes.resize(static_cast<size_t>(w.num_nodes) * kWideWords, 0u);
         uint32_t tri_base = static_cast<uint32_t>(w.tri_order.size());
-        words[3] = ebytes[0] | ebytes[1] << 8 | ebytes[2] << 16 | imask << 24;
+        words[3] |= imask << 24;
         words[4] = child_base;
         words[5] = tri_base;
-        uint8_t meta[8] = {0}, qb[6][8] = {{0}};
+        uint8_t meta[8] = {0};
         uint32_t counts = 0, rank = 0, leaves = 0;
         for (int s = 0; s < 8; s++) {
             int i = child_in[s];
             if (i < 0)
                 continue;
             item const &c = ch[i];
-            for (int a = 0; a < 3; a++) {
-                double lo = std::floor((static_cast<double>(c.b.lo[a]) - org[a]) / step[a]) - 1.0;
-                double hi = std::ceil((static_cast<double>(c.b.hi[a]) - org[a]) / step[a]) + 1.0;
-                qb[a][s] = static_cast<uint8_t>(std::max(0.0, std::min(255.0, lo)));
-                qb[3 + a][s] = static_cast<uint8_t>(std::max(0.0, std::min(255.0, hi)));
-            }
             if (imask >> s & 1) {
                 q.push_back({c, child_base + rank, jb.depth + 1});
                 rank++;
@@ -254,7 +235,6 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
             }
         }
         std::memcpy(&words[6], meta, 8);
-        std::memcpy(&words[8], qb, 48);
         words[20] = counts;
         words[21] = leaves;
         std::memcpy(&w.nodes[static_cast<size_t>(jb.node) * kWideWords], words, sizeof(words));

@@ -48,6 +48,36 @@ void pack_materials(e8g_material const *m, uint32_t n, std::vector<DevMaterial> 
     fs.albedo[0] = fs.albedo[1] = fs.albedo[2] = 0.8f;
 }
 
+void mesh_areas(packed_scene &s, uint32_t m) {
+    float cum = 0;
+    for (uint32_t t = s.mesh_toff[m]; t < s.mesh_toff[m + 1]; t++) {
+        float const *p0 = &s.vpos[4 * static_cast<size_t>(s.tidx[4 * static_cast<size_t>(t)])];
+        float const *p1 = &s.vpos[4 * static_cast<size_t>(s.tidx[4 * static_cast<size_t>(t) + 1])];
+        float const *p2 = &s.vpos[4 * static_cast<size_t>(s.tidx[4 * static_cast<size_t>(t) + 2])];
+        float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+        float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+        float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        float a = 0.5f * std::sqrt(dot3(c, c));
+        cum += a;
+        s.tri_cum[t] = cum;
+    }
+    s.mesh_area[m] = cum;
+}
+
+void light_table(packed_scene &s) {
+    s.total_power = 0;
+    const float pi = static_cast<float>(M_PI);
+    for (uint32_t l = 0; l < s.nl; l++) {
+        float k = pi * s.mesh_area[s.light_mesh[l]]; // m_power = pi * area * rad (light.cpp:20)
+        float pw[3];
+        for (int c = 0; c < 3; c++)
+            pw[c] = k * s.light_rad[4 * static_cast<size_t>(l) + c];
+        s.light_pnorm[l] = std::sqrt(dot3(pw, pw));
+        s.total_power += s.light_pnorm[l];
+        s.light_cum[l] = s.total_power;
+    }
+}
+
 void pack_scene(e8g_scene_desc const &d, packed_scene &s) {
     s.nm = d.num_meshes;
     s.nv = d.mesh_vert_offset[d.num_meshes];
@@ -68,29 +98,17 @@ void pack_scene(e8g_scene_desc const &d, packed_scene &s) {
     s.mesh_area.assign(s.nm, 0.0f);
     s.tri_cum.assign(s.nt, 0.0f);
     bool have_bound = false;
+    s.mesh_voff.assign(d.mesh_vert_offset, d.mesh_vert_offset + s.nm + 1);
     for (uint32_t m = 0; m < s.nm; m++) {
         int32_t mi = d.mesh_material ? d.mesh_material[m] : -1;
         s.mesh_mat[m] = (mi < 0 || static_cast<uint32_t>(mi) >= s.nmat) ? static_cast<int32_t>(s.nmat) : mi;
         uint32_t vb = d.mesh_vert_offset[m];
-        float cum = 0;
         for (uint32_t t = d.mesh_tri_offset[m]; t < d.mesh_tri_offset[m + 1]; t++) {
-            uint32_t g[3];
-            for (int k = 0; k < 3; k++) {
-                g[k] = vb + d.triangles[3 * static_cast<size_t>(t) + k];
-                s.tidx[4 * static_cast<size_t>(t) + k] = g[k];
-            }
+            for (int k = 0; k < 3; k++)
+                s.tidx[4 * static_cast<size_t>(t) + k] = vb + d.triangles[3 * static_cast<size_t>(t) + k];
             s.tidx[4 * static_cast<size_t>(t) + 3] = m;
-            float const *p0 = &d.positions[3 * static_cast<size_t>(g[0])];
-            float const *p1 = &d.positions[3 * static_cast<size_t>(g[1])];
-            float const *p2 = &d.positions[3 * static_cast<size_t>(g[2])];
-            float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
-            float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
-            float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-            float a = 0.5f * std::sqrt(dot3(c, c));
-            cum += a;
-            s.tri_cum[t] = cum;
         }
-        s.mesh_area[m] = cum;
+        mesh_areas(s, m);
         // trimesh::update_aabb + if_path_space::load (geometry.cpp:97-103, pathspace.cpp:17)
         for (uint32_t v = vb; v < d.mesh_vert_offset[m + 1]; v++) {
             for (int k = 0; k < 3; k++) {
@@ -111,23 +129,15 @@ void pack_scene(e8g_scene_desc const &d, packed_scene &s) {
     s.light_rad.assign(4 * static_cast<size_t>(s.nl), 0.0f);
     s.light_cum.resize(s.nl);
     s.light_pnorm.resize(s.nl);
-    s.total_power = 0;
-    const float pi = static_cast<float>(M_PI);
     for (uint32_t l = 0; l < s.nl; l++) {
         uint32_t m = d.lights[l].mesh;
         s.light_mesh[l] = m;
         if (s.mesh_light[m] < 0)
             s.mesh_light[m] = static_cast<int32_t>(l);
-        float k = pi * s.mesh_area[m]; // m_power = pi * area * rad (light.cpp:20)
-        float pw[3];
-        for (int c = 0; c < 3; c++) {
+        for (int c = 0; c < 3; c++)
             s.light_rad[4 * static_cast<size_t>(l) + c] = d.lights[l].radiance[c];
-            pw[c] = k * d.lights[l].radiance[c];
-        }
-        s.light_pnorm[l] = std::sqrt(dot3(pw, pw));
-        s.total_power += s.light_pnorm[l];
-        s.light_cum[l] = s.total_power;
     }
+    light_table(s);
     std::memcpy(s.cam.origin, d.camera.origin, sizeof(s.cam.origin));
     std::memcpy(s.cam.rot, d.camera.rot, sizeof(s.cam.rot));
     s.cam.sensor = d.camera.sensor_size;

@@ -18,6 +18,7 @@ struct packed_scene {
     std::vector<int32_t> mesh_mat;  // fail-safe remapped to nmat
     std::vector<int32_t> mesh_light;
     std::vector<uint32_t> mesh_toff;
+    std::vector<uint32_t> mesh_voff; // num_meshes + 1 prefix offsets into the vertices
     std::vector<float> mesh_area;   // trimesh::update_face_cdf (geometry.cpp:105-118)
     std::vector<float> tri_cum;
     std::vector<DevMaterial> mats;  // nmat + 1
@@ -39,7 +40,15 @@ struct packed_scene {
 // Fills everything but the BVH. Float arithmetic follows the reference (built with
 // -ffp-contract=off) so light areas, powers and the light CDF are bit-identical to corelib's.
 void pack_scene(e8g_scene_desc const &d, packed_scene &out);
+// Area prefix sums of mesh m's triangles from s.vpos (trimesh::update_face_cdf, geometry.cpp:105-118).
+void mesh_areas(packed_scene &s, uint32_t m);
+// Light powers |pi * area * L| and their CDF in light order (basic_light_sources::commit,
+// lightsources.cpp:45-52) from mesh_area and light_rad.
+void light_table(packed_scene &s);
 void pack_materials(e8g_material const *m, uint32_t n, std::vector<DevMaterial> &out);
 void build_scene_bvh(packed_scene &s, bvh_build_opts const &o);
+// ~(m ^ -1) of a row-major 4x4 matrix in the reference's float arithmetic (xform.cpp); false when
+// |det m| <= 1e-5, the reference's "matrix not invertible".
+bool reference_normal_matrix(float const m[16], float n_out[16]);
 
 } // namespace e8g

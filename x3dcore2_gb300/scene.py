@@ -79,6 +79,56 @@ def from_desc(desc):
     return Scene(voff, toff, mesh_mat, pos, nrm, tris, mats, lights, cam)
 
 
+class Mesh:
+    """One triangle mesh on the host: positions and normals (n, 3), texcoords (n, 2), triangles (m, 3)."""
+
+    def __init__(self, pos, nrm, tris, uv=None):
+        self.pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        self.nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+        self.tris = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+        self.uv = np.zeros((len(self.pos), 2), np.float32) if uv is None else np.asarray(uv, np.float32)
+
+
+def _take_mesh(lib, h):
+    try:
+        d = abi.MeshData()
+        abi.check(lib.e8g_host_mesh_data(h, C.byref(d)), what="e8g_host_mesh_data")
+        nv, nt = d.num_vertices, d.num_triangles
+        arr = np.ctypeslib.as_array
+        return Mesh(arr(d.positions, (nv * 3,)).copy() if nv else np.zeros(0, np.float32),
+                    arr(d.normals, (nv * 3,)).copy() if nv else np.zeros(0, np.float32),
+                    arr(d.triangles, (nt * 3,)).copy() if nt else np.zeros(0, np.uint32),
+                    arr(d.texcoords, (nv * 2,)).reshape(-1, 2).copy() if nv else None)
+    finally:
+        lib.e8g_host_mesh_free(h)
+
+
+def load_obj(path=None, text=None, lib=None):
+    """A Wavefront OBJ mesh read with the reference loader's rules (e8g_obj_load / e8g_obj_parse).
+    Raises E8GError with the loader's message on a malformed file."""
+    lib = lib or abi.load()
+    h = C.c_void_p()
+    err = C.create_string_buffer(512)
+    if text is not None:
+        raw = text.encode() if isinstance(text, str) else bytes(text)
+        st = lib.e8g_obj_parse(raw, len(raw), C.byref(h), err, len(err))
+    else:
+        st = lib.e8g_obj_load(str(path).encode(), C.byref(h), err, len(err))
+    if st != abi.E8G_OK:
+        raise abi.E8GError(f"{abi.STATUS_NAMES.get(st, st)}: {err.value.decode(errors='replace')}")
+    return _take_mesh(lib, h)
+
+
+def from_meshes(meshes, mesh_material, materials, lights, camera):
+    """A Scene of meshes in the given order (the reference path space's ascending object id)."""
+    voff = np.concatenate([[0], np.cumsum([len(m.pos) for m in meshes])]).astype(np.uint32)
+    toff = np.concatenate([[0], np.cumsum([len(m.tris) for m in meshes])]).astype(np.uint32)
+    pos = np.concatenate([m.pos for m in meshes]) if meshes else np.zeros((0, 3), np.float32)
+    nrm = np.concatenate([m.nrm for m in meshes]) if meshes else np.zeros((0, 3), np.float32)
+    tris = np.concatenate([m.tris for m in meshes]) if meshes else np.zeros((0, 3), np.uint32)
+    return Scene(voff, toff, mesh_material, pos, nrm, tris, list(materials), list(lights), camera)
+
+
 def generate(kind, seed=1, level=0, num_tris=0, num_materials=0, amplitude=0.0,
              roughness_lo=0.0, roughness_hi=0.0, width=0, height=0, lib=None):
     """Run one of the native generators (host code; no GPU needed)."""
