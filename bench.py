@@ -303,6 +303,20 @@ def update_leg(ctx, scene):
         for k in range(3):
             ctx.render(p)
             fr_rebuild.append(ctx.stats()["ms"])
+        # the device builder: a rebuild from the device's vertices, and the frame on its tree
+        ctx.upload(scene, layout=lay, builder=abi.BUILDER_DEVICE)
+        dev_build = []
+        for k in range(4):
+            ctx.transform_mesh(big, rot if k % 2 == 0 else np.eye(4, dtype=np.float32))
+            t0 = time.perf_counter()
+            st = ctx.commit(abi.COMMIT_REBUILD)
+            if k:
+                dev_build.append((time.perf_counter() - t0) * 1e3)
+        dev_layout = st["layout"]
+        fr_dev = []
+        for k in range(3):
+            ctx.render(p)
+            fr_dev.append(ctx.stats()["ms"])
         refit_ms = statistics.median(refit_dev)
         if lay == abi.BVH_SAH:  # per refit: triangle records, leaf walks, node boxes, vertex reduction
             alg = nt * (16 + 48 + 48) + nt * (4 + 16 + 48) + nn * 64 + (nn // 2) * 64 + nv * 16
@@ -316,6 +330,8 @@ def update_leg(ctx, scene):
             "refit_algorithmic_bytes": alg, "refit_gbs": alg / (refit_ms * 1e-3) / 1e9,
             "paths_per_s_after_refit": paths / (statistics.median(fr_refit) * 1e-3),
             "paths_per_s_after_rebuild": paths / (statistics.median(fr_rebuild) * 1e-3),
+            "device_rebuild_commit_ms": statistics.median(dev_build), "device_build_layout": dev_layout,
+            "paths_per_s_device_tree": paths / (statistics.median(fr_dev) * 1e-3),
         }
     ctx.upload(scene)
     return out

@@ -124,8 +124,18 @@ typedef struct e8g_bvh_opts {
     float tri_cost;          /* SAH triangle-test cost (reference BVH_RAY_TRIANGLE_COST = 8) */
     float node_cost;         /* SAH box-test cost (reference BVH_RAY_BOX_COST = 1) */
     uint32_t num_threads;    /* host build threads, 0 = all */
-    uint32_t layout;         /* E8G_BVH_SAH or E8G_BVH_REFERENCE */
+    uint32_t layout;         /* E8G_BVH_SAH, E8G_BVH_REFERENCE or E8G_BVH_WIDE */
+    uint32_t builder;        /* E8G_BUILDER_HOST or E8G_BUILDER_DEVICE (SAH pairs and eight-wide) */
 } e8g_bvh_opts;
+
+enum {
+    E8G_BUILDER_HOST = 0,  /* binned SAH on the host threads */
+    E8G_BUILDER_DEVICE = 1 /* on the GPU from the device's vertices: Morton order, PLOC clustering
+                              (radius 16), SAH leaf collapse (leaves of at most min(max_leaf_prims,
+                              15) triangles); no host round trip for SAH pairs, the eight-wide
+                              collapse then runs on the host. Falls back to the host builder when
+                              the tree would be deeper than the traversal stack */
+};
 
 enum {
     E8G_BVH_SAH = 0,       /* binned SAH over 3 axes, child pairs, ordered traversal */

@@ -24,6 +24,7 @@ MODE_REF_DIRECT, MODE_NORMAL, MODE_POSITION, MODE_REF_LT2 = 5, 6, 7, 8
 INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT, INTEGRATOR_PLAIN = 0, 1, 2
 RNG_MINSTD, RNG_PHILOX = 0, 1
 BVH_SAH, BVH_REFERENCE, BVH_WIDE = 0, 1, 2
+BUILDER_HOST, BUILDER_DEVICE = 0, 1
 # compositing
 TONEMAP_CLAMP, TONEMAP_ACES = 0, 1
 XFORM_REFERENCE, XFORM_NORMALS_AS_DIRECTIONS = 0, 1
@@ -64,7 +65,8 @@ class SceneDesc(C.Structure):
 
 class BvhOpts(C.Structure):
     _fields_ = [("max_leaf_prims", C.c_uint32), ("num_bins", C.c_uint32), ("tri_cost", C.c_float),
-                ("node_cost", C.c_float), ("num_threads", C.c_uint32), ("layout", C.c_uint32)]
+                ("node_cost", C.c_float), ("num_threads", C.c_uint32), ("layout", C.c_uint32),
+                ("builder", C.c_uint32)]
 
 
 class BvhStats(C.Structure):

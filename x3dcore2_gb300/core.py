@@ -59,19 +59,21 @@ class Context:
         abi.check(st, self.h, what)
 
     # ---- scene commit -------------------------------------------------------------------
-    def upload(self, scene, build=True, bvh_opts=None, layout=abi.BVH_SAH):
+    def upload(self, scene, build=True, bvh_opts=None, layout=abi.BVH_SAH, builder=abi.BUILDER_HOST):
         self._check(self.lib.e8g_scene_upload(self.h, C.byref(scene.desc)), "e8g_scene_upload")
         self.scene = scene
         if build:
-            self.build_bvh(bvh_opts, layout)
+            self.build_bvh(bvh_opts, layout, builder)
         return self
 
-    def build_bvh(self, opts=None, layout=abi.BVH_SAH):
-        """layout BVH_SAH: the fast tree; BVH_REFERENCE: corelib's own tree and visiting order."""
+    def build_bvh(self, opts=None, layout=abi.BVH_SAH, builder=abi.BUILDER_HOST):
+        """layout BVH_SAH: the fast tree; BVH_REFERENCE: corelib's own tree and visiting order;
+        builder BUILDER_DEVICE builds on the GPU."""
         if opts is None:
             opts = abi.BvhOpts()
             self.lib.e8g_default_bvh_opts(C.byref(opts))
             opts.layout = layout
+            opts.builder = builder
         self._check(self.lib.e8g_scene_build_bvh(self.h, C.byref(opts)), "e8g_scene_build_bvh")
 
     def bvh_stats(self):

@@ -3,6 +3,8 @@
 // kernels of trace.cu, mega.cu, bdpt.cu and wavefront.cu. No entry point throws.
 #include "../../include/e8g.h"
 #include "api_internal.h"
+#include "bvh_boxes.h"
+#include "gpu_build.h"
 
 #include <algorithm>
 #include <cmath>
@@ -181,47 +183,163 @@ e8g_status sync_host_vertices(e8g_ctx *c) {
     return E8G_OK;
 }
 
+namespace {
+
+// The device builder: the SAH-pair tree straight into the device buffers; the eight-wide layout
+// collapses it on the host. *built is false when the tree came out too deep (or clustering made no
+// progress): the caller then builds on the host.
+e8g_status build_on_device(e8g_ctx *c, bool *built) {
+    *built = false;
+    packed_scene &p = c->pack;
+    uint32_t nt = p.nt;
+    bvh_build_opts const &o = c->bvh_opts;
+    fill_dev_scene(c);
+    cudaError_t e = c->b_nlo.reserve(32 * static_cast<size_t>(nt));
+    if (e == cudaSuccess)
+        e = c->b_nhi.reserve(32 * static_cast<size_t>(nt));
+    if (e == cudaSuccess)
+        e = c->b_tri.reserve(48 * static_cast<size_t>(nt));
+    if (e == cudaSuccess)
+        e = c->b_gbuild.reserve(gpu_build_scratch_bytes(nt));
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "device build buffers");
+    GpuBuildIn in{};
+    in.tidx = c->dev.tidx;
+    in.vpos = c->dev.vpos;
+    in.num_tris = nt;
+    in.max_leaf = std::min<uint32_t>(o.max_leaf_prims, 15);
+    in.tri_cost = o.tri_cost;
+    in.node_cost = o.node_cost;
+    in.max_depth = kMaxTreeDepth;
+    in.num_sms = c->num_sms;
+    in.scratch = c->b_gbuild.ptr;
+    in.host_pinned = c->host_pinned;
+    in.nlo = static_cast<float4 *>(c->b_nlo.ptr);
+    in.nhi = static_cast<float4 *>(c->b_nhi.ptr);
+    in.tri = static_cast<float4 *>(c->b_tri.ptr);
+    GpuBuildOut out;
+    auto t0 = std::chrono::steady_clock::now();
+    e = gpu_build_sah_pairs(in, out, c->stream);
+    if (e == cudaErrorUnknown || (e == cudaSuccess && !out.ok))
+        return E8G_OK; // too deep or no progress: the host builds
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "device build");
+    flat_bvh bin;
+    bin.num_nodes = out.num_nodes;
+    bin.num_leaves = out.num_leaves;
+    bin.max_depth = out.max_depth;
+    bin.avg_leaf_depth = out.avg_leaf_depth;
+    bin.eps = scene_eps(out.scene_lo, out.scene_hi);
+    if (o.layout == E8G_BVH_WIDE) {
+        // the eight-wide collapse on the device; its grid covers the vertices and the camera
+        e = c->b_refit.reserve(std::max<size_t>(c->b_refit.bytes, 4 * kRefitRedWords));
+        if (e == cudaSuccess)
+            e = c->b_wide.reserve(96 * static_cast<size_t>(nt));
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "wide collapse buffers");
+        uint32_t *red = static_cast<uint32_t *>(c->b_refit.ptr);
+        launch_vertex_bounds(c->dev.vpos, p.nv, red, 8 * c->num_sms, c->stream);
+        uint32_t words[kRefitRedWords];
+        e = cudaMemcpyAsync(words, red, sizeof(words), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "vertex bounds");
+        float max_abs;
+        std::memcpy(&max_abs, &words[12], 4);
+        for (int k = 0; k < 3; k++)
+            max_abs = std::max(max_abs, std::fabs(p.cam.origin[k]));
+        GpuWideIn wi{};
+        wi.nlo = in.nlo;
+        wi.nhi = in.nhi;
+        wi.tri = in.tri;
+        wi.num_tris = nt;
+        wi.max_abs = max_abs;
+        wi.max_depth = kWideMaxDepth;
+        wi.scratch = in.scratch;
+        wi.host_pinned = c->host_pinned;
+        wi.wide = static_cast<uint4 *>(c->b_wide.ptr);
+        GpuWideOut wo;
+        e = gpu_collapse_wide(wi, wo, c->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "device wide collapse");
+        p.wide.clear();
+        p.tri.clear();
+        if (wo.ok) {
+            p.bvh = flat_bvh{};
+            p.bvh.num_nodes = wo.num_nodes;
+            p.bvh.num_leaves = bin.num_leaves;
+            p.bvh.max_depth = wo.max_depth;
+            p.bvh.eps = bin.eps;
+            p.layout = E8G_BVH_WIDE;
+        } else { // too deep for the eight-wide stack: the binary tree stays
+            p.bvh = std::move(bin);
+            p.layout = E8G_BVH_SAH;
+        }
+    } else {
+        p.wide.clear();
+        p.tri.clear();
+        p.bvh = std::move(bin);
+        p.layout = E8G_BVH_SAH;
+    }
+    p.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    *built = true;
+    return E8G_OK;
+}
+
+} // namespace
+
 e8g_status build_tree(e8g_ctx *c) {
     cudaSetDevice(c->device);
-    e8g_status st = sync_host_vertices(c);
-    if (st != E8G_OK)
-        return st;
     packed_scene &p = c->pack;
-    try {
-        build_scene_bvh(p, c->bvh_opts);
-    } catch (std::bad_alloc const &) {
-        return fail(c, E8G_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+    bool on_device = false;
+    if (c->bvh_opts.builder == E8G_BUILDER_DEVICE && c->bvh_opts.layout != E8G_BVH_REFERENCE && p.nt > 0) {
+        e8g_status st = build_on_device(c, &on_device);
+        if (st != E8G_OK)
+            return st;
     }
-    if (p.layout == E8G_BVH_REFERENCE && p.bvh.max_depth > kMaxRefTreeDepth) {
-        c->built = false;
-        return fail(c, E8G_ERR_UNSUPPORTED, "reference BVH deeper than the traversal stack (63 levels)");
+    if (!on_device) {
+        e8g_status st = sync_host_vertices(c);
+        if (st != E8G_OK)
+            return st;
+        try {
+            build_scene_bvh(p, c->bvh_opts);
+        } catch (std::bad_alloc const &) {
+            return fail(c, E8G_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+        }
+        if (p.layout == E8G_BVH_REFERENCE && p.bvh.max_depth > kMaxRefTreeDepth) {
+            c->built = false;
+            return fail(c, E8G_ERR_UNSUPPORTED, "reference BVH deeper than the traversal stack (63 levels)");
+        }
+        cudaError_t e = upload(c->b_nlo, p.bvh.lo, c->stream);
+        if (e == cudaSuccess)
+            e = upload(c->b_nhi, p.bvh.hi, c->stream);
+        if (e == cudaSuccess)
+            e = upload(c->b_wide, p.wide, c->stream);
+        if (e == cudaSuccess)
+            e = upload(c->b_tri, p.tri, c->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "BVH upload");
     }
-    cudaError_t e = upload(c->b_nlo, p.bvh.lo, c->stream);
-    if (e == cudaSuccess)
-        e = upload(c->b_nhi, p.bvh.hi, c->stream);
-    if (e == cudaSuccess)
-        e = upload(c->b_wide, p.wide, c->stream);
-    if (e == cudaSuccess)
-        e = upload(c->b_tri, p.tri, c->stream);
+    // the vertex box (if_path_space::aabb) and the largest coordinate follow the device's vertices
+    cudaError_t e = c->b_refit.reserve(std::max<size_t>(c->b_refit.bytes, 4 * kRefitRedWords));
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "bounds scratch");
+    uint32_t *red = static_cast<uint32_t *>(c->b_refit.ptr);
+    launch_vertex_bounds(static_cast<float4 const *>(c->b_vpos.ptr), p.nv, red, 8 * c->num_sms, c->stream);
+    uint32_t words[kRefitRedWords];
+    e = cudaMemcpyAsync(words, red, sizeof(words), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess)
-        return cuda_fail(c, e, "BVH upload");
-    // the vertex box (if_path_space::aabb) follows the vertices the tree was built from
-    for (uint32_t v = 0; v < p.nv; v++)
-        for (int k = 0; k < 3; k++) {
-            float x = p.vpos[4 * static_cast<size_t>(v) + k];
-            if (v == 0) {
-                p.bmin[k] = p.bmax[k] = x;
-            } else {
-                p.bmin[k] = x < p.bmin[k] ? x : p.bmin[k];
-                p.bmax[k] = p.bmax[k] < x ? x : p.bmax[k];
-            }
-        }
-    float max_abs = 0.0f;
-    for (uint32_t v = 0; v < p.nv; v++)
-        for (int k = 0; k < 3; k++)
-            max_abs = std::max(max_abs, std::fabs(p.vpos[4 * static_cast<size_t>(v) + k]));
+        return cuda_fail(c, e, "vertex bounds");
+    if (p.nv) {
+        refit_read_bounds(words, p.bmin, p.bmax);
+    }
+    float max_abs;
+    std::memcpy(&max_abs, &words[12], 4);
     for (int k = 0; k < 3; k++)
         max_abs = std::max(max_abs, std::fabs(p.cam.origin[k]));
     c->tree_max_abs = max_abs;
@@ -259,6 +377,7 @@ void e8g_default_bvh_opts(e8g_bvh_opts *o) {
     o->node_cost = 1.0f;
     o->num_threads = 0;
     o->layout = E8G_BVH_SAH;
+    o->builder = E8G_BUILDER_HOST;
 }
 
 void e8g_default_params(e8g_render_params *p, uint32_t mode, uint32_t width, uint32_t height, uint32_t spp) {
@@ -411,7 +530,10 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
         bo.num_threads = o->num_threads;
         if (o->layout > E8G_BVH_WIDE)
             return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH layout");
+        if (o->builder > E8G_BUILDER_DEVICE)
+            return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH builder");
         bo.layout = o->layout;
+        bo.builder = o->builder;
     }
     c->bvh_opts = bo;
     return build_tree(c);

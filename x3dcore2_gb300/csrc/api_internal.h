@@ -57,13 +57,13 @@ struct e8g_ctx {
     e8g::bvh_build_opts bvh_opts{};
     bool dirty = false, host_stale = false, refit_ready = false;
     float tree_max_abs = 0;
-    e8g::dev_buffer b_refit, b_vpos0, b_vnrm0;
+    e8g::dev_buffer b_refit, b_vpos0, b_vnrm0, b_gbuild; // b_gbuild: device builder scratch
 
     std::vector<e8g::dev_buffer *> all_buffers() {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
                 &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch,
-                &b_refit, &b_vpos0, &b_vnrm0};
+                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild};
     }
 };
 

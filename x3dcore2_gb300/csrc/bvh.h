@@ -21,7 +21,8 @@ struct bvh_build_opts {
     float tri_cost = 1.0f;
     float node_cost = 1.0f;
     uint32_t num_threads = 0;
-    uint32_t layout = 0; // 0: SAH child pairs, 1: the reference's tree
+    uint32_t layout = 0; // 0: SAH child pairs, 1: the reference's tree, 2: eight-wide
+    uint32_t builder = 0; // 0: host, 1: device (gpu_build.cu)
 };
 
 struct flat_bvh {

@@ -351,6 +351,11 @@ void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float c
                                                                 R.ex_hi, R.red);
 }
 
+void launch_vertex_bounds(float4 const *vpos, uint32_t nv, uint32_t *red, int grid_cap, cudaStream_t st) {
+    k_refit_init<<<1, 32, 0, st>>>(red);
+    k_refit_verts<<<min(blocks_for(nv), grid_cap), kRefitBlock, 0, st>>>(vpos, nv, red);
+}
+
 void launch_transform(float4 const *vpos0, float4 const *vnrm0, float4 *vpos, float4 *vnrm, XformArgs const &X,
                       cudaStream_t st) {
     if (X.v_end > X.v_begin)

@@ -33,6 +33,8 @@ void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float c
                   cudaStream_t st);
 void launch_transform(float4 const *vpos0, float4 const *vnrm0, float4 *vpos, float4 *vnrm, XformArgs const &X,
                       cudaStream_t st);
+// The vertex box and largest |coordinate| alone into red[6..12] (kRefitRedWords words).
+void launch_vertex_bounds(float4 const *vpos, uint32_t nv, uint32_t *red, int grid_cap, cudaStream_t st);
 // The vertex box of a finished refit from its reduction words (copied to the host).
 void refit_read_bounds(uint32_t const *red_host, float bmin[3], float bmax[3]);
 

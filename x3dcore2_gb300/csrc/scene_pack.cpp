@@ -1,5 +1,6 @@
 #include "scene_pack.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -145,22 +146,26 @@ void pack_scene(e8g_scene_desc const &d, packed_scene &s) {
     s.cam.aspect = d.camera.aspect;
 }
 
-void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
-    auto t0 = std::chrono::steady_clock::now();
-    std::vector<float> p3(3 * static_cast<size_t>(s.nv));
+namespace {
+
+void scene_arrays(packed_scene const &s, std::vector<float> &p3, std::vector<uint32_t> &t3) {
+    p3.resize(3 * static_cast<size_t>(s.nv));
     for (uint32_t v = 0; v < s.nv; v++)
         for (int k = 0; k < 3; k++)
             p3[3 * static_cast<size_t>(v) + k] = s.vpos[4 * static_cast<size_t>(v) + k];
-    std::vector<uint32_t> t3(3 * static_cast<size_t>(s.nt));
+    t3.resize(3 * static_cast<size_t>(s.nt));
     for (uint32_t t = 0; t < s.nt; t++)
         for (int k = 0; k < 3; k++)
             t3[3 * static_cast<size_t>(t) + k] = s.tidx[4 * static_cast<size_t>(t) + k];
+}
+
+// Keeps the binary SAH tree (layout 0) or collapses it to eight-wide nodes (layout 2, falling
+// back to the binary tree when too deep), then writes the triangle records in tree order.
+void finish_tree(packed_scene &s, flat_bvh &&bin, uint32_t layout, std::vector<float> const &p3,
+                 std::vector<uint32_t> const &t3) {
     s.wide.clear();
-    if (o.layout == 1) {
-        s.bvh = build_bvh_reference(p3.data(), t3.data(), s.nt);
-        s.layout = 1;
-    } else if (o.layout == 2) {
-        flat_bvh bin = build_bvh(p3.data(), t3.data(), s.nt, o);
+    s.layout = 0;
+    if (layout == 2) {
         // the grid of the quantized boxes is sized for coordinates up to the scene's and the
         // camera's largest magnitude
         float max_abs = 0.0f;
@@ -174,17 +179,19 @@ void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
             s.bvh.num_nodes = w.num_nodes;
             s.bvh.num_leaves = w.num_leaves;
             s.bvh.max_depth = w.max_depth;
+            s.bvh.eps = bin.eps;
             s.bvh.tri_order = std::move(w.tri_order);
             s.wide = std::move(w.nodes);
             s.layout = 2;
         } else { // deeper than the traversal stack: keep the binary tree
             s.bvh = std::move(bin);
-            s.layout = 0;
         }
     } else {
-        s.bvh = build_bvh(p3.data(), t3.data(), s.nt, o);
-        s.layout = 0;
+        s.bvh = std::move(bin);
     }
+}
+
+void write_tri_records(packed_scene &s, std::vector<float> const &p3, std::vector<uint32_t> const &t3) {
     s.tri.assign(12 * static_cast<size_t>(s.nt), 0.0f);
     for (uint32_t k = 0; k < s.nt; k++) {
         uint32_t t = s.bvh.tri_order[k];
@@ -199,7 +206,32 @@ void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
         }
         std::memcpy(&dst[3], &t, 4);
     }
+}
+
+} // namespace
+
+void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<float> p3;
+    std::vector<uint32_t> t3;
+    scene_arrays(s, p3, t3);
+    if (o.layout == 1) {
+        s.wide.clear();
+        s.bvh = build_bvh_reference(p3.data(), t3.data(), s.nt);
+        s.layout = 1;
+    } else {
+        finish_tree(s, build_bvh(p3.data(), t3.data(), s.nt, o), o.layout, p3, t3);
+    }
+    write_tri_records(s, p3, t3);
     s.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void collapse_scene_bvh(packed_scene &s, flat_bvh &&bin) {
+    std::vector<float> p3;
+    std::vector<uint32_t> t3;
+    scene_arrays(s, p3, t3);
+    finish_tree(s, std::move(bin), 2, p3, t3);
+    write_tri_records(s, p3, t3);
 }
 
 } // namespace e8g

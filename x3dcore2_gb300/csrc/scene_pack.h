@@ -47,6 +47,9 @@ void mesh_areas(packed_scene &s, uint32_t m);
 void light_table(packed_scene &s);
 void pack_materials(e8g_material const *m, uint32_t n, std::vector<DevMaterial> &out);
 void build_scene_bvh(packed_scene &s, bvh_build_opts const &o);
+// The eight-wide layout from a binary SAH tree built elsewhere (the device builder), with the
+// triangle records in its order; keeps the binary tree when the wide one would be too deep.
+void collapse_scene_bvh(packed_scene &s, flat_bvh &&bin);
 // ~(m ^ -1) of a row-major 4x4 matrix in the reference's float arithmetic (xform.cpp); false when
 // |det m| <= 1e-5, the reference's "matrix not invertible".
 bool reference_normal_matrix(float const m[16], float n_out[16]);
