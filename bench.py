@@ -363,6 +363,21 @@ def obj_leg():
             "mb_per_s": len(text) / (best * 1e-3) / 1e6, "threads": 1}
 
 
+def run_leg(args):
+    """One extra leg alone (for profiling it): prints {"leg": name, ...}."""
+    from x3dcore2_gb300.core import Context
+    if args.leg == "obj":
+        print(json.dumps({"leg": "obj", **obj_leg()}))
+        return
+    ctx = Context(0)
+    scene, _, _, _ = make_scene(args.small)
+    ctx.upload(scene)
+    fn = {"bdpt": lambda: bdpt_leg(ctx), "batch": lambda: batch_leg(ctx), "adjoint": lambda: adjoint_leg(ctx),
+          "update": lambda: update_leg(ctx, scene)}[args.leg]
+    print(json.dumps({"leg": args.leg, **fn()}))
+    ctx.close()
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -416,9 +431,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the quality, BDPT, batch and adjoint legs")
     ap.add_argument("--no-tune", action="store_true", help="wavefront with the library defaults (profiling)")
+    ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "update", "obj"],
+                    help="run one extra leg alone on the benchmark scene and print its JSON (not a bench line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.leg:
+        return run_leg(args)
     if args.warmup < 3:
         args.warmup = 3
 

@@ -131,7 +131,7 @@ typedef struct e8g_bvh_opts {
 enum {
     E8G_BUILDER_HOST = 0,  /* binned SAH on the host threads */
     E8G_BUILDER_DEVICE = 1 /* on the GPU from the device's vertices: Morton order, PLOC clustering
-                              (radius 16), SAH leaf collapse (leaves of at most min(max_leaf_prims,
+                              (radius 24), SAH leaf collapse (leaves of at most min(max_leaf_prims,
                               15) triangles); no host round trip for SAH pairs, the eight-wide
                               collapse then runs on the host. Falls back to the host builder when
                               the tree would be deeper than the traversal stack */

@@ -1,5 +1,5 @@
 // BVH build on the device: Morton order, PLOC clustering, SAH leaf collapse, and the SAH-pair node
-// layout of the host builder (bvh.h), written breadth first.
+// layout of the host builder (bvh.h).
 //
 // 1. Per triangle: exact box, centroid, scene box; a 30-bit Morton code of the centroid in the
 //    centroids' box; a stable LSD radix sort of (code, triangle) pairs, 8 bits per pass.
@@ -14,8 +14,9 @@
 //    counts and the SAH cost min(tri_cost A n, node_cost A + C(left) + C(right)); subtrees of at
 //    most max_leaf_prims triangles whose leaf cost is not above their inner cost become leaves.
 // 4. Top-down, one launch per level: every node of the level writes its 32-byte record (boxes
-//    pushed out exactly as the host builder pushes them out, bvh_boxes.h), interior nodes take two
-//    adjacent slots for their children from a scan, leaves write their triangles' records.
+//    pushed out exactly as the host builder pushes them out, bvh_boxes.h) at its depth-first
+//    preorder slot (the host builder's order: children adjacent, the k-th interior node's at 1 + 2k,
+//    from interior-node counts of the subtrees), leaves write their triangles' records.
 // Everything is deterministic: scans, not atomics, decide every position.
 #include "bvh_boxes.h"
 #include "gpu_build.h"
@@ -33,7 +34,7 @@ constexpr int kSortItems = 8;     // keys per thread in the sort
 constexpr int kSortTile = kGB * kSortItems;
 constexpr int kScanItems = 4;     // elements per thread in the device-wide scan
 constexpr int kScanTile = 1024 * kScanItems;
-constexpr int kPlocRadius = 16;
+constexpr int kPlocRadius = 24;
 constexpr int kLeafStack = 16;    // subtree walk of a leaf (at most 15 triangles)
 
 __device__ __forceinline__ uint32_t ord_key(float f) {
@@ -402,12 +403,13 @@ __device__ __forceinline__ float box_area(float4 lo, float4 hi) {
 
 // Triangle counts, SAH cost and leaf decisions; a thread per triangle walks up.
 __global__ void k_collapse(uint32_t n, int2 const *child, uint32_t const *parent, float4 const *blo,
-                           float4 const *bhi, uint32_t *counter, uint32_t *ntris, float *cost, uint8_t *leaf,
-                           uint32_t max_leaf, float tri_cost, float node_cost) {
+                           float4 const *bhi, uint32_t *counter, uint32_t *ntris, uint32_t *icount, float *cost,
+                           uint8_t *leaf, uint32_t max_leaf, float tri_cost, float node_cost) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     ntris[i] = 1;
+    icount[i] = 0;
     cost[i] = tri_cost * box_area(blo[i], bhi[i]);
     leaf[i] = 1;
     uint32_t node = parent[i];
@@ -423,6 +425,7 @@ __global__ void k_collapse(uint32_t n, int2 const *child, uint32_t const *parent
         float as_leaf = tri_cost * area * static_cast<float>(cnt);
         bool make_leaf = cnt <= max_leaf && as_leaf <= inner;
         ntris[node] = cnt;
+        icount[node] = make_leaf ? 0u : 1u + __ldcg(&icount[c.x]) + __ldcg(&icount[c.y]);
         cost[node] = make_leaf ? as_leaf : inner;
         leaf[node] = make_leaf;
         node = parent[node];
@@ -432,7 +435,8 @@ __global__ void k_collapse(uint32_t n, int2 const *child, uint32_t const *parent
 // ------------------------------------------------------------ flatten (top-down) ----
 
 struct FlatItem {
-    uint32_t node, slot, tri_start, pad;
+    uint32_t node, slot, tri_start;
+    uint32_t pre; // interior nodes before this one in depth-first preorder
 };
 
 struct WideItem {
@@ -445,8 +449,8 @@ __global__ void k_flat_flags(FlatItem const *items, uint32_t f, uint8_t const *l
         interior[i] = leaf[items[i].node] ? 0u : 1u;
 }
 
-__global__ void k_flat_emit(FlatItem const *items, uint32_t f, uint32_t const *iscan, uint32_t slot_base, uint32_t n,
-                            int2 const *child, uint8_t const *leaf, uint32_t const *ntris, float4 const *blo,
+__global__ void k_flat_emit(FlatItem const *items, uint32_t f, uint32_t const *iscan, uint32_t n, int2 const *child,
+                            uint8_t const *leaf, uint32_t const *ntris, uint32_t const *icount, float4 const *blo,
                             float4 const *bhi, uint32_t const *order, uint4 const *tidx, float4 const *vpos,
                             uint32_t const *red, float4 *nlo, float4 *nhi, float4 *tri, FlatItem *next,
                             unsigned long long *leaf_stats) {
@@ -488,11 +492,14 @@ __global__ void k_flat_emit(FlatItem const *items, uint32_t f, uint32_t const *i
         }
         atomicAdd(&leaf_stats[0], 1ull);
     } else {
-        link = slot_base + 2 * iscan[i];
+        // depth-first preorder slots, as the host builder lays nodes out: the k-th interior node in
+        // preorder keeps its children at 1 + 2k and 2 + 2k
+        link = 1 + 2 * it.pre;
         count = 0;
         int2 c = child[it.node];
-        next[2 * iscan[i]] = FlatItem{static_cast<uint32_t>(c.x), link, it.tri_start, 0};
-        next[2 * iscan[i] + 1] = FlatItem{static_cast<uint32_t>(c.y), link + 1, it.tri_start + ntris[c.x], 0};
+        next[2 * iscan[i]] = FlatItem{static_cast<uint32_t>(c.x), link, it.tri_start, it.pre + 1};
+        next[2 * iscan[i] + 1] =
+            FlatItem{static_cast<uint32_t>(c.y), link + 1, it.tri_start + ntris[c.x], it.pre + 1 + icount[c.x]};
     }
     nlo[it.slot] = make_float4(inflate_lo(b0.x, eps), inflate_lo(b0.y, eps), inflate_lo(b0.z, eps),
                                __uint_as_float(link));
@@ -516,7 +523,7 @@ struct Scratch {
     uint32_t *red, *keys0, *vals0, *keys1, *vals1, *hist, *sums, *total;
     float4 *tlo, *thi, *blo, *bhi;
     int2 *child;
-    uint32_t *clus0, *clus1, *mflag, *kflag, *mscan, *kscan, *parent, *counter, *ntris;
+    uint32_t *clus0, *clus1, *mflag, *kflag, *mscan, *kscan, *parent, *counter, *ntris, *icount;
     int32_t *nn;
     float *cost;
     uint8_t *leaf;
@@ -558,6 +565,7 @@ Scratch carve(void *base, uint32_t n, size_t *bytes) {
     s.parent = c.take<uint32_t>(nodes);
     s.counter = c.take<uint32_t>(nodes);
     s.ntris = c.take<uint32_t>(nodes);
+    s.icount = c.take<uint32_t>(nodes);
     s.cost = c.take<float>(nodes);
     s.leaf = c.take<uint8_t>(nodes);
     s.fa = c.take<FlatItem>(nodes);
@@ -815,8 +823,8 @@ cudaError_t gpu_build_sah_pairs(GpuBuildIn const &in, GpuBuildOut &out, cudaStre
     if (num_nodes > n)
         k_tree_parents<<<blocks(num_nodes - n, kGB), kGB, 0, st>>>(s.child, n, num_nodes, s.parent);
     cudaMemsetAsync(s.counter, 0, 4 * static_cast<size_t>(num_nodes), st);
-    k_collapse<<<blocks(n, kGB), kGB, 0, st>>>(n, s.child, s.parent, s.blo, s.bhi, s.counter, s.ntris, s.cost, s.leaf,
-                                               in.max_leaf, in.tri_cost, in.node_cost);
+    k_collapse<<<blocks(n, kGB), kGB, 0, st>>>(n, s.child, s.parent, s.blo, s.bhi, s.counter, s.ntris, s.icount, s.cost,
+                                               s.leaf, in.max_leaf, in.tri_cost, in.node_cost);
     // 4. flatten level by level
     FlatItem first{root, 0, 0, 0};
     cudaMemcpyAsync(s.fa, &first, sizeof(first), cudaMemcpyHostToDevice, st);
@@ -837,7 +845,7 @@ cudaError_t gpu_build_sah_pairs(GpuBuildIn const &in, GpuBuildOut &out, cudaStre
         uint32_t g = blocks(f, kGB);
         k_flat_flags<<<g, kGB, 0, st>>>(fa, f, s.leaf, s.iflag);
         scan(s.iflag, f, s.sums, s.total, st);
-        k_flat_emit<<<g, kGB, 0, st>>>(fa, f, s.iflag, slot_base, n, s.child, s.leaf, s.ntris, s.blo, s.bhi, order,
+        k_flat_emit<<<g, kGB, 0, st>>>(fa, f, s.iflag, n, s.child, s.leaf, s.ntris, s.icount, s.blo, s.bhi, order,
                                        in.tidx, in.vpos, s.red, in.nlo, in.nhi, in.tri, fb, s.leaf_stats);
         cudaMemcpyAsync(host, s.total, 4, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
