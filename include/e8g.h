@@ -25,6 +25,7 @@
  *                       trimesh::transform                     corelib/src/geometry.cpp:76-87
  *   e8g_composite       aces_compositor / clamp_compositor     corelib/src/compositor.cpp:29-98
  *   e8g_obj_load        wavefront_obj::load_geometry           corelib/src/resource.cpp:137-255
+ *   e8g_pipeline_*      pt_render_pipeline                     corelib/src/pipeline.cpp:73-185
  *   e8g_forward / e8g_backward, e8g_batch_render: no counterpart in the reference (new).
  */
 #ifndef E8G_H
@@ -414,6 +415,49 @@ e8g_status e8g_scene_get_mesh(e8g_ctx *ctx, uint32_t mesh, float *positions, flo
  * its build_ms is the commit's time. */
 enum { E8G_COMMIT_REFIT = 0, E8G_COMMIT_REBUILD = 1 };
 e8g_status e8g_scene_commit(e8g_ctx *ctx, uint32_t mode, e8g_bvh_stats *stats);
+
+/* -------------------------------------------------------------- pipeline ---- */
+
+/* One frame of the render pipeline (pt_render_pipeline::render_frame, pipeline.cpp:73-101): the
+ * scene changes since the last frame committed (objdb::push_updates: a refit, or a build when the
+ * layout changed), samples_per_frame samples rendered, the ACES compositor applied
+ * (aces_compositor, compositor.cpp:71-98), 8-bit RGBA returned. The reference re-renders every
+ * frame from the same streams; with `progressive` the frames instead continue the sample sequence
+ * and accumulate until the scene, the camera or the settings change. */
+typedef struct e8g_pipeline_config {
+    uint32_t mode;              /* "path_tracer" */
+    uint32_t layout;            /* "path_space" */
+    uint32_t samples_per_frame; /* "samples_per_frame" */
+    uint32_t firefly_filter;    /* "firefly_filter" */
+    uint32_t auto_exposure;     /* "auto_exposure" */
+    float exposure;             /* "exposure" */
+    uint32_t num_threads;       /* "num_threads": host build threads, 0 = all */
+    uint32_t progressive;       /* "progressive" (new) */
+    uint32_t integrator;        /* "integrator" (new): megakernel, wavefront or plain */
+    uint64_t seed;              /* "seed" (new) */
+} e8g_pipeline_config;
+
+/* The reference's defaults (pt_render_pipeline::config_protocol, pipeline.cpp:103-121):
+ * unidirectional, static_bvh, 64 samples per frame, no firefly filter, fixed exposure 1. */
+void e8g_pipeline_config_default(e8g_pipeline_config *cfg);
+
+/* flex_config-style setting by name and value (pipeline.cpp:123-185):
+ *   path_tracer        normal | position | direct | unidirectional | unidirectional_lt1 |
+ *                      bidirectional_lt2 | bidirectional_mis, and mis | bidirectional_power (new)
+ *   path_space         static_bvh (SAH pairs), reference_bvh, wide_bvh (new); linear is
+ *                      E8G_ERR_UNSUPPORTED (brute force is the oracle's, not a GPU layout)
+ *   light_sources      basic
+ *   auto_exposure, firefly_filter, progressive       true | false | 1 | 0
+ *   exposure (float), samples_per_frame (> 0), num_threads, super_samples (accepted, unused, as
+ *   in the reference), seed, integrator (megakernel | wavefront | plain)
+ * Anything else is E8G_ERR_INVALID_ARG ("scene_file": scenes come from e8g_obj_load or
+ * e8g_gen_scene and e8g_scene_upload). */
+e8g_status e8g_pipeline_config_set(e8g_pipeline_config *cfg, const char *key, const char *value);
+
+/* pixels_out: host, width*height*4 bytes; rgba_out (may be NULL): host, the float image before
+ * compositing. */
+e8g_status e8g_pipeline_frame(e8g_ctx *ctx, const e8g_pipeline_config *cfg, uint32_t width, uint32_t height,
+                              uint8_t *pixels_out, float *rgba_out);
 
 /* ------------------------------------------------------------- OBJ ingest ---- */
 

@@ -128,6 +128,13 @@ class MeshData(C.Structure):
                 ("texcoords", C.POINTER(C.c_float)), ("triangles", C.POINTER(C.c_uint32))]
 
 
+class PipelineConfig(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("layout", C.c_uint32), ("samples_per_frame", C.c_uint32),
+                ("firefly_filter", C.c_uint32), ("auto_exposure", C.c_uint32), ("exposure", C.c_float),
+                ("num_threads", C.c_uint32), ("progressive", C.c_uint32), ("integrator", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
 class CompositeParams(C.Structure):
     _fields_ = [("tonemap", C.c_uint32), ("auto_exposure", C.c_uint32), ("exposure", C.c_float)]
 
@@ -167,6 +174,9 @@ SIGNATURES = {
     "e8g_scene_set_camera": (_ST, [_P, C.POINTER(Camera)]),
     "e8g_scene_get_mesh": (_ST, [_P, _U32, _P, _P]),
     "e8g_scene_commit": (_ST, [_P, _U32, C.POINTER(BvhStats)]),
+    "e8g_pipeline_config_default": (None, [C.POINTER(PipelineConfig)]),
+    "e8g_pipeline_config_set": (_ST, [C.POINTER(PipelineConfig), C.c_char_p, C.c_char_p]),
+    "e8g_pipeline_frame": (_ST, [_P, C.POINTER(PipelineConfig), _U32, _U32, _P, _P]),
     "e8g_obj_load": (_ST, [C.c_char_p, C.POINTER(_P), C.c_char_p, C.c_size_t]),
     "e8g_obj_parse": (_ST, [C.c_char_p, C.c_size_t, C.POINTER(_P), C.c_char_p, C.c_size_t]),
     "e8g_host_mesh_data": (_ST, [_P, C.POINTER(MeshData)]),

@@ -25,6 +25,20 @@ def default_params(mode, width, height, spp, **overrides):
     return p
 
 
+def pipeline_config(**settings):
+    """The pipeline's settings: the reference's defaults, then each name=value as flex_config
+    sets it (e8g_pipeline_config_set), e.g. path_tracer="bidirectional_mis", exposure=1.5."""
+    lib = abi.load()
+    cfg = abi.PipelineConfig()
+    lib.e8g_pipeline_config_default(C.byref(cfg))
+    for k, v in settings.items():
+        if isinstance(v, bool):
+            v = "true" if v else "false"
+        abi.check(lib.e8g_pipeline_config_set(C.byref(cfg), k.encode(), str(v).encode()),
+                  what=f"e8g_pipeline_config_set({k}={v})")
+    return cfg
+
+
 def path_seed(seed, pixel, sample):
     return abi.load().e8g_path_seed(seed, pixel, sample)
 
@@ -88,6 +102,14 @@ class Context:
         tris = np.zeros((st["num_tris"], 12), np.float32)
         self._check(self.lib.e8g_bvh_read(self.h, _ptr(nodes), _ptr(tris)), "e8g_bvh_read")
         return nodes, tris
+
+    def pipeline_frame(self, cfg, width, height, want_rgba=False):
+        """One pipeline frame: (8-bit RGBA pixels (h, w, 4), float image or None)."""
+        px = np.zeros((height, width, 4), np.uint8)
+        rgba = np.zeros((height, width, 4), np.float32) if want_rgba else None
+        self._check(self.lib.e8g_pipeline_frame(self.h, C.byref(cfg), width, height, _ptr(px),
+                                                None if rgba is None else _ptr(rgba)), "e8g_pipeline_frame")
+        return px, rgba
 
     # ---- incremental updates ------------------------------------------------------------
     def mesh_vertex_count(self, mesh):

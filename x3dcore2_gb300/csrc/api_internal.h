@@ -58,12 +58,16 @@ struct e8g_ctx {
     bool dirty = false, host_stale = false, refit_ready = false;
     float tree_max_abs = 0;
     e8g::dev_buffer b_refit, b_vpos0, b_vnrm0, b_gbuild; // b_gbuild: device builder scratch
+    // the render pipeline: its float frame and the settings of its last frame
+    e8g::dev_buffer b_pipe;
+    e8g_pipeline_config pipe_cfg{};
+    bool pipe_valid = false;
 
     std::vector<e8g::dev_buffer *> all_buffers() {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
                 &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch,
-                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild};
+                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild, &b_pipe};
     }
 };
 

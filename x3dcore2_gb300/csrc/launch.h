@@ -1,6 +1,7 @@
 // Kernel launchers (defined in the .cu files, called by the C ABI in api.cu).
 #pragma once
 
+#include "../../include/e8g.h"
 #include "device.cuh"
 
 namespace e8g {
@@ -53,6 +54,11 @@ void launch_first_hits_batch(BatchDev const &B, DevScene const *h_scenes, Render
                              uint64_t const *h_pix_prefix, FirstHit *fh_all, cudaStream_t st);
 void launch_resolve_batch(BatchDev const &B, uint64_t total_pix, float4 const *accum_all, float *rgba_all,
                           cudaStream_t st);
+
+// Compositing of a device float RGBA image into 8-bit pixels (composite.cu); d_scratch holds 8
+// doubles for the exposure sum.
+cudaError_t launch_composite(float const *d_rgba, uint32_t w, uint32_t h, e8g_composite_params const &cp,
+                             uint8_t *d_out, double *d_scratch, cudaStream_t st);
 
 // Bidirectional path tracing (uniform or power-heuristic weights), one thread per path.
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
