@@ -385,6 +385,110 @@ __global__ void k_ploc_apply(uint32_t const *clus, uint32_t *clus_out, int32_t c
     }
 }
 
+// The last rounds, once few clusters are left, in one block: the same rounds as the kernels above
+// (same neighbour search, tie-breaks and node numbering), without a launch and a host read per
+// round.
+constexpr int kPlocSmall = 2048;  // clusters the one-block kernel takes over at
+constexpr int kPlocSmallThreads = 1024;
+
+__global__ void __launch_bounds__(kPlocSmallThreads)
+    k_ploc_finish(uint32_t const *clus_in, uint32_t m, uint32_t base, float4 *blo, float4 *bhi, int2 *child,
+                  uint32_t *out_nodes) {
+    __shared__ uint32_t ca[kPlocSmall], cb[kPlocSmall];
+    __shared__ int32_t nn[kPlocSmall];
+    __shared__ uint32_t ms[kPlocSmall], ks[kPlocSmall];
+    __shared__ uint32_t sh[32];
+    constexpr int per = kPlocSmall / kPlocSmallThreads; // elements per thread in the scans
+    for (uint32_t i = threadIdx.x; i < m; i += kPlocSmallThreads)
+        ca[i] = clus_in[i];
+    __syncthreads();
+    uint32_t *cur = ca, *nxt = cb;
+    int rounds = 0;
+    while (m > 1 && rounds++ < 1000000) {
+        for (uint32_t i = threadIdx.x; i < m; i += kPlocSmallThreads) {
+            uint32_t node = cur[i];
+            float4 a0 = blo[node], a1 = bhi[node];
+            float best = INFINITY;
+            int bj = -1;
+            for (int d = -kPlocRadius; d <= kPlocRadius; d++) {
+                int j = static_cast<int>(i) + d;
+                if (d == 0 || j < 0 || j >= static_cast<int>(m))
+                    continue;
+                uint32_t o = cur[j];
+                float area = union_area(a0, a1, blo[o], bhi[o]);
+                if (area < best) {
+                    best = area;
+                    bj = j;
+                }
+            }
+            nn[i] = bj;
+        }
+        __syncthreads();
+        // merge flags and their exclusive scans (each thread owns `per` consecutive clusters)
+        uint32_t mf[per], kf[per], msum = 0, ksum = 0;
+#pragma unroll
+        for (int k = 0; k < per; k++) {
+            uint32_t i = threadIdx.x * per + k;
+            uint32_t merged = 0, keep = 0;
+            if (i < m) {
+                int32_t j = nn[i];
+                bool mutual = j >= 0 && nn[j] == static_cast<int32_t>(i);
+                merged = mutual && static_cast<int32_t>(i) < j;
+                keep = !(mutual && static_cast<int32_t>(i) > j);
+            }
+            mf[k] = merged;
+            kf[k] = keep;
+            msum += merged;
+            ksum += keep;
+        }
+        uint32_t mincl = block_inclusive<kPlocSmallThreads>(msum, sh);
+        uint32_t mtotal = sh[31];
+        __syncthreads();
+        uint32_t kincl = block_inclusive<kPlocSmallThreads>(ksum, sh);
+        uint32_t ktotal = sh[31];
+        __syncthreads();
+        uint32_t mrun = mincl - msum, krun = kincl - ksum;
+#pragma unroll
+        for (int k = 0; k < per; k++) {
+            uint32_t i = threadIdx.x * per + k;
+            if (i < m) {
+                ms[i] = mf[k] ? mrun : 0xFFFFFFFFu;
+                ks[i] = kf[k] ? krun : 0xFFFFFFFFu;
+            }
+            mrun += mf[k];
+            krun += kf[k];
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < m; i += kPlocSmallThreads) {
+            if (ks[i] == 0xFFFFFFFFu)
+                continue;
+            if (ms[i] != 0xFFFFFFFFu) {
+                uint32_t node = base + ms[i];
+                uint32_t a = cur[i], b = cur[nn[i]];
+                child[node] = make_int2(static_cast<int>(a), static_cast<int>(b));
+                float4 a0 = blo[a], a1 = bhi[a], b0 = blo[b], b1 = bhi[b];
+                blo[node] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f);
+                bhi[node] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
+                nxt[ks[i]] = node;
+            } else {
+                nxt[ks[i]] = cur[i];
+            }
+        }
+        __syncthreads();
+        if (mtotal == 0)
+            break; // no mutual pair (non-finite boxes): reported through the node count
+        base += mtotal;
+        m = ktotal;
+        uint32_t *t = cur;
+        cur = nxt;
+        nxt = t;
+        __threadfence_block();
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        out_nodes[0] = m == 1 ? base : 0u;
+}
+
 // ------------------------------------------------------------- collapse (bottom-up) ----
 
 __global__ void k_tree_parents(int2 const *child, uint32_t n, uint32_t num_nodes, uint32_t *parent) {
@@ -414,10 +518,12 @@ __global__ void k_collapse(uint32_t n, int2 const *child, uint32_t const *parent
     leaf[i] = 1;
     uint32_t node = parent[i];
     while (node != 0xFFFFFFFFu) {
-        __threadfence();
-        if (atomicAdd(&counter[node], 1u) == 0)
+        // the second child to arrive carries on: release of this thread's writes, acquire of the
+        // sibling's
+        uint32_t old;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(&counter[node]) : "memory");
+        if (old == 0)
             return;
-        __threadfence();
         int2 c = child[node];
         uint32_t cnt = __ldcg(&ntris[c.x]) + __ldcg(&ntris[c.y]);
         float area = box_area(blo[node], bhi[node]);
@@ -796,6 +902,20 @@ cudaError_t gpu_build_sah_pairs(GpuBuildIn const &in, GpuBuildOut &out, cudaStre
     uint32_t *ca = s.clus0, *cb = s.clus1;
     int rounds = 0;
     while (m > 1) {
+        if (m <= static_cast<uint32_t>(kPlocSmall)) {
+            // the remaining rounds in one block
+            k_ploc_finish<<<1, kPlocSmallThreads, 0, st>>>(ca, m, base, s.blo, s.bhi, s.child, s.total + 2);
+            cudaError_t e = cudaMemcpyAsync(host, s.total + 2, 4, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess)
+                return e;
+            if (host[0] == 0)
+                return cudaErrorUnknown; // no mutual pair (non-finite boxes): host build
+            base = host[0];
+            m = 1;
+            break;
+        }
         if (++rounds > 100000)
             return cudaErrorUnknown; // no progress: the caller falls back to the host build
         uint32_t g = blocks(m, kGB);

@@ -13,6 +13,7 @@
 #include "launch.h"
 #include "refit.h"
 
+#include <cstdint>
 #include <cstring>
 
 namespace e8g {
@@ -28,6 +29,14 @@ __device__ __forceinline__ uint32_t ord_of(float f) {
 }
 __device__ __forceinline__ float of_ord(uint32_t u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// Arrival at a parent: release of this thread's writes, acquire of the siblings' (their arrivals
+// are earlier in the counter's modification order).
+__device__ __forceinline__ uint32_t arrive(uint32_t *counter) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
+    return old;
 }
 
 // Block-wide min / max of `n` values per thread into red[...] with one atomic per block and word.
@@ -85,7 +94,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_verts(float4 const *vpos,
 // Triangle records (v0 | id, v1 - v0, v2 - v0) from the current vertices, and the exact box of
 // all triangles (the scene box the boxes' eps derives from).
 __global__ void __launch_bounds__(kRefitBlock) k_refit_tris(float4 *tri, uint4 const *tidx, float4 const *vpos,
-                                                             uint32_t nt, uint32_t *red) {
+                                                             uint32_t nt, uint32_t *red, float4 *tlo, float4 *thi) {
     uint32_t mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
     uint32_t mx[3] = {0, 0, 0};
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
@@ -95,6 +104,10 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_tris(float4 *tri, uint4 c
         tri[3 * static_cast<size_t>(k)] = make_float4(p0.x, p0.y, p0.z, w);
         tri[3 * static_cast<size_t>(k) + 1] = make_float4(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z, 0.0f);
         tri[3 * static_cast<size_t>(k) + 2] = make_float4(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z, 0.0f);
+        tlo[k] = make_float4(fminf(fminf(p0.x, p1.x), p2.x), fminf(fminf(p0.y, p1.y), p2.y),
+                             fminf(fminf(p0.z, p1.z), p2.z), 0.0f);
+        thi[k] = make_float4(fmaxf(fmaxf(p0.x, p1.x), p2.x), fmaxf(fmaxf(p0.y, p1.y), p2.y),
+                             fmaxf(fmaxf(p0.z, p1.z), p2.z), 0.0f);
         float c[3][3] = {{p0.x, p0.y, p0.z}, {p1.x, p1.y, p1.z}, {p2.x, p2.y, p2.z}};
 #pragma unroll
         for (int v = 0; v < 3; v++)
@@ -119,22 +132,18 @@ __device__ __forceinline__ float scene_eps_of(uint32_t const *red) {
     return scene_eps(lo, hi);
 }
 
-// Exact box of the triangles at record positions [first, first + n).
-__device__ __forceinline__ void range_box(float4 const *tri, uint4 const *tidx, float4 const *vpos, uint32_t first,
-                                          uint32_t n, float lo[3], float hi[3]) {
+// Exact box of the triangles at record positions [first, first + n), from their boxes.
+__device__ __forceinline__ void range_box(float4 const *tlo, float4 const *thi, uint32_t first, uint32_t n,
+                                          float lo[3], float hi[3]) {
     for (int a = 0; a < 3; a++) {
         lo[a] = INFINITY;
         hi[a] = -INFINITY;
     }
     for (uint32_t k = first; k < first + n; k++) {
-        uint4 g = __ldg(&tidx[__float_as_uint(__ldg(&tri[3 * static_cast<size_t>(k)].w))]);
-        uint32_t vi[3] = {g.x, g.y, g.z};
-        for (int v = 0; v < 3; v++) {
-            float4 p = __ldg(&vpos[vi[v]]);
-            lo[0] = fminf(lo[0], p.x), hi[0] = fmaxf(hi[0], p.x);
-            lo[1] = fminf(lo[1], p.y), hi[1] = fmaxf(hi[1], p.y);
-            lo[2] = fminf(lo[2], p.z), hi[2] = fmaxf(hi[2], p.z);
-        }
+        float4 a = __ldg(&tlo[k]), b = __ldg(&thi[k]);
+        lo[0] = fminf(lo[0], a.x), hi[0] = fmaxf(hi[0], b.x);
+        lo[1] = fminf(lo[1], a.y), hi[1] = fmaxf(hi[1], b.y);
+        lo[2] = fminf(lo[2], a.z), hi[2] = fmaxf(hi[2], b.z);
     }
 }
 
@@ -159,8 +168,8 @@ __device__ __forceinline__ void store_pair_node(float4 *nlo, float4 *nhi, uint32
 }
 
 __global__ void __launch_bounds__(kRefitBlock)
-    k_refit_pairs(float4 *nlo, float4 *nhi, uint32_t nn, float4 const *tri, uint4 const *tidx, float4 const *vpos,
-                  uint32_t const *parent, uint32_t *counter, float4 *ex_lo, float4 *ex_hi, uint32_t const *red) {
+    k_refit_pairs(float4 *nlo, float4 *nhi, uint32_t nn, float4 const *tlo, float4 const *thi, uint32_t const *parent,
+                  uint32_t *counter, float4 *ex_lo, float4 *ex_hi, uint32_t const *red) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn)
         return;
@@ -169,14 +178,12 @@ __global__ void __launch_bounds__(kRefitBlock)
         return;
     float eps = scene_eps_of(red);
     float lo[3], hi[3];
-    range_box(tri, tidx, vpos, __float_as_uint(nlo[i].w), count, lo, hi);
+    range_box(tlo, thi, __float_as_uint(nlo[i].w), count, lo, hi);
     store_pair_node(nlo, nhi, i, lo, hi, eps, ex_lo, ex_hi);
     uint32_t n = parent[i];
     while (n != 0xFFFFFFFFu) {
-        __threadfence();
-        if (atomicAdd(&counter[n], 1u) == 0)
+        if (arrive(&counter[n]) == 0)
             return; // the sibling's thread finishes this node
-        __threadfence();
         uint32_t c = __float_as_uint(nlo[n].w);
         float4 a0 = __ldcg(&ex_lo[c]), a1 = __ldcg(&ex_hi[c]);
         float4 b0 = __ldcg(&ex_lo[c + 1]), b1 = __ldcg(&ex_hi[c + 1]);
@@ -200,8 +207,8 @@ __global__ void k_parents_wide(uint4 const *wn, uint32_t nn, uint32_t *parent) {
         parent[base + r] = i;
 }
 
-__device__ void refit_wide_node(uint4 *wn, uint32_t i, float4 const *tri, uint4 const *tidx, float4 const *vpos,
-                                float4 *ex_lo, float4 *ex_hi, float eps, double step_min) {
+__device__ void refit_wide_node(uint4 *wn, uint32_t i, float4 const *tlo, float4 const *thi, float4 *ex_lo,
+                                float4 *ex_hi, float eps, double step_min) {
     uint32_t w[kWideWords];
     uint4 *node = wn + 6 * static_cast<size_t>(i);
 #pragma unroll
@@ -220,7 +227,7 @@ __device__ void refit_wide_node(uint4 *wn, uint32_t i, float4 const *tri, uint4 
             lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = b.x, hi[1] = b.y, hi[2] = b.z;
         } else if (leaves >> s & 1) {
             uint32_t meta = (w[6 + (s >> 2)] >> (8 * (s & 3))) & 0xFFu;
-            range_box(tri, tidx, vpos, tri_base + meta, (counts >> (4 * s)) & 0xFu, lo, hi);
+            range_box(tlo, thi, tri_base + meta, (counts >> (4 * s)) & 0xFu, lo, hi);
         } else {
             for (int a = 0; a < 3; a++)
                 slo[s][a] = shi[s][a] = 0.0f;
@@ -243,23 +250,20 @@ __device__ void refit_wide_node(uint4 *wn, uint32_t i, float4 const *tri, uint4 
 }
 
 __global__ void __launch_bounds__(kRefitBlock)
-    k_refit_wide(uint4 *wn, uint32_t nn, float4 const *tri, uint4 const *tidx, float4 const *vpos,
-                 uint32_t const *parent, uint32_t *counter, float4 *ex_lo, float4 *ex_hi, uint32_t const *red,
-                 float cam_abs) {
+    k_refit_wide(uint4 *wn, uint32_t nn, float4 const *tlo, float4 const *thi, uint32_t const *parent,
+                 uint32_t *counter, float4 *ex_lo, float4 *ex_hi, uint32_t const *red, float cam_abs) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn || (wn[6 * static_cast<size_t>(i)].w >> 24) != 0)
         return;
     float eps = scene_eps_of(red);
     double step_min = wide_step_min(fmaxf(__uint_as_float(red[12]), cam_abs));
-    refit_wide_node(wn, i, tri, tidx, vpos, ex_lo, ex_hi, eps, step_min);
+    refit_wide_node(wn, i, tlo, thi, ex_lo, ex_hi, eps, step_min);
     uint32_t n = parent[i];
     while (n != 0xFFFFFFFFu) {
-        __threadfence();
         uint32_t need = __popc(__ldcg(&wn[6 * static_cast<size_t>(n)].w) >> 24);
-        if (atomicAdd(&counter[n], 1u) + 1 < need)
+        if (arrive(&counter[n]) + 1 < need)
             return; // a later child's thread finishes this node
-        __threadfence();
-        refit_wide_node(wn, n, tri, tidx, vpos, ex_lo, ex_hi, eps, step_min);
+        refit_wide_node(wn, n, tlo, thi, ex_lo, ex_hi, eps, step_min);
         n = parent[n];
     }
 }
@@ -305,12 +309,12 @@ inline int blocks_for(uint64_t n) { return n ? static_cast<int>((n + kRefitBlock
 
 } // namespace
 
-size_t refit_scratch_bytes(uint32_t nn) {
-    return 16 * static_cast<size_t>(kRefitRedWords / 4 + 2 * static_cast<size_t>(nn)) +
-           8 * static_cast<size_t>(nn) + 16;
+size_t refit_scratch_bytes(uint32_t nn, uint32_t nt) {
+    return 4 * static_cast<size_t>(kRefitRedWords) + 32 * static_cast<size_t>(nn) + 8 * static_cast<size_t>(nn) +
+           32 * static_cast<size_t>(nt) + 16;
 }
 
-RefitScratch refit_carve(void *base, uint32_t nn) {
+RefitScratch refit_carve(void *base, uint32_t nn, uint32_t nt) {
     RefitScratch r;
     char *p = static_cast<char *>(base);
     r.red = reinterpret_cast<uint32_t *>(p);
@@ -322,6 +326,11 @@ RefitScratch refit_carve(void *base, uint32_t nn) {
     r.parent = reinterpret_cast<uint32_t *>(p);
     p += 4 * static_cast<size_t>(nn);
     r.counter = reinterpret_cast<uint32_t *>(p);
+    p += 4 * static_cast<size_t>(nn);
+    p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+    r.tlo = reinterpret_cast<float4 *>(p);
+    p += 16 * static_cast<size_t>(nt);
+    r.thi = reinterpret_cast<float4 *>(p);
     return r;
 }
 
@@ -341,13 +350,13 @@ void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float c
     cudaMemsetAsync(R.counter, 0, 4 * static_cast<size_t>(nn), st);
     k_refit_init<<<1, 32, 0, st>>>(R.red);
     k_refit_verts<<<min(blocks_for(nv), grid_cap), kRefitBlock, 0, st>>>(S.vpos, nv, R.red);
-    k_refit_tris<<<min(blocks_for(nt), grid_cap), kRefitBlock, 0, st>>>(tri, S.tidx, S.vpos, nt, R.red);
+    k_refit_tris<<<min(blocks_for(nt), grid_cap), kRefitBlock, 0, st>>>(tri, S.tidx, S.vpos, nt, R.red, R.tlo, R.thi);
     if (S.layout == 2)
-        k_refit_wide<<<blocks_for(nn), kRefitBlock, 0, st>>>(const_cast<uint4 *>(S.wnodes), nn, tri, S.tidx, S.vpos,
-                                                               R.parent, R.counter, R.ex_lo, R.ex_hi, R.red, cam_abs);
+        k_refit_wide<<<blocks_for(nn), kRefitBlock, 0, st>>>(const_cast<uint4 *>(S.wnodes), nn, R.tlo, R.thi, R.parent,
+                                                               R.counter, R.ex_lo, R.ex_hi, R.red, cam_abs);
     else
         k_refit_pairs<<<blocks_for(nn), kRefitBlock, 0, st>>>(const_cast<float4 *>(S.nlo), const_cast<float4 *>(S.nhi),
-                                                                nn, tri, S.tidx, S.vpos, R.parent, R.counter, R.ex_lo,
+                                                                nn, R.tlo, R.thi, R.parent, R.counter, R.ex_lo,
                                                                 R.ex_hi, R.red);
 }
 

@@ -14,6 +14,7 @@ struct RefitScratch {
     float4 *ex_lo, *ex_hi; // exact (not pushed-out) box of every node
     uint32_t *parent;      // parent node, 0xFFFFFFFF for the root
     uint32_t *counter;     // children finished, per node
+    float4 *tlo, *thi;     // exact box of every triangle record
 };
 
 // trimesh::transform of the vertices [v_begin, v_end): m the matrix, n the normal matrix (both
@@ -23,8 +24,8 @@ struct XformArgs {
     uint32_t v_begin, v_end, directions;
 };
 
-size_t refit_scratch_bytes(uint32_t num_nodes);
-RefitScratch refit_carve(void *base, uint32_t num_nodes);
+size_t refit_scratch_bytes(uint32_t num_nodes, uint32_t num_tris);
+RefitScratch refit_carve(void *base, uint32_t num_nodes, uint32_t num_tris);
 // Parent links of the current tree (once per build).
 void launch_refit_parents(DevScene const &S, RefitScratch const &R, cudaStream_t st);
 // Triangle records, scene and vertex boxes, then every node bottom-up. cam_abs: the camera

@@ -196,10 +196,10 @@ e8g_status e8g_scene_commit(e8g_ctx *c, uint32_t mode, e8g_bvh_stats *stats) {
             return st;
         c->bvh_stats.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     } else {
-        cudaError_t e = c->b_refit.reserve(refit_scratch_bytes(p.bvh.num_nodes));
+        cudaError_t e = c->b_refit.reserve(refit_scratch_bytes(p.bvh.num_nodes, p.nt));
         if (e != cudaSuccess)
             return cuda_fail(c, e, "refit scratch");
-        RefitScratch R = refit_carve(c->b_refit.ptr, p.bvh.num_nodes);
+        RefitScratch R = refit_carve(c->b_refit.ptr, p.bvh.num_nodes, p.nt);
         fill_dev_scene(c);
         cudaEventRecord(c->ev0, c->stream);
         if (!c->refit_ready)

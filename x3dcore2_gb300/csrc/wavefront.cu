@@ -142,13 +142,11 @@ __global__ void __launch_bounds__(256, 4)
             float4 b = W.beta_pdf[s];
             beta = xyz(b);
             last_pdf = b.w;
-            float4 pm = W.p_mesh[s];
-            p = xyz(pm);
-            mesh = __float_as_int(pm.w);
-            float4 nd = W.n_depth[s];
-            n = xyz(nd);
-            depth = __float_as_uint(nd.w);
-            o = xyz(W.o[s]);
+            // a stored slot always waits for its extension hit: the vertex comes from the hit, so
+            // only the direction and the depth travel between bounces
+            float4 od = W.o[s];
+            o = xyz(od);
+            depth = __float_as_uint(od.w);
             rng = RngSlot<R>::load(args_of<MULTI>(A0, B, sid), pixel, sample, W.rng[s]);
         }
         if (state == kWaitHit) { // complete the extension ray shot last bounce
@@ -307,9 +305,7 @@ __global__ void __launch_bounds__(256, 4)
                         W.sid[s] = sid;
                 }
                 W.beta_pdf[s] = make_float4(beta.x, beta.y, beta.z, last_pdf);
-                W.p_mesh[s] = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
-                W.n_depth[s] = make_float4(n.x, n.y, n.z, __uint_as_float(depth));
-                W.o[s] = make_float4(o.x, o.y, o.z, 0.0f);
+                W.o[s] = make_float4(o.x, o.y, o.z, __uint_as_float(depth));
                 W.rng[s] = RngSlot<R>::store(rng);
                 busy_local++;
             }
@@ -524,8 +520,6 @@ static WfSlots carve(char *base, uint32_t capacity, size_t *total) {
     W.rng = reinterpret_cast<uint32_t *>(take(Q * 4));
     W.sid = reinterpret_cast<uint32_t *>(take(Q * 4));
     W.beta_pdf = reinterpret_cast<float4 *>(take(Q * 16));
-    W.p_mesh = reinterpret_cast<float4 *>(take(Q * 16));
-    W.n_depth = reinterpret_cast<float4 *>(take(Q * 16));
     W.o = reinterpret_cast<float4 *>(take(Q * 16));
     W.hit = reinterpret_cast<float4 *>(take(Q * 16));
     W.sh_o = reinterpret_cast<float4 *>(take(Q * 16));

@@ -9,7 +9,7 @@ namespace e8g {
 struct WfSlots {
     uint32_t capacity;
     uint32_t *state, *pixel, *sample, *out, *rng, *sid; // sid: scene index (many-scene wavefront)
-    float4 *beta_pdf, *p_mesh, *n_depth, *o, *hit;
+    float4 *beta_pdf, *o, *hit; // o: direction towards the previous vertex | depth
     float4 *sh_o, *sh_d, *sh_c; // shadow queue: origin | out, direction | tmax, contribution
     float4 *ext_o, *ext_d;      // extension queue: origin | slot, direction
     void *counters;
