@@ -339,35 +339,6 @@ __global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Cou
     }
 }
 
-// Queue entries handed to a warp's idle lanes: the warp takes a chunk of kWfChunk consecutive
-// entries with one atomic and deals them out in order, so idle lanes can be refilled at any step
-// for the price of a ballot, not an atomic. `im` is the mask of lanes that want an entry (the same
-// in every lane); returns this lane's entry (meaningful in lanes of `im`; past the queue's end
-// once it is drained).
-constexpr uint32_t kWfChunk = 64;
-struct WarpChunk {
-    uint32_t next = 0, end = 0;
-};
-__device__ __forceinline__ uint32_t chunk_take(WarpChunk &c, uint32_t im, uint32_t *head) {
-    uint32_t want = __popc(im), avail = c.end - c.next;
-    uint32_t r = __popc(im & ((1u << lane_id()) - 1u));
-    uint32_t nb = 0;
-    if (avail < want) {
-        int leader = __ffs(im) - 1;
-        if (static_cast<int>(lane_id()) == leader)
-            nb = atomicAdd(head, kWfChunk);
-        nb = __shfl_sync(~0u, nb, leader);
-    }
-    uint32_t qq = r < avail ? c.next + r : nb + (r - avail);
-    if (avail < want) {
-        c.next = nb + (want - avail);
-        c.end = nb + kWfChunk;
-    } else {
-        c.next += want;
-    }
-    return qq;
-}
-
 // Persistent trace kernel with per-lane dynamic fetch: a lane whose ray is finished takes the
 // next queue entry; lanes are refilled together (one atomic) once at least `threshold` of them
 // are idle, or when none is busy. WIDE: the eight-wide tree (one node visit per step), else the
@@ -391,14 +362,18 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
     bool exhausted = false;
     TravState T;
     WideTrav TW;
-    WarpChunk chunk;
     while (true) {
         bool idle = q == kNone && !exhausted;
         uint32_t im = __ballot_sync(~0u, idle);
         uint32_t busy = __ballot_sync(~0u, q != kNone);
         if (im && (__popc(im) >= threshold || busy == 0)) {
-            uint32_t qq = chunk_take(chunk, im, head);
+            int leader = __ffs(im) - 1;
+            uint32_t base = 0;
+            if (static_cast<int>(lane) == leader)
+                base = atomicAdd(head, static_cast<uint32_t>(__popc(im)));
+            base = __shfl_sync(~0u, base, leader);
             if (idle) {
+                uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
                 if (qq < n) {
                     q = qq;
                     float3 ro, rd;
@@ -463,14 +438,18 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
     uint32_t q = kNone;
     bool exhausted = false;
     WideTrav T;
-    WarpChunk chunk;
     while (true) {
         bool idle = q == kNone && !exhausted;
         uint32_t im = __ballot_sync(~0u, idle);
         uint32_t busy = __ballot_sync(~0u, q != kNone);
         if (im && (__popc(im) >= threshold || busy == 0)) {
-            uint32_t qq = chunk_take(chunk, im, head);
+            int leader = __ffs(im) - 1;
+            uint32_t base = 0;
+            if (static_cast<int>(lane) == leader)
+                base = atomicAdd(head, static_cast<uint32_t>(__popc(im)));
+            base = __shfl_sync(~0u, base, leader);
             if (idle) {
+                uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
                 if (qq < n) {
                     q = qq;
                     uint32_t sid;
