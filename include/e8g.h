@@ -116,13 +116,14 @@ typedef struct e8g_scene_desc {
     e8g_camera camera;
 } e8g_scene_desc;
 
-/* Build options of the SAH layout. e8g_default_bvh_opts gives values tuned for the GPU traversal
- * (8, 32, 1, 1); the reference's own constants are 4, 20, 8, 1 (pathspace.cpp:121-124). The
+/* Build options of the SAH layouts. e8g_default_bvh_opts gives values tuned for the GPU traversal
+ * (8, 32, 0, 1: a triangle cost <= 0 takes the layout's tuned value, 1 for SAH pairs and 3 for the
+ * eight-wide tree); the reference's own constants are 4, 20, 8, 1 (pathspace.cpp:121-124). The
  * reference layout ignores them: it always builds the reference's tree. */
 typedef struct e8g_bvh_opts {
     uint32_t max_leaf_prims; /* largest leaf (reference BVH_MAX_PRIMS = 4) */
     uint32_t num_bins;       /* SAH bins per axis, 2..64 (reference BVH_BUCKET_COUNT = 20) */
-    float tri_cost;          /* SAH triangle-test cost (reference BVH_RAY_TRIANGLE_COST = 8) */
+    float tri_cost;          /* SAH triangle-test cost (reference BVH_RAY_TRIANGLE_COST = 8); <= 0: tuned */
     float node_cost;         /* SAH box-test cost (reference BVH_RAY_BOX_COST = 1) */
     uint32_t num_threads;    /* host build threads, 0 = all */
     uint32_t layout;         /* E8G_BVH_SAH, E8G_BVH_REFERENCE or E8G_BVH_WIDE */
@@ -305,8 +306,10 @@ e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
 /* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity
  * {2^20, 2^21, 2^22}, bounces per graph {2, 4, 8} and warp refill threshold {0, 4, 8, 12, 16, 24}
  * (the number of idle lanes at which a trace kernel hands its idle lanes new rays; 0 = one ray
- * per thread) on a short render of `params` (at most 8 spp), and keeps the fastest for this
- * context and its current tree. Without it: 2^21 slots, 4 bounces per graph, threshold 16. */
+ * per thread) on a short render of `params` (at most 8 spp), times the four fastest again on a
+ * render of at most 32 spp, and keeps the fastest of those for this context and its current
+ * tree. cand_ms are the short renders' times. Without it: 2^21 slots, 4 bounces per graph,
+ * threshold 16. */
 #define E8G_TUNE_MAX_CANDIDATES 64
 typedef struct e8g_tune_result {
     uint32_t capacity;          /* chosen number of path slots */

@@ -208,7 +208,7 @@ e8g_status build_on_device(e8g_ctx *c, bool *built) {
     in.vpos = c->dev.vpos;
     in.num_tris = nt;
     in.max_leaf = std::min<uint32_t>(o.max_leaf_prims, 15);
-    in.tri_cost = o.tri_cost;
+    in.tri_cost = effective_tri_cost(o);
     in.node_cost = o.node_cost;
     in.max_depth = kMaxTreeDepth;
     in.num_sms = c->num_sms;
@@ -373,7 +373,7 @@ void e8g_default_bvh_opts(e8g_bvh_opts *o) {
         return;
     o->max_leaf_prims = 8;
     o->num_bins = 32;
-    o->tri_cost = 1.0f;
+    o->tri_cost = 0.0f; // the layout's tuned value
     o->node_cost = 1.0f;
     o->num_threads = 0;
     o->layout = E8G_BVH_SAH;

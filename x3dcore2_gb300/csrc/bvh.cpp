@@ -165,6 +165,7 @@ flat_bvh build_bvh(float const *pos, uint32_t const *tris, uint32_t num_tris, bv
         return out;
     builder b;
     b.o = o;
+    b.o.tri_cost = effective_tri_cost(o);
     b.pb.resize(num_tris);
     b.pc.resize(3 * static_cast<size_t>(num_tris));
     b.ids.resize(num_tris);

@@ -265,6 +265,35 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                 r.threshold = th;
             }
             }
+    // Short renders favour small slot pools (a frame's tail weighs more in them): the four fastest
+    // candidates are timed again on a render of up to 32 samples per pixel, and the fastest of
+    // those is kept.
+    uint32_t spp2 = std::max<uint32_t>(p.spp, std::min<uint32_t>(params->spp, 32));
+    if (spp2 > p.spp && r.num_candidates > 1) {
+        uint32_t order[E8G_TUNE_MAX_CANDIDATES];
+        for (uint32_t i = 0; i < r.num_candidates; i++)
+            order[i] = i;
+        std::sort(order, order + r.num_candidates, [&r](uint32_t a, uint32_t b) { return r.cand_ms[a] < r.cand_ms[b]; });
+        e8g_render_params p2 = p;
+        p2.spp = spp2;
+        best = 1e300;
+        for (uint32_t k = 0; k < std::min<uint32_t>(4, r.num_candidates); k++) {
+            uint32_t i = order[k];
+            c->wf_capacity = r.cand_capacity[i];
+            c->wf_bounces = r.cand_bounces[i];
+            c->wf_threshold = r.cand_threshold[i];
+            s = render_image(c, &p2, static_cast<float *>(c->b_img.ptr), nullptr);
+            if (s != E8G_OK)
+                return s;
+            double ms = c->stats.kernel_ms;
+            if (ms < best) {
+                best = ms;
+                r.capacity = r.cand_capacity[i];
+                r.bounces_per_graph = r.cand_bounces[i];
+                r.threshold = r.cand_threshold[i];
+            }
+        }
+    }
     c->wf_capacity = r.capacity;
     c->wf_bounces = r.bounces_per_graph;
     c->wf_threshold = r.threshold;

@@ -220,7 +220,9 @@ void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
         s.bvh = build_bvh_reference(p3.data(), t3.data(), s.nt);
         s.layout = 1;
     } else {
-        finish_tree(s, build_bvh(p3.data(), t3.data(), s.nt, o), o.layout, p3, t3);
+        bvh_build_opts ob = o;
+        ob.tri_cost = effective_tri_cost(o);
+        finish_tree(s, build_bvh(p3.data(), t3.data(), s.nt, ob), o.layout, p3, t3);
     }
     write_tri_records(s, p3, t3);
     s.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
