@@ -142,11 +142,19 @@ def test_device_wide_collapse_equals_host_collapse(ctx, collapse_checker, tmp_pa
     the host collapse (bvh_wide.cpp) writes for the same binary tree."""
     import subprocess
     from test_wide_bvh import dump
+    import ctypes as C
     sc = SCENES[name]()
-    ctx.upload(sc, layout=abi.BVH_SAH, builder=abi.BUILDER_DEVICE)
+
+    def opts(layout):  # the same binary tree for both layouts: an explicit triangle cost
+        o = abi.BvhOpts()
+        ctx.lib.e8g_default_bvh_opts(C.byref(o))
+        o.layout, o.builder, o.tri_cost = layout, abi.BUILDER_DEVICE, 3.0
+        return o
+    ctx.upload(sc, build=False)
+    ctx.build_bvh(opts(abi.BVH_SAH))
     nodes_b, tris_b = ctx.bvh_read()
     nn = ctx.bvh_stats()["num_nodes"]
-    ctx.upload(sc, layout=abi.BVH_WIDE, builder=abi.BUILDER_DEVICE)
+    ctx.build_bvh(opts(abi.BVH_WIDE))
     st = ctx.bvh_stats()
     assert st["layout"] == abi.BVH_WIDE
     nodes_w, tris_w = ctx.bvh_read()
