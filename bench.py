@@ -36,9 +36,10 @@ WORKLOAD = dict(workload="displaced_icosphere_l8_1080p_64spp", triangles=1310730
 # profiles/: dram__bytes_read.sum + dram__bytes_write.sum over one frame of a 480x270, 8-spp
 # render of the same scene divided by its 1,036,800 paths, scaled to the full frame by its path
 # count. SAH pairs + megakernel: 212.6 MB + 12.5 MB (profiles/megakernel_icosphere_l8.md);
-# eight-wide tree + wavefront: 527.9 MB over the frame's 38 launches (shade, the combined trace
-# kernel, first hits, resolve; profiles/wavefront_wide_icosphere_l8.md).
-TRAFFIC_BYTES_PER_PATH = {("sah", "megakernel"): 217.1, ("wide", "wavefront"): 509.1}
+# eight-wide tree + wavefront: 7.59 GB over the 62 launches of a 1080p 8-spp frame of the same
+# scene, 16.6 M paths in steady state (shade, the combined trace kernel, first hits, resolve;
+# profiles/wavefront_wide_icosphere_l8.md).
+TRAFFIC_BYTES_PER_PATH = {("sah", "megakernel"): 217.1, ("wide", "wavefront"): 457.7}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
 
 
