@@ -322,6 +322,9 @@ typedef struct e8g_tune_result {
     double cand_ms[E8G_TUNE_MAX_CANDIDATES];
 } e8g_tune_result;
 e8g_status e8g_wavefront_tune(e8g_ctx *ctx, const e8g_render_params *params, e8g_tune_result *result);
+/* Sets the wavefront configuration directly: slot capacity (1024 .. 2^26), bounces captured per
+ * graph (1 .. 16) and warp refill threshold (0 .. 32). */
+e8g_status e8g_wavefront_set(e8g_ctx *ctx, uint32_t capacity, uint32_t bounces_per_graph, uint32_t threshold);
 
 /* Largest image (width * height) e8g_render_dev_noalloc accepts. */
 #define E8G_NOALLOC_MAX_PIXELS 65536u

@@ -221,3 +221,21 @@ def test_progressive_accumulation_equals_one_render(ctx):
     first = d.cpu().numpy()
     four = ctx.render(p)
     assert np.allclose(first, four, rtol=1e-5, atol=1e-6)
+
+
+def test_wavefront_set_pins_the_configuration(ctx):
+    """e8g_wavefront_set: any valid configuration renders the same image (the paths are the
+    same; only slot counts and graph sizes change); out-of-range values are refused."""
+    sc = S.displaced_icosphere(level=4, seed=2, num_materials=8, width=64, height=48)
+    ctx.upload(sc, layout=abi.BVH_WIDE)
+    p = default_params(abi.MODE_MIS, 64, 48, 8, seed=6, max_depth=8, rr_start=3,
+                       integrator=abi.INTEGRATOR_WAVEFRONT)
+    imgs = []
+    for cap, b, th in ((1 << 12, 1, 0), (1 << 16, 8, 24), (1 << 20, 2, 12)):
+        abi.check(ctx.lib.e8g_wavefront_set(ctx.h, cap, b, th), ctx.h, "set")
+        imgs.append(ctx.render(p))
+    for im in imgs[1:]:
+        close = np.abs(im - imgs[0]) <= np.maximum(1e-4 * np.abs(imgs[0]), 1e-5)
+        assert close.mean() >= 0.999
+    for bad in ((512, 2, 12), (1 << 20, 0, 12), (1 << 20, 2, 33)):
+        assert ctx.lib.e8g_wavefront_set(ctx.h, *bad) == 1  # E8G_ERR_INVALID_ARG

@@ -162,6 +162,7 @@ SIGNATURES = {
     "e8g_composite_dev": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P, _P]),
     "e8g_count_traversal": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(RenderStats)]),
     "e8g_wavefront_tune": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(TuneResult)]),
+    "e8g_wavefront_set": (_ST, [_P, _U32, _U32, _U32]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
     "e8g_forward": (_ST, [_P, C.POINTER(RenderParams), _P]),
     "e8g_backward": (_ST, [_P, _P, _P, _P]),

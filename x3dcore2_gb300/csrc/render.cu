@@ -302,6 +302,18 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     return E8G_OK;
 }
 
+e8g_status e8g_wavefront_set(e8g_ctx *c, uint32_t capacity, uint32_t bounces, uint32_t threshold) {
+    using namespace e8g;
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    if (capacity < 1024 || capacity > (1u << 26) || bounces < 1 || bounces > 16 || threshold > 32)
+        return fail(c, E8G_ERR_INVALID_ARG, "wavefront configuration out of range");
+    c->wf_capacity = capacity;
+    c->wf_bounces = bounces;
+    c->wf_threshold = threshold;
+    return E8G_OK;
+}
+
 e8g_status e8g_forward(e8g_ctx *c, e8g_render_params const *p, float *rgba_out) {
     using namespace e8g;
     e8g_status s = check_ready(c);
