@@ -304,12 +304,12 @@ e8g_status e8g_render_progressive(e8g_ctx *ctx, const e8g_render_params *params,
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
 
 /* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity
- * {2^20, 2^21, 2^22}, bounces per graph {2, 4, 8} and warp refill threshold {0, 4, 8, 12, 16, 24}
- * (the number of idle lanes at which a trace kernel hands its idle lanes new rays; 0 = one ray
- * per thread) on a short render of `params` (at most 8 spp), times the four fastest again on a
- * render of at most 32 spp, and keeps the fastest of those for this context and its current
- * tree. cand_ms are the short renders' times. Without it: 2^21 slots, 4 bounces per graph,
- * threshold 16. */
+ * {2^20 .. 2^24}, bounces per graph {2, 4} and warp refill threshold {4, 8, 12, 16, 24} (the
+ * number of idle lanes at which a trace kernel hands its idle lanes new rays) on a short render
+ * of `params` (at most 8 spp), then each capacity's fastest pair again on a render of at most 64
+ * spp (long renders favour large slot pools), and keeps the fastest of those for this context
+ * and its current tree. cand_ms are the short renders' times. Without it: 2^21 slots, 4 bounces
+ * per graph, threshold 16. */
 #define E8G_TUNE_MAX_CANDIDATES 64
 typedef struct e8g_tune_result {
     uint32_t capacity;          /* chosen number of path slots */

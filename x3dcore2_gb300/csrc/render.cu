@@ -233,9 +233,9 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     cudaError_t e = c->b_img.reserve(bytes);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "image buffer");
-    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
-    const uint32_t bnc[] = {2, 4, 8};
-    const uint32_t thr[] = {0, 4, 8, 12, 16, 24};
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    const uint32_t bnc[] = {2, 4};
+    const uint32_t thr[] = {4, 8, 12, 16, 24};
     e8g_tune_result r{};
     double best = 1e300;
     for (uint32_t cap : caps)
@@ -265,32 +265,34 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                 r.threshold = th;
             }
             }
-    // Short renders favour small slot pools (a frame's tail weighs more in them): the four fastest
-    // candidates are timed again on a render of up to 32 samples per pixel, and the fastest of
-    // those is kept.
-    uint32_t spp2 = std::max<uint32_t>(p.spp, std::min<uint32_t>(params->spp, 32));
-    if (spp2 > p.spp && r.num_candidates > 1) {
-        uint32_t order[E8G_TUNE_MAX_CANDIDATES];
-        for (uint32_t i = 0; i < r.num_candidates; i++)
-            order[i] = i;
-        std::sort(order, order + r.num_candidates, [&r](uint32_t a, uint32_t b) { return r.cand_ms[a] < r.cand_ms[b]; });
+    // Short renders favour small slot pools (the frame's tail weighs more in them, and larger
+    // pools amortise every bounce's fixed cost over more rays only in long renders): each
+    // capacity's fastest (bounces, threshold) pair is timed again on a render of up to 64 samples
+    // per pixel, and the fastest of those is kept.
+    uint32_t spp2 = std::max<uint32_t>(p.spp, std::min<uint32_t>(params->spp, 64));
+    if (spp2 > p.spp) {
         e8g_render_params p2 = p;
         p2.spp = spp2;
         best = 1e300;
-        for (uint32_t k = 0; k < std::min<uint32_t>(4, r.num_candidates); k++) {
-            uint32_t i = order[k];
-            c->wf_capacity = r.cand_capacity[i];
-            c->wf_bounces = r.cand_bounces[i];
-            c->wf_threshold = r.cand_threshold[i];
+        for (uint32_t cap : caps) {
+            int bi = -1;
+            for (uint32_t i = 0; i < r.num_candidates; i++)
+                if (r.cand_capacity[i] == cap && (bi < 0 || r.cand_ms[i] < r.cand_ms[bi]))
+                    bi = static_cast<int>(i);
+            if (bi < 0)
+                continue;
+            c->wf_capacity = cap;
+            c->wf_bounces = r.cand_bounces[bi];
+            c->wf_threshold = r.cand_threshold[bi];
             s = render_image(c, &p2, static_cast<float *>(c->b_img.ptr), nullptr);
             if (s != E8G_OK)
                 return s;
             double ms = c->stats.kernel_ms;
             if (ms < best) {
                 best = ms;
-                r.capacity = r.cand_capacity[i];
-                r.bounces_per_graph = r.cand_bounces[i];
-                r.threshold = r.cand_threshold[i];
+                r.capacity = cap;
+                r.bounces_per_graph = r.cand_bounces[bi];
+                r.threshold = r.cand_threshold[bi];
             }
         }
     }
