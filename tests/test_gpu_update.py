@@ -318,3 +318,26 @@ def test_reference_layout_commit_keeps_reference_hit_identities(ctx):
     assert np.array_equal(got["mesh"], want["mesh"]) and np.array_equal(got["tri"], want["tri"])
     hit = want["mesh"] >= 0
     assert np.array_equal(got["t"][hit].view(np.uint32), want["t"][hit].view(np.uint32))
+
+
+def test_update_entry_points_refuse_bad_arguments(lib):
+    """Error paths: no scene, a mesh out of range, a NULL array, an unknown commit mode or
+    transform flag: a status, never a crash."""
+    import ctypes as C
+    from x3dcore2_gb300 import abi as A
+    with Context(0) as c:
+        m = np.eye(4, dtype=np.float32)
+        assert lib.e8g_scene_commit(c.h, A.COMMIT_REFIT, None) == 4           # E8G_ERR_NO_SCENE
+        assert lib.e8g_scene_transform_mesh(c.h, 0, m.ctypes.data, 0) == 4
+        sc = S.cornell(16, 16)
+        c.upload(sc)
+        nm = len(sc.mesh_mat)
+        pos = np.zeros((1 << 12, 3), np.float32)
+        assert lib.e8g_scene_update_mesh(c.h, nm, pos.ctypes.data, None) == 1  # E8G_ERR_INVALID_ARG
+        assert lib.e8g_scene_update_mesh(c.h, 0, None, None) == 1
+        assert lib.e8g_scene_transform_mesh(c.h, nm, m.ctypes.data, 0) == 1
+        assert lib.e8g_scene_transform_mesh(c.h, 0, m.ctypes.data, 7) == 1
+        assert lib.e8g_scene_commit(c.h, 9, None) == 1
+        assert lib.e8g_scene_get_mesh(c.h, nm, None, None) == 1
+        # nothing changed, so the scene still renders
+        c.render(default_params(abi.MODE_MIS, 16, 16, 1))
