@@ -68,6 +68,7 @@ void fill_dev_scene(e8g_ctx *c) {
     S.tidx = static_cast<uint4 const *>(c->b_tidx.ptr);
     S.vpos = static_cast<float4 const *>(c->b_vpos.ptr);
     S.vnrm = static_cast<float4 const *>(c->b_vnrm.ptr);
+    S.vtx = static_cast<float4 const *>(c->b_vtx.ptr);
     S.mesh_mat = static_cast<int32_t const *>(c->b_mesh_mat.ptr);
     S.mesh_light = static_cast<int32_t const *>(c->b_mesh_light.ptr);
     S.mesh_toff = static_cast<uint32_t const *>(c->b_mesh_toff.ptr);
@@ -327,6 +328,11 @@ e8g_status build_tree(e8g_ctx *c) {
     cudaError_t e = c->b_refit.reserve(std::max<size_t>(c->b_refit.bytes, 4 * kRefitRedWords));
     if (e != cudaSuccess)
         return cuda_fail(c, e, "bounds scratch");
+    e = c->b_vtx.reserve(std::max<size_t>(32 * static_cast<size_t>(p.nv), 32));
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "shading vertices");
+    launch_interleave(static_cast<float4 const *>(c->b_vpos.ptr), static_cast<float4 const *>(c->b_vnrm.ptr), p.nv,
+                      static_cast<float4 *>(c->b_vtx.ptr), c->stream);
     uint32_t *red = static_cast<uint32_t *>(c->b_refit.ptr);
     launch_vertex_bounds(static_cast<float4 const *>(c->b_vpos.ptr), p.nv, red, 8 * c->num_sms, c->stream);
     uint32_t words[kRefitRedWords];

@@ -35,7 +35,7 @@ struct e8g_ctx {
     e8g_render_stats stats{};
     uint32_t launches = 0;
     // scene
-    e8g::dev_buffer b_nlo, b_nhi, b_wide, b_tri, b_tidx, b_vpos, b_vnrm, b_mesh_mat, b_mesh_light, b_mesh_toff, b_mesh_area,
+    e8g::dev_buffer b_nlo, b_nhi, b_wide, b_tri, b_tidx, b_vpos, b_vnrm, b_vtx, b_mesh_mat, b_mesh_light, b_mesh_toff, b_mesh_area,
         b_tri_cum, b_mats, b_light_mesh, b_light_rad, b_light_cum, b_light_pnorm;
     // render scratch
     e8g::dev_buffer b_fh, b_accum, b_work, b_img, b_io0, b_io1, b_counts;
@@ -64,7 +64,7 @@ struct e8g_ctx {
     bool pipe_valid = false;
 
     std::vector<e8g::dev_buffer *> all_buffers() {
-        return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
+        return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_vtx, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
                 &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch,
                 &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild, &b_pipe};

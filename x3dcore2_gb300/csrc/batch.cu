@@ -61,7 +61,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     // host: pack, build, stage
     staged st;
     struct offs {
-        size_t nlo, nhi, wide, tri, tidx, vpos, vnrm, mesh_mat, mesh_light, mesh_toff, mesh_area, tri_cum, mats, light_mesh,
+        size_t nlo, nhi, wide, tri, tidx, vpos, vnrm, vtx, mesh_mat, mesh_light, mesh_toff, mesh_area, tri_cum, mats, light_mesh,
             light_rad, light_cum, light_pnorm;
     };
     std::vector<offs> off(n);
@@ -95,6 +95,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
             o.tidx = st.put(p.tidx);
             o.vpos = st.put(p.vpos);
             o.vnrm = st.put(p.vnrm);
+            o.vtx = st.put(p.vtx);
             o.mesh_mat = st.put(p.mesh_mat);
             o.mesh_light = st.put(p.mesh_light);
             o.mesh_toff = st.put(p.mesh_toff);
@@ -139,6 +140,7 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         S.tidx = reinterpret_cast<uint4 const *>(base + o.tidx);
         S.vpos = reinterpret_cast<float4 const *>(base + o.vpos);
         S.vnrm = reinterpret_cast<float4 const *>(base + o.vnrm);
+        S.vtx = reinterpret_cast<float4 const *>(base + o.vtx);
         S.mesh_mat = reinterpret_cast<int32_t const *>(base + o.mesh_mat);
         S.mesh_light = reinterpret_cast<int32_t const *>(base + o.mesh_light);
         S.mesh_toff = reinterpret_cast<uint32_t const *>(base + o.mesh_toff);

@@ -37,6 +37,8 @@ struct DevScene {
     const uint4 *tidx;      // per global triangle: global vertex indices, mesh
     const float4 *vpos;     // per vertex
     const float4 *vnrm;     // per vertex
+    const float4 *vtx;      // per vertex, for shading: (position, normal.x), (normal.y, normal.z, 0, 0),
+                            // one 32-byte sector per vertex instead of one in each array above
     const int32_t *mesh_mat;   // per mesh: material index (fail-safe remapped to nmat)
     const int32_t *mesh_light; // per mesh: light index or -1
     const uint32_t *mesh_toff; // num_meshes + 1
@@ -547,11 +549,20 @@ struct Vert {
 };
 
 // Interpolated vertex and renormalised normal of a hit (pathspace.cpp:385-409).
+// A vertex's position and normal from the interleaved shading copy (one sector).
+__device__ __forceinline__ void shading_vertex(const DevScene &S, uint32_t i, float3 &p, float3 &n) {
+    float4 a = __ldg(&S.vtx[2 * static_cast<size_t>(i)]), b = __ldg(&S.vtx[2 * static_cast<size_t>(i) + 1]);
+    p = f3(a.x, a.y, a.z);
+    n = f3(a.w, b.x, b.y);
+}
+
 __device__ __forceinline__ Vert make_vert(const DevScene &S, const Hit &h) {
     uint4 ti = __ldg(&S.tidx[h.tri]);
     float b0 = 1.0f - h.b1 - h.b2; // tensor.h:723
-    float3 p0 = xyz(__ldg(&S.vpos[ti.x])), p1 = xyz(__ldg(&S.vpos[ti.y])), p2 = xyz(__ldg(&S.vpos[ti.z]));
-    float3 n0 = xyz(__ldg(&S.vnrm[ti.x])), n1 = xyz(__ldg(&S.vnrm[ti.y])), n2 = xyz(__ldg(&S.vnrm[ti.z]));
+    float3 p0, p1, p2, n0, n1, n2;
+    shading_vertex(S, ti.x, p0, n0);
+    shading_vertex(S, ti.y, p1, n1);
+    shading_vertex(S, ti.z, p2, n2);
     Vert v;
     v.p = add(add(scale(p0, b0), scale(p1, h.b1)), scale(p2, h.b2));
     v.n = normalize(add(add(scale(n0, b0), scale(n1, h.b1)), scale(n2, h.b2)));
@@ -844,8 +855,10 @@ __device__ __forceinline__ Surf mesh_sample(const DevScene &S, uint32_t mesh, R 
     float b0 = 1 - r;
     float b1 = r * v;
     float b2 = 1 - b0 - b1;
-    float3 p0 = xyz(__ldg(&S.vpos[ti.x])), p1 = xyz(__ldg(&S.vpos[ti.y])), p2 = xyz(__ldg(&S.vpos[ti.z]));
-    float3 n0 = xyz(__ldg(&S.vnrm[ti.x])), n1 = xyz(__ldg(&S.vnrm[ti.y])), n2 = xyz(__ldg(&S.vnrm[ti.z]));
+    float3 p0, p1, p2, n0, n1, n2;
+    shading_vertex(S, ti.x, p0, n0);
+    shading_vertex(S, ti.y, p1, n1);
+    shading_vertex(S, ti.z, p2, n2);
     Surf s;
     s.p = add(add(scale(p0, b0), scale(p1, b1)), scale(p2, b2));
     s.n = normalize(add(add(scale(n0, b0), scale(n1, b1)), scale(n2, b2)));

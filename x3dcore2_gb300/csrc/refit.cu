@@ -360,6 +360,22 @@ void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float c
                                                                 R.ex_hi, R.red);
 }
 
+namespace {
+__global__ void k_interleave(float4 const *vpos, float4 const *vnrm, uint32_t nv, float4 *vtx) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv)
+        return;
+    float4 p = vpos[v], n = vnrm[v];
+    vtx[2 * static_cast<size_t>(v)] = make_float4(p.x, p.y, p.z, n.x);
+    vtx[2 * static_cast<size_t>(v) + 1] = make_float4(n.y, n.z, 0.0f, 0.0f);
+}
+} // namespace
+
+void launch_interleave(float4 const *vpos, float4 const *vnrm, uint32_t nv, float4 *vtx, cudaStream_t st) {
+    if (nv)
+        k_interleave<<<blocks_for(nv), kRefitBlock, 0, st>>>(vpos, vnrm, nv, vtx);
+}
+
 void launch_vertex_bounds(float4 const *vpos, uint32_t nv, uint32_t *red, int grid_cap, cudaStream_t st) {
     k_refit_init<<<1, 32, 0, st>>>(red);
     k_refit_verts<<<min(blocks_for(nv), grid_cap), kRefitBlock, 0, st>>>(vpos, nv, red);

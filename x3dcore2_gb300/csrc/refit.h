@@ -34,6 +34,8 @@ void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float c
                   cudaStream_t st);
 void launch_transform(float4 const *vpos0, float4 const *vnrm0, float4 *vpos, float4 *vnrm, XformArgs const &X,
                       cudaStream_t st);
+// The interleaved shading copy of the vertices (DevScene::vtx, 2 float4 per vertex).
+void launch_interleave(float4 const *vpos, float4 const *vnrm, uint32_t nv, float4 *vtx, cudaStream_t st);
 // The vertex box and largest |coordinate| alone into red[6..12] (kRefitRedWords words).
 void launch_vertex_bounds(float4 const *vpos, uint32_t nv, uint32_t *red, int grid_cap, cudaStream_t st);
 // The vertex box of a finished refit from its reduction words (copied to the host).

@@ -92,6 +92,12 @@ void pack_scene(e8g_scene_desc const &d, packed_scene &s) {
             s.vpos[4 * static_cast<size_t>(v) + k] = d.positions[3 * static_cast<size_t>(v) + k];
             s.vnrm[4 * static_cast<size_t>(v) + k] = d.normals[3 * static_cast<size_t>(v) + k];
         }
+    s.vtx.assign(8 * static_cast<size_t>(s.nv), 0.0f);
+    for (uint32_t v = 0; v < s.nv; v++)
+        for (int k = 0; k < 3; k++) {
+            s.vtx[8 * static_cast<size_t>(v) + k] = d.positions[3 * static_cast<size_t>(v) + k];
+            s.vtx[8 * static_cast<size_t>(v) + 3 + k] = d.normals[3 * static_cast<size_t>(v) + k];
+        }
     s.tidx.assign(4 * static_cast<size_t>(s.nt), 0u);
     s.mesh_mat.resize(s.nm);
     s.mesh_light.assign(s.nm, -1);

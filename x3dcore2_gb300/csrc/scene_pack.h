@@ -14,6 +14,7 @@ namespace e8g {
 struct packed_scene {
     uint32_t nm = 0, nv = 0, nt = 0, nmat = 0, nl = 0;
     std::vector<float> vpos, vnrm;  // 4 floats per vertex
+    std::vector<float> vtx;         // 8 floats per vertex: position, normal (the shading copy, DevScene::vtx)
     std::vector<uint32_t> tidx;     // 4 per triangle: global vertex indices, mesh
     std::vector<int32_t> mesh_mat;  // fail-safe remapped to nmat
     std::vector<int32_t> mesh_light;

@@ -206,6 +206,7 @@ e8g_status e8g_scene_commit(e8g_ctx *c, uint32_t mode, e8g_bvh_stats *stats) {
             launch_refit_parents(c->dev, R, c->stream);
         float cam_abs = camera_abs(p);
         launch_refit(c->dev, R, p.nv, cam_abs, 8 * c->num_sms, c->stream);
+        launch_interleave(c->dev.vpos, c->dev.vnrm, p.nv, static_cast<float4 *>(c->b_vtx.ptr), c->stream);
         cudaEventRecord(c->ev1, c->stream);
         uint32_t red[kRefitRedWords];
         e = cudaGetLastError();
