@@ -126,7 +126,7 @@ typedef struct e8g_bvh_opts {
     float tri_cost;          /* SAH triangle-test cost (reference BVH_RAY_TRIANGLE_COST = 8); <= 0: tuned */
     float node_cost;         /* SAH box-test cost (reference BVH_RAY_BOX_COST = 1) */
     uint32_t num_threads;    /* host build threads, 0 = all */
-    uint32_t layout;         /* E8G_BVH_SAH, E8G_BVH_REFERENCE or E8G_BVH_WIDE */
+    uint32_t layout;         /* E8G_BVH_SAH, E8G_BVH_REFERENCE, E8G_BVH_WIDE or E8G_BVH_LINEAR */
     uint32_t builder;        /* E8G_BUILDER_HOST or E8G_BUILDER_DEVICE (SAH pairs and eight-wide) */
 } e8g_bvh_opts;
 
@@ -143,8 +143,11 @@ enum {
     E8G_BVH_SAH = 0,       /* binned SAH over 3 axes, child pairs, ordered traversal */
     E8G_BVH_REFERENCE = 1, /* the reference's own tree and visiting order (pathspace.cpp:121-456):
                               hit identities match the reference bit for bit, ties included */
-    E8G_BVH_WIDE = 2       /* the SAH tree collapsed to eight-wide nodes with quantized child
+    E8G_BVH_WIDE = 2,      /* the SAH tree collapsed to eight-wide nodes with quantized child
                               boxes (96 bytes per node), octant-ordered traversal: the fastest */
+    E8G_BVH_LINEAR = 3     /* no tree: every triangle in mesh order, the first of equal distances
+                              kept (linear_path_space_layout, pathspace.cpp:36-114); for tiny
+                              scenes and as the reference's brute-force ground truth */
 };
 
 typedef struct e8g_bvh_stats {
@@ -417,7 +420,7 @@ e8g_status e8g_scene_get_mesh(e8g_ctx *ctx, uint32_t mesh, float *positions, flo
  * build). The tree's quality degrades as geometry moves far from where it was built; rebuild then.
  * E8G_COMMIT_REBUILD builds a new tree on the host with the last build options.
  * The reference layout (E8G_BVH_REFERENCE) always rebuilds, as the reference does on every commit,
- * so its hit identities stay the reference's. stats (may be NULL) receives the tree's statistics;
+ * so its hit identities stay the reference's; the linear layout rewrites its triangle records. stats (may be NULL) receives the tree's statistics;
  * its build_ms is the commit's time. */
 enum { E8G_COMMIT_REFIT = 0, E8G_COMMIT_REBUILD = 1 };
 e8g_status e8g_scene_commit(e8g_ctx *ctx, uint32_t mode, e8g_bvh_stats *stats);
@@ -450,8 +453,8 @@ void e8g_pipeline_config_default(e8g_pipeline_config *cfg);
 /* flex_config-style setting by name and value (pipeline.cpp:123-185):
  *   path_tracer        normal | position | direct | unidirectional | unidirectional_lt1 |
  *                      bidirectional_lt2 | bidirectional_mis, and mis | bidirectional_power (new)
- *   path_space         static_bvh (SAH pairs), reference_bvh, wide_bvh (new); linear is
- *                      E8G_ERR_UNSUPPORTED (brute force is the oracle's, not a GPU layout)
+ *   path_space         static_bvh (SAH pairs), linear (E8G_BVH_LINEAR), reference_bvh,
+ *                      wide_bvh (new)
  *   light_sources      basic
  *   auto_exposure, firefly_filter, progressive       true | false | 1 | 0
  *   exposure (float), samples_per_frame (> 0), num_threads, super_samples (accepted, unused, as

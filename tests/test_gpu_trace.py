@@ -7,6 +7,7 @@ import golden_util as G
 import oracle_bind as ob
 from x3dcore2_gb300 import abi
 from x3dcore2_gb300 import scene as S
+from x3dcore2_gb300.core import default_params
 
 pytestmark = pytest.mark.gpu
 
@@ -116,3 +117,41 @@ def test_trace_without_scene_is_an_error(lib):
     with Context(0) as c:
         with pytest.raises(E8GError, match="NO_SCENE"):
             c.trace_closest(np.zeros((1, 6), np.float32))
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_linear_layout_matches_the_reference_linear_path_space(ctx, name):
+    """E8G_BVH_LINEAR against the oracle's restatement of linear_path_space_layout
+    (pathspace.cpp:36-114): every hit's mesh, triangle, distance and barycentrics bit for bit,
+    ties included (both keep the first triangle in mesh order), and every any-hit answer."""
+    d = G.load(name)
+    sc = G.scene_from(d)
+    ctx.upload(sc, layout=abi.BVH_LINEAR)
+    st = ctx.bvh_stats()
+    assert st["layout"] == abi.BVH_LINEAR and st["num_nodes"] == 0
+    osc = ob.OracleScene(sc)
+    rng = np.random.default_rng(4)
+    lo, hi = sc.pos.min(0), sc.pos.max(0)
+    dirs = rng.normal(0, 1, (4000, 3))
+    rays = np.concatenate([d["rays"], ob.rays_array(rng.uniform(lo, hi, (4000, 3)).astype(np.float32),
+                                                    (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(np.float32))])
+    g = ctx.trace_closest(rays)
+    o = osc.trace_closest(rays, use_bvh=False)
+    assert np.array_equal(g["mesh"], o["mesh"]) and np.array_equal(g["tri"], o["tri"])
+    hit = o["mesh"] >= 0
+    assert np.array_equal(g["t"][hit].view(np.uint32), o["t"][hit].view(np.uint32))
+    assert np.array_equal(g["b"][hit].view(np.uint32), o["b"][hit].view(np.uint32))
+    tmax = np.full(len(rays), 2.0, np.float32)
+    assert np.array_equal(ctx.trace_any(rays, 1e-4, tmax), osc.trace_any(rays, np.full(len(rays), 1e-4, np.float32), tmax,
+                                                                          use_bvh=False))
+
+
+def test_linear_layout_renders_like_the_trees(ctx):
+    sc = S.cornell(40, 32)
+    p = default_params(abi.MODE_REF_LT1, 40, 32, 4, seed=2)
+    ctx.upload(sc, layout=abi.BVH_REFERENCE)
+    want = ctx.render(p)
+    ctx.upload(sc, layout=abi.BVH_LINEAR)
+    got = ctx.render(p)
+    close = np.abs(got - want) <= np.maximum(1e-4 * np.abs(want), 1e-5)
+    assert close.mean() >= 0.999

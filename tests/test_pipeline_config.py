@@ -30,10 +30,11 @@ def test_other_settings(lib):
         abi.BVH_WIDE, 16, 1, 1, 1.75)
     assert (c.progressive, c.integrator, c.seed, c.num_threads) == (1, abi.INTEGRATOR_WAVEFRONT, 42, 3)
     assert pipeline_config(path_space="reference_bvh").layout == abi.BVH_REFERENCE
+    assert pipeline_config(path_space="linear").layout == abi.BVH_LINEAR
 
 
 @pytest.mark.parametrize("key,value,status", [
-    ("path_tracer", "photon_mapping", "INVALID_ARG"), ("path_space", "linear", "UNSUPPORTED"),
+    ("path_tracer", "photon_mapping", "INVALID_ARG"),
     ("path_space", "kd_tree", "INVALID_ARG"), ("samples_per_frame", "0", "INVALID_ARG"),
     ("samples_per_frame", "-3", "INVALID_ARG"), ("exposure", "bright", "INVALID_ARG"),
     ("auto_exposure", "maybe", "INVALID_ARG"), ("light_sources", "sky", "INVALID_ARG"),

@@ -23,7 +23,7 @@ MODE_REF_UNI, MODE_REF_LT1, MODE_MIS, MODE_REF_BDPT, MODE_BDPT_POWER = 0, 1, 2, 
 MODE_REF_DIRECT, MODE_NORMAL, MODE_POSITION, MODE_REF_LT2 = 5, 6, 7, 8
 INTEGRATOR_MEGAKERNEL, INTEGRATOR_WAVEFRONT, INTEGRATOR_PLAIN = 0, 1, 2
 RNG_MINSTD, RNG_PHILOX = 0, 1
-BVH_SAH, BVH_REFERENCE, BVH_WIDE = 0, 1, 2
+BVH_SAH, BVH_REFERENCE, BVH_WIDE, BVH_LINEAR = 0, 1, 2, 3
 BUILDER_HOST, BUILDER_DEVICE = 0, 1
 # compositing
 TONEMAP_CLAMP, TONEMAP_ACES = 0, 1

@@ -249,7 +249,8 @@ cudaError_t launch_adjoint(DevScene const &S, RenderArgs const &A, FirstHit cons
     size_t smem = static_cast<size_t>(S.nmat) * 4 * sizeof(float);
     if (smem + kStackWords * kBlock * sizeof(uint32_t) > 200 * 1024)
         return cudaErrorInvalidValue;
-    auto kern = S.layout == 1 ? k_adjoint<1> : (S.layout == 2 ? k_adjoint<2> : k_adjoint<0>);
+    auto kern = S.layout == 1 ? k_adjoint<1>
+                              : (S.layout == 2 ? k_adjoint<2> : (S.layout == 3 ? k_adjoint<3> : k_adjoint<0>));
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess)
         return e;

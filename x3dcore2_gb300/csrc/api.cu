@@ -294,7 +294,8 @@ e8g_status build_tree(e8g_ctx *c) {
     cudaSetDevice(c->device);
     packed_scene &p = c->pack;
     bool on_device = false;
-    if (c->bvh_opts.builder == E8G_BUILDER_DEVICE && c->bvh_opts.layout != E8G_BVH_REFERENCE && p.nt > 0) {
+    if (c->bvh_opts.builder == E8G_BUILDER_DEVICE && c->bvh_opts.layout != E8G_BVH_REFERENCE &&
+        c->bvh_opts.layout != E8G_BVH_LINEAR && p.nt > 0) {
         e8g_status st = build_on_device(c, &on_device);
         if (st != E8G_OK)
             return st;
@@ -534,7 +535,7 @@ e8g_status e8g_scene_build_bvh(e8g_ctx *c, e8g_bvh_opts const *o) {
         bo.tri_cost = o->tri_cost;
         bo.node_cost = o->node_cost;
         bo.num_threads = o->num_threads;
-        if (o->layout > E8G_BVH_WIDE)
+        if (o->layout > E8G_BVH_LINEAR)
             return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH layout");
         if (o->builder > E8G_BUILDER_DEVICE)
             return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH builder");

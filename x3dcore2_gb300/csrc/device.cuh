@@ -51,7 +51,7 @@ struct DevScene {
     const float *light_pnorm;  // |power| per light
     uint32_t nmat, nl, nm, nnodes, ntris;
     uint32_t layout; // 0: SAH child pairs (ordered traversal), 1: the reference's tree and order,
-                     // 2: eight-wide quantized nodes
+                     // 2: eight-wide quantized nodes, 3: no tree (every triangle, in order)
     float total_power;
     float bmin[3], bmax[3]; // if_path_space::aabb() for the position tracer
     DevCamera cam;
@@ -409,6 +409,35 @@ __device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d,
     return false;
 }
 
+// linear_path_space_layout::intersect / has_intersect (pathspace.cpp:36-114): every triangle in
+// mesh order (the records of the linear layout are in global triangle order), the first of equal
+// distances kept (strict <), an any-hit query returning at the first triangle it hits.
+template <bool COUNT>
+__device__ __forceinline__ Hit trace_linear(const DevScene &S, float3 o, float3 d, float tmin, float tmax, bool any,
+                                            TraceCounters *cnt) {
+    Hit h;
+    h.t = INFINITY;
+    h.tri = 0xFFFFFFFFu;
+    h.b1 = h.b2 = 0.0f;
+    for (uint32_t k = 0; k < S.ntris; k++) {
+        float4 a = __ldg(&S.tri[3 * static_cast<size_t>(k)]);
+        float4 b = __ldg(&S.tri[3 * static_cast<size_t>(k) + 1]);
+        float4 c = __ldg(&S.tri[3 * static_cast<size_t>(k) + 2]);
+        if (COUNT)
+            cnt->tris++;
+        float t0, b1, b2;
+        if (tri_test(o, d, a, b, c, tmin, tmax, t0, b1, b2) && t0 < h.t) {
+            h.t = t0;
+            h.tri = __float_as_uint(a.w);
+            h.b1 = b1;
+            h.b2 = b2;
+            if (any)
+                return h;
+        }
+    }
+    return h;
+}
+
 // One query in a given layout: closest hit (any = false) or any hit (any = true) on [tmin, tmax].
 // Kernels on the hot path call this from a single site, so each holds one inlined traversal.
 template <int LAYOUT, bool COUNT>
@@ -427,6 +456,8 @@ __device__ __forceinline__ Hit trace_l(const DevScene &S, float3 o, float3 d, fl
         return wide_trace(W, o, d, tmin, tmax, any, stk, kBlock, COUNT ? &cnt->nodes : nullptr,
                           COUNT ? &cnt->tris : nullptr);
     }
+    if (LAYOUT == 3)
+        return trace_linear<COUNT>(S, o, d, tmin, tmax, any, cnt);
     return trace_sah<COUNT>(S, o, d, tmin, tmax, any, stk, cnt);
 }
 
@@ -439,6 +470,8 @@ __device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3
     if (S.layout == 2)
         return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes}, o, d, 1e-4f, 1000.0f, false, stk, kBlock,
                                COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr);
+    if (S.layout == 3)
+        return trace_linear<COUNT>(S, o, d, 1e-4f, 1000.0f, false, cnt);
     return trace_l<0, COUNT>(S, o, d, 1e-4f, 1000.0f, false, stk, cnt);
 }
 
@@ -452,6 +485,8 @@ __device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d,
         return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes}, o, d, tmin, tmax, true, stk, kBlock,
                                COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr)
                    .tri != 0xFFFFFFFFu;
+    if (S.layout == 3)
+        return trace_linear<COUNT>(S, o, d, tmin, tmax, true, cnt).tri != 0xFFFFFFFFu;
     return trace_l<0, COUNT>(S, o, d, tmin, tmax, true, stk, cnt).tri != 0xFFFFFFFFu;
 }
 

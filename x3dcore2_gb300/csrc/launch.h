@@ -29,12 +29,15 @@ void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *f
                        unsigned long long *work, unsigned long long *counters, int grid, cudaStream_t st,
                        bool plain = false);
 int megakernel_blocks_per_sm();
-// The same for one tree layout (mega_l0.cu: SAH pairs, mega_l1.cu: reference, mega_l2.cu: wide).
+// The same for one tree layout (mega_l0.cu: SAH pairs, mega_l1.cu: reference, mega_l2.cu: wide,
+// mega_l3.cu: linear).
 void launch_mega_l0(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                     unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
 void launch_mega_l1(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                     unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
 void launch_mega_l2(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                    unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
+void launch_mega_l3(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
                     unsigned long long *work, unsigned long long *counters, int grid, bool plain, cudaStream_t st);
 
 // Many scenes, one persistent launch (SAH-pair or eight-wide trees, any stream kind).

@@ -34,6 +34,8 @@ void launch_megakernel(DevScene const &S, RenderArgs const &A, FirstHit const *f
         launch_mega_l1(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
     else if (S.layout == 2)
         launch_mega_l2(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
+    else if (S.layout == 3)
+        launch_mega_l3(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
     else
         launch_mega_l0(S, A, fh, accum, path_rgb, work, counters, grid, plain, st);
 }

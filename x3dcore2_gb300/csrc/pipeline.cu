@@ -94,7 +94,7 @@ e8g_status e8g_pipeline_config_set(e8g_pipeline_config *c, char const *key, char
         else if (v == "wide_bvh")
             c->layout = E8G_BVH_WIDE;
         else if (v == "linear")
-            return E8G_ERR_UNSUPPORTED;
+            c->layout = E8G_BVH_LINEAR;
         else
             return E8G_ERR_INVALID_ARG;
         return E8G_OK;
@@ -156,7 +156,7 @@ e8g_status e8g_pipeline_frame(e8g_ctx *c, e8g_pipeline_config const *cfg, uint32
         return fail(c, E8G_ERR_INVALID_ARG, "bad pipeline arguments");
     if (!c->uploaded)
         return fail(c, E8G_ERR_NO_SCENE, "no scene uploaded");
-    if (cfg->layout > E8G_BVH_WIDE)
+    if (cfg->layout > E8G_BVH_LINEAR)
         return fail(c, E8G_ERR_INVALID_ARG, "unknown BVH layout");
     if (cfg->progressive && cfg->firefly_filter)
         return fail(c, E8G_ERR_UNSUPPORTED, "progressive frames do not run the firefly clamp");

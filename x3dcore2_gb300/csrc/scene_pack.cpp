@@ -225,6 +225,13 @@ void build_scene_bvh(packed_scene &s, bvh_build_opts const &o) {
         s.wide.clear();
         s.bvh = build_bvh_reference(p3.data(), t3.data(), s.nt);
         s.layout = 1;
+    } else if (o.layout == 3) { // no tree: the records in global triangle order
+        s.wide.clear();
+        s.bvh = flat_bvh{};
+        s.bvh.tri_order.resize(s.nt);
+        for (uint32_t t = 0; t < s.nt; t++)
+            s.bvh.tri_order[t] = t;
+        s.layout = 3;
     } else {
         bvh_build_opts ob = o;
         ob.tri_cost = effective_tri_cost(o);

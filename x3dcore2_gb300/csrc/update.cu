@@ -188,7 +188,8 @@ e8g_status e8g_scene_commit(e8g_ctx *c, uint32_t mode, e8g_bvh_stats *stats) {
         return fail(c, E8G_ERR_INVALID_ARG, "unknown commit mode");
     cudaSetDevice(c->device);
     packed_scene &p = c->pack;
-    bool refit = mode == E8G_COMMIT_REFIT && c->built && p.layout != E8G_BVH_REFERENCE && p.nt > 0;
+    bool refit = mode == E8G_COMMIT_REFIT && c->built && p.layout != E8G_BVH_REFERENCE &&
+                 p.layout != E8G_BVH_LINEAR && p.nt > 0;
     if (!refit) {
         auto t0 = std::chrono::steady_clock::now();
         e8g_status st = build_tree(c);
