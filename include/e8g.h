@@ -349,6 +349,13 @@ e8g_status e8g_render_dev_noalloc(e8g_ctx *ctx, const e8g_render_params *params,
  * rays traced, BVH nodes whose box was fetched and triangles tested. */
 e8g_status e8g_count_traversal(e8g_ctx *ctx, const e8g_render_params *params, e8g_render_stats *stats);
 
+/* Per-path radiance for explicit primary rays (if_path_tracer::sample, pathtracer.h:59-63): path i
+ * starts at ray i, whose first hit is traced as compute_first_hit traces it (back-facing hits are
+ * misses, pathtracer.cpp:456-472), and draws from the stream of (params->seed, i,
+ * params->sample_offset). params->width and height are ignored. rgb_out is 3*n floats. */
+e8g_status e8g_render_rays(e8g_ctx *ctx, const e8g_render_params *params, const e8g_ray *rays, uint32_t n,
+                           float *rgb_out);
+
 /* Per-path radiance for an explicit list of (pixel, sample) pairs: rgb_out is 3*n floats. */
 e8g_status e8g_render_paths(e8g_ctx *ctx, const e8g_render_params *params, const uint32_t *pixel,
                             const uint32_t *sample, uint32_t n, float *rgb_out);

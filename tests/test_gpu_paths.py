@@ -8,6 +8,7 @@ import pytest
 import golden_util as G
 import oracle_bind as ob
 from x3dcore2_gb300 import abi
+from x3dcore2_gb300 import scene as S
 from x3dcore2_gb300.core import default_params
 
 pytestmark = pytest.mark.gpu
@@ -151,3 +152,17 @@ def test_bdpt_power_paths_match_oracle(ctx, rng, max_len):
     else:
         ref = osc.render_paths(abi.MODE_BDPT_POWER, w, h, px, samples, policy=pol, rng=abi.RNG_PHILOX, seed=17)
     assert match_fraction(got, ref) >= 0.99
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_MIS, abi.MODE_REF_BDPT, abi.MODE_REF_LT2])
+def test_render_rays_equals_render_paths_for_camera_rays(ctx, mode):
+    """e8g_render_rays (if_path_tracer::sample's surface): the camera rays of the pixels, given as
+    explicit rays, give every path's radiance bit for bit as e8g_render_paths does."""
+    sc = S.cornell(24, 20)
+    ctx.upload(sc, layout=abi.BVH_REFERENCE)
+    p = default_params(mode, 24, 20, 1, seed=5)
+    rays = ctx.camera_rays(24, 20)
+    a = ctx.render_rays(p, rays)
+    px = np.arange(24 * 20, dtype=np.uint32)
+    b = ctx.render_paths(p, px, np.zeros_like(px))
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))

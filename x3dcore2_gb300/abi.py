@@ -164,6 +164,7 @@ SIGNATURES = {
     "e8g_wavefront_tune": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(TuneResult)]),
     "e8g_wavefront_set": (_ST, [_P, _U32, _U32, _U32]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
+    "e8g_render_rays": (_ST, [_P, C.POINTER(RenderParams), _P, _U32, _P]),
     "e8g_forward": (_ST, [_P, C.POINTER(RenderParams), _P]),
     "e8g_backward": (_ST, [_P, _P, _P, _P]),
     "e8g_set_materials": (_ST, [_P, C.POINTER(Material), _U32]),

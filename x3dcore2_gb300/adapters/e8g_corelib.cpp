@@ -232,6 +232,50 @@ void gpu_image_renderer::commit_scene(scene_storage &next) {
     m_have_scene = true;
 }
 
+uint32_t mode_of(e8::pathtracer_factory::pt_type type) {
+    switch (type) {
+    case e8::pathtracer_factory::unidirect:
+        return E8G_MODE_REF_UNI;
+    case e8::pathtracer_factory::bidirect_mis:
+        return E8G_MODE_REF_BDPT;
+    case e8::pathtracer_factory::bidirect_lt2:
+        return E8G_MODE_REF_LT2;
+    case e8::pathtracer_factory::direct:
+        return E8G_MODE_REF_DIRECT;
+    case e8::pathtracer_factory::normal:
+        return E8G_MODE_NORMAL;
+    case e8::pathtracer_factory::position:
+        return E8G_MODE_POSITION;
+    default:
+        return E8G_MODE_REF_LT1;
+    }
+}
+
+gpu_path_tracer::gpu_path_tracer(e8g_ctx *ctx, e8::pathtracer_factory::pt_type type)
+    : m_ctx(ctx), m_mode(mode_of(type)) {}
+
+std::vector<e8util::vec3> gpu_path_tracer::sample(e8util::rng &rng, std::vector<e8util::ray> const &rays,
+                                                  first_hits const &, e8::if_path_space const &,
+                                                  e8::if_material_container const &,
+                                                  e8::if_light_sources const &) const {
+    std::vector<e8g_ray> in(rays.size());
+    for (size_t i = 0; i < rays.size(); i++)
+        for (int k = 0; k < 3; k++) {
+            in[i].o[k] = rays[i].o()(k);
+            in[i].d[k] = rays[i].v()(k);
+        }
+    e8g_render_params p;
+    e8g_default_params(&p, m_mode, 1, 1, 1);
+    p.seed = static_cast<uint64_t>(rng.draw() * 4294967296.0);
+    std::vector<float> rgb(3 * rays.size());
+    if (e8g_render_rays(m_ctx, &p, in.data(), static_cast<uint32_t>(rays.size()), rgb.data()) != E8G_OK)
+        throw std::runtime_error(std::string("e8g: ") + e8g_last_error(m_ctx));
+    std::vector<e8util::vec3> out(rays.size());
+    for (size_t i = 0; i < rays.size(); i++)
+        out[i] = e8util::vec3{rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]};
+    return out;
+}
+
 e8::pt_image_renderer::numerical_stats
 gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space const &path_space,
                            e8::if_material_container const &mats, e8::if_light_sources const &light_sources,
@@ -243,29 +287,7 @@ gpu_image_renderer::render(e8::if_compositor *compositor, e8::if_path_space cons
     scene_storage next;
     pack_scene(ps, mc, ls, pc, next);
     commit_scene(next);
-    uint32_t mode = E8G_MODE_REF_LT1;
-    switch (m_type) {
-    case e8::pathtracer_factory::unidirect:
-        mode = E8G_MODE_REF_UNI;
-        break;
-    case e8::pathtracer_factory::bidirect_mis:
-        mode = E8G_MODE_REF_BDPT;
-        break;
-    case e8::pathtracer_factory::bidirect_lt2:
-        mode = E8G_MODE_REF_LT2;
-        break;
-    case e8::pathtracer_factory::direct:
-        mode = E8G_MODE_REF_DIRECT;
-        break;
-    case e8::pathtracer_factory::normal:
-        mode = E8G_MODE_NORMAL;
-        break;
-    case e8::pathtracer_factory::position:
-        mode = E8G_MODE_POSITION;
-        break;
-    default:
-        break;
-    }
+    uint32_t mode = mode_of(m_type);
     unsigned w = compositor->width(), h = compositor->height();
     e8g_render_params p;
     e8g_default_params(&p, mode, w, h, num_samps);

@@ -112,6 +112,29 @@ struct scene_storage {
 void pack_scene(gpu_path_space_layout const &ps, gpu_material_container const &mats,
                 gpu_light_sources const &lights, gpu_pinhole_camera const &cam, scene_storage &out);
 
+// The e8g mode of a tracer type (pathtracerfact.h:12): unidirect -> E8G_MODE_REF_UNI,
+// unidirect_lt1 -> E8G_MODE_REF_LT1, bidirect_mis -> E8G_MODE_REF_BDPT, bidirect_lt2 ->
+// E8G_MODE_REF_LT2, direct, normal, position.
+uint32_t mode_of(e8::pathtracer_factory::pt_type type);
+
+// if_path_tracer on the GPU (pathtracer.h:59-63), for code that drives tracers one batch of rays
+// at a time (the reference's own tests do): sample() traces every ray's path on the context,
+// whose scene the caller uploaded from the same containers (pack_scene + e8g_scene_upload +
+// e8g_scene_build_bvh). Path i's first hit is computed on the device from ray i, as
+// compute_first_hit computes the cached ones; its stream is keyed by one draw of `rng` and i.
+class gpu_path_tracer : public e8::if_path_tracer {
+  public:
+    gpu_path_tracer(e8g_ctx *ctx, e8::pathtracer_factory::pt_type type);
+    std::vector<e8util::vec3> sample(e8util::rng &rng, std::vector<e8util::ray> const &rays,
+                                     first_hits const &first_hits, e8::if_path_space const &path_space,
+                                     e8::if_material_container const &mats,
+                                     e8::if_light_sources const &light_sources) const override;
+
+  private:
+    e8g_ctx *m_ctx;
+    uint32_t m_mode;
+};
+
 // pt_image_renderer on the GPU: same render() signature and meaning; the tracer type selects
 // the integrator (unidirect -> E8G_MODE_REF_UNI, unidirect_lt1 -> E8G_MODE_REF_LT1,
 // bidirect_mis -> E8G_MODE_REF_BDPT, direct, normal, position).

@@ -191,6 +191,14 @@ class Context:
                                               len(pixels), _ptr(out)), "e8g_render_paths")
         return out
 
+    def render_rays(self, params, rays):
+        """Per-path radiance for explicit primary rays ((n, 6): origin, direction)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        out = np.zeros((len(rays), 3), np.float32)
+        self._check(self.lib.e8g_render_rays(self.h, C.byref(params), _ptr(rays), len(rays), _ptr(out)),
+                    "e8g_render_rays")
+        return out
+
     def composite(self, rgba, tonemap=abi.TONEMAP_ACES, auto_exposure=True, exposure=1.0):
         """e8g_composite: the reference's compositors on a float (h, w, 4) image -> uint8 RGBA."""
         rgba = np.ascontiguousarray(rgba, np.float32)

@@ -812,4 +812,50 @@ e8g_status e8g_render_paths(e8g_ctx *c, e8g_render_params const *p, uint32_t con
     return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "render_paths");
 }
 
+e8g_status e8g_render_rays(e8g_ctx *c, e8g_render_params const *params, e8g_ray const *rays, uint32_t n,
+                           float *rgb_out) {
+    e8g_status s = check_ready(c);
+    if (s != E8G_OK)
+        return s;
+    if (!params)
+        return fail(c, E8G_ERR_INVALID_ARG, "NULL params");
+    if (n == 0)
+        return E8G_OK;
+    if (!rays || !rgb_out)
+        return fail(c, E8G_ERR_INVALID_ARG, "NULL buffers");
+    e8g_render_params p = *params; // one path per ray: the "image" is the ray list
+    p.width = n;
+    p.height = 1;
+    p.spp = 1;
+    p.firefly = 0;
+    s = validate_params(c, &p);
+    if (s != E8G_OK)
+        return s;
+    cudaSetDevice(c->device);
+    size_t rb = static_cast<size_t>(n) * sizeof(e8g_ray), lb = static_cast<size_t>(n) * sizeof(uint32_t),
+           ob = static_cast<size_t>(n) * 3 * sizeof(float);
+    cudaError_t e = c->b_io0.reserve(rb + 2 * lb);
+    if (e == cudaSuccess)
+        e = c->b_io1.reserve(ob);
+    if (e == cudaSuccess)
+        e = c->b_fh.reserve(static_cast<size_t>(n) * sizeof(FirstHit));
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "ray buffers");
+    char *base = static_cast<char *>(c->b_io0.ptr);
+    float *drays = reinterpret_cast<float *>(base);
+    uint32_t *dpx = reinterpret_cast<uint32_t *>(base + rb), *dsm = dpx + n;
+    e = cudaMemcpyAsync(drays, rays, rb, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "ray upload");
+    launch_first_hits_rays(c->dev, drays, n, static_cast<FirstHit *>(c->b_fh.ptr), p.sample_offset, dpx, dsm,
+                           c->stream);
+    s = render_list(c, &p, dpx, dsm, n, static_cast<float *>(c->b_io1.ptr), true);
+    if (s != E8G_OK)
+        return s;
+    e = cudaMemcpyAsync(rgb_out, c->b_io1.ptr, ob, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "render_rays");
+}
+
 } // extern "C"

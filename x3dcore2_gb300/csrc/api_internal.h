@@ -95,8 +95,9 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
                          FirstHit const *fh_all = nullptr);
 
 // Per-path radiance for device lists of pixels and samples into d_rgb (3 floats per path).
+// first_hits_ready: the first-hit cache already holds path i's first hit at index list_pixel[i].
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,
-                       uint32_t n, float *d_rgb);
+                       uint32_t n, float *d_rgb, bool first_hits_ready = false);
 
 } // namespace e8g
 

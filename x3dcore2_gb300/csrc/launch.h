@@ -13,6 +13,10 @@ struct LaunchCfg {
 
 void launch_first_hits(DevScene const &S, uint32_t w, uint32_t h, FirstHit *out, cudaStream_t st);
 void launch_camera_rays(DevScene const &S, uint32_t w, uint32_t h, float *rays6, cudaStream_t st);
+// First hits of explicit rays (ray i into out[i]) and the lists that make path i start there:
+// pixel[i] = i, samples[i] = sample.
+void launch_first_hits_rays(DevScene const &S, float const *rays6, uint32_t n, FirstHit *out, uint32_t sample,
+                            uint32_t *pixel, uint32_t *samples, cudaStream_t st);
 void launch_trace_closest(DevScene const &S, float const *rays6, uint32_t n, float *hits5, cudaStream_t st);
 void launch_trace_any(DevScene const &S, float const *rays6, float const *tmin, float const *tmax, uint32_t n,
                       uint8_t *occ, cudaStream_t st);

@@ -191,9 +191,9 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
 }
 
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,
-                       uint32_t n, float *d_rgb) {
+                       uint32_t n, float *d_rgb, bool first_hits_ready) {
     c->launches = 0;
-    e8g_status s = first_hits(c, p->width, p->height);
+    e8g_status s = first_hits_ready ? E8G_OK : first_hits(c, p->width, p->height);
     if (s != E8G_OK)
         return s;
     RenderArgs A = make_args(p);

@@ -31,6 +31,43 @@ __global__ void __launch_bounds__(kBlock) k_first_hits(DevScene S, uint32_t w, u
     out[i] = f;
 }
 
+// compute_first_hit for explicit rays: ray i's first hit into out[i].
+__global__ void __launch_bounds__(kBlock) k_first_hits_rays(DevScene S, float const *rays6, uint32_t n,
+                                                             FirstHit *out) {
+    __shared__ uint32_t stk[kStackWords * kBlock];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float3 o = f3(rays6[6 * i], rays6[6 * i + 1], rays6[6 * i + 2]);
+    float3 d = f3(rays6[6 * i + 3], rays6[6 * i + 4], rays6[6 * i + 5]);
+    Hit hit = trace_closest<false>(S, o, d, stk + threadIdx.x, nullptr);
+    FirstHit f;
+    f.d = make_float4(d.x, d.y, d.z, 0.0f);
+    int32_t mesh = -1, light = -1;
+    float3 p = f3(0, 0, 0), nn = f3(0, 0, 0);
+    if (hit.tri != 0xFFFFFFFFu) {
+        Vert v = make_vert(S, hit);
+        if (dot(v.n, neg(d)) > 0) {
+            mesh = v.mesh;
+            p = v.p;
+            nn = v.n;
+            light = __ldg(&S.mesh_light[mesh]);
+        }
+    }
+    f.p = make_float4(p.x, p.y, p.z, __int_as_float(mesh));
+    f.n = make_float4(nn.x, nn.y, nn.z, __int_as_float(light));
+    out[i] = f;
+}
+
+// Identity pixel list and a constant sample list for explicit rays.
+__global__ void k_ray_lists(uint32_t n, uint32_t sample, uint32_t *pixel, uint32_t *samples) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        pixel[i] = i;
+        samples[i] = sample;
+    }
+}
+
 __global__ void k_camera_rays(DevScene S, uint32_t w, uint32_t h, float *rays6) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w * h)
@@ -153,6 +190,13 @@ static inline int blocks(uint32_t n, int b) { return static_cast<int>((n + b - 1
 
 void launch_first_hits(DevScene const &S, uint32_t w, uint32_t h, FirstHit *out, cudaStream_t st) {
     k_first_hits<<<blocks(w * h, kBlock), kBlock, 0, st>>>(S, w, h, out);
+}
+void launch_first_hits_rays(DevScene const &S, float const *rays6, uint32_t n, FirstHit *out, uint32_t sample,
+                            uint32_t *pixel, uint32_t *samples, cudaStream_t st) {
+    if (!n)
+        return;
+    k_first_hits_rays<<<blocks(n, kBlock), kBlock, 0, st>>>(S, rays6, n, out);
+    k_ray_lists<<<blocks(n, 256), 256, 0, st>>>(n, sample, pixel, samples);
 }
 void launch_camera_rays(DevScene const &S, uint32_t w, uint32_t h, float *rays6, cudaStream_t st) {
     k_camera_rays<<<blocks(w * h, 256), 256, 0, st>>>(S, w, h, rays6);
