@@ -823,9 +823,9 @@ e8g_status e8g_render_rays(e8g_ctx *c, e8g_render_params const *params, e8g_ray 
         return E8G_OK;
     if (!rays || !rgb_out)
         return fail(c, E8G_ERR_INVALID_ARG, "NULL buffers");
-    e8g_render_params p = *params; // one path per ray: the "image" is the ray list
-    p.width = n;
-    p.height = 1;
+    e8g_render_params p = *params; // one path per ray (list mode: the image size only has to be valid)
+    p.width = n < 2 ? 2 : n;
+    p.height = 2;
     p.spp = 1;
     p.firefly = 0;
     s = validate_params(c, &p);
