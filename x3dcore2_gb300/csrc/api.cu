@@ -267,6 +267,7 @@ e8g_status build_on_device(e8g_ctx *c, bool *built) {
         p.wide.clear();
         p.tri.clear();
         if (wo.ok) {
+            p.wide_levels.assign(wo.level_start, wo.level_start + wo.max_depth + 1);
             p.bvh = flat_bvh{};
             p.bvh.num_nodes = wo.num_nodes;
             p.bvh.num_leaves = bin.num_leaves;

@@ -128,6 +128,8 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
     while (!q.empty()) {
         job jb = q.front();
         q.pop_front();
+        if (jb.depth > w.level_start.size()) // the queue is breadth first: a level's nodes are contiguous
+            w.level_start.push_back(jb.node);
         w.max_depth = std::max(w.max_depth, jb.depth);
         // collect up to eight children
         item ch[8];
@@ -239,6 +241,7 @@ wide_bvh collapse_wide(flat_bvh const &b, float const *pos, uint32_t const *tris
         words[21] = leaves;
         std::memcpy(&w.nodes[static_cast<size_t>(jb.node) * kWideWords], words, sizeof(words));
     }
+    w.level_start.push_back(w.num_nodes);
     w.ok = w.max_depth <= kWideMaxDepth;
     return w;
 }

@@ -36,6 +36,7 @@ struct wide_bvh {
     uint32_t num_nodes = 0;
     uint32_t num_leaves = 0;         // leaf slots
     uint32_t max_depth = 0;          // levels of wide nodes
+    std::vector<uint32_t> level_start; // first node of every level (breadth-first), then num_nodes
     bool ok = false;                 // false: deeper than kWideMaxDepth (use the binary tree)
 };
 

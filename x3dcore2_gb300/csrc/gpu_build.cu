@@ -1019,13 +1019,15 @@ cudaError_t gpu_collapse_wide(GpuWideIn const &in, GpuWideOut &out, cudaStream_t
     cudaError_t e = cudaMemcpyAsync(s.wa, &root, sizeof(root), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess)
         return e;
-    uint32_t f = 1, next_base = 1, tri_running = 0, depth = 0;
+    uint32_t f = 1, next_base = 1, tri_running = 0, depth = 0, level_first = 0;
     WideItem *wa = s.wa, *wb = s.wb;
     while (f > 0) {
-        if (++depth > in.max_depth || f > n || next_base > n + 1) {
+        if (++depth > in.max_depth || depth >= 32 || f > n || next_base > n + 1) {
             out.ok = false; // too deep for the eight-wide stack: keep the binary tree
             return cudaSuccess;
         }
+        out.level_start[depth - 1] = level_first; // this level's nodes are [level_first, next_base)
+        level_first = next_base;
         uint32_t g = blocks(f, kGB);
         k_wide_plan<<<g, kGB, 0, st>>>(wa, f, in.nlo, in.nhi, s.wslots, s.mscan, s.kscan);
         scan(s.mscan, f, s.sums, s.total, st);
@@ -1050,6 +1052,7 @@ cudaError_t gpu_collapse_wide(GpuWideIn const &in, GpuWideOut &out, cudaStream_t
         return e;
     out.num_nodes = next_base;
     out.max_depth = depth;
+    out.level_start[depth] = next_base;
     out.ok = true;
     return cudaGetLastError();
 }

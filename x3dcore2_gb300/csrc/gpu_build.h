@@ -47,6 +47,7 @@ struct GpuWideIn {
 };
 struct GpuWideOut {
     uint32_t num_nodes = 0, max_depth = 0;
+    uint32_t level_start[32] = {0}; // first node of every level (breadth first), then num_nodes
     bool ok = false; // false: deeper than max_depth (the binary tree stays)
 };
 cudaError_t gpu_collapse_wide(GpuWideIn const &in, GpuWideOut &out, cudaStream_t st);

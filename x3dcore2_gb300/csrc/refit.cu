@@ -7,7 +7,8 @@
 // vertices pushed out by |v| * 1e-6 + eps, eps from the scene's exact box, and eight-wide nodes
 // re-quantize their children on a fresh grid. One pass goes bottom-up: a thread starts at every
 // leaf-holding node, and at each parent the last child to arrive (an atomic counter per node)
-// carries on upwards with the union of the children's exact boxes. No thread ever waits.
+// carries on upwards with the union of the children's exact boxes; no thread ever waits. The
+// eight-wide tree, breadth first and at most 16 levels deep, is refitted one level per launch.
 #include "bvh_boxes.h"
 #include "bvh_wide.h"
 #include "launch.h"
@@ -196,17 +197,6 @@ __global__ void __launch_bounds__(kRefitBlock)
 
 // ------------------------------------------------------------------- eight-wide ----
 
-__global__ void k_parents_wide(uint4 const *wn, uint32_t nn, uint32_t *parent) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nn)
-        return;
-    uint32_t imask = wn[6 * static_cast<size_t>(i)].w >> 24;
-    uint32_t base = wn[6 * static_cast<size_t>(i) + 1].x;
-    int n = __popc(imask);
-    for (int r = 0; r < n; r++)
-        parent[base + r] = i;
-}
-
 __device__ void refit_wide_node(uint4 *wn, uint32_t i, float4 const *tlo, float4 const *thi, float4 *ex_lo,
                                 float4 *ex_hi, float eps, double step_min) {
     uint32_t w[kWideWords];
@@ -249,23 +239,17 @@ __device__ void refit_wide_node(uint4 *wn, uint32_t i, float4 const *tlo, float4
     ex_hi[i] = make_float4(nhi[0], nhi[1], nhi[2], 0.0f);
 }
 
+// One level of the eight-wide tree (its nodes are contiguous: the layout is breadth first),
+// after every deeper level: the children's exact boxes are final, so nothing waits or counts.
 __global__ void __launch_bounds__(kRefitBlock)
-    k_refit_wide(uint4 *wn, uint32_t nn, float4 const *tlo, float4 const *thi, uint32_t const *parent,
-                 uint32_t *counter, float4 *ex_lo, float4 *ex_hi, uint32_t const *red, float cam_abs) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nn || (wn[6 * static_cast<size_t>(i)].w >> 24) != 0)
+    k_refit_wide_level(uint4 *wn, uint32_t first, uint32_t count, float4 const *tlo, float4 const *thi,
+                       float4 *ex_lo, float4 *ex_hi, uint32_t const *red, float cam_abs) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count)
         return;
     float eps = scene_eps_of(red);
     double step_min = wide_step_min(fmaxf(__uint_as_float(red[12]), cam_abs));
-    refit_wide_node(wn, i, tlo, thi, ex_lo, ex_hi, eps, step_min);
-    uint32_t n = parent[i];
-    while (n != 0xFFFFFFFFu) {
-        uint32_t need = __popc(__ldcg(&wn[6 * static_cast<size_t>(n)].w) >> 24);
-        if (arrive(&counter[n]) + 1 < need)
-            return; // a later child's thread finishes this node
-        refit_wide_node(wn, n, tlo, thi, ex_lo, ex_hi, eps, step_min);
-        n = parent[n];
-    }
+    refit_wide_node(wn, first + k, tlo, thi, ex_lo, ex_hi, eps, step_min);
 }
 
 // ------------------------------------------------------------------ transform ----
@@ -336,25 +320,30 @@ RefitScratch refit_carve(void *base, uint32_t nn, uint32_t nt) {
 
 void launch_refit_parents(DevScene const &S, RefitScratch const &R, cudaStream_t st) {
     uint32_t nn = S.nnodes;
+    if (S.layout == 2) // the eight-wide refit goes level by level instead
+        return;
     cudaMemsetAsync(R.parent, 0xFF, 4 * static_cast<size_t>(nn), st);
-    if (S.layout == 2)
-        k_parents_wide<<<blocks_for(nn), kRefitBlock, 0, st>>>(S.wnodes, nn, R.parent);
-    else
-        k_parents_pairs<<<blocks_for(nn), kRefitBlock, 0, st>>>(S.nlo, S.nhi, nn, R.parent);
+    k_parents_pairs<<<blocks_for(nn), kRefitBlock, 0, st>>>(S.nlo, S.nhi, nn, R.parent);
 }
 
 void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float cam_abs, int grid_cap,
-                  cudaStream_t st) {
+                  uint32_t const *wide_levels, uint32_t num_levels, cudaStream_t st) {
     uint32_t nn = S.nnodes, nt = S.ntris;
     float4 *tri = const_cast<float4 *>(S.tri);
-    cudaMemsetAsync(R.counter, 0, 4 * static_cast<size_t>(nn), st);
+    if (S.layout != 2)
+        cudaMemsetAsync(R.counter, 0, 4 * static_cast<size_t>(nn), st);
     k_refit_init<<<1, 32, 0, st>>>(R.red);
     k_refit_verts<<<min(blocks_for(nv), grid_cap), kRefitBlock, 0, st>>>(S.vpos, nv, R.red);
     k_refit_tris<<<min(blocks_for(nt), grid_cap), kRefitBlock, 0, st>>>(tri, S.tidx, S.vpos, nt, R.red, R.tlo, R.thi);
-    if (S.layout == 2)
-        k_refit_wide<<<blocks_for(nn), kRefitBlock, 0, st>>>(const_cast<uint4 *>(S.wnodes), nn, R.tlo, R.thi, R.parent,
-                                                               R.counter, R.ex_lo, R.ex_hi, R.red, cam_abs);
-    else
+    if (S.layout == 2) {
+        for (uint32_t l = num_levels; l-- > 0;) { // deepest level first
+            uint32_t first = wide_levels[l], count = wide_levels[l + 1] - wide_levels[l];
+            if (count)
+                k_refit_wide_level<<<blocks_for(count), kRefitBlock, 0, st>>>(const_cast<uint4 *>(S.wnodes), first,
+                                                                              count, R.tlo, R.thi, R.ex_lo, R.ex_hi,
+                                                                              R.red, cam_abs);
+        }
+    } else
         k_refit_pairs<<<blocks_for(nn), kRefitBlock, 0, st>>>(const_cast<float4 *>(S.nlo), const_cast<float4 *>(S.nhi),
                                                                 nn, R.tlo, R.thi, R.parent, R.counter, R.ex_lo,
                                                                 R.ex_hi, R.red);

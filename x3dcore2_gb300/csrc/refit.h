@@ -30,8 +30,9 @@ RefitScratch refit_carve(void *base, uint32_t num_nodes, uint32_t num_tris);
 void launch_refit_parents(DevScene const &S, RefitScratch const &R, cudaStream_t st);
 // Triangle records, scene and vertex boxes, then every node bottom-up. cam_abs: the camera
 // origin's largest |coordinate| (the eight-wide grid's smallest step covers it).
+// wide_levels: the eight-wide layout's level boundaries (num_levels + 1 entries, host memory).
 void launch_refit(DevScene const &S, RefitScratch const &R, uint32_t nv, float cam_abs, int grid_cap,
-                  cudaStream_t st);
+                  uint32_t const *wide_levels, uint32_t num_levels, cudaStream_t st);
 void launch_transform(float4 const *vpos0, float4 const *vnrm0, float4 *vpos, float4 *vnrm, XformArgs const &X,
                       cudaStream_t st);
 // The interleaved shading copy of the vertices (DevScene::vtx, 2 float4 per vertex).

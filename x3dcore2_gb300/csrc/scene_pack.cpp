@@ -188,6 +188,7 @@ void finish_tree(packed_scene &s, flat_bvh &&bin, uint32_t layout, std::vector<f
             s.bvh.eps = bin.eps;
             s.bvh.tri_order = std::move(w.tri_order);
             s.wide = std::move(w.nodes);
+            s.wide_levels = std::move(w.level_start);
             s.layout = 2;
         } else { // deeper than the traversal stack: keep the binary tree
             s.bvh = std::move(bin);

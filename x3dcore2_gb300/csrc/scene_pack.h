@@ -33,6 +33,7 @@ struct packed_scene {
     // order and counts in `bvh`.
     flat_bvh bvh;
     std::vector<uint32_t> wide;
+    std::vector<uint32_t> wide_levels; // first node of every level of `wide`, then its node count
     std::vector<float> tri;         // 12 floats per BVH position
     double build_ms = 0;
     uint32_t layout = 0;

@@ -206,7 +206,10 @@ e8g_status e8g_scene_commit(e8g_ctx *c, uint32_t mode, e8g_bvh_stats *stats) {
         if (!c->refit_ready)
             launch_refit_parents(c->dev, R, c->stream);
         float cam_abs = camera_abs(p);
-        launch_refit(c->dev, R, p.nv, cam_abs, 8 * c->num_sms, c->stream);
+        uint32_t nlev = p.wide_levels.empty() ? 0u : static_cast<uint32_t>(p.wide_levels.size() - 1);
+        if (p.layout == E8G_BVH_WIDE && (nlev == 0 || p.wide_levels.back() != p.bvh.num_nodes))
+            return fail(c, E8G_ERR_INTERNAL, "eight-wide tree without level boundaries");
+        launch_refit(c->dev, R, p.nv, cam_abs, 8 * c->num_sms, p.wide_levels.data(), nlev, c->stream);
         launch_interleave(c->dev.vpos, c->dev.vnrm, p.nv, static_cast<float4 *>(c->b_vtx.ptr), c->stream);
         cudaEventRecord(c->ev1, c->stream);
         uint32_t red[kRefitRedWords];
