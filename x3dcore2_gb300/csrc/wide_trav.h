@@ -206,17 +206,8 @@ E8G_HD void wide_begin(WideTrav &T, float3 o, float3 d, float tmin, float tmax, 
     T.h.b1 = T.h.b2 = 0.0f;
 }
 
-// Visits T.node: tests its eight child boxes, the triangles of every hit leaf slot, and moves
-// T.node to the next node (the first hit interior child in octant order; the rest go on the
-// stack as one entry). Returns true when the ray is finished (stack empty, or an any-hit found).
-E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride, uint32_t *cnt_nodes,
-                      uint32_t *cnt_tris) {
-    uint4 const *np = W.nodes + 6 * static_cast<size_t>(T.node);
-    uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
-          n5 = hd_ld(np + 5);
-    uint32_t counts = n5.x, leaves = n5.y;
-    if (cnt_nodes)
-        (*cnt_nodes)++;
+// The eight child boxes of a node against [T.tmin, T.cull]: bit s set when slot s is hit.
+E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3, uint4 n4, uint32_t leaves) {
     const uint32_t oct = T.oct;
     // plane of byte q on axis a: p + q * step = (p - 2^15 step) + (1 + q 2^-15) * 2^15 step, so
     // t = (1 + q 2^-15) * S + O with S = 2^15 step / d and O = (p - 2^15 step - o) / d
@@ -253,25 +244,29 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
             hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
         }
     }
-    uint32_t hit_leaf = hits & leaves;
+    return hits;
+}
+
+// Moves T.node to the next node: the first hit interior child in octant order (the other hit
+// interior children go on the stack as one entry), else the stack's top. Returns false when
+// there is none.
+E8G_HD bool wide_advance(WideTrav &T, uint32_t hits, uint32_t imask, uint32_t base, uint32_t *stk, int stride) {
+    const uint32_t oct = T.oct;
     uint32_t hit_int = hd_xor_perm(hits & imask, oct);
-    // the next node: the first hit interior child in octant order (the rest go on the stack),
-    // else the stack's top
-    bool more = true;
-    uint32_t next = 0;
     if (hit_int) {
         uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
         hit_int &= hit_int - 1u;
         uint32_t s = k ^ oct;
-        uint32_t base = n1.x;
         if (hit_int && T.sp < kWideStack) {
             stk[2 * T.sp * stride] = base;
             stk[(2 * T.sp + 1) * stride] = imask << 8 | hit_int;
             T.sp++;
         }
-        next = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
-    } else if (T.sp > 0) {
-        uint32_t base = stk[2 * (T.sp - 1) * stride];
+        T.node = base + static_cast<uint32_t>(hd_popc(imask & ((1u << s) - 1u)));
+        return true;
+    }
+    if (T.sp > 0) {
+        uint32_t sbase = stk[2 * (T.sp - 1) * stride];
         uint32_t info = stk[(2 * (T.sp - 1) + 1) * stride];
         uint32_t m = info & 0xFFu, im = info >> 8;
         uint32_t k = static_cast<uint32_t>(hd_ffs(m) - 1);
@@ -281,35 +276,58 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
         else
             T.sp--;
         uint32_t s = k ^ oct;
-        next = base + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
-    } else {
-        more = false;
+        T.node = sbase + static_cast<uint32_t>(hd_popc(im & ((1u << s) - 1u)));
+        return true;
     }
-    // triangles of the hit leaf slots
+    return false;
+}
+
+// The triangles of leaf slot s of a node (its words 5-7 and 20: tri_base, meta, counts).
+// Returns true when an any-hit ray found its occluder.
+E8G_HD bool wide_leaf_slot(WideView const &W, WideTrav &T, uint32_t s, uint32_t tri_base, uint32_t meta_lo,
+                           uint32_t meta_hi, uint32_t counts, uint32_t *cnt_tris) {
+    uint32_t meta = (s < 4 ? meta_lo : meta_hi) >> (8u * (s & 3u)) & 0xFFu;
+    uint32_t k0 = tri_base + meta, k1 = k0 + ((counts >> (4u * s)) & 0xFu);
+    for (uint32_t k = k0; k < k1; k++) {
+        float4 a = hd_ld(W.tri + 3 * static_cast<size_t>(k));
+        float4 b = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 1);
+        float4 c = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 2);
+        if (cnt_tris)
+            (*cnt_tris)++;
+        float t0, b1, b2;
+        if (hd_tri_test(T.o, T.d, a, b, c, T.tmin, T.cull, t0, b1, b2) && t0 < T.h.t) {
+            T.h.t = t0;
+            T.h.tri = hd_f2u(a.w);
+            T.h.b1 = b1;
+            T.h.b2 = b2;
+            if (T.any)
+                return true;
+            T.cull = t0;
+        }
+    }
+    return false;
+}
+
+// Visits T.node: tests its eight child boxes, the triangles of every hit leaf slot, and moves
+// T.node to the next node (the first hit interior child in octant order; the rest go on the
+// stack as one entry). Returns true when the ray is finished (stack empty, or an any-hit found).
+E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride, uint32_t *cnt_nodes,
+                      uint32_t *cnt_tris) {
+    uint4 const *np = W.nodes + 6 * static_cast<size_t>(T.node);
+    uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
+          n5 = hd_ld(np + 5);
+    uint32_t counts = n5.x, leaves = n5.y;
+    if (cnt_nodes)
+        (*cnt_nodes)++;
+    uint32_t hits = wide_child_hits(T, n0, n2, n3, n4, leaves);
+    bool more = wide_advance(T, hits, n0.w >> 24, n1.x, stk, stride);
+    uint32_t hit_leaf = hits & leaves;
     while (hit_leaf) {
         uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
         hit_leaf &= hit_leaf - 1u;
-        uint32_t meta = (s < 4 ? n1.z : n1.w) >> (8u * (s & 3u)) & 0xFFu;
-        uint32_t k0 = n1.y + meta, k1 = k0 + ((counts >> (4u * s)) & 0xFu);
-        for (uint32_t k = k0; k < k1; k++) {
-            float4 a = hd_ld(W.tri + 3 * static_cast<size_t>(k));
-            float4 b = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 1);
-            float4 c = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 2);
-            if (cnt_tris)
-                (*cnt_tris)++;
-            float t0, b1, b2;
-            if (hd_tri_test(T.o, T.d, a, b, c, T.tmin, T.cull, t0, b1, b2) && t0 < T.h.t) {
-                T.h.t = t0;
-                T.h.tri = hd_f2u(a.w);
-                T.h.b1 = b1;
-                T.h.b2 = b2;
-                if (T.any)
-                    return true;
-                T.cull = t0;
-            }
-        }
+        if (wide_leaf_slot(W, T, s, n1.y, n1.z, n1.w, counts, cnt_tris))
+            return true;
     }
-    T.node = next;
     return !more;
 }
 
