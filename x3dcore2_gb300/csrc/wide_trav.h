@@ -77,6 +77,18 @@ E8G_HD float hd_rcp(float x) {
     return 1.0f / x;
 #endif
 }
+// Reciprocal for the box tests only, within 1 ulp on the device (one MUFU instruction); the
+// boxes are pushed out by about 1e-6 of the scene's extent, far more than a 1-ulp change of the
+// slab distances, so no box that a hit lies in is culled.
+E8G_HD float hd_rcp_box(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
+}
 E8G_HD uint4 hd_ld(uint4 const *p) {
 #if defined(__CUDA_ARCH__)
     return __ldg(p);
@@ -192,9 +204,9 @@ E8G_HD void wide_begin(WideTrav &T, float3 o, float3 d, float tmin, float tmax, 
     // would turn the factored plane distance q * (step / d) + (p - o) / d into 0 * inf or
     // inf - inf. The nudged ray moves less than 1e-27 off its line over t <= 1000, and boxes are
     // inflated far beyond that, so no box a triangle hit lies in is culled; triangle tests use d.
-    T.ix = 1.0f / (fabsf(d.x) < 1e-30f ? copysignf(1e-30f, d.x) : d.x);
-    T.iy = 1.0f / (fabsf(d.y) < 1e-30f ? copysignf(1e-30f, d.y) : d.y);
-    T.iz = 1.0f / (fabsf(d.z) < 1e-30f ? copysignf(1e-30f, d.z) : d.z);
+    T.ix = hd_rcp_box(fabsf(d.x) < 1e-30f ? copysignf(1e-30f, d.x) : d.x);
+    T.iy = hd_rcp_box(fabsf(d.y) < 1e-30f ? copysignf(1e-30f, d.y) : d.y);
+    T.iz = hd_rcp_box(fabsf(d.z) < 1e-30f ? copysignf(1e-30f, d.z) : d.z);
     T.oct = (T.ix < 0.0f ? 1u : 0u) | (T.iy < 0.0f ? 2u : 0u) | (T.iz < 0.0f ? 4u : 0u);
     T.tmin = tmin;
     T.cull = tmax;
