@@ -436,19 +436,19 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
     constexpr uint32_t kNone = 0xFFFFFFFFu;
     WideView WV{S0.wnodes, S0.tri, S0.nnodes};
     uint32_t q = kNone;
-    bool exhausted = false;
+    bool drained = false; // the same in every lane: the queue had no entry left for this warp
     WideTrav T;
     while (true) {
-        bool idle = q == kNone && !exhausted;
-        uint32_t im = __ballot_sync(~0u, idle);
         uint32_t busy = __ballot_sync(~0u, q != kNone);
+        uint32_t im = drained ? 0u : ~busy; // idle lanes
         if (im && (__popc(im) >= threshold || busy == 0)) {
             int leader = __ffs(im) - 1;
             uint32_t base = 0;
             if (static_cast<int>(lane) == leader)
                 base = atomicAdd(head, static_cast<uint32_t>(__popc(im)));
             base = __shfl_sync(~0u, base, leader);
-            if (idle) {
+            drained = base + static_cast<uint32_t>(__popc(im)) >= n; // the head only grows
+            if (q == kNone) {
                 uint32_t qq = base + __popc(im & ((1u << lane) - 1u));
                 if (qq < n) {
                     q = qq;
@@ -466,14 +466,12 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
                         DevScene const &S = B.scenes[sid];
                         WV = WideView{S.wnodes, S.tri, S.nnodes};
                     }
-                } else {
-                    exhausted = true;
                 }
             }
             busy = __ballot_sync(~0u, q != kNone);
         }
         if (busy == 0) {
-            if (__ballot_sync(~0u, !exhausted) == 0)
+            if (drained)
                 break;
             continue;
         }
