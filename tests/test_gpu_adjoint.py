@@ -178,3 +178,31 @@ def test_backward_needs_forward(lib):
             c.backward(np.zeros((16, 16, 3), np.float32))
         with pytest.raises(E8GError, match="INVALID_ARG"):  # the adjoint replays MIS + Philox paths
             c.forward(default_params(abi.MODE_REF_LT1, 16, 16, 1))
+
+
+def test_autograd_function_gives_the_adjoints_gradients(ctx):
+    """x3dcore2_gb300.autograd.render: torch's backward through the differentiable render gives
+    e8g_backward's gradients of the same loss, and a second render on the context before the
+    first graph's backward is refused."""
+    import torch
+    from x3dcore2_gb300 import autograd as AG
+    sc, base, p, target = setup(ctx, 32, 24, 8)
+    albedo = torch.tensor([list(m.albedo) for m in base], dtype=torch.float32, requires_grad=True)
+    rough = torch.tensor([m.roughness for m in base], dtype=torch.float32, requires_grad=True)
+    img = AG.render(ctx, p, albedo, rough)
+    assert img.shape == (24, 32, 3)
+    loss = ((img - torch.from_numpy(target[..., :3])) ** 2).sum()
+    loss.backward()
+    ctx.set_materials(base)
+    ref = ctx.forward(p)
+    # pixels sum their samples with atomics: the same render up to the order of those sums
+    np.testing.assert_allclose(ref[..., :3], img.detach().numpy(), rtol=1e-5, atol=1e-6)
+    _, dl = loss_and_grad(ref, target)
+    da, dr = ctx.backward(dl)
+    assert np.abs(da).max() > 0 and np.abs(dr).max() > 0
+    np.testing.assert_allclose(albedo.grad.numpy(), da, rtol=1e-3, atol=1e-4 * np.abs(da).max())
+    np.testing.assert_allclose(rough.grad.numpy(), dr, rtol=1e-3, atol=1e-4 * np.abs(dr).max())
+    first = AG.render(ctx, p, albedo.detach().requires_grad_(), rough.detach().requires_grad_())
+    AG.render(ctx, p, albedo.detach().requires_grad_(), rough.detach().requires_grad_())
+    with pytest.raises(RuntimeError, match="another differentiable render"):
+        first.sum().backward()
