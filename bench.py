@@ -176,6 +176,61 @@ def quality_leg(ctx, p, img64, results):
                                        for k, r in results.items()}}
 
 
+def cornell_leg(ctx, threads, cpu_budget_s=6.0):
+    """The small configuration: the Cornell room (two rotated boxes, a 0.25 x 0.25 ceiling light of
+    radiance (17, 12, 4); 36 triangles) at 256x256, 16 spp, depth 5, SAH pairs. The reference's
+    direct-lighting estimator (E8G_MODE_REF_LT1: unidirect_lt1 with the depth cap; the wavefront
+    runs MIS only, so plain and megakernel) and MIS (the three integrators). Per estimator: GPU
+    paths/s from the kernel time, relMSE of the 16-spp frame against a 4096-spp frame of the same
+    estimator with independent streams (epsilon 1e-2), and the oracle's restatement of
+    unidirect_lt1 on the host cores rendering the whole frame."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300 import scene as S
+    from x3dcore2_gb300.core import default_params
+    w = h = 256
+    spp = 16
+    sc = S.cornell(w, h)
+    ctx.upload(sc, layout=abi.BVH_SAH)
+    out = {"width": w, "height": h, "spp": spp, "max_depth": 5, "triangles": int(sc.desc.mesh_tri_offset[sc.desc.num_meshes])}
+    for name, mode, integs in (("ref_lt1", abi.MODE_REF_LT1, ("plain", "megakernel")),
+                               ("mis", abi.MODE_MIS, ("plain", "megakernel", "wavefront"))):
+        p = default_params(mode, w, h, spp, seed=1, max_depth=5)
+        if mode == abi.MODE_REF_LT1:
+            lt1 = p
+        row = {}
+        for integ in integs:
+            p.integrator = INTEGRATORS[integ]
+            for _ in range(3):
+                ctx.render(p)
+            ms = []
+            for _ in range(20):
+                img = ctx.render(p)
+                ms.append(ctx.stats()["kernel_ms"])
+            row[integ] = {"kernel_ms": statistics.mean(ms), "paths_per_s": w * h * spp / (statistics.mean(ms) / 1e3)}
+        q = abi.RenderParams.from_buffer_copy(p)
+        q.spp, q.seed, q.integrator = 4096, 4242, abi.INTEGRATOR_MEGAKERNEL
+        ref = ctx.render(q)[..., :3].astype(np.float64)
+        rel = float(np.mean((img[..., :3].astype(np.float64) - ref) ** 2 / (ref ** 2 + 1e-2)))
+        row["relmse"] = rel
+        row["spp_for_relmse_1e-3"] = spp * rel / 1e-3
+        out[name] = row
+    import oracle_bind as ob
+    osc = ob.OracleScene(sc)
+    pol = ob.OPolicy(lt1.max_depth, lt1.rr_start, lt1.rr_prob, 8)  # the GPU frame's depth cap and roulette
+    n_spp, paths, secs = 1, 0, 0.0
+    while secs < cpu_budget_s:
+        t = time.time()
+        osc.render(abi.MODE_REF_LT1, w, h, n_spp, seed=1, policy=pol, threads=threads)
+        secs += time.time() - t
+        paths += w * h * n_spp
+        n_spp *= 2
+    out["cpu_oracle"] = {"paths_per_s": paths / secs, "threads": threads, "kind": "port",
+                         "sample": f"whole {w}x{h} frame, unidirect_lt1 restated (oracle), {paths // (w * h)} spp"}
+    return out
+
+
 def bdpt_leg(ctx):
     """Bidirectional MIS on the benchmark scene (still uploaded) at 1280x720, subpaths of at most 6
     vertices, 32 spp: power-heuristic weights (E8G_MODE_BDPT_POWER) and the reference's uniform
@@ -374,7 +429,8 @@ def run_leg(args):
     scene, _, _, _ = make_scene(args.small)
     ctx.upload(scene)
     fn = {"bdpt": lambda: bdpt_leg(ctx), "batch": lambda: batch_leg(ctx), "adjoint": lambda: adjoint_leg(ctx),
-          "update": lambda: update_leg(ctx, scene)}[args.leg]
+          "update": lambda: update_leg(ctx, scene),
+          "cornell": lambda: cornell_leg(ctx, os.cpu_count() or 1)}[args.leg]
     print(json.dumps({"leg": args.leg, **fn()}))
     ctx.close()
 
@@ -432,7 +488,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the quality, BDPT, batch and adjoint legs")
     ap.add_argument("--no-tune", action="store_true", help="wavefront with the library defaults (profiling)")
-    ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "update", "obj"],
+    ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "update", "obj", "cornell"],
                     help="run one extra leg alone on the benchmark scene and print its JSON (not a bench line)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -598,6 +654,7 @@ def main():
         line["adjoint"] = adjoint_leg(ctx)
         line["update"] = update_leg(ctx, scene)
         line["obj_ingest"] = obj_leg()
+        line["cornell"] = cornell_leg(ctx, os.cpu_count() or 1)
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         v, kind, sample, ref_build_s = cpu_sample(scene, w, h, args.cpu_budget, os.cpu_count() or 1, timing_ref=False)
         if "update" in line and ref_build_s is not None:
