@@ -78,7 +78,7 @@ E8G_BOX_HD void wide_quantize(float const lo[8][3], float const hi[8][3], uint32
     // is clamped to the grid's ends and every quantized plane lies at least one step outside the
     // (already pushed-out) child box: the slack absorbs the rounding of the traversal's plane
     // arithmetic.
-    double step[3];
+    double inv_step[3]; // 2^-e: dividing by the step 2^e is this exact product
     float org[3];
     uint32_t ebytes = 0;
     for (int a = 0; a < 3; a++) {
@@ -86,9 +86,9 @@ E8G_BOX_HD void wide_quantize(float const lo[8][3], float const hi[8][3], uint32
         double want = ext / 251.0;
         want = want > step_min ? want : step_min;
         int e = wide_exponent(want);
-        step[a] = ldexp(1.0, e);
+        inv_step[a] = ldexp(1.0, -e);
         ebytes |= static_cast<uint32_t>(e + 127) << (8 * a);
-        double l = static_cast<double>(u_lo[a]) - step[a];
+        double l = static_cast<double>(u_lo[a]) - ldexp(1.0, e);
         float f = static_cast<float>(l);
         if (static_cast<double>(f) > l)
             f = nextafterf(f, -INFINITY);
@@ -101,8 +101,8 @@ E8G_BOX_HD void wide_quantize(float const lo[8][3], float const hi[8][3], uint32
         if (!(present >> s & 1))
             continue;
         for (int a = 0; a < 3; a++) {
-            double ql = floor((static_cast<double>(lo[s][a]) - org[a]) / step[a]) - 1.0;
-            double qh = ceil((static_cast<double>(hi[s][a]) - org[a]) / step[a]) + 1.0;
+            double ql = floor((static_cast<double>(lo[s][a]) - org[a]) * inv_step[a]) - 1.0;
+            double qh = ceil((static_cast<double>(hi[s][a]) - org[a]) * inv_step[a]) + 1.0;
             ql = ql < 0.0 ? 0.0 : (ql > 255.0 ? 255.0 : ql);
             qh = qh < 0.0 ? 0.0 : (qh > 255.0 ? 255.0 : qh);
             // byte s of plane a (lo) and plane 3 + a (hi); 8 bytes per plane, little endian
