@@ -62,6 +62,22 @@ int main(int argc, char **argv) {
     for (uint32_t t = 0; t < nt; t++)
         record(t, &grec[3 * t]);
     WideView W{reinterpret_cast<uint4 const *>(w.nodes.data()), rec.data(), w.num_nodes};
+    // level boundaries (the refit's launches): one per level, increasing, ending at the node
+    // count, and every interior child of a level-L node in level L + 1
+    uint64_t bad_levels = 0;
+    if (w.level_start.size() != w.max_depth + 1 || w.level_start.empty() || w.level_start[0] != 0 ||
+        w.level_start.back() != w.num_nodes)
+        bad_levels++;
+    for (uint32_t L = 0; !bad_levels && L < w.max_depth; L++) {
+        if (w.level_start[L] >= w.level_start[L + 1])
+            bad_levels++;
+        for (uint32_t i = w.level_start[L]; i < w.level_start[L + 1]; i++) {
+            uint32_t const *nd = &w.nodes[kWideWords * static_cast<size_t>(i)];
+            uint32_t imask = nd[3] >> 24, nch = static_cast<uint32_t>(__builtin_popcount(imask));
+            if (nch && (L + 2 > w.max_depth || nd[4] < w.level_start[L + 1] || nd[4] + nch > w.level_start[L + 2]))
+                bad_levels++;
+        }
+    }
 
     std::uniform_real_distribution<float> U(0.0f, 1.0f);
     uint64_t bad_t = 0, bad_tri = 0, bad_any = 0, hits = 0, visits = 0, tested = 0;
@@ -137,9 +153,10 @@ int main(int argc, char **argv) {
     }
     std::printf("{\"tris\": %u, \"binary_nodes\": %u, \"wide_nodes\": %u, \"wide_depth\": %u, \"ok\": %d, "
                 "\"rays\": %u, \"hits\": %llu, \"bad_t\": %llu, \"bad_tri\": %llu, \"bad_any\": %llu, "
-                "\"visits_per_ray\": %.3f, \"tris_per_ray\": %.3f}\n",
+                "\"visits_per_ray\": %.3f, \"tris_per_ray\": %.3f, \"bad_levels\": %llu}\n",
                 nt, b.num_nodes, w.num_nodes, w.max_depth, w.ok ? 1 : 0, nrays, (unsigned long long)hits,
                 (unsigned long long)bad_t, (unsigned long long)bad_tri, (unsigned long long)bad_any,
-                nrays ? double(visits) / nrays : 0.0, nrays ? double(tested) / nrays : 0.0);
-    return (bad_t || bad_tri || bad_any || !w.ok) ? 1 : 0;
+                nrays ? double(visits) / nrays : 0.0, nrays ? double(tested) / nrays : 0.0,
+                (unsigned long long)bad_levels);
+    return (bad_t || bad_tri || bad_any || bad_levels || !w.ok) ? 1 : 0;
 }

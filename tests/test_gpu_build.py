@@ -174,3 +174,19 @@ def test_device_wide_collapse_equals_host_collapse(ctx, collapse_checker, tmp_pa
     host_order = out[2 + 24 * wn:]
     assert np.array_equal(nodes_w.view(np.uint32), host_nodes)
     assert np.array_equal(np.ascontiguousarray(tris_w[:, 3]).view(np.uint32), host_order)
+
+
+@pytest.mark.parametrize("name", ["soup", "ico"])
+def test_refit_of_device_wide_tree_keeps_its_bytes(ctx, name):
+    """The refit walks the eight-wide tree level by level from the boundaries its builder recorded;
+    on a device-built tree (boundaries from the device collapse) a refit of the unchanged scene
+    writes the bytes that build wrote."""
+    sc = SCENES[name]()
+    ctx.upload(sc, layout=abi.BVH_WIDE, builder=abi.BUILDER_DEVICE)
+    assert ctx.bvh_stats()["layout"] == abi.BVH_WIDE
+    nodes0, tris0 = ctx.bvh_read()
+    st = ctx.commit(abi.COMMIT_REFIT)
+    assert st["layout"] == abi.BVH_WIDE
+    nodes1, tris1 = ctx.bvh_read()
+    assert np.array_equal(nodes0, nodes1)
+    assert np.array_equal(tris0.view(np.uint32), tris1.view(np.uint32))

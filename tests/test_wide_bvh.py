@@ -66,6 +66,7 @@ def test_wide_traversal_matches_brute_force(checker, tmp_path, name):
     res = json.loads(r.stdout)
     assert r.returncode == 0, res
     assert res["ok"] == 1 and res["bad_t"] == 0 and res["bad_tri"] == 0 and res["bad_any"] == 0
+    assert res["bad_levels"] == 0
     assert res["wide_depth"] <= 32
     # an eight-wide node replaces about three binary levels
     assert res["wide_nodes"] * 3 < res["binary_nodes"] or res["binary_nodes"] < 64
