@@ -110,6 +110,30 @@ def test_refit_of_unchanged_scene_writes_the_build_bytes(ctx, layout, which):
     assert np.array_equal(tris0.view(np.uint32), tris1.view(np.uint32))
 
 
+@pytest.mark.parametrize("builder", [abi.BUILDER_HOST, abi.BUILDER_DEVICE])
+@pytest.mark.parametrize("n", [1, 2, 9, 40])
+def test_refit_of_tiny_wide_trees(ctx, n, builder):
+    """Small eight-wide trees (a soup of n triangles in its room: one to three levels): the refit
+    of the unchanged scene writes the build's bytes, and after moving every vertex the hits equal
+    a fresh build's."""
+    sc = S.soup(n, seed=n, width=16, height=16)
+    ctx.upload(sc, layout=abi.BVH_WIDE, builder=builder)
+    assert ctx.bvh_stats()["layout"] == abi.BVH_WIDE
+    nodes0, tris0 = ctx.bvh_read()
+    ctx.commit(abi.COMMIT_REFIT)
+    nodes1, tris1 = ctx.bvh_read()
+    assert np.array_equal(nodes0, nodes1)
+    assert np.array_equal(tris0.view(np.uint32), tris1.view(np.uint32))
+    pos = deformed(sc, 3, 0.05)
+    push_all(ctx, sc, pos)
+    ctx.commit(abi.COMMIT_REFIT)
+    rays = random_rays(sc, 3000, n)
+    with Context(0) as fresh:
+        fresh.upload(with_vertices(sc, pos, sc.nrm), layout=abi.BVH_WIDE)
+        want = fresh.trace_closest(rays)
+    compare_hits(ctx.trace_closest(rays), want["mesh"], want["tri"], want["t"], min_match=1.0)
+
+
 def test_refit_boxes_after_deformation_are_the_exact_unions(ctx):
     sc = S.soup(2500, seed=6)
     ctx.upload(sc, layout=abi.BVH_SAH)
