@@ -60,6 +60,25 @@ E8G_BOX_HD int wide_exponent(double want) {
     return e < -126 ? -126 : (e > 127 ? 127 : e);
 }
 
+// floor and ceil of (v - org) * inv, with inv a power of two, from the exact difference: s + err
+// = v - org exactly (Knuth's TwoSum in single precision), s * inv is exact, and a float quotient
+// is at least one of its ulps away from the next integer, so only an integer quotient can move,
+// by the sign of err. The same result as the double-precision expression whenever v - org is
+// exact in double (exponents within 29 of each other), without double arithmetic (slow on this
+// GPU).
+E8G_BOX_HD void wide_grid_floor_ceil(float v, float org, float inv, float &fl, float &cl) {
+    float s = v - org;
+    float bb = s - v;
+    float err = (v - (s - bb)) + (-org - bb);
+    float q = s * inv;
+    fl = floorf(q);
+    cl = ceilf(q);
+    if (fl == q && err < 0.0f)
+        fl -= 1.0f;
+    if (cl == q && err > 0.0f)
+        cl += 1.0f;
+}
+
 // Fills a node's grid and quantized child boxes: words[0..2] (grid origin), the exponent bytes of
 // words[3] (the interior mask byte is left alone) and words[8..19]. lo/hi hold the pushed-out
 // boxes of the eight slots; only slots in `present` are used.
@@ -78,7 +97,7 @@ E8G_BOX_HD void wide_quantize(float const lo[8][3], float const hi[8][3], uint32
     // is clamped to the grid's ends and every quantized plane lies at least one step outside the
     // (already pushed-out) child box: the slack absorbs the rounding of the traversal's plane
     // arithmetic.
-    double inv_step[3]; // 2^-e: dividing by the step 2^e is this exact product
+    float inv_step[3]; // 2^-e: dividing by the step 2^e is this exact product
     float org[3];
     uint32_t ebytes = 0;
     for (int a = 0; a < 3; a++) {
@@ -86,7 +105,7 @@ E8G_BOX_HD void wide_quantize(float const lo[8][3], float const hi[8][3], uint32
         double want = ext / 251.0;
         want = want > step_min ? want : step_min;
         int e = wide_exponent(want);
-        inv_step[a] = ldexp(1.0, -e);
+        inv_step[a] = ldexpf(1.0f, -e);
         ebytes |= static_cast<uint32_t>(e + 127) << (8 * a);
         double l = static_cast<double>(u_lo[a]) - ldexp(1.0, e);
         float f = static_cast<float>(l);
@@ -101,10 +120,12 @@ E8G_BOX_HD void wide_quantize(float const lo[8][3], float const hi[8][3], uint32
         if (!(present >> s & 1))
             continue;
         for (int a = 0; a < 3; a++) {
-            double ql = floor((static_cast<double>(lo[s][a]) - org[a]) * inv_step[a]) - 1.0;
-            double qh = ceil((static_cast<double>(hi[s][a]) - org[a]) * inv_step[a]) + 1.0;
-            ql = ql < 0.0 ? 0.0 : (ql > 255.0 ? 255.0 : ql);
-            qh = qh < 0.0 ? 0.0 : (qh > 255.0 ? 255.0 : qh);
+            float fl, cl, unused;
+            wide_grid_floor_ceil(lo[s][a], org[a], inv_step[a], fl, unused);
+            wide_grid_floor_ceil(hi[s][a], org[a], inv_step[a], unused, cl);
+            float ql = fl - 1.0f, qh = cl + 1.0f;
+            ql = ql < 0.0f ? 0.0f : (ql > 255.0f ? 255.0f : ql);
+            qh = qh < 0.0f ? 0.0f : (qh > 255.0f ? 255.0f : qh);
             // byte s of plane a (lo) and plane 3 + a (hi); 8 bytes per plane, little endian
             qb[2 * a + (s >> 2)] |= static_cast<uint32_t>(ql) << (8 * (s & 3));
             qb[2 * (3 + a) + (s >> 2)] |= static_cast<uint32_t>(qh) << (8 * (s & 3));
