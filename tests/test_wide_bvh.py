@@ -70,3 +70,38 @@ def test_wide_traversal_matches_brute_force(checker, tmp_path, name):
     assert res["wide_depth"] <= 32
     # an eight-wide node replaces about three binary levels
     assert res["wide_nodes"] * 3 < res["binary_nodes"] or res["binary_nodes"] < 64
+
+
+def test_grid_floor_ceil_is_exact(tmp_path):
+    """The eight-wide quantization's plane arithmetic (single precision, TwoSum difference) gives
+    the exact floor and ceiling of (v - org) / 2^e, checked with rational arithmetic on random
+    planes, planes on grid lines, one ulp beside them, and subnormals beside large origins."""
+    import ctypes as C
+    import subprocess
+    from fractions import Fraction
+    lib_path = tmp_path / "gfc.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-o", str(lib_path),
+                    f"-I{CSRC}", os.path.join(ROOT, "tests", "cpp", "grid_floor_ceil.cpp")], check=True)
+    lib = C.CDLL(str(lib_path))
+    rng = np.random.default_rng(5)
+    n = 60000
+    e = rng.integers(-40, 40, n)
+    step = np.ldexp(np.float32(1), e).astype(np.float32)
+    org = (rng.integers(-3000, 3000, n) * step * rng.choice([1, 3, 64], n)).astype(np.float32)
+    k = rng.integers(0, 254, n)
+    v = (org.astype(np.float64) + k * step.astype(np.float64)).astype(np.float32)
+    kind = rng.integers(0, 5, n)
+    v = np.where(kind == 1, np.nextafter(v, np.float32(-np.inf)), v)
+    v = np.where(kind == 2, np.nextafter(v, np.float32(np.inf)), v)
+    v = np.where(kind == 3, (v * rng.uniform(0.9, 1.1, n)).astype(np.float32), v)
+    v = np.where(kind == 4, np.float32(1.4e-45) * rng.choice([-1, 1], n), v).astype(np.float32)
+    inv = np.ldexp(np.float32(1), -e).astype(np.float32)
+    fl = np.zeros(n, np.float32)
+    cl = np.zeros(n, np.float32)
+    f = np.ctypeslib.as_ctypes
+    lib.grid_floor_ceil(f(v), f(org), f(inv), C.c_int(n), f(fl), f(cl))
+    for i in range(n):
+        q = (Fraction(float(v[i])) - Fraction(float(org[i]))) * Fraction(float(inv[i]))
+        fq = q.numerator // q.denominator
+        cq = -((-q.numerator) // q.denominator)
+        assert (fl[i], cl[i]) == (fq, cq), (v[i], org[i], e[i], fl[i], cl[i], fq, cq)
