@@ -11,9 +11,11 @@ Philox streams). A step is one full render of that frame.
 
 Prints one JSON line. `value` is paths/s over the device-resident render; `e2e` is the same
 metric through the public C ABI call with the image read back to pinned host memory each step.
-The reference arm (--impl reference) times the reference's CPU tracer (unidirect_lt1) on the
-host cores: the reference compiled from its own sources when present, else the oracle's C
-restatement of it.
+The reference arm (--impl reference) times the reference's own CPU tracer (pt_image_renderer with
+unidirect_lt1, compiled from its unmodified sources with its release flags) on the host cores, on
+the same scene and camera at a quarter of the resolution in each axis (pixels spread uniformly over
+the frame); the scene comes from the stand-alone generator library, so that process never maps the
+GPU library. Where the reference sources are absent it times the oracle's C restatement instead.
 """
 import argparse
 import ctypes as C
@@ -29,9 +31,20 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "paths/s at fixed relMSE, plain vs wavefront-batched; adjoint/forward time"
+# The workload both arms name in `config` (identical dicts). What each arm computes per path is in
+# its own top-level "estimator" object.
 WORKLOAD = dict(workload="displaced_icosphere_l8_1080p_64spp", triangles=1310730, width=1920,
-                height=1080, spp=64, max_depth=8, rr_start=3, materials=512, lights=4,
-                estimator="nee+bsdf power-heuristic MIS", rng="philox4x32-10")
+                height=1080, spp=64, materials=512, lights=4,
+                l2="GPU arm: flushed between timed steps (256 MB write); host arm: not applicable")
+GPU_ESTIMATOR = dict(name="nee+bsdf power-heuristic MIS (E8G_MODE_MIS)", max_depth=8, rr_start=3, rr_prob=0.5,
+                     rng="philox4x32-10")
+REF_ESTIMATOR = dict(name="unidirect_lt1 (the reference's direct-lighting tracer: NEE + BSDF continuation, no MIS)",
+                     max_depth=None, rr_start=2, rr_prob=0.5, rng="minstd, one stream per thread",
+                     note="the reference has no MIS tracer and no depth cap; its paths are shorter than the GPU "
+                          "arm's (see the GPU line's like_for_like leg for the GPU on this estimator)")
+# The host arms' sample of the frame: the same scene and camera at a quarter of the resolution in
+# each axis, so its pixels are spread uniformly over the whole 1920x1080 view (sky included).
+REF_SAMPLE_W, REF_SAMPLE_H = 480, 270
 # DRAM traffic per path of a (tree, integrator) combination, from the ncu captures summarised in
 # profiles/: dram__bytes_read.sum + dram__bytes_write.sum over one frame of a 480x270, 8-spp
 # render of the same scene divided by its 1,036,800 paths, scaled to the full frame by its path
@@ -119,40 +132,120 @@ def make_scene(small):
     return (S.displaced_icosphere(level=8, seed=1, num_materials=512, width=1920, height=1080), 1920, 1080, 64)
 
 
-def cpu_sample(scene, width, height, budget_s, threads, timing_ref):
-    """Times the reference's CPU tracer (unidirect_lt1, the reference's direct-lighting
-    integrator) on a centred crop of the same frame: the reference itself when it is compiled
-    here, else the oracle's restatement. Returns (paths/s, kind, sample description, seconds of
-    the restated reference BVH build (its commit) or None)."""
+def ref_scene_host(small):
+    """The benchmark scene built by the stand-alone generator library (oracle/libe8scenegen.so, the
+    same source as the GPU library's generators): the host arms never map the GPU library."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import numpy as np
+    import oracle_bind as ob
+    from x3dcore2_gb300 import scene as S
+    g = ob.scenegen()
+    if small:
+        return S.displaced_icosphere(level=5, seed=1, num_materials=512, width=320, height=180, lib=g)
+    return S.displaced_icosphere(level=8, seed=1, num_materials=512, width=1920, height=1080, lib=g)
+
+
+def ref_tracer(scene):
+    """(render(spp) -> (seconds, paths), kind, description) for the reference's CPU tracer on the
+    host cores: the reference compiled from its own sources with its release flags
+    (oracle/_ref/libe8ref_timing.so, pt_image_renderer::render with unidirect_lt1 and every host
+    thread) when its sources are present, else the oracle's C restatement of the same estimator
+    with the reference's policy (RR from depth 2, no depth cap)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_bind as ob
     from x3dcore2_gb300 import abi
-    cw, ch = 96, 54
-    x0, y0 = (width - cw) // 2, (height - ch) // 2
-    if timing_ref and ob.os.path.exists(ob.REF_TIMING_LIB):
-        # the reference renders whole frames; time a reduced-resolution frame of the same scene
+    threads = os.cpu_count() or 1
+    w, h = REF_SAMPLE_W, REF_SAMPLE_H
+    if not os.path.exists(ob.REF_TIMING_LIB) and ob.reference_src() is not None:
+        subprocess.run(["make", "-s", "-j2", "-C", ob.ORACLE_DIR, "ref"], check=True)
+    if os.path.exists(ob.REF_TIMING_LIB):
         rs = ob.RefScene(scene, timing=True)
-        spp = threads
-        img, secs, taken = rs.render(abi.MODE_REF_LT1, cw, ch, spp, threads)
-        return (cw * ch * taken / secs, "reference", f"{cw}x{ch} frame, {taken} spp, unidirect_lt1, {threads} threads",
-                None)
-    t0 = time.time()
+
+        def render(spp):
+            _, secs, taken = rs.render(abi.MODE_REF_LT1, w, h, spp, threads)
+            return secs, w * h * taken
+        return render, "reference", threads, (
+            f"{w}x{h} frame of the same scene and camera (pixels spread uniformly over the 1920x1080 view), "
+            f"the reference's pt_image_renderer::render with unidirect_lt1, compiled from its unmodified sources "
+            f"with -Ofast -flto native, {threads} threads")
     osc = ob.OracleScene(scene)
-    build_s = time.time() - t0
-    spp, total_paths, total_s = 1, 0, 0.0
-    while total_s < budget_s:
-        t = time.time()
-        osc.render(abi.MODE_REF_LT1, width, height, spp, seed=1, crop=(x0, y0, x0 + cw, y0 + ch), threads=threads)
-        dt = time.time() - t
-        total_paths += cw * ch * spp
-        total_s += dt
-        spp *= 2
-        if dt * 2 + total_s > budget_s * 1.5:
-            break
-    return (total_paths / total_s, "port", (f"{cw}x{ch} crop of the {width}x{height} frame, unidirect_lt1 restated "
-                                            f"(oracle), {threads} threads, {total_s:.1f} s render, BVH build {build_s:.1f} s"),
-            build_s)
+
+    def render_port(spp):
+        t = time.perf_counter()
+        osc.render(abi.MODE_REF_LT1, w, h, spp, seed=1, policy=ob.REF_POLICY, threads=threads)
+        return time.perf_counter() - t, w * h * spp
+    return render_port, "port", threads, (
+        f"{w}x{h} frame of the same scene and camera (pixels spread uniformly over the 1920x1080 view), "
+        f"unidirect_lt1 restated by the oracle (reference sources absent), {threads} threads")
+
+
+def cpu_sample(scene, budget_s):
+    """The reference's CPU tracer timed on the host cores over about budget_s seconds (see
+    ref_tracer), plus the oracle's restatement on the same sample for a few seconds where the
+    reference itself ran. Returns the cpu_baseline object."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind as ob
+    from x3dcore2_gb300 import abi
+    render, kind, threads, sample = ref_tracer(scene)
+    spp = threads
+    render(spp)  # warm-up (thread pool, page faults)
+    secs = paths = 0
+    while secs < budget_s:
+        dt, n = render(spp)
+        secs += dt
+        paths += n
+    out = {"value": paths / secs, "unit": "paths/s", "cores": threads, "kind": kind,
+           "sample": f"{sample}; {paths} paths in {secs:.1f} s"}
+    if kind == "reference":
+        osc = ob.OracleScene(scene)
+        t = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t < min(budget_s, 6.0):
+            osc.render(abi.MODE_REF_LT1, REF_SAMPLE_W, REF_SAMPLE_H, threads, seed=1 + n, policy=ob.REF_POLICY,
+                       threads=threads)
+            n += 1
+        out["port_value"] = REF_SAMPLE_W * REF_SAMPLE_H * threads * n / (time.perf_counter() - t)
+        out["port_note"] = "the oracle's C restatement of unidirect_lt1 on the same sample (-O2, no fast-math)"
+    return out
+
+
+def reference_commit_s(scene):
+    """Seconds of the reference's own tree build (its path space's commit) for the benchmark scene,
+    restated by the oracle on one thread."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind as ob
+    t0 = time.time()
+    ob.OracleScene(scene)
+    return time.time() - t0
+
+
+def like_for_like_leg(ctx, w, h, spp, d_img, stream):
+    """The GPU on the host arm's estimator: E8G_MODE_REF_LT1 (unidirect_lt1 step for step, minstd
+    streams) with the reference's own policy (Russian roulette from depth 2 at p = 0.5, no depth cap)
+    over the whole benchmark frame, on the tree the headline used, plain and megakernel (the
+    wavefront runs MIS only). Device time per frame, L2 flushed between frames."""
+    import torch
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300.core import default_params
+    p = default_params(abi.MODE_REF_LT1, w, h, spp, seed=1)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {"mode": "E8G_MODE_REF_LT1", "policy": {"max_depth": p.max_depth, "rr_start": p.rr_start,
+                                                  "rr_prob": p.rr_prob}, "width": w, "height": h, "spp": spp}
+    for integ in ("plain", "megakernel"):
+        p.integrator = INTEGRATORS[integ]
+        for _ in range(2):
+            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+        ms = []
+        for _ in range(3):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        out[integ] = {"ms": statistics.mean(ms), "paths_per_s": w * h * spp / (statistics.mean(ms) / 1e3)}
+    del flush
+    return out
 
 
 def quality_leg(ctx, p, img64, results):
@@ -435,38 +528,48 @@ def run_leg(args):
     ctx.close()
 
 
+def mapped_repo_libraries():
+    """The shared libraries of this working tree mapped into this process (Linux /proc)."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")}
+    except OSError:
+        return None
+    return sorted(os.path.relpath(x, ROOT) for x in paths if x.startswith(ROOT + os.sep))
+
+
 def run_reference_arm(args):
+    """The reference's own CPU tracer on the host cores (see ref_tracer): one step renders the
+    host sample of the frame at one sample per host thread. Never maps the GPU library."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_bind as ob
-    from x3dcore2_gb300 import abi
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"], check=True)
-    scene, w, h, _ = make_scene(args.small)
-    threads = os.cpu_count() or 1
-    kind = "port"
-    osc = ob.OracleScene(scene)
-    cw, ch = 64, 36
-    x0, y0 = (w - cw) // 2, (h - ch) // 2
-    spp = 2
+    subprocess.run(["make", "-s", "-C", ob.ORACLE_DIR, "all", "gen"], check=True)
+    scene = ref_scene_host(args.small)
+    render, kind, threads, sample = ref_tracer(scene)
+    spp = threads
     for _ in range(args.warmup):
-        osc.render(abi.MODE_REF_LT1, w, h, 1, seed=1, crop=(x0, y0, x0 + cw, y0 + ch), threads=threads)
-    t0 = time.time()
-    for k in range(args.steps):
-        osc.render(abi.MODE_REF_LT1, w, h, spp, seed=1, offset=k * spp, crop=(x0, y0, x0 + cw, y0 + ch),
-                   threads=threads)
-    dt = time.time() - t0
-    paths = cw * ch * spp * args.steps
-    v = paths / dt
+        render(spp)
+    secs = paths = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt, n = render(spp)
+        secs += dt
+        paths += n
+    wall = time.perf_counter() - t0
+    v = paths / secs
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "paths/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1000 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": dict(WORKLOAD),
+            "data": "synthetic (seeded procedural scene)", "config": dict(WORKLOAD),
+            "estimator": REF_ESTIMATOR,
             "cpu_baseline": {"value": v, "unit": "paths/s", "cores": threads, "kind": kind,
-                             "sample": f"{cw}x{ch} centre crop of the {w}x{h} frame, {spp} spp per step, "
-                                       "unidirect_lt1 (the reference's CPU tracer restated by the oracle)"},
-            "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": f"{sample}; {paths // args.steps} paths per step, {secs:.1f} s timed "
+                                       f"({wall:.1f} s wall)"},
+            "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "mapped_repo_libraries": mapped_repo_libraries()}
     print(json.dumps(line))
 
 
@@ -628,8 +731,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": dict(WORKLOAD, integrator=best_integ, bvh_layout=best_lay,
-                       l2="flushed between steps (256 MB write)",
+        "config": dict(WORKLOAD),
+        "estimator": GPU_ESTIMATOR,
+        "detail": dict(integrator=best_integ, bvh_layout=best_lay,
                        integrators={f"{k[0]}/{k[1]}": {kk: (round(vv, 4) if isinstance(vv, float) else vv)
                                                        for kk, vv in r.items()} for k, r in results.items()},
                        trees=trees, wavefront_tune={k: {kk: v for kk, v in t.items() if kk != "candidates"}
@@ -648,6 +752,7 @@ def main():
         "clocks": clk,
     }
     if rank == 0 and not args.no_extras and world == 1:
+        line["like_for_like"] = like_for_like_leg(ctx, w, h, spp, d_img, stream)
         line["quality"] = quality_leg(ctx, p, img64, results)
         line["bdpt"] = bdpt_leg(ctx)
         line["batch"] = batch_leg(ctx)
@@ -656,13 +761,12 @@ def main():
         line["obj_ingest"] = obj_leg()
         line["cornell"] = cornell_leg(ctx, os.cpu_count() or 1)
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        v, kind, sample, ref_build_s = cpu_sample(scene, w, h, args.cpu_budget, os.cpu_count() or 1, timing_ref=False)
-        if "update" in line and ref_build_s is not None:
+        line["cpu_baseline"] = cpu_sample(scene, args.cpu_budget)
+        if "update" in line:
             # the reference rebuilds its whole tree on every commit (pathspace.cpp:292-328)
-            line["update"]["reference_commit_ms"] = {"value": ref_build_s * 1e3, "kind": kind, "threads": 1,
+            line["update"]["reference_commit_ms"] = {"value": reference_commit_s(scene) * 1e3, "kind": "port",
+                                                     "threads": 1,
                                                      "note": "the reference's tree build restated (oracle), one thread"}
-        line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": os.cpu_count() or 1, "kind": kind,
-                                "sample": sample}
     if rank == 0:
         print(json.dumps(line))
     ctx.close()

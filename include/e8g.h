@@ -341,7 +341,14 @@ e8g_status e8g_wavefront_set(e8g_ctx *ctx, uint32_t capacity, uint32_t bounces_p
  *   - the scene must already be uploaded and built (those calls allocate, once, beforehand);
  *   - the first call on a device looks up the array's device address: make it before any
  *     stream capture;
- *   - all calls share the one array: calls that overlap on the GPU race, so serialise them.
+ *   - all calls share the one array: calls that overlap on the GPU race, so serialise them;
+ *   - E8G_INTEGRATOR_WAVEFRONT renders with the persistent megakernel here (its slot pool would
+ *     need memory); the paths, and so the image, are the ones the wavefront renders;
+ *     E8G_INTEGRATOR_PLAIN runs the plain kernel; the firefly clamp is refused
+ *     (E8G_ERR_UNSUPPORTED);
+ *   - the array's address is cached per device: a cudaDeviceReset frees the array with every
+ *     other allocation of that device, and the library must not be called on that device again
+ *     in this process.
  * Asynchronous on `stream` (NULL = the context's stream); the caller synchronises. */
 e8g_status e8g_render_dev_noalloc(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
                                   void *stream);

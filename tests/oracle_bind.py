@@ -15,6 +15,38 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "libe8oracle.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libe8ref.so")
 REF_TIMING_LIB = os.path.join(ORACLE_DIR, "_ref", "libe8ref_timing.so")
+SCENEGEN_LIB = os.path.join(ORACLE_DIR, "libe8scenegen.so")
+# The reference checkout: E8G_REFERENCE_ROOT, by default /root/reference. Where there is none, the
+# unmodified copy of its corelib sources that `make -C oracle ship` puts in the git-ignored
+# reference install folder (baseline/_ref) stands in for it.
+REFERENCE_ROOT = os.environ.get("E8G_REFERENCE_ROOT", "/root/reference")
+SHIPPED_ROOT = os.path.join(ROOT, "baseline", "_ref")
+
+
+def reference_root():
+    """The reference checkout, else the shipped copy, else None."""
+    for r in (REFERENCE_ROOT, SHIPPED_ROOT):
+        if os.path.isfile(os.path.join(r, "corelib", "src", "renderer.cpp")):
+            return r
+    return None
+
+
+def reference_src():
+    r = reference_root()
+    return os.path.join(r, "corelib", "src") if r else None
+
+
+def reference_testdata(name):
+    """A folder of the reference's testdata/ (checkout or shipped copy), or None."""
+    for r in (REFERENCE_ROOT, SHIPPED_ROOT):
+        d = os.path.join(r, "testdata", name)
+        if os.path.isdir(d):
+            return d
+    return None
+
+
+def build_reference():
+    subprocess.run(["make", "-s", "-j2", "-C", ORACLE_DIR, "ref"], check=True)
 
 
 class OHit(C.Structure):
@@ -82,6 +114,21 @@ def oracle():
             f.argtypes = a
         _oracle = lib
     return _oracle
+
+
+_scenegen = None
+
+
+def scenegen():
+    """The seeded scene generators built on their own (oracle/libe8scenegen.so, from the same
+    source as the GPU library's), for processes that time the reference on the host cores and
+    must not map the GPU library. Pass it as `lib=` to x3dcore2_gb300.scene's generators."""
+    global _scenegen
+    if _scenegen is None:
+        if not os.path.exists(SCENEGEN_LIB):
+            subprocess.run(["make", "-s", "-C", ORACLE_DIR, "gen"], check=True)
+        _scenegen = abi.load(SCENEGEN_LIB)
+    return _scenegen
 
 
 _refs = {}

@@ -22,7 +22,7 @@ def test_adapters_pack_the_reference_scene(tmp_path, reference, oracle, lib):
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", src,
            os.path.join(ROOT, "x3dcore2_gb300", "adapters", "e8g_corelib.cpp"),
            f"-I{os.path.join(ROOT, 'include')}", f"-I{os.path.join(ROOT, 'x3dcore2_gb300', 'adapters')}",
-           f"-I{ob.ORACLE_DIR}", "-I/root/reference/corelib/src", f"-I{os.path.join(ob.ORACLE_DIR, 'qt_stub')}",
+           f"-I{ob.ORACLE_DIR}", f"-I{ob.reference_src()}", f"-I{os.path.join(ob.ORACLE_DIR, 'qt_stub')}",
            ob.REF_LIB, ob.ORACLE_LIB, os.path.join(ROOT, "x3dcore2_gb300", "libe8g.so"),
            f"-Wl,-rpath,{os.path.dirname(ob.REF_LIB)}:{ob.ORACLE_DIR}:{os.path.join(ROOT, 'x3dcore2_gb300')}",
            "-lpthread", "-o", str(exe)]

@@ -78,3 +78,15 @@ def test_stale_graph_and_bad_shapes_are_refused():
         AG.render(ctx, params(2, 2), torch.zeros(3, 3), r, base=base)
     with pytest.raises(ValueError):
         AG.render(ctx, params(2, 2), a, torch.zeros(2, 1), base=base)
+
+
+def test_image_and_gradients_follow_the_tensors_dtype():
+    base = [material(abi.MAT_OREN_NAYAR, [0.5, 0.5, 0.5], 0.0), material(abi.MAT_COOK_TORR, [0.5, 0.4, 0.3], 0.2)]
+    ctx = FakeCtx(base)
+    a = torch.full((2, 3), 0.5, dtype=torch.float64, requires_grad=True)
+    r = torch.full((2,), 0.3, dtype=torch.float32, requires_grad=True)
+    img = AG.render(ctx, params(2, 2), a, r, base=base)
+    assert img.dtype == torch.float64 and img.device == a.device
+    img.sum().backward()
+    assert a.grad.dtype == torch.float64 and r.grad.dtype == torch.float32
+    np.testing.assert_array_equal(a.grad.numpy(), np.full((2, 3), 2.0))

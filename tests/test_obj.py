@@ -14,7 +14,7 @@ import oracle_bind as ob
 from x3dcore2_gb300 import scene as S
 from x3dcore2_gb300.abi import E8GError
 
-REF_TESTDATA = "/root/reference/testdata/cornellbox"
+REF_TESTDATA = ob.reference_testdata("cornellbox")
 
 
 def mine(text):
@@ -81,7 +81,7 @@ def test_obj_loader_matches_live_reference_random(lib, reference, tmp_path):
     assert loaded >= 40
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_TESTDATA), reason="reference test data not on this machine")
+@pytest.mark.skipif(REF_TESTDATA is None, reason="reference test data not on this machine")
 def test_obj_loader_matches_live_reference_on_its_test_data(lib, reference):
     names = sorted(f for f in os.listdir(REF_TESTDATA) if f.endswith(".obj"))
     assert len(names) == 8

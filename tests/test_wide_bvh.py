@@ -105,3 +105,20 @@ def test_grid_floor_ceil_is_exact(tmp_path):
         fq = q.numerator // q.denominator
         cq = -((-q.numerator) // q.denominator)
         assert (fl[i], cl[i]) == (fq, cq), (v[i], org[i], e[i], fl[i], cl[i], fq, cq)
+
+
+def test_build_flags_keep_exact_float_arithmetic():
+    """The device copy of the exact plane arithmetic (bvh_boxes.h) is compiled by nvcc; its
+    exactness needs FMA contraction off, no flush-to-zero and IEEE division and square root. The
+    build refuses flags that break that."""
+    import pytest
+
+    from x3dcore2_gb300 import build as B
+    B.check_exact_flags()
+    for extra in (["--use_fast_math"], ["-ftz=true"], ["--prec-div=false"]):
+        with pytest.raises(RuntimeError):
+            B.check_exact_flags(B.NVFLAGS + extra)
+    with pytest.raises(RuntimeError):
+        B.check_exact_flags([f for f in B.NVFLAGS if f != "--fmad=false"])
+    with pytest.raises(RuntimeError):
+        B.check_exact_flags(None, B.CXXFLAGS + ["-ffast-math"])

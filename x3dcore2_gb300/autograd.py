@@ -2,10 +2,12 @@
 
 `render(ctx, params, albedo, roughness)` renders the uploaded scene with per-material albedo
 (num_materials, 3) and roughness (num_materials,) taken from the tensors, and returns the
-(height, width, 3) float32 image; its backward replays every path on the device and returns
+(height, width, 3) image; its backward replays every path on the device and returns
 dLoss/d(albedo) and dLoss/d(roughness). Only Oren-Nayar and Cook-Torrance materials take the
 tensors' values (the fail-safe and mixture entries keep theirs and get zero gradients), as
-e8g_backward defines. The tensors live on the host; the device work stays inside the library.
+e8g_backward defines. The tensors may live on any device and in any floating dtype: their values
+cross the C ABI as host float32, the image comes back on albedo's device and dtype, and each
+gradient on its own tensor's device and dtype.
 
 e8g_backward replays the last e8g_forward of its context, so a graph's backward must run before
 another differentiable render on the same context; the binding checks this and raises.
@@ -35,7 +37,9 @@ class _Render(torch.autograd.Function):
         fctx.core = ctx
         fctx.token = ctx._adjoint_token
         fctx.shape = (params.height, params.width)
-        return torch.from_numpy(np.ascontiguousarray(img[..., :3]))
+        fctx.like = ((albedo.device, albedo.dtype), (roughness.device, roughness.dtype))
+        out = torch.from_numpy(np.ascontiguousarray(img[..., :3]))
+        return out.to(device=albedo.device, dtype=albedo.dtype)
 
     @staticmethod
     def backward(fctx, grad_img):
@@ -45,7 +49,9 @@ class _Render(torch.autograd.Function):
         h, w = fctx.shape
         g = grad_img.detach().to(torch.float32).cpu().numpy().reshape(h, w, 3)
         da, dr = ctx.backward(g)
-        return torch.from_numpy(da), torch.from_numpy(dr), None, None, None
+        (ad, at), (rd, rt) = fctx.like
+        return (torch.from_numpy(da).to(device=ad, dtype=at), torch.from_numpy(dr).to(device=rd, dtype=rt),
+                None, None, None)
 
 
 def render(ctx, params, albedo, roughness, base=None):

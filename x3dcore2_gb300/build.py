@@ -25,6 +25,28 @@ NVFLAGS = ["-std=c++17", "-O3", ARCH, "-lineinfo", "--fmad=false", "-Xcompiler",
            "-Xptxas", "-warn-spills", f"-I{os.path.join(ROOT, 'include')}"]
 
 
+# The exact single-precision arithmetic of the tree boxes (bvh_boxes.h: the TwoSum plane
+# differences and power-of-two scalings that make device refits equal host builds byte for byte)
+# and the reference's operation order in the bit-exact modes hold only without FMA contraction,
+# without flush-to-zero and without approximate division or square root. Nothing in the device
+# code can detect these flags, so the build refuses to run with them.
+_FORBIDDEN_NVFLAGS = ("--use_fast_math", "-use_fast_math", "--ftz=true", "-ftz=true", "--prec-div=false",
+                      "-prec-div=false", "--prec-sqrt=false", "-prec-sqrt=false", "--fmad=true", "-fmad=true")
+
+
+def check_exact_flags(nvflags=None, cxxflags=None):
+    """Raises if the flags would break the exact arithmetic the trees and bit-exact modes need."""
+    nv = NVFLAGS if nvflags is None else nvflags
+    cx = CXXFLAGS if cxxflags is None else cxxflags
+    bad = [f for f in nv if f in _FORBIDDEN_NVFLAGS]
+    if "--fmad=false" not in nv:
+        bad.append("missing --fmad=false")
+    if "-ffp-contract=off" not in cx or any(f in cx for f in ("-ffast-math", "-Ofast")):
+        bad.append("host flags need -ffp-contract=off and no fast math")
+    if bad:
+        raise RuntimeError("build flags break exact float arithmetic: " + ", ".join(bad))
+
+
 def _nvcc():
     p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(p):
@@ -47,6 +69,7 @@ def _compile(cmd):
 
 
 def build(verbose=False, jobs=None):
+    check_exact_flags()
     os.makedirs(BUILD, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         [os.path.join(ROOT, "include", "e8g.h")]
