@@ -46,14 +46,27 @@ REF_ESTIMATOR = dict(name="unidirect_lt1 (the reference's direct-lighting tracer
 # each axis, so its pixels are spread uniformly over the whole 1920x1080 view (sky included).
 REF_SAMPLE_W, REF_SAMPLE_H = 480, 270
 # DRAM traffic per path of a (tree, integrator) combination, from the ncu captures summarised in
-# profiles/: dram__bytes_read.sum + dram__bytes_write.sum over one frame of a 480x270, 8-spp
-# render of the same scene divided by its 1,036,800 paths, scaled to the full frame by its path
-# count. SAH pairs + megakernel: 212.6 MB + 12.5 MB (profiles/megakernel_icosphere_l8.md);
-# eight-wide tree + wavefront: 7.59 GB over the 62 launches of a 1080p 8-spp frame of the same
-# scene, 16.6 M paths in steady state (shade, the combined trace kernel, first hits, resolve;
-# profiles/wavefront_wide_icosphere_l8.md).
-TRAFFIC_BYTES_PER_PATH = {("sah", "megakernel"): 217.1, ("wide", "wavefront"): 457.7}
+# profiles/ (dram__bytes_read.sum + dram__bytes_write.sum divided by the paths of the captured
+# frame, scaled to the timed frame by its path count): "kernel" is the dominant kernel alone, "loop"
+# every kernel of the integrator. SAH pairs + megakernel: one 480x270, 8-spp frame (1,036,800
+# paths; profiles/megakernel_icosphere_l8.md). Eight-wide tree + wavefront: the launches of a
+# 1080p 8-spp frame (16,588,800 paths in steady state; profiles/wavefront_wide_icosphere_l8.md).
+TRAFFIC_BYTES_PER_PATH = {("sah", "megakernel"): {"kernel": 217.1, "loop": 217.1},
+                          ("wide", "wavefront"): {"kernel": 206.3, "loop": 457.7}}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
+
+
+def l2_read_peak(ctx):
+    """The L2 read bandwidth of this GPU (GB/s, best of three) from the library's own streaming
+    kernel over a 64 MiB buffer (e8g_l2_read_bandwidth)."""
+    from x3dcore2_gb300 import abi
+    lib = abi.load()
+    best = 0.0
+    for _ in range(3):
+        v = C.c_double()
+        abi.check(lib.e8g_l2_read_bandwidth(ctx.h, 64 << 20, 20, C.byref(v)), ctx.h, "e8g_l2_read_bandwidth")
+        best = max(best, v.value)
+    return best
 
 
 def read_peaks():
@@ -221,8 +234,8 @@ def reference_commit_s(scene):
 def like_for_like_leg(ctx, w, h, spp, d_img, stream):
     """The GPU on the host arm's estimator: E8G_MODE_REF_LT1 (unidirect_lt1 step for step, minstd
     streams) with the reference's own policy (Russian roulette from depth 2 at p = 0.5, no depth cap)
-    over the whole benchmark frame, on the tree the headline used, plain and megakernel (the
-    wavefront runs MIS only). Device time per frame, L2 flushed between frames."""
+    over the whole benchmark frame, plain and megakernel (the wavefront runs MIS only) on both fast
+    trees. Device time per frame, L2 flushed between frames. Leaves the SAH pairs built."""
     import torch
     from x3dcore2_gb300 import abi
     from x3dcore2_gb300.core import default_params
@@ -230,20 +243,26 @@ def like_for_like_leg(ctx, w, h, spp, d_img, stream):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     out = {"mode": "E8G_MODE_REF_LT1", "policy": {"max_depth": p.max_depth, "rr_start": p.rr_start,
                                                   "rr_prob": p.rr_prob}, "width": w, "height": h, "spp": spp}
-    for integ in ("plain", "megakernel"):
-        p.integrator = INTEGRATORS[integ]
-        for _ in range(2):
-            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
-        ms = []
-        for _ in range(3):
-            flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
-            b.record(stream)
-            b.synchronize()
-            ms.append(a.elapsed_time(b))
-        out[integ] = {"ms": statistics.mean(ms), "paths_per_s": w * h * spp / (statistics.mean(ms) / 1e3)}
+    best = 0.0
+    for lay, code in (("wide", abi.BVH_WIDE), ("sah", abi.BVH_SAH)):
+        ctx.build_bvh(layout=code)
+        for integ in ("plain", "megakernel"):
+            p.integrator = INTEGRATORS[integ]
+            for _ in range(2):
+                ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+            ms = []
+            for _ in range(3):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.render_dev(p, d_img.data_ptr(), stream.cuda_stream)
+                b.record(stream)
+                b.synchronize()
+                ms.append(a.elapsed_time(b))
+            v = w * h * spp / (statistics.mean(ms) / 1e3)
+            out[f"{lay}/{integ}"] = {"ms": statistics.mean(ms), "paths_per_s": v}
+            best = max(best, v)
+    out["best_paths_per_s"] = best
     del flush
     return out
 
@@ -540,7 +559,7 @@ def mapped_repo_libraries():
 
 def run_reference_arm(args):
     """The reference's own CPU tracer on the host cores (see ref_tracer): one step renders the
-    host sample of the frame at one sample per host thread. Never maps the GPU library."""
+    host sample of the frame at two samples per host thread. Never maps the GPU library."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
@@ -549,7 +568,7 @@ def run_reference_arm(args):
     subprocess.run(["make", "-s", "-C", ob.ORACLE_DIR, "all", "gen"], check=True)
     scene = ref_scene_host(args.small)
     render, kind, threads, sample = ref_tracer(scene)
-    spp = threads
+    spp = 2 * threads  # about 0.75 s of the reference per step on 16 Grace cores
     for _ in range(args.warmup):
         render(spp)
     secs = paths = 0
@@ -650,6 +669,9 @@ def main():
                                for i in range(r.num_candidates)]}
 
     results, tunes, trees = {}, {}, {}
+    # the wavefront records CUDA events around its trace and shading kernels in every bounce graph
+    # (the per-kernel times of the roofline); the other integrators run one kernel each
+    ctx.set_kernel_timing(True)
     clocks = ClockSampler(local)
     clocks.start()
     for lay in layouts:
@@ -666,7 +688,7 @@ def main():
             barrier()
             starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
             ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-            kernel_ms, launches = [], 0
+            kernel_ms, launches, trace_ms, shade_ms, trace_launches = [], 0, [], [], 0
             for k in range(args.steps):
                 flush.zero_()  # L2 flush between timed steps (outside the event pair)
                 starts[k].record(stream)
@@ -674,6 +696,9 @@ def main():
                 ends[k].record(stream)
                 st = ctx.stats()
                 kernel_ms.append(st["kernel_ms"])
+                trace_ms.append(st["trace_ms"])
+                shade_ms.append(st["shade_ms"])
+                trace_launches += st["trace_launches"]
                 launches += st["launches"]
             barrier()
             total_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends))
@@ -683,6 +708,9 @@ def main():
                 total_ms = float(t.item())
             results[(lay, integ)] = dict(ms_per_step=total_ms / args.steps, kernel_ms=statistics.mean(kernel_ms),
                                          launches=launches)
+            if integ == "wavefront":
+                results[(lay, integ)].update(trace_ms=statistics.mean(trace_ms), shade_ms=statistics.mean(shade_ms),
+                                             trace_launches_per_step=trace_launches / args.steps)
     clk = clocks.stop()
     paths_per_step = w * h * spp
     for r in results.values():
@@ -717,14 +745,23 @@ def main():
     e2e_value = paths_per_step * world / (statistics.mean(e2e_ms) / 1000.0)
 
     peak, peak_kind = read_peaks()
-    mean_kernel_ms = results[best]["kernel_ms"]
+    l2_peak = l2_read_peak(ctx)
+    rb = results[best]
+    loop_ms = rb["kernel_ms"]  # the integrator's whole device time per frame (first hits and resolve excluded)
     node_bytes = bvh["node_bytes"] // max(bvh["num_nodes"], 1)  # 32 (binary node) or 96 (wide node)
     alg_bytes = node_bytes * counts["nodes"] + 48 * counts["tris"]
-    achieved = alg_bytes / (mean_kernel_ms / 1000.0) / 1e9
     per_path = TRAFFIC_BYTES_PER_PATH.get(best)
-    traffic = per_path * paths_per_step if per_path else None
-    roof_kernel = {"plain": "k_plain (baseline per-path kernel)", "megakernel": "k_mega (megakernel)",
-                   "wavefront": "wavefront kernels (whole bounce loop: shade + trace)"}[best_integ]
+    if best_integ == "wavefront":
+        # the dominant kernel is the trace kernel: every traversal byte is fetched there
+        dom_ms, dom_launches = rb["trace_ms"], rb["trace_launches_per_step"]
+        dom_name = ("k_wf_trace_wide_both (extension and shadow rays of a bounce, eight-wide tree)" if best_lay == "wide"
+                    else "k_wf_trace_dyn (extension and shadow rays, SAH pairs)")
+    else:
+        dom_ms, dom_launches = loop_ms, 1
+        dom_name = {"plain": "k_plain (baseline per-path kernel)", "megakernel": "k_mega (megakernel)"}[best_integ]
+    achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
+    achieved_loop = alg_bytes / (loop_ms / 1000.0) / 1e9
+    traffic = per_path["kernel"] * paths_per_step / dom_launches if per_path else None
     commit_s = trees[best_lay]["build_s"]
 
     line = {
@@ -745,14 +782,26 @@ def main():
                 "d2h_bytes_per_step": w * h * 16},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": roof_kernel, "kernel_ms": mean_kernel_ms, "node_bytes": node_bytes,
-                     "algorithmic_bytes": alg_bytes, "rays": counts["rays"], "nodes": counts["nodes"],
-                     "tris": counts["tris"], "rays_per_s": counts["rays"] / (mean_kernel_ms / 1000.0)},
+                     "kernel": dom_name, "kernel_ms_per_step": dom_ms, "launches_per_step": dom_launches,
+                     "algorithmic_bytes_per_launch": alg_bytes / dom_launches,
+                     "avg_launch_ms": dom_ms / dom_launches,
+                     "l2_peak": l2_peak, "frac_l2": achieved / l2_peak if l2_peak else None,
+                     "node_bytes": node_bytes, "algorithmic_bytes_per_step": alg_bytes, "rays": counts["rays"],
+                     "nodes": counts["nodes"], "tris": counts["tris"],
+                     "traffic_note": "DRAM bytes per launch from the ncu capture summarised in profiles/ "
+                                     "(per path, scaled by the paths of a launch)"},
+        "roofline_loop": {"achieved": achieved_loop, "unit": "GB/s", "frac": achieved_loop / peak,
+                          "frac_l2": achieved_loop / l2_peak if l2_peak else None, "loop_ms_per_step": loop_ms,
+                          "trace_ms_per_step": rb.get("trace_ms"), "shade_ms_per_step": rb.get("shade_ms"),
+                          "traffic": per_path["loop"] * paths_per_step if per_path else None,
+                          "note": "the same algorithmic bytes over the integrator's whole device time per frame "
+                                  "(shading included)"},
         "gpu_launches": launches,
         "clocks": clk,
     }
     if rank == 0 and not args.no_extras and world == 1:
         line["like_for_like"] = like_for_like_leg(ctx, w, h, spp, d_img, stream)
+        build(best_lay)
         line["quality"] = quality_leg(ctx, p, img64, results)
         line["bdpt"] = bdpt_leg(ctx)
         line["batch"] = batch_leg(ctx)

@@ -242,6 +242,11 @@ typedef struct e8g_render_stats {
     uint64_t tris;      /* triangles tested (when counted) */
     uint32_t launches;  /* kernels launched by the call */
     uint32_t counted;   /* 1 when rays/nodes/tris are filled */
+    double trace_ms;    /* wavefront only, with e8g_set_kernel_timing on: device time of its trace
+                           kernels over the render (CUDA events around each launch); else 0 */
+    double shade_ms;    /* the same for its shading kernels (queue reset included) */
+    uint32_t trace_launches; /* trace kernels the wavefront launched (when timed) */
+    uint32_t pad_;
 } e8g_render_stats;
 
 /* ------------------------------------------------------------ batch ---- */
@@ -305,6 +310,14 @@ e8g_status e8g_render_dev(e8g_ctx *ctx, const e8g_render_params *params, float *
 e8g_status e8g_render_progressive(e8g_ctx *ctx, const e8g_render_params *params, int reset, float *d_rgba_out,
                                   void *stream);
 e8g_status e8g_get_render_stats(const e8g_ctx *ctx, e8g_render_stats *stats);
+/* Nonzero: the wavefront integrator records CUDA events around its shading and trace kernels of
+ * every bounce (event-record nodes in its bounce graph) and fills trace_ms / shade_ms of the
+ * render stats. A measurement aid with no counterpart in the reference; off by default. */
+e8g_status e8g_set_kernel_timing(e8g_ctx *ctx, int on);
+/* Measurement aid: the GPU's L2 read bandwidth in GB/s (*gbs), from `reps` passes of a streaming
+ * kernel over a buffer of `bytes` (>= 1 MiB, allocated and freed by the call) that fits in L2 —
+ * the second denominator of the traversal roofline. No counterpart in the reference. */
+e8g_status e8g_l2_read_bandwidth(e8g_ctx *ctx, uint64_t bytes, uint32_t reps, double *gbs);
 
 /* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity
  * {2^20 .. 2^24}, bounces per graph {2, 4} and warp refill threshold {4, 8, 12, 16, 24} (the

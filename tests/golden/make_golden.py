@@ -55,6 +55,24 @@ def paths_fixture(name, sc, w, h, npaths, seed, modes, rng_seed=0):
     print(name, {k: v.shape for k, v in out.items() if hasattr(v, "shape")})
 
 
+def mixture_scene():
+    """The Cornell room with the reference's composite materials on its surfaces: a wall without a
+    material (the fail-safe Lambert, material.cpp:54-76), mixtures (mat_mixture, :78-106) of a
+    Lambert wall with a GGX metal and of that metal with a rough Oren-Nayar, and a plain metal
+    box."""
+    sc = S.cornell(64, 48)
+    mats = sc.material_list() + [
+        S.material(abi.MAT_COOK_TORR, (0.8, 0.7, 0.5), 0.3, (2.5, 0.0)),     # 4
+        S.material(abi.MAT_OREN_NAYAR, (0.4, 0.6, 0.8), 0.2),                # 5
+        S.material(abi.MAT_MIXTURE, mix=(4, 5), ratio=0.35),                 # 6
+        S.material(abi.MAT_MIXTURE, mix=(0, 4), ratio=0.7),                  # 7
+    ]
+    mm = np.array(sc.mesh_mat, np.int32).copy()
+    mm[1], mm[2], mm[5], mm[6] = -1, 7, 6, 4
+    return S.Scene(sc.voff, sc.toff, mm, sc.pos, sc.nrm, sc.tris, mats, list(sc.lights[:sc.num_lights]),
+                   sc.camera)
+
+
 def bsdf_fixture():
     # tst_material.cpp:28-179: cook_torr(0.787, r 0.2/0.25, ior 2.93) and oren_nayar(sigma 0.078)
     mats = [S.material(abi.MAT_COOK_TORR, (0.787, 0.787, 0.787), 0.25, (2.93, 0.0)),
@@ -224,6 +242,7 @@ def main(only=()):
                                      48, 27, 384, 3, ["uni", "lt1", "bdpt", "direct", "lt2"]),
         "soup": lambda: paths_fixture("soup.npz", S.soup(3000, seed=2, width=40, height=40), 40, 40, 256, 9,
                                       ["lt1", "bdpt", "direct", "lt2"]),
+        "mixture": lambda: paths_fixture("mixture.npz", mixture_scene(), 64, 48, 768, 13, all_modes, rng_seed=4),
         "renderer": renderer_fixture,  # reads cornell.npz, so it runs after it
         "composite": composite_fixture,
         "transform": transform_fixture,

@@ -1,7 +1,10 @@
 """Per-path radiance on the GPU fed the reference's own draw stream (one std::minstd_rand0
 stream per path, seeded like the golden fixtures): must match the compiled reference's radiance
-within 1e-4 relative on >= 99% of paths. Paths that differ are the ones where CUDA's sinf/cosf/
-atanf (<= 2 ulp) moved a direction across a triangle edge or a sampling branch."""
+within 1e-4 relative on >= 99.9% of paths (99.5% for the bidirectional tracers, whose paths
+evaluate several times more transcendentals). Paths that differ are the ones where CUDA's sinf/
+cosf/atanf (<= 2 ulp) moved a direction across a triangle edge or a sampling branch. The mixture
+fixture holds the reference's composite materials: mat_mixture and the fail-safe Lambert of a
+mesh without a material (material.cpp:54-106)."""
 import numpy as np
 import pytest
 
@@ -23,7 +26,7 @@ def match_fraction(a, b, rtol=RTOL, atol=1e-6):
     return np.all(ok, axis=1).mean()
 
 
-@pytest.mark.parametrize("name", ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz"])
+@pytest.mark.parametrize("name", ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz", "mixture.npz"])
 def test_paths_match_reference_golden(ctx, name):
     d = G.load(name)
     ctx.upload(G.scene_from(d), layout=abi.BVH_REFERENCE)
@@ -36,7 +39,8 @@ def test_paths_match_reference_golden(ctx, name):
         frac = match_fraction(got, d["rad_" + mname])
         # BDPT on the closed furnace sphere chains 16 BSDF samples per path; an ulp difference in
         # sinf/cosf (CUDA vs glibc, neither correctly rounded) moves more of those paths
-        need = 0.98 if mname == "bdpt" else 0.99
+        need = 0.995 if mname in ("bdpt", "lt2") else 0.999
+        print(f"{name} {mname}: {frac:.5f} of paths within {RTOL}")
         assert frac >= need, (name, mname, frac)
 
 
@@ -57,7 +61,8 @@ def test_bdpt_paths_match_oracle(ctx, max_len):
     got = ctx.render_paths(p, px, samples)
     seeds = np.array([ob.oracle().o_path_seed(5, int(a), int(b)) for a, b in zip(px, samples)], np.uint32)
     ref = osc.render_paths(abi.MODE_REF_BDPT, w, h, px, seeds, policy=ob.OPolicy(0, 2, 0.5, max_len))
-    assert match_fraction(got, ref) >= 0.99
+    frac = match_fraction(got, ref)
+    assert frac >= 0.995, frac
 
 
 @pytest.mark.parametrize("pol", POLICIES)
@@ -81,7 +86,7 @@ def test_paths_match_oracle_with_policies(ctx, pol, mode, rng):
     else:
         ref = osc.render_paths(mode, w, h, px, samples, policy=opol, rng=abi.RNG_PHILOX, seed=seed)
     frac = match_fraction(got, ref)
-    assert frac >= 0.99, frac
+    assert frac >= 0.999, frac
 
 
 def test_philox_stream_matches_oracle(ctx):
@@ -128,7 +133,8 @@ def test_wavefront_paths_match_oracle(ctx, rng, layout):
         ref = osc.render_paths(abi.MODE_MIS, w, h, px, seeds, policy=pol)
     else:
         ref = osc.render_paths(abi.MODE_MIS, w, h, px, samples, policy=pol, rng=abi.RNG_PHILOX, seed=31)
-    assert match_fraction(got, ref) >= 0.99
+    frac = match_fraction(got, ref)
+    assert frac >= 0.999, frac
 
 
 @pytest.mark.parametrize("rng", [abi.RNG_PHILOX, abi.RNG_MINSTD])
@@ -151,7 +157,8 @@ def test_bdpt_power_paths_match_oracle(ctx, rng, max_len):
         ref = osc.render_paths(abi.MODE_BDPT_POWER, w, h, px, seeds, policy=pol)
     else:
         ref = osc.render_paths(abi.MODE_BDPT_POWER, w, h, px, samples, policy=pol, rng=abi.RNG_PHILOX, seed=17)
-    assert match_fraction(got, ref) >= 0.99
+    frac = match_fraction(got, ref)
+    assert frac >= 0.995, frac
 
 
 @pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_MIS, abi.MODE_REF_BDPT, abi.MODE_REF_LT2])

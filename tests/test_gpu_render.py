@@ -21,8 +21,9 @@ def rel_mse(img, ref, eps=1e-2):
 @pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_REF_UNI, abi.MODE_MIS, abi.MODE_REF_DIRECT,
                                   abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER, abi.MODE_REF_LT2])
 def test_image_matches_oracle_same_streams(ctx, mode, layout):
-    """Same draw streams: >= 98% of pixels agree to 1e-4; the rest are pixels with a path that
-    took another branch after a last-ulp difference (sinf/cosf/atanf) or an edge tie."""
+    """Same draw streams: >= 99.5% of pixels (8 paths each) agree to 1e-4; the rest are pixels
+    with a path that took another branch after a last-ulp difference (sinf/cosf/atanf) or an edge
+    tie."""
     sc = S.cornell(48, 40)
     ctx.upload(sc, layout=layout)
     osc = ob.OracleScene(sc)
@@ -32,7 +33,7 @@ def test_image_matches_oracle_same_streams(ctx, mode, layout):
     ref = osc.render(mode, 48, 40, 8, seed=9, policy=pol, rng=p.rng)[..., :3]
     assert np.all(np.isfinite(img)) and np.all(img >= 0)
     close = np.all(np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-6), axis=-1)
-    assert close.mean() >= 0.98, close.mean()
+    assert close.mean() >= 0.995, close.mean()
     assert rel_mse(img, ref) < 2e-3, rel_mse(img, ref)
 
 
@@ -181,7 +182,7 @@ def test_firefly_clamp_matches_oracle(ctx, mode, rng):
         ob.firefly_add(est.reshape(h, w, 3), acc)
     ref = acc * np.float32(1.0 / spp)
     close = np.all(np.abs(got - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-6), axis=-1)
-    assert close.mean() >= 0.98, close.mean()
+    assert close.mean() >= 0.995, close.mean()
     assert not np.allclose(got, plain)
 
 
@@ -239,3 +240,49 @@ def test_wavefront_set_pins_the_configuration(ctx):
         assert close.mean() >= 0.999
     for bad in ((512, 2, 12), (1 << 20, 0, 12), (1 << 20, 2, 33)):
         assert ctx.lib.e8g_wavefront_set(ctx.h, *bad) == 1  # E8G_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("layout", [abi.BVH_SAH, abi.BVH_WIDE])
+@pytest.mark.parametrize("mode", [abi.MODE_REF_LT1, abi.MODE_MIS, abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER])
+def test_mixture_and_fail_safe_image_matches_oracle(ctx, mode, layout):
+    """The mixture fixture's room (a wall without a material, mixtures of a Lambert wall with a
+    GGX metal and of that metal with a rough Oren-Nayar, material.cpp:54-106) rendered as a whole
+    image on the fast trees: equal to the oracle's image of the same streams (the oracle equals
+    the compiled reference on this scene path for path)."""
+    d = G.load("mixture.npz")
+    sc = G.scene_from(d)
+    w, h = int(d["width"]), int(d["height"])
+    ctx.upload(sc, layout=layout)
+    osc = ob.OracleScene(sc)
+    p = default_params(mode, w, h, 4, seed=21, max_depth=6 if mode == abi.MODE_MIS else 0, bdpt_max_len=6)
+    img = ctx.render(p)[..., :3]
+    pol = ob.OPolicy(p.max_depth, p.rr_start, p.rr_prob, p.bdpt_max_len)
+    ref = osc.render(mode, w, h, 4, seed=21, policy=pol, rng=p.rng)[..., :3]
+    assert np.all(np.isfinite(img)) and np.all(img >= 0) and img.sum() > 0
+    close = np.all(np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-6), axis=-1)
+    print(f"mixture image mode {mode} layout {layout}: {close.mean():.5f} of pixels within 1e-4")
+    assert close.mean() >= 0.995, close.mean()
+
+
+def test_wavefront_kernel_timing_leaves_the_image_and_fills_the_stats(ctx):
+    """e8g_set_kernel_timing: event records in the bounce graph time the trace and shading kernels;
+    the image is the untimed one (identical paths), the kernel times fit inside the render's."""
+    import ctypes as C
+    sc = S.cornell(96, 64)
+    ctx.upload(sc, layout=abi.BVH_WIDE)
+    p = default_params(abi.MODE_MIS, 96, 64, 8, seed=3, max_depth=6, integrator=abi.INTEGRATOR_WAVEFRONT)
+    plain = ctx.render(p)
+    assert ctx.stats()["trace_ms"] == 0.0
+    ctx.set_kernel_timing(True)
+    try:
+        timed = ctx.render(p)
+        st = ctx.stats()
+    finally:
+        ctx.set_kernel_timing(False)
+    close = np.all(np.abs(timed - plain) <= np.maximum(1e-4 * np.abs(plain), 1e-6), axis=-1)
+    assert close.mean() >= 0.999
+    assert st["trace_ms"] > 0 and st["shade_ms"] > 0 and st["trace_launches"] > 0
+    assert st["trace_ms"] + st["shade_ms"] <= st["kernel_ms"] * 1.001
+    gbs = C.c_double()
+    assert ctx.lib.e8g_l2_read_bandwidth(ctx.h, 64 << 20, 4, C.byref(gbs)) == 0
+    assert 1000 < gbs.value < 100000, gbs.value  # GB/s: far above HBM's few TB/s, below nonsense

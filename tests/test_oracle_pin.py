@@ -17,7 +17,7 @@ from x3dcore2_gb300 import scene as S
 EXACT = platform.machine() in ("x86_64", "AMD64")
 MODES = {"uni": abi.MODE_REF_UNI, "lt1": abi.MODE_REF_LT1, "bdpt": abi.MODE_REF_BDPT,
          "direct": abi.MODE_REF_DIRECT, "normal": abi.MODE_NORMAL, "position": abi.MODE_POSITION, "lt2": abi.MODE_REF_LT2}
-FIXTURES = ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz"]
+FIXTURES = ["cornell.npz", "furnace.npz", "ico.npz", "soup.npz", "mixture.npz"]
 
 
 def agree(a, b, rtol=1e-4, frac=0.995):

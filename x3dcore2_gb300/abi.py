@@ -95,7 +95,8 @@ class RenderParams(C.Structure):
 class RenderStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("kernel_ms", C.c_double), ("paths", C.c_uint64),
                 ("rays", C.c_uint64), ("nodes", C.c_uint64), ("tris", C.c_uint64),
-                ("launches", C.c_uint32), ("counted", C.c_uint32)]
+                ("launches", C.c_uint32), ("counted", C.c_uint32), ("trace_ms", C.c_double),
+                ("shade_ms", C.c_double), ("trace_launches", C.c_uint32), ("pad_", C.c_uint32)]
 
 
 class BatchItem(C.Structure):
@@ -157,6 +158,8 @@ SIGNATURES = {
     "e8g_render_dev": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_render_dev_noalloc": (_ST, [_P, C.POINTER(RenderParams), _P, _P]),
     "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
+    "e8g_set_kernel_timing": (_ST, [_P, C.c_int]),
+    "e8g_l2_read_bandwidth": (_ST, [_P, C.c_uint64, _U32, C.POINTER(C.c_double)]),
     "e8g_render_progressive": (_ST, [_P, C.POINTER(RenderParams), C.c_int, _P, _P]),
     "e8g_composite": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P]),
     "e8g_composite_dev": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P, _P]),

@@ -208,6 +208,10 @@ class Context:
         self._check(self.lib.e8g_composite(self.h, _ptr(rgba), w, h, C.byref(cp), _ptr(out)), "e8g_composite")
         return out
 
+    def set_kernel_timing(self, on=True):
+        """e8g_set_kernel_timing: the wavefront times its trace and shading kernels per bounce."""
+        self._check(self.lib.e8g_set_kernel_timing(self.h, int(on)), "e8g_set_kernel_timing")
+
     def stats(self):
         s = abi.RenderStats()
         self._check(self.lib.e8g_get_render_stats(self.h, C.byref(s)), "e8g_get_render_stats")

@@ -465,6 +465,8 @@ e8g_status e8g_destroy(e8g_ctx *c) {
         cudaEventDestroy(c->ev2);
     if (c->ev3)
         cudaEventDestroy(c->ev3);
+    for (cudaEvent_t ev : c->kt_events)
+        cudaEventDestroy(ev);
     if (c->stream)
         cudaStreamDestroy(c->stream);
     if (c->host_pinned)
@@ -765,6 +767,13 @@ e8g_status e8g_count_traversal(e8g_ctx *c, e8g_render_params const *p, e8g_rende
     c->stats.counted = 1;
     if (out)
         *out = c->stats;
+    return E8G_OK;
+}
+
+e8g_status e8g_set_kernel_timing(e8g_ctx *c, int on) {
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    c->kernel_timing = on != 0;
     return E8G_OK;
 }
 

@@ -45,6 +45,12 @@ struct e8g_ctx {
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
     uint32_t wf_capacity = 1u << 21, wf_bounces = 4, wf_threshold = 16;
+    // per-kernel timing of the wavefront (e8g_set_kernel_timing): three events per bounce of the
+    // graph (bounce start, shading done, trace done) and the sums over the current render
+    bool kernel_timing = false;
+    std::vector<cudaEvent_t> kt_events;
+    double kt_trace_ms = 0, kt_shade_ms = 0;
+    uint32_t kt_trace_launches = 0;
     void *host_pinned = nullptr;
     // progressive rendering: samples in the accumulator, and the image they belong to
     uint64_t prog_spp = 0;

@@ -92,11 +92,21 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     // capture `bounces` bounces once, replay until no slot is busy and no path is left
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    bool timed = c->kernel_timing;
+    while (timed && c->kt_events.size() < 3 * static_cast<size_t>(bounces)) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreate(&ev);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "kernel timing events");
+        c->kt_events.push_back(ev);
+    }
+    uint32_t traces_per_bounce = layout == 2 && threshold > 0 ? 1u : 2u;
     e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront capture");
     for (uint32_t k = 0; k < bounces; k++)
-        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, threshold, total, B, c->stream);
+        wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, threshold, total, B, c->stream,
+                          timed ? c->kt_events.data() + 3 * k : nullptr);
     e = cudaStreamEndCapture(c->stream, &graph);
     if (e == cudaSuccess)
         e = cudaGraphInstantiate(&exec, graph, 0);
@@ -118,6 +128,16 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
         if (e != cudaSuccess)
             break;
         c->launches += (layout == 2 && threshold > 0 ? 3 : 4) * bounces; // reset, shade, trace(s)
+        if (timed) { // the replay has finished: read its bounces' event pairs
+            for (uint32_t k = 0; k < bounces; k++) {
+                float a = 0, b = 0;
+                cudaEventElapsedTime(&a, c->kt_events[3 * k], c->kt_events[3 * k + 1]);
+                cudaEventElapsedTime(&b, c->kt_events[3 * k + 1], c->kt_events[3 * k + 2]);
+                c->kt_shade_ms += a;
+                c->kt_trace_ms += b;
+            }
+            c->kt_trace_launches += traces_per_bounce * bounces;
+        }
         if (host->busy == 0 && host->next_path >= total)
             break;
     }
@@ -155,6 +175,8 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
     if (e != cudaSuccess)
         return cuda_fail(c, e, "render clear");
     RenderArgs A = make_args(p);
+    c->kt_trace_ms = c->kt_shade_ms = 0;
+    c->kt_trace_launches = 0;
     cudaEventRecord(c->ev2, c->stream);
     if (p->firefly)
         s = run_firefly(c, p, A, static_cast<float4 *>(c->b_accum.ptr), d_counts);
@@ -187,6 +209,9 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
     c->stats.paths = npix * p->spp;
     c->stats.launches = c->launches;
     c->stats.counted = 0;
+    c->stats.trace_ms = c->kt_trace_ms;
+    c->stats.shade_ms = c->kt_shade_ms;
+    c->stats.trace_launches = c->kt_trace_launches;
     return E8G_OK;
 }
 
@@ -389,6 +414,8 @@ e8g_status e8g_backward(e8g_ctx *c, float const *dl_dimage, float *d_albedo, flo
     c->stats.kernel_ms = kms;
     c->stats.paths = npix * p.spp;
     c->stats.launches = 2;
+    c->stats.trace_ms = c->stats.shade_ms = 0;
+    c->stats.trace_launches = 0;
     return E8G_OK;
 }
 

@@ -21,6 +21,11 @@ namespace {
 
 enum : uint32_t { kEmpty = 0, kAtVertex = 1, kWaitHit = 2 };
 
+// Refill rounds per slot and bounce: a lane skips paths whose camera ray missed the scene for at
+// most this many rounds (a frame that is half sky leaves a slot empty after 8 rounds with
+// probability 1/256).
+constexpr int kRefillRounds = 8;
+
 struct Counters {
     unsigned long long next_path; // global path counter
     uint32_t shadow_n, ext_n;      // queue lengths of the current bounce
@@ -179,11 +184,16 @@ __global__ void __launch_bounds__(256, 4)
                 }
             }
         }
-        // refill empty slots, one atomic per warp
+        // refill empty slots, one atomic per warp per round. A path whose camera ray left the
+        // scene (its cached first hit is a miss) has no vertex and contributes nothing, so the
+        // lane draws again, up to kRefillRounds rounds, instead of leaving the slot idle for the
+        // whole bounce; the megakernel's refill does the same.
         bool want = in && state == kEmpty;
         bool refilled = false;
-        uint32_t mask = __ballot_sync(~0u, want);
-        if (mask) {
+        for (int round = 0; round < kRefillRounds; round++) {
+            uint32_t mask = __ballot_sync(~0u, want);
+            if (!mask)
+                break;
             int leader = __ffs(mask) - 1;
             unsigned long long base = 0;
             if (static_cast<int>(lane_id()) == leader)
@@ -191,40 +201,46 @@ __global__ void __launch_bounds__(256, 4)
             base = __shfl_sync(~0u, base, leader);
             if (want) {
                 uint64_t idx = base + __popc(mask & ((1u << lane_id()) - 1u));
-                uint32_t nsid = 0;
-                uint64_t local = idx, pbase = 0;
-                if (MULTI && idx < total_paths) { // the scene whose path range holds idx
-                    uint32_t lo = 0, hi = B.n;
-                    while (hi - lo > 1) {
-                        uint32_t mi = (lo + hi) >> 1;
-                        if (B.path_prefix[mi] <= idx)
-                            lo = mi;
-                        else
-                            hi = mi;
+                if (idx >= total_paths) {
+                    want = false; // the path counter only grows: nothing left for this lane
+                } else {
+                    uint32_t nsid = 0;
+                    uint64_t local = idx, pbase = 0;
+                    if (MULTI) { // the scene whose path range holds idx
+                        uint32_t lo = 0, hi = B.n;
+                        while (hi - lo > 1) {
+                            uint32_t mi = (lo + hi) >> 1;
+                            if (B.path_prefix[mi] <= idx)
+                                lo = mi;
+                            else
+                                hi = mi;
+                        }
+                        nsid = lo;
+                        local = idx - B.path_prefix[lo];
+                        pbase = B.pix_prefix[lo];
                     }
-                    nsid = lo;
-                    local = idx - B.path_prefix[lo];
-                    pbase = B.pix_prefix[lo];
-                }
-                RenderArgs const &A = args_of<MULTI>(A0, B, nsid);
-                if (idx < total_paths && path_coords(A, local, pixel, sample, out)) {
-                    FirstHit f = fh[pbase + pixel];
-                    int32_t m = __float_as_int(f.p.w);
-                    if (m >= 0) {
-                        sid = nsid;
-                        out += static_cast<uint32_t>(pbase);
-                        p = xyz(f.p);
-                        n = xyz(f.n);
-                        o = neg(xyz(f.d));
-                        mesh = m;
-                        depth = 0;
-                        beta = f3(1.0f, 1.0f, 1.0f);
-                        rng = RngSlot<R>::fresh(A, MULTI ? splitmix64(A.seed) : mix0, pixel, sample);
-                        int32_t light = __float_as_int(f.n.w);
-                        if (light >= 0)
-                            emit_to(A, accum, path_rgb, out, light_radiance(scene_of<MULTI>(S0, B, sid), light, o, n));
-                        state = kAtVertex;
-                        refilled = true;
+                    RenderArgs const &A = args_of<MULTI>(A0, B, nsid);
+                    if (path_coords(A, local, pixel, sample, out)) {
+                        FirstHit f = fh[pbase + pixel];
+                        int32_t m = __float_as_int(f.p.w);
+                        if (m >= 0) {
+                            sid = nsid;
+                            out += static_cast<uint32_t>(pbase);
+                            p = xyz(f.p);
+                            n = xyz(f.n);
+                            o = neg(xyz(f.d));
+                            mesh = m;
+                            depth = 0;
+                            beta = f3(1.0f, 1.0f, 1.0f);
+                            rng = RngSlot<R>::fresh(A, MULTI ? splitmix64(A.seed) : mix0, pixel, sample);
+                            int32_t light = __float_as_int(f.n.w);
+                            if (light >= 0)
+                                emit_to(A, accum, path_rgb, out,
+                                        light_radiance(scene_of<MULTI>(S0, B, sid), light, o, n));
+                            state = kAtVertex;
+                            refilled = true;
+                            want = false;
+                        }
                     }
                 }
             }
@@ -561,18 +577,26 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
 }
 
 // One bounce: reset queue lengths, shade, then the trace kernel(s). B (or null): the scene table
-// of a many-scene wavefront (eight-wide trees, dynamic fetch).
+// of a many-scene wavefront (eight-wide trees, dynamic fetch). timing (or null): three events
+// recorded at the bounce's start, after its shading and after its trace kernel(s).
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
                        float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, uint64_t total_paths,
-                       BatchDev const *B, cudaStream_t st) {
+                       BatchDev const *B, cudaStream_t st, cudaEvent_t const *timing) {
     auto *cnt = reinterpret_cast<Counters *>(W.counters);
+    auto mark = [&](int k) {
+        if (timing)
+            cudaEventRecordWithFlags(timing[k], st, cudaEventRecordExternal);
+    };
+    mark(0);
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
     if (B) {
         if (A.rng == E8G_RNG_MINSTD)
             k_wf_shade<RngMinstd, true><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr, total_paths);
         else
             k_wf_shade<RngPhilox, true><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr, total_paths);
+        mark(1);
         k_wf_trace_wide_both<true><<<trace_grid, kBlock, 0, st>>>(S, A, *B, W, cnt, accum, nullptr, threshold);
+        mark(2);
         return;
     }
     BatchDev none{};
@@ -580,6 +604,7 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
         k_wf_shade<RngMinstd, false><<<shade_grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
     else
         k_wf_shade<RngPhilox, false><<<shade_grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+    mark(1);
     if (threshold > 0 && S.layout == 0) {
         k_wf_trace_dyn<true, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
         k_wf_trace_dyn<false, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
@@ -589,6 +614,7 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
         k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
         k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);
     }
+    mark(2);
 }
 
 cudaError_t wf_init(WfSlots const &W, cudaStream_t st) {
