@@ -2442,6 +2442,82 @@ void o_path_gradient_f64(const o_scene *s, uint64_t seed, const o_policy *pol, u
     rgb_out[2] = Ltot.z;
 }
 
+/* The same gradient summed over a whole image: every pixel's spp paths (samples 0 .. spp - 1),
+ * each weighted by dl[pixel] / spp (float, as the device weights them). Pixels are handed out in
+ * chunks to num_threads threads; each sums into its own arrays, merged at the end. */
+typedef struct ograd_job {
+    const o_scene *s;
+    uint64_t seed;
+    const o_policy *pol;
+    uint32_t w, h, spp;
+    const float *dl;
+    double *da, *dr;
+    uint32_t next;
+    pthread_mutex_t mu;
+} ograd_job;
+
+static void *grad_worker(void *p) {
+    ograd_job *j = (ograd_job *)p;
+    uint32_t nm = j->s->nmat, npix = j->w * j->h;
+    double *da = (double *)calloc((size_t)nm * 4 + 4, sizeof(double));
+    double *dr = da + 3 * (size_t)nm + 2;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        uint32_t k0 = j->next;
+        j->next = k0 + 16 < npix ? k0 + 16 : npix;
+        pthread_mutex_unlock(&j->mu);
+        if (k0 >= npix)
+            break;
+        uint32_t k1 = k0 + 16 < npix ? k0 + 16 : npix;
+        for (uint32_t px = k0; px < k1; px++) {
+            float wgt[3];
+            for (int c = 0; c < 3; c++)
+                wgt[c] = j->dl[3 * (size_t)px + c] / (float)j->spp;
+            double rgb[3];
+            for (uint32_t smp = 0; smp < j->spp; smp++)
+                o_path_gradient_f64(j->s, j->seed, j->pol, j->w, j->h, px, smp, wgt, da, dr, rgb);
+        }
+    }
+    pthread_mutex_lock(&j->mu);
+    for (uint32_t i = 0; i < 3 * nm; i++)
+        j->da[i] += da[i];
+    for (uint32_t i = 0; i < nm; i++)
+        j->dr[i] += dr[i];
+    pthread_mutex_unlock(&j->mu);
+    free(da);
+    return NULL;
+}
+
+void o_image_gradient_f64(const o_scene *s, uint64_t seed, const o_policy *pol, uint32_t width,
+                          uint32_t height, uint32_t spp, const float *dl, double *d_albedo,
+                          double *d_roughness, int num_threads) {
+    ograd_job j;
+    memset(&j, 0, sizeof(j));
+    j.s = s;
+    j.seed = seed;
+    j.pol = pol;
+    j.w = width;
+    j.h = height;
+    j.spp = spp;
+    j.dl = dl;
+    j.da = d_albedo;
+    j.dr = d_roughness;
+    memset(d_albedo, 0, sizeof(double) * 3 * s->nmat);
+    memset(d_roughness, 0, sizeof(double) * s->nmat);
+    pthread_mutex_init(&j.mu, NULL);
+    if (num_threads <= 1) {
+        grad_worker(&j);
+    } else {
+        pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)num_threads);
+        for (int i = 0; i < num_threads; i++)
+            pthread_create(&th[i], NULL, grad_worker, &j);
+        for (int i = 0; i < num_threads; i++)
+            pthread_join(th[i], NULL);
+        free(th);
+    }
+    pthread_mutex_destroy(&j.mu);
+}
+
 /* ------------------------------------------------------------- transform -- */
 /* trimesh::transform, geometry.cpp:76-87, on mat<4,4> of tensor.h. */
 

@@ -112,6 +112,12 @@ void o_bsdf_sample(const o_scene *s, int32_t m, uint32_t seed, const float n[3],
 void o_path_gradient_f64(const o_scene *s, uint64_t seed, const o_policy *pol, uint32_t width,
                          uint32_t height, uint32_t pixel, uint32_t sample, const float w[3],
                          double *d_albedo, double *d_roughness, double rgb_out[3]);
+/* The sum of o_path_gradient_f64 over every pixel of a width x height image and samples
+ * 0 .. spp - 1, each path weighted by dl[3 * pixel ..] / spp; d_albedo (3 per material) and
+ * d_roughness are overwritten. num_threads threads. */
+void o_image_gradient_f64(const o_scene *s, uint64_t seed, const o_policy *pol, uint32_t width,
+                          uint32_t height, uint32_t spp, const float *dl, double *d_albedo,
+                          double *d_roughness, int num_threads);
 
 #ifdef __cplusplus
 }

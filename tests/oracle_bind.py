@@ -107,6 +107,8 @@ def oracle():
             "o_bsdf_sample": (None, [_P, C.c_int32, _U, _P, _P, _U, _P, _P]),
             "o_path_gradient_f64": (None, [_P, C.c_uint64, C.POINTER(OPolicy), _U, _U, _U, _U, _P,
                                            _P, _P, _P]),
+            "o_image_gradient_f64": (None, [_P, C.c_uint64, C.POINTER(OPolicy), _U, _U, _U, _P, _P, _P,
+                                            C.c_int]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -238,6 +240,16 @@ class OracleScene:
         self.lib.o_render(self.h, mode, rng, seed, C.byref(policy), w, h, spp, offset, x0, y0, x1,
                           y1, ptr(out), threads)
         return out.reshape(y1 - y0, x1 - x0, 4)
+
+    def image_gradient(self, seed, policy, w, h, spp, dl, threads=8):
+        """FP64 path-replay gradient of the MIS image (Philox streams) under the upstream image
+        gradient dl (h, w, 3): (d_albedo (materials, 3), d_roughness (materials,))."""
+        nm = self.scene.desc.num_materials
+        da = np.zeros(nm * 3, np.float64)
+        dr = np.zeros(nm, np.float64)
+        dl = np.ascontiguousarray(dl, np.float32).reshape(-1)
+        self.lib.o_image_gradient_f64(self.h, seed, C.byref(policy), w, h, spp, ptr(dl), ptr(da), ptr(dr), threads)
+        return da.reshape(nm, 3), dr
 
     def render_task(self, mode, w, h, spp, firefly=False, task_seed=33, policy=None):
         """pt_image_renderer::render with one task: the reference's own sequential stream."""
