@@ -48,7 +48,8 @@ typedef enum e8g_status {
     E8G_ERR_UNSUPPORTED = 6,
     E8G_ERR_TIMEOUT = 7,
     E8G_ERR_INTERNAL = 8,
-    E8G_ERR_NO_DEVICE = 9
+    E8G_ERR_NO_DEVICE = 9,
+    E8G_ERR_CANCELLED = 10 /* e8g_cancel stopped the call; its outputs are unspecified */
 } e8g_status;
 
 typedef struct e8g_ctx e8g_ctx;
@@ -319,6 +320,40 @@ e8g_status e8g_set_kernel_timing(e8g_ctx *ctx, int on);
  * the second denominator of the traversal roofline. No counterpart in the reference. */
 e8g_status e8g_l2_read_bandwidth(e8g_ctx *ctx, uint64_t bytes, uint32_t reps, double *gbs);
 
+/* ------------------------------------------------- robustness and control ---- *
+ * None of these has a counterpart in the reference, whose errors are C++ exceptions. */
+
+/* Checks a scene description the way e8g_scene_upload does, without a GPU: sizes, indices,
+ * material and light references, finite positions, normals, camera, material and light values,
+ * and a positive total light power. Returns E8G_OK, or E8G_ERR_INVALID_ARG with the reason in msg
+ * (msg_cap bytes, may be NULL). */
+e8g_status e8g_scene_validate(const e8g_scene_desc *desc, char *msg, size_t msg_cap);
+
+/* Caps the device memory the context's buffers may hold (0 = no limit, the default). An upload,
+ * build or render that would need more fails with E8G_ERR_OUT_OF_MEMORY, as a failed cudaMalloc
+ * does, and the context stays usable: a failed upload or build leaves no scene or no tree (the
+ * next render reports E8G_ERR_NO_SCENE or E8G_ERR_NOT_BUILT) until one succeeds. For callers
+ * with a memory budget, and for testing the out-of-memory paths. */
+e8g_status e8g_set_memory_limit(e8g_ctx *ctx, uint64_t bytes);
+/* Device memory the context's buffers hold now. */
+e8g_status e8g_memory_used(const e8g_ctx *ctx, uint64_t *bytes);
+
+/* Asks the call running on the context (from another host thread), or the next one, to stop:
+ * it returns E8G_ERR_CANCELLED after its kernels in flight have finished, at its next host-side
+ * step (between wavefront graph replays, firefly sample chunks, tuner renders, batch scenes) or
+ * at its start. A single kernel is never interrupted. The request is consumed by the call that
+ * honours it. */
+e8g_status e8g_cancel(e8g_ctx *ctx);
+
+/* Checkpoint of progressive rendering (e8g_render_progressive): the running sums of the
+ * accumulator (width * height float4, rgb sums and sample weight), its image size and the samples
+ * taken. e8g_progressive_save with accum = NULL only reports the size and samples.
+ * e8g_progressive_load puts a saved state back (same scene, same parameters), after which
+ * progressive calls continue the sample sequence where the saved one stopped: the resumed image
+ * equals the uninterrupted one up to the order of float additions. */
+e8g_status e8g_progressive_save(e8g_ctx *ctx, float *accum, uint32_t *width, uint32_t *height, uint64_t *spp);
+e8g_status e8g_progressive_load(e8g_ctx *ctx, const float *accum, uint32_t width, uint32_t height, uint64_t spp);
+
 /* Wavefront autotuner: times the wavefront integrator for each candidate slot capacity
  * {2^20 .. 2^24}, bounces per graph {2, 4} and warp refill threshold {4, 8, 12, 16, 24} (the
  * number of idle lanes at which a trace kernel hands its idle lanes new rays) on a short render
@@ -336,11 +371,27 @@ typedef struct e8g_tune_result {
     uint32_t cand_bounces[E8G_TUNE_MAX_CANDIDATES];
     uint32_t cand_threshold[E8G_TUNE_MAX_CANDIDATES];
     double cand_ms[E8G_TUNE_MAX_CANDIDATES];
+    uint32_t shade_variant;     /* chosen block shape of the shading kernel (0 .. num_shade - 1) */
+    uint32_t num_shade;         /* shapes timed */
+    double shade_ms[8];         /* device time of the render with each shape */
+    uint32_t from_cache;        /* e8g_wavefront_tune_cached: 1 when the choice came from the file */
+    uint32_t pad_;
 } e8g_tune_result;
 e8g_status e8g_wavefront_tune(e8g_ctx *ctx, const e8g_render_params *params, e8g_tune_result *result);
 /* Sets the wavefront configuration directly: slot capacity (1024 .. 2^26), bounces captured per
  * graph (1 .. 16) and warp refill threshold (0 .. 32). */
 e8g_status e8g_wavefront_set(e8g_ctx *ctx, uint32_t capacity, uint32_t bounces_per_graph, uint32_t threshold);
+/* Block shape of the wavefront's shading kernel: 0 = 256 threads x 4 blocks per SM (64 registers),
+ * 1 = 256 x 3 (80), 2 = 256 x 5 (48), 3 = 128 x 8 (64). */
+e8g_status e8g_wavefront_set_shade(e8g_ctx *ctx, uint32_t variant);
+/* e8g_wavefront_tune with a cache of choices in a JSON file (`cache_path`): the key is the scene
+ * and frame size bucket (tree layout, stream kind, log2 of the triangle count, of the pixels and of
+ * min(spp, 64)). A key found in the file sets its configuration without tuning (result->from_cache
+ * = 1); otherwise the tuner runs and its choice is added to the file (written to a temporary file
+ * and renamed over it). A missing or unreadable file counts as empty. No counterpart in the
+ * reference. */
+e8g_status e8g_wavefront_tune_cached(e8g_ctx *ctx, const e8g_render_params *params, const char *cache_path,
+                                     e8g_tune_result *result);
 
 /* Largest image (width * height) e8g_render_dev_noalloc accepts. */
 #define E8G_NOALLOC_MAX_PIXELS 65536u

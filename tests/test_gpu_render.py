@@ -286,3 +286,36 @@ def test_wavefront_kernel_timing_leaves_the_image_and_fills_the_stats(ctx):
     gbs = C.c_double()
     assert ctx.lib.e8g_l2_read_bandwidth(ctx.h, 64 << 20, 4, C.byref(gbs)) == 0
     assert 1000 < gbs.value < 100000, gbs.value  # GB/s: far above HBM's few TB/s, below nonsense
+
+
+def test_wavefront_tuner_cache_and_shade_shapes(ctx, tmp_path):
+    """e8g_wavefront_tune searches the shading kernel's block shapes too; e8g_wavefront_tune_cached
+    writes its choice to a JSON file keyed by the scene and frame size bucket and takes it from
+    there the next time; every shape renders the same image."""
+    import ctypes as C
+    import json
+    sc = S.cornell(128, 96)
+    ctx.upload(sc, layout=abi.BVH_WIDE)
+    p = default_params(abi.MODE_MIS, 128, 96, 4, seed=3, max_depth=6, integrator=abi.INTEGRATOR_WAVEFRONT)
+    path = str(tmp_path / "tune.json").encode()
+    r = abi.TuneResult()
+    assert ctx.lib.e8g_wavefront_tune_cached(ctx.h, C.byref(p), path, C.byref(r)) == 0
+    assert r.from_cache == 0 and r.num_shade == 4 and r.shade_variant < 4
+    assert all(r.shade_ms[i] > 0 for i in range(4))
+    with open(path) as f:
+        d = json.load(f)
+    (key, entry), = d.items()
+    assert "layout2" in key and entry["capacity"] == r.capacity and entry["shade"] == r.shade_variant
+    r2 = abi.TuneResult()
+    assert ctx.lib.e8g_wavefront_tune_cached(ctx.h, C.byref(p), path, C.byref(r2)) == 0
+    assert r2.from_cache == 1 and (r2.capacity, r2.bounces_per_graph, r2.threshold, r2.shade_variant) == \
+        (r.capacity, r.bounces_per_graph, r.threshold, r.shade_variant)
+    base = None
+    for v in range(4):
+        assert ctx.lib.e8g_wavefront_set_shade(ctx.h, v) == 0
+        img = ctx.render(p)
+        if base is None:
+            base = img
+        close = np.all(np.abs(img - base) <= np.maximum(1e-4 * np.abs(base), 1e-6), axis=-1)
+        assert close.mean() >= 0.999, v
+    assert ctx.lib.e8g_wavefront_set_shade(ctx.h, 4) == 1

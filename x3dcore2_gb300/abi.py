@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "libe8g.so")
 E8G_OK = 0
 STATUS_NAMES = {
     0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "NO_SCENE", 5: "NOT_BUILT",
-    6: "UNSUPPORTED", 7: "TIMEOUT", 8: "INTERNAL", 9: "NO_DEVICE",
+    6: "UNSUPPORTED", 7: "TIMEOUT", 8: "INTERNAL", 9: "NO_DEVICE", 10: "CANCELLED",
 }
 
 # materials
@@ -108,7 +108,8 @@ class TuneResult(C.Structure):
     _fields_ = [("capacity", C.c_uint32), ("bounces_per_graph", C.c_uint32), ("threshold", C.c_uint32),
                 ("num_candidates", C.c_uint32), ("cand_capacity", C.c_uint32 * 64),
                 ("cand_bounces", C.c_uint32 * 64), ("cand_threshold", C.c_uint32 * 64),
-                ("cand_ms", C.c_double * 64)]
+                ("cand_ms", C.c_double * 64), ("shade_variant", C.c_uint32), ("num_shade", C.c_uint32),
+                ("shade_ms", C.c_double * 8), ("from_cache", C.c_uint32), ("pad_", C.c_uint32)]
 
 
 class GenOpts(C.Structure):
@@ -160,12 +161,20 @@ SIGNATURES = {
     "e8g_get_render_stats": (_ST, [_P, C.POINTER(RenderStats)]),
     "e8g_set_kernel_timing": (_ST, [_P, C.c_int]),
     "e8g_l2_read_bandwidth": (_ST, [_P, C.c_uint64, _U32, C.POINTER(C.c_double)]),
+    "e8g_scene_validate": (_ST, [C.POINTER(SceneDesc), C.c_char_p, C.c_size_t]),
+    "e8g_set_memory_limit": (_ST, [_P, C.c_uint64]),
+    "e8g_memory_used": (_ST, [_P, C.POINTER(C.c_uint64)]),
+    "e8g_cancel": (_ST, [_P]),
+    "e8g_progressive_save": (_ST, [_P, _P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(C.c_uint64)]),
+    "e8g_progressive_load": (_ST, [_P, _P, _U32, _U32, C.c_uint64]),
     "e8g_render_progressive": (_ST, [_P, C.POINTER(RenderParams), C.c_int, _P, _P]),
     "e8g_composite": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P]),
     "e8g_composite_dev": (_ST, [_P, _P, C.c_uint32, C.c_uint32, C.POINTER(CompositeParams), _P, _P]),
     "e8g_count_traversal": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(RenderStats)]),
     "e8g_wavefront_tune": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(TuneResult)]),
     "e8g_wavefront_set": (_ST, [_P, _U32, _U32, _U32]),
+    "e8g_wavefront_set_shade": (_ST, [_P, _U32]),
+    "e8g_wavefront_tune_cached": (_ST, [_P, C.POINTER(RenderParams), C.c_char_p, C.POINTER(TuneResult)]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
     "e8g_render_rays": (_ST, [_P, C.POINTER(RenderParams), _P, _U32, _P]),
     "e8g_forward": (_ST, [_P, C.POINTER(RenderParams), _P]),

@@ -25,12 +25,28 @@ e8g_status fail(e8g_ctx *ctx, e8g_status st, std::string const &msg) {
 }
 
 e8g_status cuda_fail(e8g_ctx *ctx, cudaError_t e, char const *what) {
+    if (e == cudaErrorMemoryAllocation) {
+        size_t cap = ctx ? ctx->budget.cap : 0;
+        return fail(ctx, E8G_ERR_OUT_OF_MEMORY,
+                    std::string(what) + ": out of device memory" +
+                        (cap ? " (context limit " + std::to_string(cap) + " bytes)" : std::string()));
+    }
     return fail(ctx, E8G_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool take_cancel(e8g_ctx *c) {
+    if (!c->cancel.load(std::memory_order_acquire))
+        return false;
+    cudaStreamSynchronize(c->stream);
+    c->cancel.store(false, std::memory_order_release);
+    return true;
 }
 
 void dev_buffer::release() {
     if (ptr)
         cudaFree(ptr);
+    if (budget)
+        budget->used -= bytes;
     ptr = nullptr;
     bytes = 0;
 }
@@ -38,13 +54,18 @@ void dev_buffer::release() {
 cudaError_t dev_buffer::reserve(size_t n) {
     if (n <= bytes)
         return cudaSuccess;
+    if (budget && budget->cap && budget->used - bytes + n > budget->cap)
+        return cudaErrorMemoryAllocation;
     release();
     cudaError_t e = cudaMalloc(&ptr, n);
     if (e != cudaSuccess) {
+        cudaGetLastError(); // not sticky: keep it out of later launch checks
         ptr = nullptr;
         return e;
     }
     bytes = n;
+    if (budget)
+        budget->used += n;
     return cudaSuccess;
 }
 
@@ -292,7 +313,9 @@ e8g_status build_on_device(e8g_ctx *c, bool *built) {
 } // namespace
 
 e8g_status build_tree(e8g_ctx *c) {
+    nvtx_range range("e8g build tree");
     cudaSetDevice(c->device);
+    c->built = false; // buffers are replaced below: no render until the build completes
     packed_scene &p = c->pack;
     bool on_device = false;
     if (c->bvh_opts.builder == E8G_BUILDER_DEVICE && c->bvh_opts.layout != E8G_BVH_REFERENCE &&
@@ -425,6 +448,8 @@ e8g_status e8g_create(e8g_ctx **out, e8g_device_opts const *opts) {
     if (!c)
         return E8G_ERR_OUT_OF_MEMORY;
     c->device = dev;
+    for (dev_buffer *b : c->all_buffers())
+        b->budget = &c->budget;
     cudaError_t e = cudaSetDevice(dev);
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -481,7 +506,10 @@ e8g_status e8g_scene_upload(e8g_ctx *c, e8g_scene_desc const *d) {
     char const *bad = e8g_validate_desc(d);
     if (bad)
         return fail(c, E8G_ERR_INVALID_ARG, bad);
+    nvtx_range range("e8g_scene_upload");
     cudaSetDevice(c->device);
+    // the previous scene is gone from here on: a failure below leaves no scene
+    c->uploaded = c->built = false;
     try {
         c->pack = packed_scene();
         pack_scene(*d, c->pack);
@@ -767,6 +795,65 @@ e8g_status e8g_count_traversal(e8g_ctx *c, e8g_render_params const *p, e8g_rende
     c->stats.counted = 1;
     if (out)
         *out = c->stats;
+    return E8G_OK;
+}
+
+e8g_status e8g_set_memory_limit(e8g_ctx *c, uint64_t bytes) {
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    c->budget.cap = static_cast<size_t>(bytes);
+    return E8G_OK;
+}
+
+e8g_status e8g_memory_used(e8g_ctx const *c, uint64_t *bytes) {
+    if (!c || !bytes)
+        return E8G_ERR_INVALID_ARG;
+    *bytes = c->budget.used;
+    return E8G_OK;
+}
+
+e8g_status e8g_cancel(e8g_ctx *c) {
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    c->cancel.store(true, std::memory_order_release);
+    return E8G_OK;
+}
+
+e8g_status e8g_progressive_save(e8g_ctx *c, float *accum, uint32_t *width, uint32_t *height, uint64_t *spp) {
+    if (!c || !width || !height || !spp)
+        return E8G_ERR_INVALID_ARG;
+    *width = c->prog_spp ? c->prog_w : 0;
+    *height = c->prog_spp ? c->prog_h : 0;
+    *spp = c->prog_spp;
+    if (!accum || c->prog_spp == 0)
+        return E8G_OK;
+    cudaSetDevice(c->device);
+    size_t bytes = static_cast<size_t>(c->prog_w) * c->prog_h * sizeof(float4);
+    cudaError_t e = cudaMemcpyAsync(accum, c->b_accum.ptr, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "progressive save");
+}
+
+e8g_status e8g_progressive_load(e8g_ctx *c, float const *accum, uint32_t width, uint32_t height, uint64_t spp) {
+    if (!c || !accum || width == 0 || height == 0 || spp == 0)
+        return fail(c, E8G_ERR_INVALID_ARG, "progressive load: empty state");
+    if (static_cast<uint64_t>(width) * height > (1ull << 28) || spp > 0xFFFFFFFFull)
+        return fail(c, E8G_ERR_INVALID_ARG, "progressive load: state out of range");
+    cudaSetDevice(c->device);
+    size_t bytes = static_cast<size_t>(width) * height * sizeof(float4);
+    cudaError_t e = c->b_accum.reserve(bytes);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->b_accum.ptr, accum, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        c->prog_spp = 0;
+        return cuda_fail(c, e, "progressive load");
+    }
+    c->prog_w = width;
+    c->prog_h = height;
+    c->prog_spp = spp;
     return E8G_OK;
 }
 

@@ -7,16 +7,38 @@
 #include "refit.h"
 #include "scene_pack.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+#include <atomic>
 #include <string>
 #include <vector>
 
 namespace e8g {
 
+// Device memory a context may hold (e8g_set_memory_limit): cap 0 = no limit.
+struct mem_budget {
+    size_t cap = 0;
+    size_t used = 0;
+};
+
 struct dev_buffer {
     void *ptr = nullptr;
     size_t bytes = 0;
+    mem_budget *budget = nullptr;
+    // Grows the buffer to n bytes (contents not kept). A request beyond the context's memory
+    // limit fails with cudaErrorMemoryAllocation before anything is freed; a failed cudaMalloc
+    // leaves the buffer empty.
     cudaError_t reserve(size_t n);
     void release();
+};
+
+// An NVTX range for the lifetime of the object (named phases in Nsight timelines; no cost
+// without a tool attached).
+struct nvtx_range {
+    explicit nvtx_range(char const *name) { nvtxRangePushA(name); }
+    ~nvtx_range() { nvtxRangePop(); }
+    nvtx_range(nvtx_range const &) = delete;
+    nvtx_range &operator=(nvtx_range const &) = delete;
 };
 
 } // namespace e8g
@@ -44,13 +66,16 @@ struct e8g_ctx {
     e8g_render_params fwd_params{};
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
-    uint32_t wf_capacity = 1u << 21, wf_bounces = 4, wf_threshold = 16;
+    uint32_t wf_capacity = 1u << 21, wf_bounces = 4, wf_threshold = 16, wf_shade_variant = 0;
     // per-kernel timing of the wavefront (e8g_set_kernel_timing): three events per bounce of the
     // graph (bounce start, shading done, trace done) and the sums over the current render
     bool kernel_timing = false;
     std::vector<cudaEvent_t> kt_events;
     double kt_trace_ms = 0, kt_shade_ms = 0;
     uint32_t kt_trace_launches = 0;
+    // device memory limit of the context's buffers, and the cancellation request (e8g_cancel)
+    e8g::mem_budget budget;
+    std::atomic<bool> cancel{false};
     void *host_pinned = nullptr;
     // progressive rendering: samples in the accumulator, and the image they belong to
     uint64_t prog_spp = 0;
@@ -82,6 +107,8 @@ namespace e8g {
 e8g_status fail(e8g_ctx *ctx, e8g_status st, std::string const &msg);
 e8g_status cuda_fail(e8g_ctx *ctx, cudaError_t e, char const *what);
 e8g_status check_ready(e8g_ctx *c);
+// A pending e8g_cancel: waits for the context's stream, clears the request and returns true.
+bool take_cancel(e8g_ctx *c);
 e8g_status validate_params(e8g_ctx *c, e8g_render_params const *p);
 RenderArgs make_args(e8g_render_params const *p);
 e8g_status first_hits(e8g_ctx *c, uint32_t w, uint32_t h);

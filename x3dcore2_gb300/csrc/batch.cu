@@ -56,6 +56,9 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     for (uint32_t k = 0; k < n; k++)
         use_wf = use_wf && items[k].params.integrator == E8G_INTEGRATOR_WAVEFRONT &&
                  items[k].params.mode == E8G_MODE_MIS && items[k].params.rng == items[0].params.rng;
+    nvtx_range range("e8g_batch_render");
+    if (take_cancel(c))
+        return fail(c, E8G_ERR_CANCELLED, "batch cancelled");
     cudaSetDevice(c->device);
     c->prog_spp = 0; // the batch reuses the accumulator
     // host: pack, build, stage

@@ -123,9 +123,10 @@ struct ref_builder {
         bucket buckets[20];
         float width = range[axis] / 20;
         for (unsigned i = start; i < end; i++) {
-            unsigned ib = static_cast<unsigned>((prims[i].centroid[axis] - b.mn[axis]) / width);
-            if (ib == 20)
-                ib = 19;
+            // a node whose primitives all sit at one point has width 0: the reference divides 0 by
+            // 0 and converts the NaN to an index (undefined behaviour); here they go to bucket 0
+            float q = width > 0 ? (prims[i].centroid[axis] - b.mn[axis]) / width : 0.0f;
+            unsigned ib = q >= 19.0f ? 19u : static_cast<unsigned>(q);
             buckets[ib].bound = merge(buckets[ib].bound, prims[i].bound);
             buckets[ib].num_prims++;
         }

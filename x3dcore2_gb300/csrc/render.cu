@@ -6,7 +6,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
+#include <map>
+#include <string>
 
 namespace e8g {
 
@@ -51,6 +54,8 @@ e8g_status run_firefly(e8g_ctx *c, e8g_render_params const *p, RenderArgs const 
         return cuda_fail(c, e, "firefly sample images");
     float *est = static_cast<float *>(c->b_ff.ptr);
     for (uint32_t s0 = 0; s0 < p->spp; s0 += K) {
+        if (take_cancel(c))
+            return fail(c, E8G_ERR_CANCELLED, "render cancelled");
         uint32_t k = std::min(K, p->spp - s0);
         RenderArgs B = A;
         B.spp = k;
@@ -86,7 +91,8 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     e = wf_init(W, c->stream);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront init");
-    int shade_grid = static_cast<int>(std::min<uint64_t>((Q + 255) / 256, static_cast<uint64_t>(c->num_sms) * 8));
+    uint32_t shade_variant = B ? 0u : c->wf_shade_variant;
+    int shade_grid = wf_shade_grid(shade_variant, Q, c->num_sms);
     int trace_grid = persistent_grid(c, wf_trace_blocks_per_sm(layout, threshold));
     auto const *fh = B ? fh_all : static_cast<FirstHit const *>(c->b_fh.ptr);
     // capture `bounces` bounces once, replay until no slot is busy and no path is left
@@ -106,7 +112,7 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
         return cuda_fail(c, e, "wavefront capture");
     for (uint32_t k = 0; k < bounces; k++)
         wf_enqueue_bounce(c->dev, A, fh, W, accum, path_rgb, shade_grid, trace_grid, threshold, total, B, c->stream,
-                          timed ? c->kt_events.data() + 3 * k : nullptr);
+                          timed ? c->kt_events.data() + 3 * k : nullptr, shade_variant);
     e = cudaStreamEndCapture(c->stream, &graph);
     if (e == cudaSuccess)
         e = cudaGraphInstantiate(&exec, graph, 0);
@@ -119,7 +125,12 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     // every path needs at most kHardDepth + 2 bounces; slots refill continuously
     uint64_t max_replays = ((total + Q - 1) / Q + 1) * (kHardDepth + 2) / bounces + 16;
     uint64_t r = 0;
+    bool cancelled = false;
     for (; r < max_replays; r++) {
+        if (take_cancel(c)) {
+            cancelled = true;
+            break;
+        }
         e = cudaGraphLaunch(exec, c->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(host, W.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream);
@@ -145,6 +156,8 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     cudaGraphDestroy(graph);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "wavefront run");
+    if (cancelled)
+        return fail(c, E8G_ERR_CANCELLED, "render cancelled");
     if (r == max_replays)
         return fail(c, E8G_ERR_INTERNAL, "wavefront did not drain");
     return E8G_OK;
@@ -154,6 +167,9 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
                         uint64_t prior_spp) {
     if (counts && (p->mode == E8G_MODE_REF_BDPT || p->mode == E8G_MODE_BDPT_POWER || p->mode == E8G_MODE_REF_LT2))
         return fail(c, E8G_ERR_UNSUPPORTED, "traversal counters cover the unidirectional integrators");
+    nvtx_range range("e8g render");
+    if (take_cancel(c))
+        return fail(c, E8G_ERR_CANCELLED, "render cancelled");
     c->launches = 0;
     size_t npix = static_cast<size_t>(p->width) * p->height;
     cudaError_t e = c->b_accum.reserve(npix * sizeof(float4));
@@ -251,6 +267,10 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
         return s;
     if (params->mode != E8G_MODE_MIS)
         return fail(c, E8G_ERR_INVALID_ARG, "the wavefront integrator runs E8G_MODE_MIS");
+    nvtx_range range("e8g_wavefront_tune");
+    // a tuner run that fails (or is cancelled) leaves the configuration it found
+    const uint32_t keep_cap = c->wf_capacity, keep_b = c->wf_bounces, keep_th = c->wf_threshold,
+                   keep_shade = c->wf_shade_variant;
     e8g_render_params p = *params;
     p.integrator = E8G_INTEGRATOR_WAVEFRONT;
     p.spp = std::max<uint32_t>(1, std::min<uint32_t>(p.spp, 8)); // long enough for slots to refill steadily
@@ -272,8 +292,10 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
             double ms = 1e300;
             for (int rep = 0; rep < 2; rep++) { // first run warms caches and builds nothing twice
                 s = render_image(c, &p, static_cast<float *>(c->b_img.ptr), nullptr);
-                if (s != E8G_OK)
+                if (s != E8G_OK) {
+                    c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
                     return s;
+                }
                 ms = std::min(ms, c->stats.kernel_ms);
             }
             if (r.num_candidates < E8G_TUNE_MAX_CANDIDATES) {
@@ -310,8 +332,10 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
             c->wf_bounces = r.cand_bounces[bi];
             c->wf_threshold = r.cand_threshold[bi];
             s = render_image(c, &p2, static_cast<float *>(c->b_img.ptr), nullptr);
-            if (s != E8G_OK)
+            if (s != E8G_OK) {
+                c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
                 return s;
+            }
             double ms = c->stats.kernel_ms;
             if (ms < best) {
                 best = ms;
@@ -324,6 +348,33 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     c->wf_capacity = r.capacity;
     c->wf_bounces = r.bounces_per_graph;
     c->wf_threshold = r.threshold;
+    // the shading kernel's block shape, on the longest render of the search
+    {
+        e8g_render_params p3 = p;
+        p3.spp = spp2;
+        double best_ms = 1e300;
+        r.shade_variant = keep_shade;
+        for (uint32_t v = 0; v < kWfShadeVariants; v++) {
+            c->wf_shade_variant = v;
+            double ms = 1e300;
+            for (int rep = 0; rep < 2; rep++) {
+                s = render_image(c, &p3, static_cast<float *>(c->b_img.ptr), nullptr);
+                if (s != E8G_OK) {
+                    c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
+                    c->wf_shade_variant = keep_shade;
+                    return s;
+                }
+                ms = std::min(ms, c->stats.kernel_ms);
+            }
+            r.shade_ms[v] = ms;
+            if (ms < best_ms) {
+                best_ms = ms;
+                r.shade_variant = v;
+            }
+        }
+        r.num_shade = kWfShadeVariants;
+        c->wf_shade_variant = r.shade_variant;
+    }
     if (res)
         *res = r;
     return E8G_OK;
@@ -338,6 +389,122 @@ e8g_status e8g_wavefront_set(e8g_ctx *c, uint32_t capacity, uint32_t bounces, ui
     c->wf_capacity = capacity;
     c->wf_bounces = bounces;
     c->wf_threshold = threshold;
+    return E8G_OK;
+}
+
+e8g_status e8g_wavefront_set_shade(e8g_ctx *c, uint32_t variant) {
+    using namespace e8g;
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    if (variant >= kWfShadeVariants)
+        return fail(c, E8G_ERR_INVALID_ARG, "unknown shading block shape");
+    c->wf_shade_variant = variant;
+    return E8G_OK;
+}
+
+namespace {
+
+// One line of the tuning cache: "key": {"capacity": C, "bounces": B, "threshold": T, "shade": S, "ms": M}
+struct tune_entry {
+    uint32_t capacity = 0, bounces = 0, threshold = 0, shade = 0;
+    double ms = 0;
+};
+
+uint32_t log2_bucket(uint64_t v) {
+    uint32_t b = 0;
+    while (v > 1) {
+        v >>= 1;
+        b++;
+    }
+    return b;
+}
+
+std::map<std::string, tune_entry> read_tune_cache(char const *path) {
+    std::map<std::string, tune_entry> out;
+    FILE *f = std::fopen(path, "r");
+    if (!f)
+        return out;
+    char line[512];
+    while (std::fgets(line, sizeof(line), f)) {
+        char key[200];
+        tune_entry t;
+        if (std::sscanf(line, " \"%199[^\"]\": {\"capacity\": %u, \"bounces\": %u, \"threshold\": %u, \"shade\": %u, "
+                              "\"ms\": %lf",
+                        key, &t.capacity, &t.bounces, &t.threshold, &t.shade, &t.ms) == 6 &&
+            t.capacity >= 1024 && t.capacity <= (1u << 26) && t.bounces >= 1 && t.bounces <= 16 &&
+            t.threshold <= 32 && t.shade < e8g::kWfShadeVariants)
+            out[key] = t;
+    }
+    std::fclose(f);
+    return out;
+}
+
+bool write_tune_cache(char const *path, std::map<std::string, tune_entry> const &m) {
+    std::string tmp = std::string(path) + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "w");
+    if (!f)
+        return false;
+    std::fprintf(f, "{\n");
+    size_t i = 0;
+    for (auto const &kv : m) {
+        std::fprintf(f, "  \"%s\": {\"capacity\": %u, \"bounces\": %u, \"threshold\": %u, \"shade\": %u, \"ms\": %.4f}%s\n",
+                     kv.first.c_str(), kv.second.capacity, kv.second.bounces, kv.second.threshold, kv.second.shade,
+                     kv.second.ms, ++i < m.size() ? "," : "");
+    }
+    std::fprintf(f, "}\n");
+    bool ok = std::fclose(f) == 0;
+    return ok && std::rename(tmp.c_str(), path) == 0;
+}
+
+} // namespace
+
+e8g_status e8g_wavefront_tune_cached(e8g_ctx *c, e8g_render_params const *params, char const *path,
+                                     e8g_tune_result *res) {
+    using namespace e8g;
+    e8g_status s = check_ready(c);
+    if (s != E8G_OK)
+        return s;
+    s = validate_params(c, params);
+    if (s != E8G_OK)
+        return s;
+    if (!path || !*path)
+        return fail(c, E8G_ERR_INVALID_ARG, "no cache path");
+    char key[200];
+    std::snprintf(key, sizeof(key), "layout%u/rng%u/tris2^%u/pixels2^%u/spp2^%u", c->pack.layout, params->rng,
+                  log2_bucket(c->pack.nt), log2_bucket(static_cast<uint64_t>(params->width) * params->height),
+                  log2_bucket(std::min<uint32_t>(std::max<uint32_t>(params->spp, 1), 64)));
+    std::map<std::string, tune_entry> cache = read_tune_cache(path);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        c->wf_capacity = it->second.capacity;
+        c->wf_bounces = it->second.bounces;
+        c->wf_threshold = it->second.threshold;
+        c->wf_shade_variant = it->second.shade;
+        if (res) {
+            *res = e8g_tune_result{};
+            res->capacity = it->second.capacity;
+            res->bounces_per_graph = it->second.bounces;
+            res->threshold = it->second.threshold;
+            res->shade_variant = it->second.shade;
+            res->from_cache = 1;
+        }
+        return E8G_OK;
+    }
+    e8g_tune_result r{};
+    s = e8g_wavefront_tune(c, params, &r);
+    if (s != E8G_OK)
+        return s;
+    tune_entry t;
+    t.capacity = r.capacity;
+    t.bounces = r.bounces_per_graph;
+    t.threshold = r.threshold;
+    t.shade = r.shade_variant;
+    t.ms = r.shade_ms[r.shade_variant];
+    cache[key] = t;
+    if (!write_tune_cache(path, cache))
+        return fail(c, E8G_ERR_INVALID_ARG, std::string("cannot write the tuning cache ") + path);
+    if (res)
+        *res = r;
     return E8G_OK;
 }
 

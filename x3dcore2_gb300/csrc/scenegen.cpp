@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <unordered_map>
 
@@ -464,6 +465,20 @@ char const *e8g_validate_desc(e8g_scene_desc const *d) {
         if (d->mesh_material && d->mesh_material[m] >= static_cast<int32_t>(d->num_materials))
             return "mesh material index out of range";
     }
+    uint32_t nv_total = d->mesh_vert_offset[d->num_meshes];
+    for (size_t i = 0; i < 3 * static_cast<size_t>(nv_total); i++)
+        if (!std::isfinite(d->positions[i]) || !std::isfinite(d->normals[i]))
+            return "vertex positions and normals must be finite";
+    e8g_camera const &cam = d->camera;
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(cam.origin[k]))
+            return "camera origin must be finite";
+    for (int k = 0; k < 9; k++)
+        if (!std::isfinite(cam.rot[k]))
+            return "camera rotation must be finite";
+    if (!(cam.sensor_size > 0) || !(cam.focal_len > 0) || !(cam.aspect > 0) || !std::isfinite(cam.sensor_size) ||
+        !std::isfinite(cam.focal_len) || !std::isfinite(cam.aspect))
+        return "camera sensor size, focal length and aspect must be finite and positive";
     if (d->num_lights == 0)
         return "scene has no lights";
     for (uint32_t l = 0; l < d->num_lights; l++) {
@@ -471,11 +486,36 @@ char const *e8g_validate_desc(e8g_scene_desc const *d) {
             return "light mesh index out of range";
         if (d->mesh_tri_offset[d->lights[l].mesh + 1] == d->mesh_tri_offset[d->lights[l].mesh])
             return "light mesh has no triangles";
+        for (int k = 0; k < 3; k++)
+            if (!std::isfinite(d->lights[l].radiance[k]) || d->lights[l].radiance[k] < 0)
+                return "light radiance must be finite and non-negative";
     }
+    // the light CDF divides by the total power (lightsources.cpp:45-52): some light must emit
+    double total = 0;
+    for (uint32_t l = 0; l < d->num_lights; l++) {
+        e8g_light const &L = d->lights[l];
+        uint32_t m = L.mesh, v0 = d->mesh_vert_offset[m];
+        double area = 0;
+        for (uint32_t t = d->mesh_tri_offset[m]; t < d->mesh_tri_offset[m + 1]; t++) {
+            float const *a = d->positions + 3 * static_cast<size_t>(v0 + d->triangles[3 * t]);
+            float const *b = d->positions + 3 * static_cast<size_t>(v0 + d->triangles[3 * t + 1]);
+            float const *c = d->positions + 3 * static_cast<size_t>(v0 + d->triangles[3 * t + 2]);
+            double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, w[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            double x = u[1] * w[2] - u[2] * w[1], y = u[2] * w[0] - u[0] * w[2], z = u[0] * w[1] - u[1] * w[0];
+            area += 0.5 * std::sqrt(x * x + y * y + z * z);
+        }
+        total += area * (L.radiance[0] + L.radiance[1] + L.radiance[2]);
+    }
+    if (!(total > 0))
+        return "the lights emit no power (zero radiance or zero area)";
     for (uint32_t i = 0; i < d->num_materials; i++) {
         e8g_material const &m = d->materials[i];
         if (m.type > E8G_MAT_MIXTURE)
             return "unknown material type";
+        if (!std::isfinite(m.albedo[0]) || !std::isfinite(m.albedo[1]) || !std::isfinite(m.albedo[2]) ||
+            !std::isfinite(m.roughness) || !std::isfinite(m.ior_re) || !std::isfinite(m.ior_im) ||
+            !std::isfinite(m.ratio))
+            return "material values must be finite";
         if (m.type == E8G_MAT_MIXTURE) {
             if (m.mix0 < 0 || m.mix1 < 0 || m.mix0 >= static_cast<int32_t>(d->num_materials) ||
                 m.mix1 >= static_cast<int32_t>(d->num_materials))
@@ -488,6 +528,14 @@ char const *e8g_validate_desc(e8g_scene_desc const *d) {
 }
 
 extern "C" {
+
+e8g_status e8g_scene_validate(e8g_scene_desc const *d, char *msg, size_t cap) {
+    char const *bad = e8g_validate_desc(d);
+    if (msg && cap) {
+        std::snprintf(msg, cap, "%s", bad ? bad : "");
+    }
+    return bad ? E8G_ERR_INVALID_ARG : E8G_OK;
+}
 
 e8g_status e8g_gen_scene(e8g_gen_opts const *o, e8g_host_scene **out) {
     if (!o || !out)

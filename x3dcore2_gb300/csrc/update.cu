@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cmath>
 #include <cstring>
 
 using namespace e8g;
@@ -62,6 +63,9 @@ e8g_status e8g_scene_update_mesh(e8g_ctx *c, uint32_t mesh, float const *positio
     cudaSetDevice(c->device);
     packed_scene &p = c->pack;
     uint32_t v0 = p.mesh_voff[mesh], v1 = p.mesh_voff[mesh + 1];
+    for (size_t i = 0; i < 3 * static_cast<size_t>(v1 - v0); i++)
+        if (!std::isfinite(positions[i]) || (normals && !std::isfinite(normals[i])))
+            return fail(c, E8G_ERR_INVALID_ARG, "vertex positions and normals must be finite");
     for (uint32_t v = v0; v < v1; v++)
         for (int k = 0; k < 3; k++) {
             p.vpos[4 * static_cast<size_t>(v) + k] = positions[3 * static_cast<size_t>(v - v0) + k];
@@ -104,6 +108,9 @@ e8g_status e8g_scene_transform_mesh(e8g_ctx *c, uint32_t mesh, float const m[16]
         return st;
     if (!m || flags > E8G_XFORM_NORMALS_AS_DIRECTIONS)
         return fail(c, E8G_ERR_INVALID_ARG, "bad transform arguments");
+    for (int k = 0; k < 16; k++)
+        if (!std::isfinite(m[k]))
+            return fail(c, E8G_ERR_INVALID_ARG, "transform must be finite");
     XformArgs X{};
     std::memcpy(X.m, m, sizeof(X.m));
     if (!reference_normal_matrix(m, X.n))

@@ -15,6 +15,8 @@
 #include "../../include/e8g.h"
 #include "wavefront.h"
 
+#include <algorithm>
+
 namespace e8g {
 
 namespace {
@@ -118,11 +120,11 @@ __device__ __forceinline__ RenderArgs const &args_of(RenderArgs const &A0, Batch
 
 // Shading of every slot. MULTI: paths of many scenes share the slots; a slot keeps its path's
 // scene index, `out` is the path's pixel in the concatenated accumulator and first hits are
-// indexed the same way. Four blocks of 256 per SM (64 registers): shading waits on slot and
-// vertex loads, and the extra warps hide more of them (5% faster than three blocks at 80
-// registers on the 1.3M-triangle frame).
-template <class R, bool MULTI>
-__global__ void __launch_bounds__(256, 4)
+// indexed the same way. Shading waits on slot and vertex loads: more resident warps hide more of
+// them, fewer registers spill more. The block shape (THREADS, MINB resident blocks per SM, which
+// sets the register cap) is one of kShadeVariants, chosen by the wavefront tuner.
+template <class R, bool MULTI, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_wf_shade(const __grid_constant__ DevScene S0, const __grid_constant__ RenderArgs A0, BatchDev B,
                FirstHit const *__restrict__ fh, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
                uint64_t total_paths) {
@@ -576,12 +578,44 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
     return n > 0 ? n : 1;
 }
 
+// The shading kernel's block shapes: threads per block and resident blocks per SM (the register
+// cap is 65536 / (threads x blocks)).
+constexpr int kShadeShape[kWfShadeVariants][2] = {{256, 4}, {256, 3}, {256, 5}, {128, 8}};
+
+int wf_shade_threads(uint32_t variant) { return kShadeShape[variant < kWfShadeVariants ? variant : 0][0]; }
+
+int wf_shade_grid(uint32_t variant, uint32_t capacity, int num_sms) {
+    variant = variant < kWfShadeVariants ? variant : 0;
+    int t = kShadeShape[variant][0], b = kShadeShape[variant][1];
+    return static_cast<int>(std::min<uint64_t>((capacity + t - 1) / t, static_cast<uint64_t>(num_sms) * b * 2));
+}
+
+template <class R>
+static void launch_shade(uint32_t variant, int grid, cudaStream_t st, DevScene const &S, RenderArgs const &A,
+                         FirstHit const *fh, WfSlots const &W, Counters *cnt, float4 *accum, float *path_rgb,
+                         uint64_t total_paths) {
+    BatchDev none{};
+    switch (variant) {
+    case 1:
+        k_wf_shade<R, false, 256, 3><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        break;
+    case 2:
+        k_wf_shade<R, false, 256, 5><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        break;
+    case 3:
+        k_wf_shade<R, false, 128, 8><<<grid, 128, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        break;
+    default:
+        k_wf_shade<R, false, 256, 4><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+    }
+}
+
 // One bounce: reset queue lengths, shade, then the trace kernel(s). B (or null): the scene table
 // of a many-scene wavefront (eight-wide trees, dynamic fetch). timing (or null): three events
 // recorded at the bounce's start, after its shading and after its trace kernel(s).
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
                        float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, uint64_t total_paths,
-                       BatchDev const *B, cudaStream_t st, cudaEvent_t const *timing) {
+                       BatchDev const *B, cudaStream_t st, cudaEvent_t const *timing, uint32_t shade_variant) {
     auto *cnt = reinterpret_cast<Counters *>(W.counters);
     auto mark = [&](int k) {
         if (timing)
@@ -589,11 +623,13 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
     };
     mark(0);
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
-    if (B) {
+    if (B) { // the many-scene form shades with the first block shape
         if (A.rng == E8G_RNG_MINSTD)
-            k_wf_shade<RngMinstd, true><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr, total_paths);
+            k_wf_shade<RngMinstd, true, 256, 4><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr,
+                                                                             total_paths);
         else
-            k_wf_shade<RngPhilox, true><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr, total_paths);
+            k_wf_shade<RngPhilox, true, 256, 4><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr,
+                                                                             total_paths);
         mark(1);
         k_wf_trace_wide_both<true><<<trace_grid, kBlock, 0, st>>>(S, A, *B, W, cnt, accum, nullptr, threshold);
         mark(2);
@@ -601,9 +637,9 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
     }
     BatchDev none{};
     if (A.rng == E8G_RNG_MINSTD)
-        k_wf_shade<RngMinstd, false><<<shade_grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        launch_shade<RngMinstd>(shade_variant, shade_grid, st, S, A, fh, W, cnt, accum, path_rgb, total_paths);
     else
-        k_wf_shade<RngPhilox, false><<<shade_grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        launch_shade<RngPhilox>(shade_variant, shade_grid, st, S, A, fh, W, cnt, accum, path_rgb, total_paths);
     mark(1);
     if (threshold > 0 && S.layout == 0) {
         k_wf_trace_dyn<true, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);

@@ -24,7 +24,13 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold);
 // B: the scene table of a many-scene wavefront (eight-wide trees, threshold > 0), or null.
 void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
                        float *path_rgb, int shade_grid, int trace_grid, uint32_t threshold, uint64_t total_paths,
-                       BatchDev const *B, cudaStream_t st, cudaEvent_t const *timing = nullptr);
+                       BatchDev const *B, cudaStream_t st, cudaEvent_t const *timing = nullptr,
+                       uint32_t shade_variant = 0);
+// Block shapes of the shading kernel (the tuner's choice): the number of them, the threads of
+// one, and the grid of a bounce over `capacity` slots.
+constexpr uint32_t kWfShadeVariants = 4;
+int wf_shade_threads(uint32_t variant);
+int wf_shade_grid(uint32_t variant, uint32_t capacity, int num_sms);
 uint32_t *wf_busy_ptr(WfSlots const &W);
 unsigned long long *wf_next_ptr(WfSlots const &W);
 

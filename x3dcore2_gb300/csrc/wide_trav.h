@@ -70,6 +70,21 @@ E8G_HD float hd_fma(float a, float b, float c) {
     return std::fmaf(a, b, c);
 #endif
 }
+// Two fused multiply-adds a0 * b + c and a1 * b + c with one instruction on sm_100 and later
+// (fma.rn.f32x2: each lane rounds like fmaf, so host and device results are equal).
+E8G_HD void hd_fma2(float a0, float a1, float b, float c, float &r0, float &r1) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    unsigned long long a, bb, cc, d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(bb) : "f"(b));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(cc) : "f"(c));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(bb), "l"(cc));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r0), "=f"(r1) : "l"(d));
+#else
+    r0 = hd_fma(a0, b, c);
+    r1 = hd_fma(a1, b, c);
+#endif
+}
 E8G_HD float hd_rcp(float x) {
 #if defined(__CUDA_ARCH__)
     return __frcp_rn(x);
@@ -248,9 +263,10 @@ E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3,
 #pragma unroll
 #endif
         for (uint32_t j = 0; j < 4; j++) {
-            float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
-            float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
-            float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
+            float tnx, tfx, tny, tfy, tnz, tfz; // near and far plane of an axis share S and O
+            hd_fma2(hd_qf(wnx, j), hd_qf(wfx, j), sx, ox, tnx, tfx);
+            hd_fma2(hd_qf(wny, j), hd_qf(wfy, j), sy, oy, tny, tfy);
+            hd_fma2(hd_qf(wnz, j), hd_qf(wfz, j), sz, oz, tnz, tfz);
             float tn = fmaxf(hd_max3(tnx, tny, tnz), T.tmin);
             float tf = fminf(hd_min3(tfx, tfy, tfz), T.cull);
             hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
