@@ -665,6 +665,7 @@ def main():
         pw = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
         abi.check(lib.e8g_wavefront_tune(ctx.h, C.byref(pw), C.byref(r)), ctx.h, "e8g_wavefront_tune")
         return {"capacity": r.capacity, "bounces_per_graph": r.bounces_per_graph, "threshold": r.threshold,
+                "shade_variant": r.shade_variant, "shade_ms": [round(r.shade_ms[i], 3) for i in range(r.num_shade)],
                 "candidates": [[r.cand_capacity[i], r.cand_bounces[i], r.cand_threshold[i], round(r.cand_ms[i], 3)]
                                for i in range(r.num_candidates)]}
 

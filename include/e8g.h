@@ -371,7 +371,7 @@ typedef struct e8g_tune_result {
     uint32_t cand_bounces[E8G_TUNE_MAX_CANDIDATES];
     uint32_t cand_threshold[E8G_TUNE_MAX_CANDIDATES];
     double cand_ms[E8G_TUNE_MAX_CANDIDATES];
-    uint32_t shade_variant;     /* chosen block shape of the shading kernel (0 .. num_shade - 1) */
+    uint32_t shade_variant;     /* chosen shape of the shading kernel (0 .. num_shade - 1) */
     uint32_t num_shade;         /* shapes timed */
     double shade_ms[8];         /* device time of the render with each shape */
     uint32_t from_cache;        /* e8g_wavefront_tune_cached: 1 when the choice came from the file */
@@ -381,8 +381,10 @@ e8g_status e8g_wavefront_tune(e8g_ctx *ctx, const e8g_render_params *params, e8g
 /* Sets the wavefront configuration directly: slot capacity (1024 .. 2^26), bounces captured per
  * graph (1 .. 16) and warp refill threshold (0 .. 32). */
 e8g_status e8g_wavefront_set(e8g_ctx *ctx, uint32_t capacity, uint32_t bounces_per_graph, uint32_t threshold);
-/* Block shape of the wavefront's shading kernel: 0 = 256 threads x 4 blocks per SM (64 registers),
- * 1 = 256 x 3 (80), 2 = 256 x 5 (48), 3 = 128 x 8 (64). */
+/* Shape of the wavefront's shading kernel (threads x resident blocks per SM, register cap, the
+ * materials' code inlined or out of line): 0 = 256 x 4 (64 registers), 1 = 256 x 3 (80),
+ * 2 = 256 x 4 out of line, 3 = 256 x 3 out of line, 4 = 256 x 5 (48) out of line, 5 = 128 x 8 (64)
+ * out of line. */
 e8g_status e8g_wavefront_set_shade(e8g_ctx *ctx, uint32_t variant);
 /* e8g_wavefront_tune with a cache of choices in a JSON file (`cache_path`): the key is the scene
  * and frame size bucket (tree layout, stream kind, log2 of the triangle count, of the pixels and of

@@ -133,13 +133,22 @@ int main() {
         std::vector<e8util::vec3> got = gt.sample(rng, rays, none, R.ps, R.mc, R.ls);
         uint64_t seed = static_cast<uint64_t>(shadow.draw() * 4294967296.0);
         std::unique_ptr<e8::if_path_tracer> ref_tracer(e8::pathtracer_factory(tc.type, e8::pathtracer_factory::options()).create());
-        unsigned ok = 0;
+        unsigned ok = 0, shown = 0;
         for (size_t i = 0; i < rays.size(); i++) {
             std::vector<e8util::ray> one{rays[i]};
             auto hits = e8::if_path_tracer::compute_first_hit(one, R.ps, R.ls);
-            e8util::rng pr(e8g_path_seed(seed, static_cast<uint32_t>(i), 0));
+            uint32_t ps = e8g_path_seed(seed, static_cast<uint32_t>(i), 0);
+            e8util::rng pr(ps);
             e8util::vec3 r = ref_tracer->sample(pr, one, hits, R.ps, R.mc, R.ls)[0];
-            ok += close(got[i](0), r(0), 1e-4f) && close(got[i](1), r(1), 1e-4f) && close(got[i](2), r(2), 1e-4f);
+            bool same = close(got[i](0), r(0), 1e-4f) && close(got[i](1), r(1), 1e-4f) && close(got[i](2), r(2), 1e-4f);
+            ok += same;
+            if (!same && shown++ < 4) {
+                uint32_t px = static_cast<uint32_t>(5 * i);
+                float orc[3];
+                o_render_paths(os, tc.mode, E8G_RNG_MINSTD, 0, &pol, w, h, &px, &ps, 1, orc, 1);
+                std::printf("  path %zu (pixel %u, seed %u): reference %g %g %g, gpu %g %g %g, oracle %g %g %g\n", i, px,
+                            ps, r(0), r(1), r(2), got[i](0), got[i](1), got[i](2), orc[0], orc[1], orc[2]);
+            }
         }
         double frac = static_cast<double>(ok) / rays.size();
         std::printf("%s gpu_path_tracer::sample = reference sample() on %.4f of %zu paths\n", tc.name, frac,

@@ -163,7 +163,9 @@ struct RngPhilox {
         block = 0;
         lane = 4;
     }
-    __device__ __forceinline__ void refill() {
+    // Out of line: next() is inlined at every draw site, and one copy of the ten rounds serves all
+    // of them (the shading kernels' code otherwise overflows the instruction cache).
+    __device__ __noinline__ void refill() {
         uint32_t c0 = block, c1 = pixel, c2 = sample, c3 = 0x0E8A0E8Au;
         uint32_t a = k0, b = k1;
 #pragma unroll
@@ -714,13 +716,21 @@ __device__ __forceinline__ float3 eval_leaf(const DevMaterial &m, float3 n, floa
     return scale(albedo, kInvPi); // mat_fail_safe, material.cpp:64-68
 }
 
+// One out-of-line copy of a leaf material's code for kernels whose instruction footprint
+// overflows the instruction cache (OUT = true in the BSDF functions below): every call site
+// then shares it instead of inlining both materials' code again. Same arithmetic either way.
+static __device__ __noinline__ float3 eval_leaf_call(const DevMaterial &m, float3 n, float3 o, float3 i) {
+    return eval_leaf(m, n, o, i);
+}
+
+template <bool OUT = false>
 __device__ __forceinline__ float3 bsdf_eval(const DevScene &S, const DevMaterial &m, float3 n, float3 o, float3 i) {
     if (m.type == 3) { // mat_mixture, material.cpp:90-93
-        float3 f0 = eval_leaf(S.mats[m.mix0], n, o, i);
-        float3 f1 = eval_leaf(S.mats[m.mix1], n, o, i);
+        float3 f0 = OUT ? eval_leaf_call(S.mats[m.mix0], n, o, i) : eval_leaf(S.mats[m.mix0], n, o, i);
+        float3 f1 = OUT ? eval_leaf_call(S.mats[m.mix1], n, o, i) : eval_leaf(S.mats[m.mix1], n, o, i);
         return add(scale(f0, m.ratio), scale(f1, 1 - m.ratio));
     }
-    return eval_leaf(m, n, o, i);
+    return OUT ? eval_leaf_call(m, n, o, i) : eval_leaf(m, n, o, i);
 }
 
 template <class R>
@@ -750,6 +760,11 @@ __device__ __forceinline__ float3 sample_leaf(const DevMaterial &m, R &rng, floa
     float3 i = cos_hemisphere(n, rng); // oren_nayar / fail-safe, material.cpp:70-76, :163-169
     dens = dot(i, n) / kPi;
     return i;
+}
+
+template <class R>
+__device__ __noinline__ float3 sample_leaf_call(const DevMaterial &m, R &rng, float &dens, float3 n, float3 o) {
+    return sample_leaf(m, rng, dens, n, o);
 }
 
 // Reference sampling (mat_mixture returns the picked lobe's density x its weight, :95-106).
@@ -788,30 +803,35 @@ __device__ __forceinline__ float pdf_leaf(const DevMaterial &m, float3 n, float3
     float c = dot(i, n);
     return c > 0.0f ? c / kPi : 0.0f;
 }
-__device__ __forceinline__ float bsdf_pdf(const DevScene &S, const DevMaterial &m, float3 n, float3 o, float3 i) {
-    if (m.type == 3)
-        return m.ratio * pdf_leaf(S.mats[m.mix0], n, o, i) + (1 - m.ratio) * pdf_leaf(S.mats[m.mix1], n, o, i);
+static __device__ __noinline__ float pdf_leaf_call(const DevMaterial &m, float3 n, float3 o, float3 i) {
     return pdf_leaf(m, n, o, i);
 }
+template <bool OUT = false>
+__device__ __forceinline__ float bsdf_pdf(const DevScene &S, const DevMaterial &m, float3 n, float3 o, float3 i) {
+    if (m.type == 3) {
+        float p0 = OUT ? pdf_leaf_call(S.mats[m.mix0], n, o, i) : pdf_leaf(S.mats[m.mix0], n, o, i);
+        float p1 = OUT ? pdf_leaf_call(S.mats[m.mix1], n, o, i) : pdf_leaf(S.mats[m.mix1], n, o, i);
+        return m.ratio * p0 + (1 - m.ratio) * p1;
+    }
+    return OUT ? pdf_leaf_call(m, n, o, i) : pdf_leaf(m, n, o, i);
+}
 // Product-mode sampling: a mixture reports its true mixture density.
-template <class R>
+template <bool OUT = false, class R>
 __device__ __forceinline__ float3 bsdf_sample_mis(const DevScene &S, const DevMaterial &m, R &rng, float &pdf,
                                                   float3 n, float3 o) {
     if (m.type == 3) {
         float lobe_pdf;
         float3 i;
-        if (rng.next() < m.ratio)
-            i = sample_leaf(S.mats[m.mix0], rng, lobe_pdf, n, o);
-        else
-            i = sample_leaf(S.mats[m.mix1], rng, lobe_pdf, n, o);
+        DevMaterial const &lobe = rng.next() < m.ratio ? S.mats[m.mix0] : S.mats[m.mix1];
+        i = OUT ? sample_leaf_call(lobe, rng, lobe_pdf, n, o) : sample_leaf(lobe, rng, lobe_pdf, n, o);
         if (lobe_pdf == 0.0f) {
             pdf = 0.0f;
             return f3(0, 0, 0);
         }
-        pdf = bsdf_pdf(S, m, n, o, i);
+        pdf = bsdf_pdf<OUT>(S, m, n, o, i);
         return i;
     }
-    return sample_leaf(m, rng, pdf, n, o);
+    return OUT ? sample_leaf_call(m, rng, pdf, n, o) : sample_leaf(m, rng, pdf, n, o);
 }
 
 // -------------------------------------------------------------------- lights ----

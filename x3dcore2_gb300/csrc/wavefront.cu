@@ -122,8 +122,10 @@ __device__ __forceinline__ RenderArgs const &args_of(RenderArgs const &A0, Batch
 // scene index, `out` is the path's pixel in the concatenated accumulator and first hits are
 // indexed the same way. Shading waits on slot and vertex loads: more resident warps hide more of
 // them, fewer registers spill more. The block shape (THREADS, MINB resident blocks per SM, which
-// sets the register cap) is one of kShadeVariants, chosen by the wavefront tuner.
-template <class R, bool MULTI, int THREADS, int MINB>
+// sets the register cap) and OUT (the materials' code out of line, one copy for every call site:
+// the inlined form overflows the instruction cache) are one of kShadeShape, chosen by the
+// wavefront tuner.
+template <class R, bool MULTI, int THREADS, int MINB, bool OUT>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_wf_shade(const __grid_constant__ DevScene S0, const __grid_constant__ RenderArgs A0, BatchDev B,
                FirstHit const *__restrict__ fh, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
@@ -275,10 +277,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 float3 wi = neg(ln);
                 float cos_x = dot(n, wi);
                 if (cos_l > 0.0f && cos_x > 0.0f) {
-                    float3 f = bsdf_eval(S, m, n, o, wi);
+                    float3 f = bsdf_eval<OUT>(S, m, n, o, wi);
                     if (!vequals0(f)) {
                         float p_l = pmf * ls.area_dens * r2 / cos_l;
-                        float p_b = bsdf_pdf(S, m, n, o, wi);
+                        float p_b = bsdf_pdf<OUT>(S, m, n, o, wi);
                         float w = power_heuristic(p_l, p_b);
                         sh_c = scale(mul(mul(beta, f), light_rad(S, light)), cos_x * w / p_l);
                         sh_dir = wi;
@@ -287,11 +289,11 @@ __global__ void __launch_bounds__(THREADS, MINB)
                     }
                 }
                 float pdf;
-                float3 i = bsdf_sample_mis(S, m, rng, pdf, n, o);
+                float3 i = bsdf_sample_mis<OUT>(S, m, rng, pdf, n, o);
                 if (pdf > 0.0f) {
                     float cw = dot(n, i);
                     if (cw > 0.0f) {
-                        float3 f = bsdf_eval(S, m, n, o, i);
+                        float3 f = bsdf_eval<OUT>(S, m, n, o, i);
                         beta = mul(beta, scale(f, cw / pdf));
                         o = neg(i);
                         last_pdf = pdf;
@@ -578,9 +580,10 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
     return n > 0 ? n : 1;
 }
 
-// The shading kernel's block shapes: threads per block and resident blocks per SM (the register
-// cap is 65536 / (threads x blocks)).
-constexpr int kShadeShape[kWfShadeVariants][2] = {{256, 4}, {256, 3}, {256, 5}, {128, 8}};
+// The shading kernel's shapes: threads per block, resident blocks per SM (the register cap is
+// 65536 / (threads x blocks)) and whether the materials' code is out of line.
+constexpr int kShadeShape[kWfShadeVariants][3] = {{256, 4, 0}, {256, 3, 0}, {256, 4, 1},
+                                                  {256, 3, 1}, {256, 5, 1}, {128, 8, 1}};
 
 int wf_shade_threads(uint32_t variant) { return kShadeShape[variant < kWfShadeVariants ? variant : 0][0]; }
 
@@ -597,16 +600,22 @@ static void launch_shade(uint32_t variant, int grid, cudaStream_t st, DevScene c
     BatchDev none{};
     switch (variant) {
     case 1:
-        k_wf_shade<R, false, 256, 3><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        k_wf_shade<R, false, 256, 3, false><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
         break;
     case 2:
-        k_wf_shade<R, false, 256, 5><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        k_wf_shade<R, false, 256, 4, true><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
         break;
     case 3:
-        k_wf_shade<R, false, 128, 8><<<grid, 128, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        k_wf_shade<R, false, 256, 3, true><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        break;
+    case 4:
+        k_wf_shade<R, false, 256, 5, true><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        break;
+    case 5:
+        k_wf_shade<R, false, 128, 8, true><<<grid, 128, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
         break;
     default:
-        k_wf_shade<R, false, 256, 4><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
+        k_wf_shade<R, false, 256, 4, false><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
     }
 }
 
@@ -625,11 +634,11 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
     if (B) { // the many-scene form shades with the first block shape
         if (A.rng == E8G_RNG_MINSTD)
-            k_wf_shade<RngMinstd, true, 256, 4><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr,
-                                                                             total_paths);
+            k_wf_shade<RngMinstd, true, 256, 4, false><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr,
+                                                                                    total_paths);
         else
-            k_wf_shade<RngPhilox, true, 256, 4><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr,
-                                                                             total_paths);
+            k_wf_shade<RngPhilox, true, 256, 4, false><<<shade_grid, 256, 0, st>>>(S, A, *B, fh, W, cnt, accum, nullptr,
+                                                                                    total_paths);
         mark(1);
         k_wf_trace_wide_both<true><<<trace_grid, kBlock, 0, st>>>(S, A, *B, W, cnt, accum, nullptr, threshold);
         mark(2);

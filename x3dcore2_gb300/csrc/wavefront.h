@@ -28,7 +28,7 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
                        uint32_t shade_variant = 0);
 // Block shapes of the shading kernel (the tuner's choice): the number of them, the threads of
 // one, and the grid of a bounce over `capacity` slots.
-constexpr uint32_t kWfShadeVariants = 4;
+constexpr uint32_t kWfShadeVariants = 6;
 int wf_shade_threads(uint32_t variant);
 int wf_shade_grid(uint32_t variant, uint32_t capacity, int num_sms);
 uint32_t *wf_busy_ptr(WfSlots const &W);
