@@ -346,18 +346,29 @@ def cornell_leg(ctx, threads, cpu_budget_s=6.0):
 def bdpt_leg(ctx):
     """Bidirectional MIS on the benchmark scene (still uploaded) at 1280x720, subpaths of at most 6
     vertices, 32 spp: power-heuristic weights (E8G_MODE_BDPT_POWER) and the reference's uniform
-    weights (E8G_MODE_REF_BDPT)."""
+    weights (E8G_MODE_REF_BDPT). Per mode the traversal roofline of its kernel (one launch per
+    frame): algorithmic bytes from the counted run (node bytes per node box fetched + 48 B per
+    triangle tested) over the kernel's device time, against the measured HBM copy bandwidth."""
     from x3dcore2_gb300 import abi
     from x3dcore2_gb300.core import default_params
-    out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6}
-    for name, mode in (("power", abi.MODE_BDPT_POWER), ("uniform", abi.MODE_REF_BDPT)):
+    peak, _ = read_peaks()
+    st = ctx.bvh_stats()
+    node_bytes = st["node_bytes"] // max(st["num_nodes"], 1)
+    out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6, "node_bytes": node_bytes}
+    for name, mode, kern in (("power", abi.MODE_BDPT_POWER, "k_bdpt_power"), ("uniform", abi.MODE_REF_BDPT, "k_bdpt_ref")):
         p = default_params(mode, 1280, 720, 32, seed=1, bdpt_max_len=6)
         ctx.render(p)
         ms = []
         for _ in range(2):
             ctx.render(p)
             ms.append(ctx.stats()["kernel_ms"])
-        out[name] = {"kernel_ms": statistics.mean(ms), "paths_per_s": 1280 * 720 * 32 / (statistics.mean(ms) / 1000.0)}
+        kms = statistics.mean(ms)
+        c = ctx.count_traversal(p)
+        alg = node_bytes * c["nodes"] + 48 * c["tris"]
+        out[name] = {"kernel_ms": kms, "paths_per_s": 1280 * 720 * 32 / (kms / 1000.0),
+                     "roofline": {"kernel": kern, "rays": c["rays"], "nodes": c["nodes"], "tris": c["tris"],
+                                  "algorithmic_bytes": alg, "achieved_gbs": alg / (kms / 1e3) / 1e9,
+                                  "frac": alg / (kms / 1e3) / 1e9 / peak}}
     return out
 
 
@@ -421,6 +432,75 @@ def adjoint_leg(ctx):
             bwd.append(b)
     return {"triangles": sc.num_tris, "materials": 256, "forward_ms": statistics.mean(fwd),
             "backward_ms": statistics.mean(bwd), "ratio": statistics.mean(bwd) / statistics.mean(fwd)}
+
+
+def adjoint_fd_leg(ctx, spps=(1024, 4096, 16384)):
+    """How the gap between the path-replay roughness gradient and central finite differences
+    (h = 1e-3, common random numbers) shrinks with the sample count, on the differentiable
+    configuration (level-7 displaced icosphere, 256 materials, 512x512, depth 6): the replayed
+    gradient holds each sampled GGX direction fixed and differentiates the path's weight, the
+    finite differences move the directions with the roughness, so the two agree in expectation
+    and differ by sampling noise. The four largest roughness entries at the smallest count are
+    followed at every count. Images for the differences are summed in float64 from 64-sample
+    chunks of the same streams."""
+    import numpy as np
+    import torch
+    from x3dcore2_gb300 import abi
+    from x3dcore2_gb300 import scene as S
+    from x3dcore2_gb300.core import default_params
+    W = H = 512
+    sc = S.displaced_icosphere(level=7, seed=5, num_materials=256, width=W, height=H)
+    ctx.upload(sc)
+    base = sc.material_list()
+    rng = np.random.default_rng(3)
+    pert = []
+    for m in base:
+        q = abi.Material.from_buffer_copy(m)
+        if q.type in (abi.MAT_OREN_NAYAR, abi.MAT_COOK_TORR):
+            q.albedo[:] = list(np.clip(np.array(list(m.albedo)) + rng.normal(0, 0.05, 3), 0.05, 0.95))
+        if q.type == abi.MAT_COOK_TORR:
+            q.roughness = float(np.clip(m.roughness + rng.normal(0, 0.05), 0.05, 1.0))
+        pert.append(q)
+    ctx.set_materials(pert)
+    tgt = torch.from_numpy(ctx.render(default_params(abi.MODE_MIS, W, H, 64, seed=2, max_depth=6, rr_start=3))
+                           [..., :3].astype(np.float64)).cuda()
+    stream = torch.cuda.current_stream()
+    buf = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+
+    def image(mats, spp, chunk=64):
+        ctx.set_materials(mats)
+        q = default_params(abi.MODE_MIS, W, H, chunk, seed=1, max_depth=6, rr_start=3)
+        acc = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+        for k in range(spp // chunk):
+            q.sample_offset = k * chunk
+            ctx.render_dev(q, buf.data_ptr(), stream.cuda_stream)
+            acc += buf[..., :3].double()
+        return acc / (spp // chunk)
+
+    metal = [m for m in range(len(base)) if base[m].type == abi.MAT_COOK_TORR]
+    out, entries = {"h": 1e-3, "spp": {}}, None
+    for spp in spps:
+        t0 = time.time()
+        img = image(base, spp)
+        ctx.set_materials(base)
+        ctx.forward(default_params(abi.MODE_MIS, W, H, spp, seed=1, max_depth=6, rr_start=3))
+        _, dr = ctx.backward((2 * (img - tgt)).float().cpu().numpy())
+        if entries is None:
+            entries = sorted(metal, key=lambda m: -abs(dr[m]))[:4]
+        rows = []
+        for m in entries:
+            plus = [abi.Material.from_buffer_copy(x) for x in base]
+            minus = [abi.Material.from_buffer_copy(x) for x in base]
+            plus[m].roughness += 1e-3
+            minus[m].roughness -= 1e-3
+            lp = float(((image(plus, spp) - tgt) ** 2).sum())
+            lm = float(((image(minus, spp) - tgt) ** 2).sum())
+            fd = (lp - lm) / 2e-3
+            rows.append({"material": m, "fd": fd, "adjoint": float(dr[m]), "rel_gap": abs(float(dr[m]) - fd) / abs(fd)})
+        out["spp"][spp] = {"entries": rows, "max_rel_gap": max(r["rel_gap"] for r in rows),
+                           "mean_rel_gap": sum(r["rel_gap"] for r in rows) / len(rows), "seconds": time.time() - t0}
+    ctx.set_materials(base)
+    return out
 
 
 def update_leg(ctx, scene):
@@ -541,7 +621,7 @@ def run_leg(args):
     scene, _, _, _ = make_scene(args.small)
     ctx.upload(scene)
     fn = {"bdpt": lambda: bdpt_leg(ctx), "batch": lambda: batch_leg(ctx), "adjoint": lambda: adjoint_leg(ctx),
-          "update": lambda: update_leg(ctx, scene),
+          "update": lambda: update_leg(ctx, scene), "adjoint_fd": lambda: adjoint_fd_leg(ctx),
           "cornell": lambda: cornell_leg(ctx, os.cpu_count() or 1)}[args.leg]
     print(json.dumps({"leg": args.leg, **fn()}))
     ctx.close()
@@ -610,7 +690,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the quality, BDPT, batch and adjoint legs")
     ap.add_argument("--no-tune", action="store_true", help="wavefront with the library defaults (profiling)")
-    ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "update", "obj", "cornell"],
+    ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "adjoint_fd", "update", "obj", "cornell"],
                     help="run one extra leg alone on the benchmark scene and print its JSON (not a bench line)")
     args = ap.parse_args()
     if args.impl == "reference":

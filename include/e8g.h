@@ -419,7 +419,9 @@ e8g_status e8g_wavefront_tune_cached(e8g_ctx *ctx, const e8g_render_params *para
 e8g_status e8g_render_dev_noalloc(e8g_ctx *ctx, const e8g_render_params *params, float *d_rgba_out,
                                   void *stream);
 /* Runs the render once with traversal counters on (not for timing) and returns the number of
- * rays traced, BVH nodes whose box was fetched and triangles tested. */
+ * rays traced, BVH nodes whose box was fetched and triangles tested. Every mode but
+ * E8G_MODE_REF_LT2 (E8G_ERR_UNSUPPORTED); the wavefront integrator is counted through the
+ * megakernel, which traces the same rays. */
 e8g_status e8g_count_traversal(e8g_ctx *ctx, const e8g_render_params *params, e8g_render_stats *stats);
 
 /* Per-path radiance for explicit primary rays (if_path_tracer::sample, pathtracer.h:59-63): path i

@@ -319,3 +319,20 @@ def test_wavefront_tuner_cache_and_shade_shapes(ctx, tmp_path):
         close = np.all(np.abs(img - base) <= np.maximum(1e-4 * np.abs(base), 1e-6), axis=-1)
         assert close.mean() >= 0.999, v
     assert ctx.lib.e8g_wavefront_set_shade(ctx.h, 4) == 1
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER])
+def test_bidirectional_traversal_counts(ctx, mode):
+    """e8g_count_traversal covers the bidirectional kernels (the roofline's algorithmic bytes): the
+    counted render traces rays, fetches node boxes and tests triangles, and its image is the
+    uncounted one."""
+    sc = S.cornell(64, 48)
+    ctx.upload(sc, layout=abi.BVH_WIDE)
+    p = default_params(mode, 64, 48, 4, seed=2, bdpt_max_len=6)
+    img = ctx.render(p)
+    c = ctx.count_traversal(p)
+    assert c["counted"] == 1 and c["rays"] > 64 * 48 * 4 and c["nodes"] > c["rays"] and c["tris"] > 0
+    again = ctx.render(p)
+    np.testing.assert_allclose(again, img, rtol=1e-5, atol=1e-6)
+    with pytest.raises(Exception, match="UNSUPPORTED"):
+        ctx.count_traversal(default_params(abi.MODE_REF_LT2, 64, 48, 1))

@@ -23,16 +23,18 @@ struct PV { // sampled_pathlet (pathtracer.cpp:12-40)
     int32_t light;
 };
 
-template <class R>
+template <bool COUNT, class R>
 __device__ __forceinline__ uint32_t sample_subpath(DevScene const &S, R &rng, PV *path, uint32_t depth,
-                                                   uint32_t max_len, uint32_t *stk) {
+                                                   uint32_t max_len, uint32_t *stk, TraceCounters *cnt) {
     while (depth != max_len) { // sample_path, pathtracer.cpp:73-95
         PV const &prev = path[depth - 1];
         float w_dens;
         float3 i = bsdf_sample_ref(S, vert_mat(S, prev.mesh), rng, w_dens, prev.n, prev.v);
         if (feq0(w_dens))
             return depth;
-        Hit h = trace_closest<false>(S, prev.p, i, stk, nullptr);
+        if (COUNT)
+            cnt->rays++;
+        Hit h = trace_closest<COUNT>(S, prev.p, i, stk, cnt);
         if (h.tri == 0xFFFFFFFFu)
             return depth;
         Vert nv = make_vert(S, h);
@@ -51,22 +53,26 @@ __device__ __forceinline__ uint32_t sample_subpath(DevScene const &S, R &rng, PV
 }
 
 // transport_illum_source (pathtracer.cpp:152-176)
+template <bool COUNT>
 __device__ __forceinline__ float3 illum_source(DevScene const &S, int light, float3 pl, float3 nl, PV const &tv,
-                                               uint32_t *stk) {
+                                               uint32_t *stk, TraceCounters *cnt) {
     float3 l = sub(tv.p, pl);
     float3 illum = light_eval(S, light, l, nl, tv.n);
     if (vequals0(illum))
         return f3(0, 0, 0);
     float dist = norm(l);
     float3 i = divs(neg(l), dist);
-    if (!trace_any<false>(S, tv.p, i, 1e-4f, dist - 1e-3f, stk, nullptr))
+    if (COUNT)
+        cnt->rays++;
+    if (!trace_any<COUNT>(S, tv.p, i, 1e-4f, dist - 1e-3f, stk, cnt))
         return mul(illum, bsdf_eval(S, vert_mat(S, tv.mesh), tv.n, tv.v, i));
     return f3(0, 0, 0);
 }
 
 // transport_all_connectible_subpaths (pathtracer.cpp:351-452)
+template <bool COUNT>
 __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, PV const *lp, uint32_t llen, float3 em_p,
-                              float3 em_n, float em_area_dens, int light, uint32_t *stk) {
+                              float3 em_n, float em_area_dens, int light, uint32_t *stk, TraceCounters *cnt) {
     if (clen == 0)
         return f3(0, 0, 0);
     float3 cam_pre[kMaxSub], light_pre[kMaxSub];
@@ -102,7 +108,7 @@ __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, P
                 wsum += cw;
             } else if (light_plen == 0) {
                 PV const &cj = cam[cam_plen - 1];
-                float3 ti = divs(illum_source(S, light, em_p, em_n, cj, stk), em_area_dens);
+                float3 ti = divs(illum_source<COUNT>(S, light, em_p, em_n, cj, stk, cnt), em_area_dens);
                 float3 pr = divs(mul(ti, cam_pre[cam_plen - 1]), cam[0].dens);
                 psum = add(psum, scale(pr, cw));
                 wsum += cw;
@@ -114,7 +120,9 @@ __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, P
                 join = divs(join, jd);
                 float cos_wo = dot(lj.n, join);
                 float cos_wi = dot(cj.n, neg(join));
-                if (cos_wo > 0.0f && cos_wi > 0.0f && !trace_any<false>(S, lj.p, join, 1e-3f, jd - 1e-3f, stk, nullptr)) {
+                if (COUNT && cos_wo > 0.0f && cos_wi > 0.0f)
+                    cnt->rays++;
+                if (cos_wo > 0.0f && cos_wi > 0.0f && !trace_any<COUNT>(S, lj.p, join, 1e-3f, jd - 1e-3f, stk, cnt)) {
                     float3 le = divs(light_projected(S, light, neg(lp[0].v), em_n), lp[0].dens * em_area_dens);
                     float3 lsi = mul(le, light_pre[light_plen - 1]);
                     float to_area = cos_wi * cos_wo / (jd * jd);
@@ -162,9 +170,9 @@ __device__ __forceinline__ float vpdf(DevScene const &S, BV const &v, float3 wo,
     return bsdf_pdf(S, vert_mat(S, v.mesh), v.n, wo, wi);
 }
 
-template <class R>
+template <bool COUNT, class R>
 __device__ uint32_t bdp_walk(DevScene const &S, R &rng, BV *path, uint32_t len, uint32_t max_len, float3 wo,
-                             uint32_t *stk) {
+                             uint32_t *stk, TraceCounters *cnt) {
     while (len < max_len) {
         BV &cur = path[len - 1];
         const DevMaterial &m = vert_mat(S, cur.mesh);
@@ -176,7 +184,9 @@ __device__ uint32_t bdp_walk(DevScene const &S, R &rng, BV *path, uint32_t len, 
         if (cw <= 0.0f)
             break;
         float3 f = bsdf_eval(S, m, cur.n, wo, i);
-        Hit h = trace_closest<false>(S, cur.p, i, stk, nullptr);
+        if (COUNT)
+            cnt->rays++;
+        Hit h = trace_closest<COUNT>(S, cur.p, i, stk, cnt);
         if (h.tri == 0xFFFFFFFFu)
             break;
         Vert nv = make_vert(S, h);
@@ -198,8 +208,9 @@ __device__ uint32_t bdp_walk(DevScene const &S, R &rng, BV *path, uint32_t len, 
     return len;
 }
 
+template <bool COUNT>
 __device__ float3 connect_power(DevScene const &S, BV *cam, uint32_t clen, BV *lp, uint32_t llen, uint32_t maxlen,
-                                float3 o0, int light, uint32_t *stk) {
+                                float3 o0, int light, uint32_t *stk, TraceCounters *cnt) {
     float3 L = f3(0, 0, 0);
     for (uint32_t t = 1; t <= clen; t++) {
         for (uint32_t sl = 0; sl <= llen; sl++) {
@@ -246,7 +257,9 @@ __device__ float3 connect_power(DevScene const &S, BV *cam, uint32_t clen, BV *l
                 }
                 if (vequals0(fl))
                     continue;
-                if (trace_any<false>(S, cv.p, dir, 1e-4f, dist - 1e-3f, stk, nullptr))
+                if (COUNT)
+                    cnt->rays++;
+                if (trace_any<COUNT>(S, cv.p, dir, 1e-4f, dist - 1e-3f, stk, cnt))
                     continue;
                 float G = cos_c * cos_l / d2;
                 contrib = scale(mul(mul(mul(cv.beta, fc), fl), lv.beta), G);
@@ -300,9 +313,28 @@ template <> __device__ __forceinline__ void seed_path<RngPhilox>(RngPhilox &rng,
 }
 
 
-template <class R>
+// Adds a thread's traversal counts (rays traced, node boxes fetched, triangles tested) to the
+// three device counters, one atomic per warp and counter.
+__device__ __forceinline__ void flush_counts(TraceCounters const &cnt, unsigned long long *counters) {
+    unsigned long long a = cnt.rays, b = cnt.nodes, c = cnt.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(~0u, a, off);
+        b += __shfl_down_sync(~0u, b, off);
+        c += __shfl_down_sync(~0u, c, off);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(&counters[0], a);
+        atomicAdd(&counters[1], b);
+        atomicAdd(&counters[2], c);
+    }
+}
+
+// COUNT: the instrumented instantiation that counts traversal work into counters[0..2].
+template <class R, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
-                                                     float4 *accum, float *path_rgb, unsigned long long *work) {
+                                                     float4 *accum, float *path_rgb, unsigned long long *work,
+                                                     unsigned long long *counters) {
+    TraceCounters cnt{0, 0, 0};
     __shared__ uint32_t stk_all[kStackWords * kBlock];
     uint32_t *stk = stk_all + threadIdx.x;
     const uint64_t mix = splitmix64(A.seed);
@@ -331,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
                 cam[0].n = xyz(f.n);
                 cam[0].mesh = mesh;
                 cam[0].light = __float_as_int(f.n.w);
-                clen = sample_subpath(S, rng, cam, 1, max_len, stk);
+                clen = sample_subpath<COUNT>(S, rng, cam, 1, max_len, stk, &cnt);
             }
             // sample_illum_source (:754-767), area_light::sample_emssion (light.cpp:26-32)
             float pmf;
@@ -341,7 +373,9 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
             float sa_dens = dot(em.n, w) / kPi;
             em.area_dens *= pmf;
             uint32_t llen = 0;
-            Hit h = trace_closest<false>(S, em.p, w, stk, nullptr); // sample_path from r0 (:109-120)
+            if (COUNT)
+                cnt.rays++;
+            Hit h = trace_closest<COUNT>(S, em.p, w, stk, &cnt); // sample_path from r0 (:109-120)
             if (h.tri != 0xFFFFFFFFu && max_len != 0) {
                 Vert v0 = make_vert(S, h);
                 if (!(dot(v0.n, neg(w)) <= 0.0f)) {
@@ -351,10 +385,10 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
                     lp[0].n = v0.n;
                     lp[0].mesh = v0.mesh;
                     lp[0].light = -1;
-                    llen = sample_subpath(S, rng, lp, 1, max_len, stk);
+                    llen = sample_subpath<COUNT>(S, rng, lp, 1, max_len, stk, &cnt);
                 }
             }
-            float3 L = connect_all(S, cam, clen, lp, llen, em.p, em.n, em.area_dens, light, stk);
+            float3 L = connect_all<COUNT>(S, cam, clen, lp, llen, em.p, em.n, em.area_dens, light, stk, &cnt);
             if (path_rgb) {
                 path_rgb[3 * static_cast<size_t>(out)] = L.x;
                 path_rgb[3 * static_cast<size_t>(out) + 1] = L.y;
@@ -364,11 +398,15 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
             }
         }
     }
+    if (COUNT)
+        flush_counts(cnt, counters);
 }
 
-template <class R>
+template <class R, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
-                                                       float4 *accum, float *path_rgb, unsigned long long *work) {
+                                                       float4 *accum, float *path_rgb, unsigned long long *work,
+                                                       unsigned long long *counters) {
+    TraceCounters cnt{0, 0, 0};
     __shared__ uint32_t stk_all[kStackWords * kBlock];
     uint32_t *stk = stk_all + threadIdx.x;
     const uint64_t mix = splitmix64(A.seed);
@@ -398,7 +436,7 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
                 cam[0].beta = f3(1.0f, 1.0f, 1.0f);
                 cam[0].fwd = 1.0f;
                 cam[0].rev = 0.0f;
-                clen = bdp_walk(S, rng, cam, 1, max_len, o0, stk);
+                clen = bdp_walk<COUNT>(S, rng, cam, 1, max_len, o0, stk, &cnt);
             }
             float pmf;
             int light = sample_light(S, rng, pmf);
@@ -416,7 +454,9 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
                 lp[0].beta = f3(ib, ib, ib);
                 llen = 1;
                 if (pdf_w > 0.0f && max_len > 1) {
-                    Hit h = trace_closest<false>(S, em.p, w, stk, nullptr);
+                    if (COUNT)
+                        cnt.rays++;
+                    Hit h = trace_closest<COUNT>(S, em.p, w, stk, &cnt);
                     if (h.tri != 0xFFFFFFFFu) {
                         Vert v0 = make_vert(S, h);
                         if (dot(v0.n, neg(w)) > 0.0f) {
@@ -426,12 +466,12 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
                             lp[1].beta = scale(light_rad(S, light), dot(em.n, w) / (pdf_w * lp[0].fwd));
                             lp[1].fwd = to_area(pdf_w, em.p, lp[1].p, lp[1].n);
                             lp[1].rev = 0.0f;
-                            llen = bdp_walk(S, rng, lp, 2, max_len, neg(w), stk);
+                            llen = bdp_walk<COUNT>(S, rng, lp, 2, max_len, neg(w), stk, &cnt);
                         }
                     }
                 }
             }
-            float3 L = clen ? connect_power(S, cam, clen, lp, llen, max_len, o0, light, stk) : f3(0, 0, 0);
+            float3 L = clen ? connect_power<COUNT>(S, cam, clen, lp, llen, max_len, o0, light, stk, &cnt) : f3(0, 0, 0);
             if (path_rgb) {
                 path_rgb[3 * static_cast<size_t>(out)] = L.x;
                 path_rgb[3 * static_cast<size_t>(out) + 1] = L.y;
@@ -441,13 +481,15 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
             }
         }
     }
+    if (COUNT)
+        flush_counts(cnt, counters);
 }
 
 } // namespace
 
 int bdpt_blocks_per_sm() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bdpt_ref<RngMinstd>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bdpt_ref<RngMinstd, false>, kBlock, 0);
     return n > 0 ? n : 1;
 }
 
@@ -461,7 +503,7 @@ __device__ __forceinline__ float3 lt2_join(DevScene const &S, R &rng, PV const &
     int light = sample_light(S, rng, pmf);
     Surf ls = mesh_sample(S, __ldg(&S.light_mesh[light]), rng, false);
     ls.area_dens *= pmf;
-    float3 p1 = divs(add(f3(0, 0, 0), divs(illum_source(S, light, ls.p, ls.n, tv, stk), ls.area_dens)), 1.0f);
+    float3 p1 = divs(add(f3(0, 0, 0), divs(illum_source<false>(S, light, ls.p, ls.n, tv, stk, nullptr), ls.area_dens)), 1.0f);
     float pmf2;
     int light2 = sample_light(S, rng, pmf2);
     Surf em = mesh_sample(S, __ldg(&S.light_mesh[light2]), rng, false); // area_light::sample_emssion
@@ -572,25 +614,34 @@ __global__ void __launch_bounds__(kBlock) k_lt2(DevScene S, RenderArgs A, FirstH
 }
 
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                 unsigned long long *work, int grid, cudaStream_t st) {
+                 unsigned long long *work, int grid, cudaStream_t st, unsigned long long *counters) {
+    bool minstd = A.rng == E8G_RNG_MINSTD;
     if (A.mode == E8G_MODE_BDPT_POWER) {
-        if (A.rng == E8G_RNG_MINSTD)
-            k_bdpt_power<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+        if (counters && minstd)
+            k_bdpt_power<RngMinstd, true><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
+        else if (counters)
+            k_bdpt_power<RngPhilox, true><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
+        else if (minstd)
+            k_bdpt_power<RngMinstd, false><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
         else
-            k_bdpt_power<RngPhilox><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+            k_bdpt_power<RngPhilox, false><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
         return;
     }
     if (A.mode == E8G_MODE_REF_LT2) {
-        if (A.rng == E8G_RNG_MINSTD)
+        if (minstd)
             k_lt2<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
         else
             k_lt2<RngPhilox><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
         return;
     }
-    if (A.rng == E8G_RNG_MINSTD)
-        k_bdpt_ref<RngMinstd><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+    if (counters && minstd)
+        k_bdpt_ref<RngMinstd, true><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
+    else if (counters)
+        k_bdpt_ref<RngPhilox, true><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, counters);
+    else if (minstd)
+        k_bdpt_ref<RngMinstd, false><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
     else
-        k_bdpt_ref<RngPhilox><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work);
+        k_bdpt_ref<RngPhilox, false><<<grid, kBlock, 0, st>>>(S, A, fh, accum, path_rgb, work, nullptr);
 }
 
 } // namespace e8g

@@ -218,6 +218,7 @@ __host__ __device__ __forceinline__ uint32_t path_seed(uint64_t seed_mix, uint32
 
 struct TraceCounters {
     uint32_t nodes, tris;
+    uint32_t rays; // counted by the callers that trace (the bidirectional kernels)
 };
 
 // Slab test of a node box against [tmin, tmax] (aabb::intersect, tensor.h:815-840, with the

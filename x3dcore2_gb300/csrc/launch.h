@@ -68,8 +68,9 @@ cudaError_t launch_composite(float const *d_rgba, uint32_t w, uint32_t h, e8g_co
                              uint8_t *d_out, double *d_scratch, cudaStream_t st);
 
 // Bidirectional path tracing (uniform or power-heuristic weights), one thread per path.
+// counters (or null): the instrumented run (bidirectional modes; rays, node boxes, triangles).
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                 unsigned long long *work, int grid, cudaStream_t st);
+                 unsigned long long *work, int grid, cudaStream_t st, unsigned long long *counters = nullptr);
 int bdpt_blocks_per_sm();
 
 } // namespace e8g

@@ -30,7 +30,8 @@ e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs con
     auto *work = static_cast<unsigned long long *>(c->b_work.ptr);
     auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
     if (A.mode == E8G_MODE_REF_BDPT || A.mode == E8G_MODE_BDPT_POWER || A.mode == E8G_MODE_REF_LT2) {
-        launch_bdpt(c->dev, A, fh, accum, path_rgb, work, persistent_grid(c, bdpt_blocks_per_sm()), c->stream);
+        launch_bdpt(c->dev, A, fh, accum, path_rgb, work, persistent_grid(c, bdpt_blocks_per_sm()), c->stream,
+                    d_counts);
     } else {
         int grid = persistent_grid(c, megakernel_blocks_per_sm());
         launch_megakernel(c->dev, A, fh, accum, path_rgb, work, d_counts, grid, c->stream,
@@ -165,8 +166,8 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
 
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts,
                         uint64_t prior_spp) {
-    if (counts && (p->mode == E8G_MODE_REF_BDPT || p->mode == E8G_MODE_BDPT_POWER || p->mode == E8G_MODE_REF_LT2))
-        return fail(c, E8G_ERR_UNSUPPORTED, "traversal counters cover the unidirectional integrators");
+    if (counts && p->mode == E8G_MODE_REF_LT2)
+        return fail(c, E8G_ERR_UNSUPPORTED, "traversal counters cover every integrator but bidirect_lt2");
     nvtx_range range("e8g render");
     if (take_cancel(c))
         return fail(c, E8G_ERR_CANCELLED, "render cancelled");
