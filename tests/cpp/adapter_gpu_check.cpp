@@ -6,7 +6,13 @@
 //  2. a second frame after the sphere moved (the adapter uploads the changed mesh and refits):
 //     equal to the oracle's image of the moved scene;
 //  3. gpu_path_tracer::sample (if_path_tracer::sample, pathtracer.h:59-63) on a batch of camera
-//     rays: each path equal to the reference's own tracer fed that path's stream.
+//     rays: each path equal to the oracle's path fed the same stream, and, where the reference was
+//     compiled for x86-64, to the reference's own tracer fed that stream. The reference's paths
+//     depend on the machine it was compiled for: its AArch64 build agrees with neither the oracle
+//     nor the GPU on most paths while its x86-64 build agrees with both bit for bit (it passes two
+//     draws to one call in several places, e.g. vec3_cos_hemisphere_sample(n, rng.draw(),
+//     rng.draw()), an evaluation order C++ leaves to the compiler — the likely cause). The GPU and
+//     the oracle follow the x86-64 build, to which the oracle is pinned.
 // Prints "OK ..." or "FAIL ..." and returns nonzero on failure.
 #include "adapter_scene.h"
 
@@ -133,28 +139,39 @@ int main() {
         std::vector<e8util::vec3> got = gt.sample(rng, rays, none, R.ps, R.mc, R.ls);
         uint64_t seed = static_cast<uint64_t>(shadow.draw() * 4294967296.0);
         std::unique_ptr<e8::if_path_tracer> ref_tracer(e8::pathtracer_factory(tc.type, e8::pathtracer_factory::options()).create());
-        unsigned ok = 0, shown = 0;
+        unsigned ok_ref = 0, ok_oracle = 0, shown = 0;
         for (size_t i = 0; i < rays.size(); i++) {
             std::vector<e8util::ray> one{rays[i]};
             auto hits = e8::if_path_tracer::compute_first_hit(one, R.ps, R.ls);
             uint32_t ps = e8g_path_seed(seed, static_cast<uint32_t>(i), 0);
             e8util::rng pr(ps);
             e8util::vec3 r = ref_tracer->sample(pr, one, hits, R.ps, R.mc, R.ls)[0];
-            bool same = close(got[i](0), r(0), 1e-4f) && close(got[i](1), r(1), 1e-4f) && close(got[i](2), r(2), 1e-4f);
-            ok += same;
-            if (!same && shown++ < 4) {
-                uint32_t px = static_cast<uint32_t>(5 * i);
-                float orc[3];
-                o_render_paths(os, tc.mode, E8G_RNG_MINSTD, 0, &pol, w, h, &px, &ps, 1, orc, 1);
+            // the oracle's path of the same stream starts at the camera ray of pixel 5 i, which the
+            // oracle's camera reproduces within a few ulp of the reference's ray
+            uint32_t px = static_cast<uint32_t>(5 * i);
+            float orc[3];
+            o_render_paths(os, tc.mode, E8G_RNG_MINSTD, 0, &pol, w, h, &px, &ps, 1, orc, 1);
+            bool same_ref = close(got[i](0), r(0), 1e-4f) && close(got[i](1), r(1), 1e-4f) &&
+                            close(got[i](2), r(2), 1e-4f);
+            bool same_oracle = close(got[i](0), orc[0], 1e-4f) && close(got[i](1), orc[1], 1e-4f) &&
+                               close(got[i](2), orc[2], 1e-4f);
+            ok_ref += same_ref;
+            ok_oracle += same_oracle;
+            if (!same_oracle && shown++ < 4)
                 std::printf("  path %zu (pixel %u, seed %u): reference %g %g %g, gpu %g %g %g, oracle %g %g %g\n", i, px,
                             ps, r(0), r(1), r(2), got[i](0), got[i](1), got[i](2), orc[0], orc[1], orc[2]);
-            }
         }
-        double frac = static_cast<double>(ok) / rays.size();
-        std::printf("%s gpu_path_tracer::sample = reference sample() on %.4f of %zu paths\n", tc.name, frac,
-                    rays.size());
-        if (frac < 0.995)
+        double frac_ref = static_cast<double>(ok_ref) / rays.size();
+        double frac_oracle = static_cast<double>(ok_oracle) / rays.size();
+        std::printf("%s gpu_path_tracer::sample = oracle on %.4f of %zu paths, = this machine's compiled reference "
+                    "sample() on %.4f\n",
+                    tc.name, frac_oracle, rays.size(), frac_ref);
+        if (frac_oracle < 0.995)
             failures++;
+#if defined(__x86_64__)
+        if (frac_ref < 0.995)
+            failures++;
+#endif
         o_scene_free(os);
         e8g_destroy(ctx);
     }

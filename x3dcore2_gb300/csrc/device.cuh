@@ -50,6 +50,8 @@ struct DevScene {
     const float *light_cum;    // basic_light_sources::commit CDF (lightsources.cpp:45-52)
     const float *light_pnorm;  // |power| per light
     uint32_t nmat, nl, nm, nnodes, ntris;
+    uint32_t nverts;              // vertices (bounds checks of the debug build)
+    unsigned long long *check;    // check word of the debug build (E8G_CHECKS), or null
     uint32_t layout; // 0: SAH child pairs (ordered traversal), 1: the reference's tree and order,
                      // 2: eight-wide quantized nodes, 3: no tree (every triangle, in order)
     float total_power;
@@ -263,6 +265,8 @@ __device__ __forceinline__ Hit trace_sah(const DevScene &S, float3 o, float3 d, 
     int sp = 0;
     while (true) {
         if (count == 0) {
+            if (!E8G_CHK(S.check, link + 1 < S.nnodes, kChkNode, link))
+                break;
             float4 l0 = __ldg(&S.nlo[link]), h0 = __ldg(&S.nhi[link]);
             float4 l1 = __ldg(&S.nlo[link + 1]), h1 = __ldg(&S.nhi[link + 1]);
             if (COUNT)
@@ -272,6 +276,8 @@ __device__ __forceinline__ Hit trace_sah(const DevScene &S, float3 o, float3 d, 
             bool hit1 = slab(l1, h1, o, inv, tmin, cull, tn1);
             if (hit0 && hit1) {
                 bool swap = tn1 < tn0;
+                if (!E8G_CHK(S.check, sp < kStack, kChkStack, link))
+                    break;
                 sn[sp * kBlock] = swap ? link : link + 1;
                 st[sp * kBlock] = swap ? tn0 : tn1;
                 sp++;
@@ -285,6 +291,8 @@ __device__ __forceinline__ Hit trace_sah(const DevScene &S, float3 o, float3 d, 
                 continue;
             }
         } else {
+            if (!E8G_CHK(S.check, link + count <= S.ntris, kChkTri, link + count - 1))
+                count = 0;
             for (uint32_t k = link; k < link + count; k++) {
                 float4 a = __ldg(&S.tri[3 * k]), b = __ldg(&S.tri[3 * k + 1]), c = __ldg(&S.tri[3 * k + 2]);
                 if (COUNT)
@@ -377,8 +385,14 @@ __device__ __forceinline__ bool trace_ref(const DevScene &S, float3 o, float3 d,
     while (sp > 0) {
         sp--;
         uint32_t n = stk[sp * kBlock];
+        if (!E8G_CHK(S.check, n < S.nnodes, kChkNode, n))
+            return false;
         uint32_t link = __float_as_uint(__ldg(&S.nlo[n].w));
         uint32_t count = __float_as_uint(__ldg(&S.nhi[n].w));
+        if (!E8G_CHK(S.check, count == 0 || link + count <= S.ntris, kChkTri, link + count - 1))
+            count = 0;
+        if (!E8G_CHK(S.check, count > 0 || sp + 2 <= kStackWords, kChkStack, n))
+            return false;
         if (count > 0) {
             for (uint32_t k = link; k < link + count; k++) {
                 float4 a = __ldg(&S.tri[3 * k]), b = __ldg(&S.tri[3 * k + 1]), c = __ldg(&S.tri[3 * k + 2]);
@@ -455,7 +469,7 @@ __device__ __forceinline__ Hit trace_l(const DevScene &S, float3 o, float3 d, fl
         return h;
     }
     if (LAYOUT == 2) {
-        WideView W{S.wnodes, S.tri, S.nnodes};
+        WideView W{S.wnodes, S.tri, S.nnodes, S.ntris, S.check};
         return wide_trace(W, o, d, tmin, tmax, any, stk, kBlock, COUNT ? &cnt->nodes : nullptr,
                           COUNT ? &cnt->tris : nullptr);
     }
@@ -471,7 +485,7 @@ __device__ __forceinline__ Hit trace_closest(const DevScene &S, float3 o, float3
     if (S.layout == 1)
         return trace_l<1, COUNT>(S, o, d, 1e-4f, 1000.0f, false, stk, cnt);
     if (S.layout == 2)
-        return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes}, o, d, 1e-4f, 1000.0f, false, stk, kBlock,
+        return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes, S.ntris, S.check}, o, d, 1e-4f, 1000.0f, false, stk, kBlock,
                                COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr);
     if (S.layout == 3)
         return trace_linear<COUNT>(S, o, d, 1e-4f, 1000.0f, false, cnt);
@@ -485,7 +499,7 @@ __device__ __forceinline__ bool trace_any(const DevScene &S, float3 o, float3 d,
     if (S.layout == 1)
         return trace_l<1, COUNT>(S, o, d, tmin, tmax, true, stk, cnt).tri != 0xFFFFFFFFu;
     if (S.layout == 2)
-        return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes}, o, d, tmin, tmax, true, stk, kBlock,
+        return wide_trace_call(WideView{S.wnodes, S.tri, S.nnodes, S.ntris, S.check}, o, d, tmin, tmax, true, stk, kBlock,
                                COUNT ? &cnt->nodes : nullptr, COUNT ? &cnt->tris : nullptr)
                    .tri != 0xFFFFFFFFu;
     if (S.layout == 3)
@@ -595,7 +609,12 @@ __device__ __forceinline__ void shading_vertex(const DevScene &S, uint32_t i, fl
 }
 
 __device__ __forceinline__ Vert make_vert(const DevScene &S, const Hit &h) {
-    uint4 ti = __ldg(&S.tidx[h.tri]);
+    uint32_t tri = E8G_CHK(S.check, h.tri < S.ntris, kChkTri, h.tri) ? h.tri : 0u;
+    uint4 ti = __ldg(&S.tidx[tri]);
+    if (!E8G_CHK(S.check, ti.x < S.nverts && ti.y < S.nverts && ti.z < S.nverts, kChkVertex, tri))
+        ti.x = ti.y = ti.z = 0;
+    if (!E8G_CHK(S.check, ti.w < S.nm, kChkMesh, ti.w))
+        ti.w = 0;
     float b0 = 1.0f - h.b1 - h.b2; // tensor.h:723
     float3 p0, p1, p2, n0, n1, n2;
     shading_vertex(S, ti.x, p0, n0);
@@ -627,7 +646,12 @@ __device__ __forceinline__ void camera_ray(const DevCamera &c, uint32_t x, uint3
 // ----------------------------------------------------------------- materials ----
 
 __device__ __forceinline__ const DevMaterial &vert_mat(const DevScene &S, int32_t mesh) {
-    return S.mats[__ldg(&S.mesh_mat[mesh])];
+    if (!E8G_CHK(S.check, mesh >= 0 && static_cast<uint32_t>(mesh) < S.nm, kChkMesh, mesh))
+        mesh = 0;
+    int32_t mi = __ldg(&S.mesh_mat[mesh]);
+    if (!E8G_CHK(S.check, mi >= 0 && static_cast<uint32_t>(mi) <= S.nmat, kChkMaterial, mi)) // nmat: fail-safe
+        mi = static_cast<int32_t>(S.nmat);
+    return S.mats[mi];
 }
 
 // vec3_basis (tensor.h:939-943)

@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
         // scene (its cached first hit is a miss) has no vertex and contributes nothing, so the
         // lane draws again, up to kRefillRounds rounds, instead of leaving the slot idle for the
         // whole bounce; the megakernel's refill does the same.
-        bool want = in && state == kEmpty;
+        // once the path counter has passed the last path (it only grows) no lane can refill: the
+        // frame's tail skips the atomics
+        bool want = in && state == kEmpty && *reinterpret_cast<volatile unsigned long long *>(&cnt->next_path) < total_paths;
         bool refilled = false;
         for (int round = 0; round < kRefillRounds; round++) {
             uint32_t mask = __ballot_sync(~0u, want);
@@ -225,9 +227,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
                     }
                     RenderArgs const &A = args_of<MULTI>(A0, B, nsid);
                     if (path_coords(A, local, pixel, sample, out)) {
-                        FirstHit f = fh[pbase + pixel];
-                        int32_t m = __float_as_int(f.p.w);
+                        FirstHit const &fr = fh[pbase + pixel];
+                        float4 fp = fr.p; // the mesh decides first: half the frame is sky
+                        int32_t m = __float_as_int(fp.w);
                         if (m >= 0) {
+                            FirstHit f;
+                            f.p = fp;
+                            f.n = fr.n;
+                            f.d = fr.d;
                             sid = nsid;
                             out += static_cast<uint32_t>(pbase);
                             p = xyz(f.p);
@@ -304,12 +311,16 @@ __global__ void __launch_bounds__(THREADS, MINB)
             }
         }
         uint32_t sq = warp_append(&cnt->shadow_n, push_shadow);
+        if (push_shadow && !E8G_CHK(S0.check, sq < W.capacity, kChkQueue, sq))
+            push_shadow = false;
         if (push_shadow) {
             W.sh_o[sq] = make_float4(p.x, p.y, p.z, __uint_as_float(out));
             W.sh_d[sq] = make_float4(sh_dir.x, sh_dir.y, sh_dir.z, sh_tmax);
             W.sh_c[sq] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(sid));
         }
         uint32_t eq = warp_append(&cnt->ext_n, push_ext);
+        if (push_ext && !E8G_CHK(S0.check, eq < W.capacity, kChkQueue, eq))
+            push_ext = false;
         if (push_ext) {
             W.ext_o[eq] = make_float4(p.x, p.y, p.z, __uint_as_float(s));
             W.ext_d[eq] = make_float4(-o.x, -o.y, -o.z, __uint_as_float(sid));
@@ -379,7 +390,7 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
     uint32_t *head = ANY ? &cnt->shadow_head : &cnt->ext_head;
     const uint32_t lane = lane_id();
     constexpr uint32_t kNone = 0xFFFFFFFFu;
-    const WideView WV{S.wnodes, S.tri, S.nnodes};
+    const WideView WV{S.wnodes, S.tri, S.nnodes, S.ntris, S.check};
     uint32_t q = kNone;
     bool exhausted = false;
     TravState T;
@@ -456,7 +467,7 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
     uint32_t *head = &cnt->ext_head;
     const uint32_t lane = lane_id();
     constexpr uint32_t kNone = 0xFFFFFFFFu;
-    WideView WV{S0.wnodes, S0.tri, S0.nnodes};
+    WideView WV{S0.wnodes, S0.tri, S0.nnodes, S0.ntris, S0.check};
     uint32_t q = kNone;
     bool drained = false; // the same in every lane: the queue had no entry left for this warp
     WideTrav T;
@@ -486,7 +497,7 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
                     }
                     if (MULTI) {
                         DevScene const &S = B.scenes[sid];
-                        WV = WideView{S.wnodes, S.tri, S.nnodes};
+                        WV = WideView{S.wnodes, S.tri, S.nnodes, S.ntris, S.check};
                     }
                 }
             }
@@ -501,7 +512,9 @@ __global__ void __launch_bounds__(kBlock, kWfWideBlocks)
             continue;
         if (wide_step(WV, T, stk, kBlock, nullptr, nullptr)) {
             if (q < n_ext) {
-                W.hit[__float_as_uint(W.ext_o[q].w)] = make_float4(T.h.t, __uint_as_float(T.h.tri), T.h.b1, T.h.b2);
+                uint32_t slot = __float_as_uint(W.ext_o[q].w);
+                if (E8G_CHK(S0.check, slot < W.capacity, kChkSlot, slot))
+                    W.hit[slot] = make_float4(T.h.t, __uint_as_float(T.h.tri), T.h.b1, T.h.b2);
             } else if (T.h.tri == 0xFFFFFFFFu) {
                 uint32_t sq = q - n_ext;
                 emit_to(A, accum, path_rgb, __float_as_uint(W.sh_o[sq].w), xyz(W.sh_c[sq]));

@@ -25,6 +25,32 @@
 
 namespace e8g {
 
+// Bounds checks of the debug build (E8G_CHECKS defined for the device compilation; nothing in the
+// other builds). A failed check records its code and the offending index in the check word, the
+// first failure winning, and the caller skips the access; the host reads the word after the call
+// and reports E8G_ERR_INTERNAL with both. Nothing traps.
+enum : uint32_t {
+    kChkNode = 1,     // BVH node index beyond the node array
+    kChkTri = 2,      // triangle record index beyond the triangle array
+    kChkStack = 3,    // traversal stack full
+    kChkVertex = 4,   // vertex index of a triangle beyond the vertex array
+    kChkMesh = 5,     // mesh index beyond the mesh table
+    kChkMaterial = 6, // material index beyond the material table
+    kChkLight = 7,    // light index beyond the light table
+    kChkQueue = 8,    // wavefront queue entry beyond the slot capacity
+    kChkSlot = 9      // wavefront slot index beyond the slot capacity
+};
+#if defined(E8G_CHECKS) && defined(__CUDA_ARCH__)
+__device__ __forceinline__ bool e8g_chk(unsigned long long *word, bool ok, uint32_t code, uint32_t idx) {
+    if (!ok && word)
+        atomicCAS(word, 0ull, (static_cast<unsigned long long>(code) << 32) | idx);
+    return ok;
+}
+#define E8G_CHK(word, cond, code, idx) e8g::e8g_chk((word), (cond), (code), static_cast<uint32_t>(idx))
+#else
+#define E8G_CHK(word, cond, code, idx) true
+#endif
+
 struct Hit {
     float t;
     uint32_t tri; // triangle record position (traversal) or global triangle index; 0xFFFFFFFF = miss
@@ -68,21 +94,6 @@ E8G_HD float hd_fma(float a, float b, float c) {
     return __fmaf_rn(a, b, c);
 #else
     return std::fmaf(a, b, c);
-#endif
-}
-// Two fused multiply-adds a0 * b + c and a1 * b + c with one instruction on sm_100 and later
-// (fma.rn.f32x2: each lane rounds like fmaf, so host and device results are equal).
-E8G_HD void hd_fma2(float a0, float a1, float b, float c, float &r0, float &r1) {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-    unsigned long long a, bb, cc, d;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
-    asm("mov.b64 %0, {%1, %1};" : "=l"(bb) : "f"(b));
-    asm("mov.b64 %0, {%1, %1};" : "=l"(cc) : "f"(c));
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(bb), "l"(cc));
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r0), "=f"(r1) : "l"(d));
-#else
-    r0 = hd_fma(a0, b, c);
-    r1 = hd_fma(a1, b, c);
 #endif
 }
 E8G_HD float hd_rcp(float x) {
@@ -153,6 +164,8 @@ struct WideView {
     uint4 const *nodes;  // 6 per node
     float4 const *tri;   // 3 per triangle record: (v0 | global id), (v1 - v0), (v2 - v0)
     uint32_t nnodes;
+    uint32_t ntris;                 // triangle records (bounds checks of the debug build)
+    unsigned long long *check;      // check word of the debug build, or null
 };
 
 constexpr int kWideStack = 16; // stack entries (the builder keeps the tree at most 16 levels deep);
@@ -263,10 +276,9 @@ E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3,
 #pragma unroll
 #endif
         for (uint32_t j = 0; j < 4; j++) {
-            float tnx, tfx, tny, tfy, tnz, tfz; // near and far plane of an axis share S and O
-            hd_fma2(hd_qf(wnx, j), hd_qf(wfx, j), sx, ox, tnx, tfx);
-            hd_fma2(hd_qf(wny, j), hd_qf(wfy, j), sy, oy, tny, tfy);
-            hd_fma2(hd_qf(wnz, j), hd_qf(wfz, j), sz, oz, tnz, tfz);
+            float tnx = hd_fma(hd_qf(wnx, j), sx, ox), tfx = hd_fma(hd_qf(wfx, j), sx, ox);
+            float tny = hd_fma(hd_qf(wny, j), sy, oy), tfy = hd_fma(hd_qf(wfy, j), sy, oy);
+            float tnz = hd_fma(hd_qf(wnz, j), sz, oz), tfz = hd_fma(hd_qf(wfz, j), sz, oz);
             float tn = fmaxf(hd_max3(tnx, tny, tnz), T.tmin);
             float tf = fminf(hd_min3(tfx, tfy, tfz), T.cull);
             hits |= (tn <= tf ? 1u : 0u) << (4 * half + j);
@@ -278,14 +290,15 @@ E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3,
 // Moves T.node to the next node: the first hit interior child in octant order (the other hit
 // interior children go on the stack as one entry), else the stack's top. Returns false when
 // there is none.
-E8G_HD bool wide_advance(WideTrav &T, uint32_t hits, uint32_t imask, uint32_t base, uint32_t *stk, int stride) {
+E8G_HD bool wide_advance(WideTrav &T, uint32_t hits, uint32_t imask, uint32_t base, uint32_t *stk, int stride,
+                         unsigned long long *check = nullptr) {
     const uint32_t oct = T.oct;
     uint32_t hit_int = hd_xor_perm(hits & imask, oct);
     if (hit_int) {
         uint32_t k = static_cast<uint32_t>(hd_ffs(hit_int) - 1);
         hit_int &= hit_int - 1u;
         uint32_t s = k ^ oct;
-        if (hit_int && T.sp < kWideStack) {
+        if (hit_int && E8G_CHK(check, T.sp < kWideStack, kChkStack, T.node) && T.sp < kWideStack) {
             stk[2 * T.sp * stride] = base;
             stk[(2 * T.sp + 1) * stride] = imask << 8 | hit_int;
             T.sp++;
@@ -316,6 +329,8 @@ E8G_HD bool wide_leaf_slot(WideView const &W, WideTrav &T, uint32_t s, uint32_t 
                            uint32_t meta_hi, uint32_t counts, uint32_t *cnt_tris) {
     uint32_t meta = (s < 4 ? meta_lo : meta_hi) >> (8u * (s & 3u)) & 0xFFu;
     uint32_t k0 = tri_base + meta, k1 = k0 + ((counts >> (4u * s)) & 0xFu);
+    if (!E8G_CHK(W.check, k1 <= W.ntris, kChkTri, k1 - 1))
+        return false;
     for (uint32_t k = k0; k < k1; k++) {
         float4 a = hd_ld(W.tri + 3 * static_cast<size_t>(k));
         float4 b = hd_ld(W.tri + 3 * static_cast<size_t>(k) + 1);
@@ -341,6 +356,8 @@ E8G_HD bool wide_leaf_slot(WideView const &W, WideTrav &T, uint32_t s, uint32_t 
 // stack as one entry). Returns true when the ray is finished (stack empty, or an any-hit found).
 E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride, uint32_t *cnt_nodes,
                       uint32_t *cnt_tris) {
+    if (!E8G_CHK(W.check, T.node < W.nnodes, kChkNode, T.node))
+        return true;
     uint4 const *np = W.nodes + 6 * static_cast<size_t>(T.node);
     uint4 n0 = hd_ld(np), n1 = hd_ld(np + 1), n2 = hd_ld(np + 2), n3 = hd_ld(np + 3), n4 = hd_ld(np + 4),
           n5 = hd_ld(np + 5);
@@ -348,7 +365,7 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
     if (cnt_nodes)
         (*cnt_nodes)++;
     uint32_t hits = wide_child_hits(T, n0, n2, n3, n4, leaves);
-    bool more = wide_advance(T, hits, n0.w >> 24, n1.x, stk, stride);
+    bool more = wide_advance(T, hits, n0.w >> 24, n1.x, stk, stride, W.check);
     uint32_t hit_leaf = hits & leaves;
     while (hit_leaf) {
         uint32_t s = static_cast<uint32_t>(hd_ffs(hit_leaf) - 1);
