@@ -7,7 +7,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libe8g.so")
+# E8G_LIBRARY selects another build of the library (the bounds-checked libe8g_checks.so).
+LIB_PATH = os.environ.get("E8G_LIBRARY") or os.path.join(HERE, "libe8g.so")
 
 # status codes
 E8G_OK = 0

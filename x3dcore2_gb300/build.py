@@ -16,6 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libe8g.so")
+# The bounds-checked debug build (-DE8G_CHECKS): device checks of every index a kernel reads
+# through record the first failure in a check word that the host reads after each call.
+BUILD_CHECKS = os.path.join(HERE, "_build_checks")
+LIB_CHECKS = os.path.join(HERE, "libe8g_checks.so")
 ROOT = os.path.dirname(HERE)
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -68,34 +72,38 @@ def _compile(cmd):
     return r.stderr
 
 
-def build(verbose=False, jobs=None):
+def build(verbose=False, jobs=None, checks=False):
+    """Builds libe8g.so (or, with checks, the bounds-checked debug library libe8g_checks.so) and
+    returns its path."""
     check_exact_flags()
-    os.makedirs(BUILD, exist_ok=True)
+    build_dir, lib = (BUILD_CHECKS, LIB_CHECKS) if checks else (BUILD, LIB)
+    nvflags = NVFLAGS + (["-DE8G_CHECKS"] if checks else [])
+    os.makedirs(build_dir, exist_ok=True)
     headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         [os.path.join(ROOT, "include", "e8g.h")]
     nvcc = _nvcc()
     tasks = []
     objs = []
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
             tasks.append(["g++"] + CXXFLAGS + ["-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            tasks.append([nvcc] + NVFLAGS + ["-c", src, "-o", obj])
+            tasks.append([nvcc] + nvflags + ["-c", src, "-o", obj])
     if tasks:
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(tasks), os.cpu_count() or 4)) as ex:
             for err in ex.map(_compile, tasks):
                 if verbose and err:
                     sys.stderr.write(err)
-    if tasks or not os.path.exists(LIB):
-        tmp = LIB + ".tmp"
+    if tasks or not os.path.exists(lib):
+        tmp = lib + ".tmp"
         _compile([nvcc, ARCH, "-shared", "-o", tmp] + objs + ["-lpthread"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

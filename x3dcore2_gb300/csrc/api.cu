@@ -34,6 +34,32 @@ e8g_status cuda_fail(e8g_ctx *ctx, cudaError_t e, char const *what) {
     return fail(ctx, E8G_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+e8g_status read_checks(e8g_ctx *c) {
+#if defined(E8G_CHECKS)
+    if (!c->b_check.ptr)
+        return E8G_OK;
+    unsigned long long w = 0;
+    cudaError_t e = cudaMemcpyAsync(&w, c->b_check.ptr, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "check word");
+    if (w == 0)
+        return E8G_OK;
+    cudaMemsetAsync(c->b_check.ptr, 0, 8, c->stream);
+    static char const *const names[] = {"?",          "node index",     "triangle index", "traversal stack",
+                                        "vertex index", "mesh index",   "material index", "light index",
+                                        "queue entry", "slot index"};
+    uint32_t code = static_cast<uint32_t>(w >> 32), idx = static_cast<uint32_t>(w);
+    return fail(c, E8G_ERR_INTERNAL,
+                std::string("device bounds check failed: ") + (code < 10 ? names[code] : "?") + " " +
+                    std::to_string(idx));
+#else
+    (void)c;
+    return E8G_OK;
+#endif
+}
+
 bool take_cancel(e8g_ctx *c) {
     if (!c->cancel.load(std::memory_order_acquire))
         return false;
@@ -105,6 +131,8 @@ void fill_dev_scene(e8g_ctx *c) {
     S.nm = p.nm;
     S.nnodes = p.bvh.num_nodes;
     S.ntris = p.nt;
+    S.nverts = p.nv;
+    S.check = static_cast<unsigned long long *>(c->b_check.ptr);
     S.layout = p.layout;
     S.total_power = p.total_power;
     for (int k = 0; k < 3; k++) {
@@ -467,6 +495,12 @@ e8g_status e8g_create(e8g_ctx **out, e8g_device_opts const *opts) {
         e = c->b_work.reserve(64);
     if (e == cudaSuccess)
         e = cudaMallocHost(&c->host_pinned, 64);
+#if defined(E8G_CHECKS)
+    if (e == cudaSuccess)
+        e = c->b_check.reserve(8);
+    if (e == cudaSuccess)
+        e = cudaMemset(c->b_check.ptr, 0, 8);
+#endif
     if (e != cudaSuccess) {
         delete c;
         return E8G_ERR_CUDA;
@@ -663,7 +697,7 @@ e8g_status e8g_trace_closest(e8g_ctx *c, e8g_ray const *rays, uint32_t n, e8g_hi
     e = cudaMemcpyAsync(hits, c->b_io1.ptr, hb, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "trace_closest");
+    return e == cudaSuccess ? read_checks(c) : cuda_fail(c, e, "trace_closest");
 }
 
 e8g_status e8g_trace_any(e8g_ctx *c, e8g_ray const *rays, float const *t_min, float const *t_max, uint32_t n,
@@ -694,7 +728,7 @@ e8g_status e8g_trace_any(e8g_ctx *c, e8g_ray const *rays, float const *t_min, fl
     e = cudaMemcpyAsync(occluded, docc, n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "trace_any");
+    return e == cudaSuccess ? read_checks(c) : cuda_fail(c, e, "trace_any");
 }
 
 e8g_status e8g_render_dev(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, void *stream) {
@@ -906,7 +940,7 @@ e8g_status e8g_render_paths(e8g_ctx *c, e8g_render_params const *p, uint32_t con
     e = cudaMemcpyAsync(rgb_out, c->b_io1.ptr, ob, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "render_paths");
+    return e == cudaSuccess ? read_checks(c) : cuda_fail(c, e, "render_paths");
 }
 
 e8g_status e8g_render_rays(e8g_ctx *c, e8g_render_params const *params, e8g_ray const *rays, uint32_t n,
@@ -952,7 +986,7 @@ e8g_status e8g_render_rays(e8g_ctx *c, e8g_render_params const *params, e8g_ray 
     e = cudaMemcpyAsync(rgb_out, c->b_io1.ptr, ob, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? E8G_OK : cuda_fail(c, e, "render_rays");
+    return e == cudaSuccess ? read_checks(c) : cuda_fail(c, e, "render_rays");
 }
 
 } // extern "C"

@@ -91,6 +91,8 @@ struct e8g_ctx {
     e8g::dev_buffer b_refit, b_vpos0, b_vnrm0, b_gbuild; // b_gbuild: device builder scratch
     // the render pipeline: its float frame and the settings of its last frame
     e8g::dev_buffer b_pipe;
+    // the check word of the bounds-checked debug build (E8G_CHECKS; empty otherwise)
+    e8g::dev_buffer b_check;
     e8g_pipeline_config pipe_cfg{};
     bool pipe_valid = false;
 
@@ -98,7 +100,7 @@ struct e8g_ctx {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_vtx, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
                 &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch,
-                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild, &b_pipe};
+                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild, &b_pipe, &b_check};
     }
 };
 
@@ -109,6 +111,10 @@ e8g_status cuda_fail(e8g_ctx *ctx, cudaError_t e, char const *what);
 e8g_status check_ready(e8g_ctx *c);
 // A pending e8g_cancel: waits for the context's stream, clears the request and returns true.
 bool take_cancel(e8g_ctx *c);
+// The bounds-checked debug build (E8G_CHECKS): waits for the stream, and when a device check
+// failed since the last call returns E8G_ERR_INTERNAL naming it (and clears it). E8G_OK in every
+// other build, without waiting.
+e8g_status read_checks(e8g_ctx *c);
 e8g_status validate_params(e8g_ctx *c, e8g_render_params const *p);
 RenderArgs make_args(e8g_render_params const *p);
 e8g_status first_hits(e8g_ctx *c, uint32_t w, uint32_t h);

@@ -159,6 +159,8 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
         S.nm = p.nm;
         S.nnodes = p.bvh.num_nodes;
         S.ntris = p.nt;
+        S.nverts = p.nv;
+        S.check = static_cast<unsigned long long *>(c->b_check.ptr);
         S.layout = p.layout;
         S.total_power = p.total_power;
         for (int i = 0; i < 3; i++) {
@@ -224,5 +226,5 @@ extern "C" e8g_status e8g_batch_render(e8g_ctx *c, e8g_batch_item const *items, 
     c->stats.launches = c->launches + 2; // first hits, integrator, resolve
     if (stats)
         *stats = c->stats;
-    return E8G_OK;
+    return read_checks(c);
 }

@@ -229,7 +229,7 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
     c->stats.trace_ms = c->kt_trace_ms;
     c->stats.shade_ms = c->kt_shade_ms;
     c->stats.trace_launches = c->kt_trace_launches;
-    return E8G_OK;
+    return read_checks(c);
 }
 
 e8g_status render_list(e8g_ctx *c, e8g_render_params const *p, uint32_t const *d_pixel, uint32_t const *d_sample,
@@ -584,7 +584,7 @@ e8g_status e8g_backward(e8g_ctx *c, float const *dl_dimage, float *d_albedo, flo
     c->stats.launches = 2;
     c->stats.trace_ms = c->stats.shade_ms = 0;
     c->stats.trace_launches = 0;
-    return E8G_OK;
+    return read_checks(c);
 }
 
 e8g_status e8g_set_materials(e8g_ctx *c, e8g_material const *m, uint32_t n) {
