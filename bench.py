@@ -746,6 +746,7 @@ def main():
         abi.check(lib.e8g_wavefront_tune(ctx.h, C.byref(pw), C.byref(r)), ctx.h, "e8g_wavefront_tune")
         return {"capacity": r.capacity, "bounces_per_graph": r.bounces_per_graph, "threshold": r.threshold,
                 "shade_variant": r.shade_variant, "shade_ms": [round(r.shade_ms[i], 3) for i in range(r.num_shade)],
+                "concurrent": r.concurrent, "concurrent_ms": [round(r.concurrent_ms[0], 3), round(r.concurrent_ms[1], 3)],
                 "candidates": [[r.cand_capacity[i], r.cand_bounces[i], r.cand_threshold[i], round(r.cand_ms[i], 3)]
                                for i in range(r.num_candidates)]}
 

@@ -375,7 +375,8 @@ typedef struct e8g_tune_result {
     uint32_t num_shade;         /* shapes timed */
     double shade_ms[8];         /* device time of the render with each shape */
     uint32_t from_cache;        /* e8g_wavefront_tune_cached: 1 when the choice came from the file */
-    uint32_t pad_;
+    uint32_t concurrent;        /* chosen: 1 = two slot pools interleaving on two streams */
+    double concurrent_ms[2];    /* device time of the render with one pool and with two */
 } e8g_tune_result;
 e8g_status e8g_wavefront_tune(e8g_ctx *ctx, const e8g_render_params *params, e8g_tune_result *result);
 /* Sets the wavefront configuration directly: slot capacity (1024 .. 2^26), bounces captured per
@@ -386,6 +387,10 @@ e8g_status e8g_wavefront_set(e8g_ctx *ctx, uint32_t capacity, uint32_t bounces_p
  * 2 = 256 x 4 out of line, 3 = 256 x 3 out of line, 4 = 256 x 5 (48) out of line, 5 = 128 x 8 (64)
  * out of line. */
 e8g_status e8g_wavefront_set_shade(e8g_ctx *ctx, uint32_t variant);
+/* Nonzero: the wavefront splits its slots into two pools that interleave on two streams, one
+ * pool shading while the other traces, each kernel at half of an SM's residency, so shading
+ * (latency-bound) and tracing (issue-bound) overlap on every SM. The same paths and image. */
+e8g_status e8g_wavefront_set_concurrent(e8g_ctx *ctx, int on);
 /* e8g_wavefront_tune with a cache of choices in a JSON file (`cache_path`): the key is the scene
  * and frame size bucket (tree layout, stream kind, log2 of the triangle count, of the pixels and of
  * min(spp, 64)). A key found in the file sets its configuration without tuning (result->from_cache

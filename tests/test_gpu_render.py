@@ -306,6 +306,7 @@ def test_wavefront_tuner_cache_and_shade_shapes(ctx, tmp_path):
         d = json.load(f)
     (key, entry), = d.items()
     assert "layout2" in key and entry["capacity"] == r.capacity and entry["shade"] == r.shade_variant
+    assert entry["concurrent"] == r.concurrent and r.concurrent_ms[0] > 0 and r.concurrent_ms[1] > 0
     r2 = abi.TuneResult()
     assert ctx.lib.e8g_wavefront_tune_cached(ctx.h, C.byref(p), path, C.byref(r2)) == 0
     assert r2.from_cache == 1 and (r2.capacity, r2.bounces_per_graph, r2.threshold, r2.shade_variant) == \
@@ -336,3 +337,33 @@ def test_bidirectional_traversal_counts(ctx, mode):
     np.testing.assert_allclose(again, img, rtol=1e-5, atol=1e-6)
     with pytest.raises(Exception, match="UNSUPPORTED"):
         ctx.count_traversal(default_params(abi.MODE_REF_LT2, 64, 48, 1))
+
+
+@pytest.mark.parametrize("layout", [abi.BVH_WIDE, abi.BVH_SAH])
+def test_concurrent_wavefront_renders_the_same_paths(ctx, layout):
+    """e8g_wavefront_set_concurrent: two slot pools interleaving on two streams render the same
+    paths as one pool: the image equals the megakernel's, and per-path radiance equals the
+    oracle's, for a frame much larger than the slot pools (slots refill many times)."""
+    import ctypes as C
+    sc = S.displaced_icosphere(level=4, seed=3, num_materials=16, width=160, height=120)
+    ctx.upload(sc, layout=layout)
+    p = default_params(abi.MODE_MIS, 160, 120, 16, seed=7, max_depth=8, rr_start=3)
+    ref = ctx.render(p)
+    assert ctx.lib.e8g_wavefront_set(ctx.h, 4096, 2, 12 if layout == abi.BVH_WIDE else 16) == 0
+    assert ctx.lib.e8g_wavefront_set_concurrent(ctx.h, 1) == 0
+    try:
+        p.integrator = abi.INTEGRATOR_WAVEFRONT
+        img = ctx.render(p)
+        close = np.all(np.abs(img - ref) <= np.maximum(1e-4 * np.abs(ref), 1e-6), axis=-1)
+        assert close.mean() >= 0.999, close.mean()
+        px = np.random.default_rng(4).integers(0, 160 * 120, 2000).astype(np.uint32)
+        smp = np.arange(len(px), dtype=np.uint32)
+        got = ctx.render_paths(p, px, smp)
+        osc = ob.OracleScene(sc)
+        want = osc.render_paths(abi.MODE_MIS, 160, 120, px, smp, policy=ob.OPolicy(8, 3, 0.5, 8),
+                                rng=abi.RNG_PHILOX, seed=7)
+        ok = np.all(np.abs(got - want) <= np.maximum(1e-4 * np.abs(want), 1e-6), axis=1)
+        assert ok.mean() >= 0.999, ok.mean()
+    finally:
+        ctx.lib.e8g_wavefront_set_concurrent(ctx.h, 0)
+        ctx.lib.e8g_wavefront_set(ctx.h, 1 << 21, 4, 16)

@@ -110,7 +110,8 @@ class TuneResult(C.Structure):
                 ("num_candidates", C.c_uint32), ("cand_capacity", C.c_uint32 * 64),
                 ("cand_bounces", C.c_uint32 * 64), ("cand_threshold", C.c_uint32 * 64),
                 ("cand_ms", C.c_double * 64), ("shade_variant", C.c_uint32), ("num_shade", C.c_uint32),
-                ("shade_ms", C.c_double * 8), ("from_cache", C.c_uint32), ("pad_", C.c_uint32)]
+                ("shade_ms", C.c_double * 8), ("from_cache", C.c_uint32), ("concurrent", C.c_uint32),
+                ("concurrent_ms", C.c_double * 2)]
 
 
 class GenOpts(C.Structure):
@@ -175,6 +176,7 @@ SIGNATURES = {
     "e8g_wavefront_tune": (_ST, [_P, C.POINTER(RenderParams), C.POINTER(TuneResult)]),
     "e8g_wavefront_set": (_ST, [_P, _U32, _U32, _U32]),
     "e8g_wavefront_set_shade": (_ST, [_P, _U32]),
+    "e8g_wavefront_set_concurrent": (_ST, [_P, C.c_int]),
     "e8g_wavefront_tune_cached": (_ST, [_P, C.POINTER(RenderParams), C.c_char_p, C.POINTER(TuneResult)]),
     "e8g_render_paths": (_ST, [_P, C.POINTER(RenderParams), _P, _P, _U32, _P]),
     "e8g_render_rays": (_ST, [_P, C.POINTER(RenderParams), _P, _U32, _P]),

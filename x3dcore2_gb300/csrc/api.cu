@@ -526,6 +526,12 @@ e8g_status e8g_destroy(e8g_ctx *c) {
         cudaEventDestroy(c->ev3);
     for (cudaEvent_t ev : c->kt_events)
         cudaEventDestroy(ev);
+    if (c->ev_a)
+        cudaEventDestroy(c->ev_a);
+    if (c->ev_b)
+        cudaEventDestroy(c->ev_b);
+    if (c->stream2)
+        cudaStreamDestroy(c->stream2);
     if (c->stream)
         cudaStreamDestroy(c->stream);
     if (c->host_pinned)

@@ -67,6 +67,10 @@ struct e8g_ctx {
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
     uint32_t wf_capacity = 1u << 21, wf_bounces = 4, wf_threshold = 16, wf_shade_variant = 0;
+    // concurrent wavefront: two slot pools on two streams, one shading while the other traces
+    bool wf_concurrent = false;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
     // per-kernel timing of the wavefront (e8g_set_kernel_timing): three events per bounce of the
     // graph (bounce start, shading done, trace done) and the sums over the current render
     bool kernel_timing = false;
@@ -132,6 +136,10 @@ e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, u
 e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
                          uint32_t bounces, uint32_t threshold, BatchDev const *B = nullptr,
                          FirstHit const *fh_all = nullptr);
+
+// The same with two slot pools interleaving on two streams (e8g_wavefront_set_concurrent).
+e8g_status run_wavefront_concurrent(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
+                                    uint32_t bounces, uint32_t threshold);
 
 // Per-path radiance for device lists of pixels and samples into d_rgb (3 floats per path).
 // first_hits_ready: the first-hit cache already holds path i's first hit at index list_pixel[i].

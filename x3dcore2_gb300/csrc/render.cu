@@ -23,7 +23,9 @@ struct WfCounters { // mirrors the device Counters of wavefront.cu
 e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs const &A, float4 *accum, float *path_rgb,
                           unsigned long long *d_counts) {
     if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_MIS && !d_counts)
-        return run_wavefront(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces, c->wf_threshold);
+        return c->wf_concurrent ? run_wavefront_concurrent(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces,
+                                                           c->wf_threshold)
+                                : run_wavefront(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces, c->wf_threshold);
     cudaError_t e = cudaMemsetAsync(c->b_work.ptr, 0, 64, c->stream);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "work counter");
@@ -164,6 +166,145 @@ e8g_status run_wavefront(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *
     return E8G_OK;
 }
 
+// The concurrent wavefront: the slots split into two pools A and B with their own queues and
+// counters (one path counter shared), captured on two streams in anti-phase — while A shades, B
+// traces, then A traces while B shades — with a two-way event join after every phase. Each kernel
+// is launched for half of the SM's residency, so a shading kernel (waiting on its scene gathers)
+// and a trace kernel (issue-bound on the eight-box tests) share every SM. Pool B's last phase of a
+// replay is a shading, so the run ends only when B's queues are empty too.
+e8g_status run_wavefront_concurrent(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb, uint32_t capacity,
+                                    uint32_t bounces, uint32_t threshold) {
+    uint64_t total = A.total_paths;
+    uint32_t layout = c->dev.layout;
+    uint64_t want = std::max<uint64_t>(total, 2048);
+    uint32_t Qh = static_cast<uint32_t>(std::min<uint64_t>(capacity / 2, (want / 2 + 255) / 256 * 256));
+    Qh = std::max<uint32_t>(Qh, 256);
+    size_t pool = (wf_total_bytes(Qh) + 255) & ~static_cast<size_t>(255);
+    cudaError_t e = c->b_wf.reserve(2 * pool);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront slots");
+    if (!c->stream2) {
+        e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "second stream");
+    }
+    WfSlots WA = wf_carve(c->b_wf.ptr, Qh);
+    WfSlots WB = wf_carve(static_cast<char *>(c->b_wf.ptr) + pool, Qh);
+    WB.next_path = WA.next_path;
+    e = wf_init(WA, c->stream);
+    if (e == cudaSuccess)
+        e = wf_init(WB, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront init");
+    uint32_t v = c->wf_shade_variant;
+    int shade_grid = c->num_sms * std::max(1, wf_shade_blocks(v) / 2);
+    int trace_grid = c->num_sms * std::max(1, wf_trace_blocks_per_sm(layout, threshold) / 2);
+    auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
+    cudaStream_t s0 = c->stream, s1 = c->stream2;
+    bool timed = c->kernel_timing;
+    size_t nev = 8 * static_cast<size_t>(bounces); // start and end of each of the four kernels of a step
+    while (timed && c->kt_events.size() < nev) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreate(&ev);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "kernel timing events");
+        c->kt_events.push_back(ev);
+    }
+    auto mark = [&](size_t k, cudaStream_t st) {
+        if (timed)
+            cudaEventRecordWithFlags(c->kt_events[k], st, cudaEventRecordExternal);
+    };
+    auto join = [&]() {
+        cudaEventRecord(c->ev_a, s0);
+        cudaEventRecord(c->ev_b, s1);
+        cudaStreamWaitEvent(s0, c->ev_b, 0);
+        cudaStreamWaitEvent(s1, c->ev_a, 0);
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "wavefront capture");
+    cudaEventRecord(c->ev_a, s0); // fork the second stream into the capture
+    cudaStreamWaitEvent(s1, c->ev_a, 0);
+    for (uint32_t k = 0; k < bounces; k++) {
+        size_t t = 8 * static_cast<size_t>(k);
+        mark(t, s0);
+        wf_enqueue_shade(c->dev, A, fh, WA, accum, path_rgb, shade_grid, total, s0, v);
+        mark(t + 1, s0);
+        mark(t + 2, s1);
+        wf_enqueue_trace(c->dev, A, WB, accum, path_rgb, trace_grid, threshold, s1);
+        mark(t + 3, s1);
+        join();
+        mark(t + 4, s0);
+        wf_enqueue_trace(c->dev, A, WA, accum, path_rgb, trace_grid, threshold, s0);
+        mark(t + 5, s0);
+        mark(t + 6, s1);
+        wf_enqueue_shade(c->dev, A, fh, WB, accum, path_rgb, shade_grid, total, s1, v);
+        mark(t + 7, s1);
+        join();
+    }
+    e = cudaStreamEndCapture(s0, &graph);
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return cuda_fail(c, e, "concurrent wavefront graph");
+    }
+    auto *host = static_cast<WfCounters *>(c->host_pinned); // [0]: pool A, [1]: pool B
+    uint64_t max_replays = ((total + 2 * Qh - 1) / (2 * Qh) + 1) * (kHardDepth + 3) / bounces + 16;
+    uint32_t traces_per_bounce = layout == 2 && threshold > 0 ? 1u : 2u;
+    uint64_t r = 0;
+    bool cancelled = false;
+    for (; r < max_replays; r++) {
+        if (take_cancel(c)) {
+            cancelled = true;
+            break;
+        }
+        e = cudaGraphLaunch(exec, s0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&host[0], WA.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, s0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&host[1], WB.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, s0);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s0);
+        if (e != cudaSuccess)
+            break;
+        c->launches += 2 * (2 + traces_per_bounce) * bounces;
+        if (timed) {
+            for (uint32_t k = 0; k < bounces; k++) {
+                size_t t = 8 * static_cast<size_t>(k);
+                float a = 0, b = 0, x = 0, y = 0;
+                cudaEventElapsedTime(&a, c->kt_events[t], c->kt_events[t + 1]);
+                cudaEventElapsedTime(&b, c->kt_events[t + 2], c->kt_events[t + 3]);
+                cudaEventElapsedTime(&x, c->kt_events[t + 4], c->kt_events[t + 5]);
+                cudaEventElapsedTime(&y, c->kt_events[t + 6], c->kt_events[t + 7]);
+                c->kt_shade_ms += a + y;
+                c->kt_trace_ms += b + x;
+            }
+            c->kt_trace_launches += 2 * traces_per_bounce * bounces;
+        }
+        if (host[0].busy == 0 && host[1].busy == 0 && host[1].shadow_n == 0 && host[1].ext_n == 0 &&
+            host[0].next_path >= total)
+            break;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "concurrent wavefront run");
+    if (cancelled)
+        return fail(c, E8G_ERR_CANCELLED, "render cancelled");
+    if (r == max_replays)
+        return fail(c, E8G_ERR_INTERNAL, "wavefront did not drain");
+    return E8G_OK;
+}
+
 e8g_status render_image(e8g_ctx *c, e8g_render_params const *p, float *d_rgba, unsigned long long *counts,
                         uint64_t prior_spp) {
     if (counts && p->mode == E8G_MODE_REF_LT2)
@@ -272,6 +413,8 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
     // a tuner run that fails (or is cancelled) leaves the configuration it found
     const uint32_t keep_cap = c->wf_capacity, keep_b = c->wf_bounces, keep_th = c->wf_threshold,
                    keep_shade = c->wf_shade_variant;
+    const bool keep_conc = c->wf_concurrent;
+    c->wf_concurrent = false; // the grid below runs with one pool
     e8g_render_params p = *params;
     p.integrator = E8G_INTEGRATOR_WAVEFRONT;
     p.spp = std::max<uint32_t>(1, std::min<uint32_t>(p.spp, 8)); // long enough for slots to refill steadily
@@ -295,6 +438,7 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                 s = render_image(c, &p, static_cast<float *>(c->b_img.ptr), nullptr);
                 if (s != E8G_OK) {
                     c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
+                    c->wf_concurrent = keep_conc;
                     return s;
                 }
                 ms = std::min(ms, c->stats.kernel_ms);
@@ -335,6 +479,7 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
             s = render_image(c, &p2, static_cast<float *>(c->b_img.ptr), nullptr);
             if (s != E8G_OK) {
                 c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
+                c->wf_concurrent = keep_conc;
                 return s;
             }
             double ms = c->stats.kernel_ms;
@@ -363,6 +508,7 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
                 if (s != E8G_OK) {
                     c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
                     c->wf_shade_variant = keep_shade;
+                    c->wf_concurrent = keep_conc;
                     return s;
                 }
                 ms = std::min(ms, c->stats.kernel_ms);
@@ -375,6 +521,23 @@ e8g_status e8g_wavefront_tune(e8g_ctx *c, e8g_render_params const *params, e8g_t
         }
         r.num_shade = kWfShadeVariants;
         c->wf_shade_variant = r.shade_variant;
+        // one slot pool, or two interleaving on two streams
+        r.concurrent_ms[0] = best_ms;
+        c->wf_concurrent = true;
+        double ms = 1e300;
+        for (int rep = 0; rep < 2; rep++) {
+            s = render_image(c, &p3, static_cast<float *>(c->b_img.ptr), nullptr);
+            if (s != E8G_OK) {
+                c->wf_capacity = keep_cap, c->wf_bounces = keep_b, c->wf_threshold = keep_th;
+                c->wf_shade_variant = keep_shade;
+                c->wf_concurrent = keep_conc;
+                return s;
+            }
+            ms = std::min(ms, c->stats.kernel_ms);
+        }
+        r.concurrent_ms[1] = ms;
+        r.concurrent = ms < best_ms ? 1u : 0u;
+        c->wf_concurrent = r.concurrent != 0;
     }
     if (res)
         *res = r;
@@ -393,6 +556,13 @@ e8g_status e8g_wavefront_set(e8g_ctx *c, uint32_t capacity, uint32_t bounces, ui
     return E8G_OK;
 }
 
+e8g_status e8g_wavefront_set_concurrent(e8g_ctx *c, int on) {
+    if (!c)
+        return E8G_ERR_INVALID_ARG;
+    c->wf_concurrent = on != 0;
+    return E8G_OK;
+}
+
 e8g_status e8g_wavefront_set_shade(e8g_ctx *c, uint32_t variant) {
     using namespace e8g;
     if (!c)
@@ -407,7 +577,7 @@ namespace {
 
 // One line of the tuning cache: "key": {"capacity": C, "bounces": B, "threshold": T, "shade": S, "ms": M}
 struct tune_entry {
-    uint32_t capacity = 0, bounces = 0, threshold = 0, shade = 0;
+    uint32_t capacity = 0, bounces = 0, threshold = 0, shade = 0, concurrent = 0;
     double ms = 0;
 };
 
@@ -430,8 +600,9 @@ std::map<std::string, tune_entry> read_tune_cache(char const *path) {
         char key[200];
         tune_entry t;
         if (std::sscanf(line, " \"%199[^\"]\": {\"capacity\": %u, \"bounces\": %u, \"threshold\": %u, \"shade\": %u, "
-                              "\"ms\": %lf",
-                        key, &t.capacity, &t.bounces, &t.threshold, &t.shade, &t.ms) == 6 &&
+                              "\"concurrent\": %u, \"ms\": %lf",
+                        key, &t.capacity, &t.bounces, &t.threshold, &t.shade, &t.concurrent, &t.ms) == 7 &&
+            t.concurrent <= 1 &&
             t.capacity >= 1024 && t.capacity <= (1u << 26) && t.bounces >= 1 && t.bounces <= 16 &&
             t.threshold <= 32 && t.shade < e8g::kWfShadeVariants)
             out[key] = t;
@@ -448,9 +619,11 @@ bool write_tune_cache(char const *path, std::map<std::string, tune_entry> const 
     std::fprintf(f, "{\n");
     size_t i = 0;
     for (auto const &kv : m) {
-        std::fprintf(f, "  \"%s\": {\"capacity\": %u, \"bounces\": %u, \"threshold\": %u, \"shade\": %u, \"ms\": %.4f}%s\n",
+        std::fprintf(f,
+                     "  \"%s\": {\"capacity\": %u, \"bounces\": %u, \"threshold\": %u, \"shade\": %u, "
+                     "\"concurrent\": %u, \"ms\": %.4f}%s\n",
                      kv.first.c_str(), kv.second.capacity, kv.second.bounces, kv.second.threshold, kv.second.shade,
-                     kv.second.ms, ++i < m.size() ? "," : "");
+                     kv.second.concurrent, kv.second.ms, ++i < m.size() ? "," : "");
     }
     std::fprintf(f, "}\n");
     bool ok = std::fclose(f) == 0;
@@ -481,12 +654,14 @@ e8g_status e8g_wavefront_tune_cached(e8g_ctx *c, e8g_render_params const *params
         c->wf_bounces = it->second.bounces;
         c->wf_threshold = it->second.threshold;
         c->wf_shade_variant = it->second.shade;
+        c->wf_concurrent = it->second.concurrent != 0;
         if (res) {
             *res = e8g_tune_result{};
             res->capacity = it->second.capacity;
             res->bounces_per_graph = it->second.bounces;
             res->threshold = it->second.threshold;
             res->shade_variant = it->second.shade;
+            res->concurrent = it->second.concurrent;
             res->from_cache = 1;
         }
         return E8G_OK;
@@ -500,7 +675,8 @@ e8g_status e8g_wavefront_tune_cached(e8g_ctx *c, e8g_render_params const *params
     t.bounces = r.bounces_per_graph;
     t.threshold = r.threshold;
     t.shade = r.shade_variant;
-    t.ms = r.shade_ms[r.shade_variant];
+    t.concurrent = r.concurrent;
+    t.ms = r.concurrent_ms[r.concurrent];
     cache[key] = t;
     if (!write_tune_cache(path, cache))
         return fail(c, E8G_ERR_INVALID_ARG, std::string("cannot write the tuning cache ") + path);

@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         // whole bounce; the megakernel's refill does the same.
         // once the path counter has passed the last path (it only grows) no lane can refill: the
         // frame's tail skips the atomics
-        bool want = in && state == kEmpty && *reinterpret_cast<volatile unsigned long long *>(&cnt->next_path) < total_paths;
+        bool want = in && state == kEmpty && *reinterpret_cast<volatile unsigned long long *>(W.next_path) < total_paths;
         bool refilled = false;
         for (int round = 0; round < kRefillRounds; round++) {
             uint32_t mask = __ballot_sync(~0u, want);
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
             int leader = __ffs(mask) - 1;
             unsigned long long base = 0;
             if (static_cast<int>(lane_id()) == leader)
-                base = atomicAdd(&cnt->next_path, static_cast<unsigned long long>(__popc(mask)));
+                base = atomicAdd(W.next_path, static_cast<unsigned long long>(__popc(mask)));
             base = __shfl_sync(~0u, base, leader);
             if (want) {
                 uint64_t idx = base + __popc(mask & ((1u << lane_id()) - 1u));
@@ -561,6 +561,7 @@ static WfSlots carve(char *base, uint32_t capacity, size_t *total) {
     W.ext_o = reinterpret_cast<float4 *>(take(Q * 16));
     W.ext_d = reinterpret_cast<float4 *>(take(Q * 16));
     W.counters = take(sizeof(Counters));
+    W.next_path = base ? &reinterpret_cast<Counters *>(W.counters)->next_path : nullptr;
     *total = off;
     return W;
 }
@@ -599,6 +600,7 @@ constexpr int kShadeShape[kWfShadeVariants][3] = {{256, 4, 0}, {256, 3, 0}, {256
                                                   {256, 3, 1}, {256, 5, 1}, {128, 8, 1}};
 
 int wf_shade_threads(uint32_t variant) { return kShadeShape[variant < kWfShadeVariants ? variant : 0][0]; }
+int wf_shade_blocks(uint32_t variant) { return kShadeShape[variant < kWfShadeVariants ? variant : 0][1]; }
 
 int wf_shade_grid(uint32_t variant, uint32_t capacity, int num_sms) {
     variant = variant < kWfShadeVariants ? variant : 0;
@@ -673,6 +675,31 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
         k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);
     }
     mark(2);
+}
+
+void wf_enqueue_shade(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
+                      float *path_rgb, int shade_grid, uint64_t total_paths, cudaStream_t st, uint32_t shade_variant) {
+    auto *cnt = reinterpret_cast<Counters *>(W.counters);
+    k_wf_reset<<<1, 1, 0, st>>>(cnt);
+    if (A.rng == E8G_RNG_MINSTD)
+        launch_shade<RngMinstd>(shade_variant, shade_grid, st, S, A, fh, W, cnt, accum, path_rgb, total_paths);
+    else
+        launch_shade<RngPhilox>(shade_variant, shade_grid, st, S, A, fh, W, cnt, accum, path_rgb, total_paths);
+}
+
+void wf_enqueue_trace(DevScene const &S, RenderArgs const &A, WfSlots const &W, float4 *accum, float *path_rgb,
+                      int trace_grid, uint32_t threshold, cudaStream_t st) {
+    auto *cnt = reinterpret_cast<Counters *>(W.counters);
+    BatchDev none{};
+    if (threshold > 0 && S.layout == 0) {
+        k_wf_trace_dyn<true, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+        k_wf_trace_dyn<false, false><<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb, threshold);
+    } else if (threshold > 0 && S.layout == 2) {
+        k_wf_trace_wide_both<false><<<trace_grid, kBlock, 0, st>>>(S, A, none, W, cnt, accum, path_rgb, threshold);
+    } else {
+        k_wf_shadow<<<trace_grid, kBlock, 0, st>>>(S, A, W, cnt, accum, path_rgb);
+        k_wf_extend<<<trace_grid, kBlock, 0, st>>>(S, W, cnt);
+    }
 }
 
 cudaError_t wf_init(WfSlots const &W, cudaStream_t st) {

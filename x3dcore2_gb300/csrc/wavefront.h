@@ -13,6 +13,8 @@ struct WfSlots {
     float4 *sh_o, *sh_d, *sh_c; // shadow queue: origin | out, direction | tmax, contribution
     float4 *ext_o, *ext_d;      // extension queue: origin | slot, direction
     void *counters;
+    unsigned long long *next_path; // the path counter refills draw from (shared by the pools of a
+                                   // concurrent wavefront; the pool's own counter otherwise)
 };
 
 size_t wf_total_bytes(uint32_t capacity);
@@ -33,5 +35,13 @@ int wf_shade_threads(uint32_t variant);
 int wf_shade_grid(uint32_t variant, uint32_t capacity, int num_sms);
 uint32_t *wf_busy_ptr(WfSlots const &W);
 unsigned long long *wf_next_ptr(WfSlots const &W);
+// The two halves of a bounce, for pools that interleave on two streams (concurrent wavefront):
+// queue reset + shading, and the trace kernel(s); grids are given for the residency wanted.
+void wf_enqueue_shade(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
+                      float *path_rgb, int shade_grid, uint64_t total_paths, cudaStream_t st, uint32_t shade_variant);
+void wf_enqueue_trace(DevScene const &S, RenderArgs const &A, WfSlots const &W, float4 *accum, float *path_rgb,
+                      int trace_grid, uint32_t threshold, cudaStream_t st);
+// Shading block shape's resident blocks per SM.
+int wf_shade_blocks(uint32_t variant);
 
 } // namespace e8g
