@@ -29,7 +29,7 @@ __device__ __forceinline__ uint32_t sample_subpath(DevScene const &S, R &rng, PV
     while (depth != max_len) { // sample_path, pathtracer.cpp:73-95
         PV const &prev = path[depth - 1];
         float w_dens;
-        float3 i = bsdf_sample_ref(S, vert_mat(S, prev.mesh), rng, w_dens, prev.n, prev.v);
+        float3 i = bsdf_sample_ref<true>(S, vert_mat(S, prev.mesh), rng, w_dens, prev.n, prev.v);
         if (feq0(w_dens))
             return depth;
         if (COUNT)
@@ -65,7 +65,7 @@ __device__ __forceinline__ float3 illum_source(DevScene const &S, int light, flo
     if (COUNT)
         cnt->rays++;
     if (!trace_any<COUNT>(S, tv.p, i, 1e-4f, dist - 1e-3f, stk, cnt))
-        return mul(illum, bsdf_eval(S, vert_mat(S, tv.mesh), tv.n, tv.v, i));
+        return mul(illum, bsdf_eval<true>(S, vert_mat(S, tv.mesh), tv.n, tv.v, i));
     return f3(0, 0, 0);
 }
 
@@ -81,7 +81,7 @@ __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, P
     for (uint32_t k = 0; k + 1 < clen; k++) { // projected_adjoint_brdf (:62-68)
         float3 towards = neg(cam[k + 1].v);
         float cw = dot(cam[k].n, towards);
-        float3 f = scale(bsdf_eval(S, vert_mat(S, cam[k].mesh), cam[k].n, cam[k].v, towards), cw);
+        float3 f = scale(bsdf_eval<true>(S, vert_mat(S, cam[k].mesh), cam[k].n, cam[k].v, towards), cw);
         tr = mul(tr, divs(f, cam[k + 1].dens));
         cam_pre[k + 1] = tr;
     }
@@ -90,7 +90,7 @@ __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, P
     for (uint32_t k = 0; k + 1 < llen; k++) { // projected_brdf (:54-60)
         float3 towards = neg(lp[k + 1].v);
         float cw = dot(lp[k].n, towards);
-        float3 f = scale(bsdf_eval(S, vert_mat(S, lp[k].mesh), lp[k].n, towards, lp[k].v), cw);
+        float3 f = scale(bsdf_eval<true>(S, vert_mat(S, lp[k].mesh), lp[k].n, towards, lp[k].v), cw);
         tr = mul(tr, divs(f, lp[k + 1].dens));
         light_pre[k + 1] = tr;
     }
@@ -126,8 +126,8 @@ __device__ float3 connect_all(DevScene const &S, PV const *cam, uint32_t clen, P
                     float3 le = divs(light_projected(S, light, neg(lp[0].v), em_n), lp[0].dens * em_area_dens);
                     float3 lsi = mul(le, light_pre[light_plen - 1]);
                     float to_area = cos_wi * cos_wo / (jd * jd);
-                    float3 ljw = bsdf_eval(S, vert_mat(S, lj.mesh), lj.n, join, lj.v);
-                    float3 cjw = bsdf_eval(S, vert_mat(S, cj.mesh), cj.n, cj.v, neg(join));
+                    float3 ljw = bsdf_eval<true>(S, vert_mat(S, lj.mesh), lj.n, join, lj.v);
+                    float3 cjw = bsdf_eval<true>(S, vert_mat(S, cj.mesh), cj.n, cj.v, neg(join));
                     float3 ti = scale(mul(mul(lsi, ljw), cjw), to_area);
                     float3 csr = divs(mul(ti, cam_pre[cam_plen - 1]), cam[0].dens);
                     psum = add(psum, scale(csr, cw));
@@ -167,7 +167,7 @@ __device__ __forceinline__ float to_area(float pdf_w, float3 from, float3 to, fl
 }
 
 __device__ __forceinline__ float vpdf(DevScene const &S, BV const &v, float3 wo, float3 wi) {
-    return bsdf_pdf(S, vert_mat(S, v.mesh), v.n, wo, wi);
+    return bsdf_pdf<true>(S, vert_mat(S, v.mesh), v.n, wo, wi);
 }
 
 template <bool COUNT, class R>
@@ -177,13 +177,13 @@ __device__ uint32_t bdp_walk(DevScene const &S, R &rng, BV *path, uint32_t len, 
         BV &cur = path[len - 1];
         const DevMaterial &m = vert_mat(S, cur.mesh);
         float pdf;
-        float3 i = bsdf_sample_mis(S, m, rng, pdf, cur.n, wo);
+        float3 i = bsdf_sample_mis<true>(S, m, rng, pdf, cur.n, wo);
         if (!(pdf > 0.0f))
             break;
         float cw = dot(cur.n, i);
         if (cw <= 0.0f)
             break;
-        float3 f = bsdf_eval(S, m, cur.n, wo, i);
+        float3 f = bsdf_eval<true>(S, m, cur.n, wo, i);
         if (COUNT)
             cnt->rays++;
         Hit h = trace_closest<COUNT>(S, cur.p, i, stk, cnt);
@@ -245,7 +245,7 @@ __device__ float3 connect_power(DevScene const &S, BV *cam, uint32_t clen, BV *l
                 float cos_l = dot(lv.n, neg(dir));
                 if (cos_c <= 0.0f || cos_l <= 0.0f)
                     continue;
-                float3 fc = bsdf_eval(S, vert_mat(S, cv.mesh), cv.n, wo_c, dir);
+                float3 fc = bsdf_eval<true>(S, vert_mat(S, cv.mesh), cv.n, wo_c, dir);
                 if (vequals0(fc))
                     continue;
                 float3 fl, wo_l = f3(0, 0, 0);
@@ -253,7 +253,7 @@ __device__ float3 connect_power(DevScene const &S, BV *cam, uint32_t clen, BV *l
                     fl = light_radiance(S, light, neg(dir), lv.n);
                 } else {
                     wo_l = normalize(sub(lp[sl - 2].p, lv.p));
-                    fl = bsdf_eval(S, vert_mat(S, lv.mesh), lv.n, neg(dir), wo_l);
+                    fl = bsdf_eval<true>(S, vert_mat(S, lv.mesh), lv.n, neg(dir), wo_l);
                 }
                 if (vequals0(fl))
                     continue;
@@ -523,8 +523,8 @@ __device__ __forceinline__ float3 lt2_join(DevScene const &S, R &rng, PV const &
     float cos_wi = dot(tv.n, neg(join));
     if (cos_wo > 0.0f && cos_wi > 0.0f && cos_w2 > 0.0f &&
         !trace_any<false>(S, term.p, join, 1e-4f, dist - 1e-3f, stk, nullptr)) {
-        float3 f2 = scale(mul(illum, bsdf_eval(S, vert_mat(S, term.mesh), term.n, join, tray)), cos_w2);
-        float3 p2 = scale(mul(divs(scale(f2, cos_wo), dist * dist), bsdf_eval(S, vert_mat(S, tv.mesh), tv.n, tv.v, neg(join))),
+        float3 f2 = scale(mul(illum, bsdf_eval<true>(S, vert_mat(S, term.mesh), term.n, join, tray)), cos_w2);
+        float3 p2 = scale(mul(divs(scale(f2, cos_wo), dist * dist), bsdf_eval<true>(S, vert_mat(S, tv.mesh), tv.n, tv.v, neg(join))),
                           cos_wi);
         return cam_len == 0 ? add(p1, scale(p2, 0.5f)) : scale(add(p1, p2), 0.5f);
     }
@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(kBlock) k_lt2(DevScene S, RenderArgs A, FirstH
                     }
                     float3 bid = lt2_join(S, rng, tv, depth, stk);
                     float pdf;
-                    float3 i = bsdf_sample_ref(S, vert_mat(S, tv.mesh), rng, pdf, tv.n, tv.v);
+                    float3 i = bsdf_sample_ref<true>(S, vert_mat(S, tv.mesh), rng, pdf, tv.n, tv.v);
                     Hit h = trace_closest<false>(S, tv.p, i, stk, nullptr);
                     float3 bl = divs(beta, surv);
                     if (h.tri == 0xFFFFFFFFu) {
@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(kBlock) k_lt2(DevScene S, RenderArgs A, FirstH
                     if (cw < 0.0f)
                         break;
                     L = add(L, mul(bl, bid));
-                    float3 fv = bsdf_eval(S, vert_mat(S, tv.mesh), tv.n, tv.v, i);
+                    float3 fv = bsdf_eval<true>(S, vert_mat(S, tv.mesh), tv.n, tv.v, i);
                     beta = divs(scale(mul(bl, fv), cw), pdf);
                     Vert nv = make_vert(S, h);
                     tv.v = neg(i);

@@ -793,21 +793,21 @@ __device__ __noinline__ float3 sample_leaf_call(const DevMaterial &m, R &rng, fl
 }
 
 // Reference sampling (mat_mixture returns the picked lobe's density x its weight, :95-106).
-template <class R>
+template <bool OUT = false, class R>
 __device__ __forceinline__ float3 bsdf_sample_ref(const DevScene &S, const DevMaterial &m, R &rng, float &dens,
                                                   float3 n, float3 o) {
     if (m.type == 3) {
         float3 i;
         if (rng.next() < m.ratio) {
-            i = sample_leaf(S.mats[m.mix0], rng, dens, n, o);
+            i = OUT ? sample_leaf_call(S.mats[m.mix0], rng, dens, n, o) : sample_leaf(S.mats[m.mix0], rng, dens, n, o);
             dens *= m.ratio;
         } else {
-            i = sample_leaf(S.mats[m.mix1], rng, dens, n, o);
+            i = OUT ? sample_leaf_call(S.mats[m.mix1], rng, dens, n, o) : sample_leaf(S.mats[m.mix1], rng, dens, n, o);
             dens *= 1 - m.ratio;
         }
         return i;
     }
-    return sample_leaf(m, rng, dens, n, o);
+    return OUT ? sample_leaf_call(m, rng, dens, n, o) : sample_leaf(m, rng, dens, n, o);
 }
 
 // Solid-angle density of direction i under the sampling above (product modes).

@@ -192,9 +192,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         // scene (its cached first hit is a miss) has no vertex and contributes nothing, so the
         // lane draws again, up to kRefillRounds rounds, instead of leaving the slot idle for the
         // whole bounce; the megakernel's refill does the same.
-        // once the path counter has passed the last path (it only grows) no lane can refill: the
-        // frame's tail skips the atomics
-        bool want = in && state == kEmpty && *reinterpret_cast<volatile unsigned long long *>(W.next_path) < total_paths;
+        bool want = in && state == kEmpty;
         bool refilled = false;
         for (int round = 0; round < kRefillRounds; round++) {
             uint32_t mask = __ballot_sync(~0u, want);
@@ -227,14 +225,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
                     }
                     RenderArgs const &A = args_of<MULTI>(A0, B, nsid);
                     if (path_coords(A, local, pixel, sample, out)) {
-                        FirstHit const &fr = fh[pbase + pixel];
-                        float4 fp = fr.p; // the mesh decides first: half the frame is sky
-                        int32_t m = __float_as_int(fp.w);
+                        FirstHit f = fh[pbase + pixel];
+                        int32_t m = __float_as_int(f.p.w);
                         if (m >= 0) {
-                            FirstHit f;
-                            f.p = fp;
-                            f.n = fr.n;
-                            f.d = fr.d;
                             sid = nsid;
                             out += static_cast<uint32_t>(pbase);
                             p = xyz(f.p);
