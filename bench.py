@@ -690,6 +690,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the quality, BDPT, batch and adjoint legs")
     ap.add_argument("--no-tune", action="store_true", help="wavefront with the library defaults (profiling)")
+    ap.add_argument("--wf-config", default=None,
+                    help="CAPACITY,BOUNCES,THRESHOLD: a fixed wavefront configuration instead of tuning (profiling)")
     ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "adjoint_fd", "update", "obj", "cornell"],
                     help="run one extra leg alone on the benchmark scene and print its JSON (not a bench line)")
     args = ap.parse_args()
@@ -761,7 +763,10 @@ def main():
         st = ctx.bvh_stats()
         trees[lay] = {"nodes": st["num_nodes"], "node_bytes": st["node_bytes"], "depth": st["max_depth"],
                       "build_s": round(commit_s, 3)}
-        if "wavefront" in integrators and not args.no_tune:
+        if "wavefront" in integrators and args.wf_config:
+            cap, bn, th = (int(x) for x in args.wf_config.split(","))
+            abi.check(lib.e8g_wavefront_set(ctx.h, cap, bn, th), ctx.h, "e8g_wavefront_set")
+        elif "wavefront" in integrators and not args.no_tune:
             tunes[lay] = tune_wavefront()
         for integ in integrators:
             p.integrator = INTEGRATORS[integ]
@@ -805,7 +810,7 @@ def main():
     img64 = d_img.cpu().numpy()  # the last timed frame (every combination renders the same paths)
     if best_lay != layouts[-1]:  # back to the best tree (and its wavefront tuning)
         build(best_lay)
-        if best_integ == "wavefront" and not args.no_tune:
+        if best_integ == "wavefront" and not args.no_tune and not args.wf_config:
             tunes[best_lay] = tune_wavefront()
     bvh = ctx.bvh_stats()
     p.integrator = INTEGRATORS[best_integ]
