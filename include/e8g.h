@@ -385,7 +385,8 @@ e8g_status e8g_wavefront_set(e8g_ctx *ctx, uint32_t capacity, uint32_t bounces_p
 /* Shape of the wavefront's shading kernel (threads x resident blocks per SM, register cap, the
  * materials' code inlined or out of line): 0 = 256 x 4 (64 registers), 1 = 256 x 3 (80),
  * 2 = 256 x 4 out of line, 3 = 256 x 3 out of line, 4 = 256 x 5 (48) out of line, 5 = 128 x 8 (64)
- * out of line. */
+ * out of line; 6 = 256 x 4 and 7 = 256 x 5 in the split form, where a small kernel first turns
+ * the extension hits into vertices and adds their emission, and the shading kernel reads them. */
 e8g_status e8g_wavefront_set_shade(e8g_ctx *ctx, uint32_t variant);
 /* Nonzero: the wavefront splits its slots into two pools that interleave on two streams, one
  * pool shading while the other traces, each kernel at half of an SM's residency, so shading

@@ -300,8 +300,8 @@ def test_wavefront_tuner_cache_and_shade_shapes(ctx, tmp_path):
     path = str(tmp_path / "tune.json").encode()
     r = abi.TuneResult()
     assert ctx.lib.e8g_wavefront_tune_cached(ctx.h, C.byref(p), path, C.byref(r)) == 0
-    assert r.from_cache == 0 and r.num_shade == 6 and r.shade_variant < 6
-    assert all(r.shade_ms[i] > 0 for i in range(6))
+    assert r.from_cache == 0 and r.num_shade == 8 and r.shade_variant < 8
+    assert all(r.shade_ms[i] > 0 for i in range(8))
     with open(path) as f:
         d = json.load(f)
     (key, entry), = d.items()
@@ -312,14 +312,14 @@ def test_wavefront_tuner_cache_and_shade_shapes(ctx, tmp_path):
     assert r2.from_cache == 1 and (r2.capacity, r2.bounces_per_graph, r2.threshold, r2.shade_variant) == \
         (r.capacity, r.bounces_per_graph, r.threshold, r.shade_variant)
     base = None
-    for v in range(6):
+    for v in range(8):
         assert ctx.lib.e8g_wavefront_set_shade(ctx.h, v) == 0
         img = ctx.render(p)
         if base is None:
             base = img
         close = np.all(np.abs(img - base) <= np.maximum(1e-4 * np.abs(base), 1e-6), axis=-1)
         assert close.mean() >= 0.999, v
-    assert ctx.lib.e8g_wavefront_set_shade(ctx.h, 6) == 1
+    assert ctx.lib.e8g_wavefront_set_shade(ctx.h, 8) == 1
 
 
 @pytest.mark.parametrize("mode", [abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER])

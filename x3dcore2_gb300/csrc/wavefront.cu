@@ -21,7 +21,9 @@ namespace e8g {
 
 namespace {
 
-enum : uint32_t { kEmpty = 0, kAtVertex = 1, kWaitHit = 2 };
+// kVertexReady: the split form's completion kernel has turned the slot's extension hit into its
+// vertex (slot arrays vp, vn) and added the vertex's emission.
+enum : uint32_t { kEmpty = 0, kAtVertex = 1, kWaitHit = 2, kVertexReady = 3 };
 
 // Refill rounds per slot and bounce: a lane skips paths whose camera ray missed the scene for at
 // most this many rounds (a frame that is half sky leaves a slot empty after 8 rounds with
@@ -125,7 +127,7 @@ __device__ __forceinline__ RenderArgs const &args_of(RenderArgs const &A0, Batch
 // sets the register cap) and OUT (the materials' code out of line, one copy for every call site:
 // the inlined form overflows the instruction cache) are one of kShadeShape, chosen by the
 // wavefront tuner.
-template <class R, bool MULTI, int THREADS, int MINB, bool OUT>
+template <class R, bool MULTI, int THREADS, int MINB, bool OUT, bool SPLIT = false>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_wf_shade(const __grid_constant__ DevScene S0, const __grid_constant__ RenderArgs A0, BatchDev B,
                FirstHit const *__restrict__ fh, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
@@ -158,7 +160,15 @@ __global__ void __launch_bounds__(THREADS, MINB)
             depth = __float_as_uint(od.w);
             rng = RngSlot<R>::load(args_of<MULTI>(A0, B, sid), pixel, sample, W.rng[s]);
         }
-        if (state == kWaitHit) { // complete the extension ray shot last bounce
+        if (SPLIT && state == kVertexReady) { // completed by k_wf_complete
+            float4 vp = W.vp[s], vn = W.vn[s];
+            p = xyz(vp);
+            mesh = __float_as_int(vp.w);
+            n = xyz(vn);
+            depth = __float_as_uint(vn.w);
+            state = kAtVertex;
+        }
+        if (!SPLIT && state == kWaitHit) { // complete the extension ray shot last bounce
             DevScene const &S = scene_of<MULTI>(S0, B, sid);
             float4 hv = W.hit[s];
             Hit h;
@@ -363,6 +373,47 @@ __global__ void __launch_bounds__(kBlock) k_wf_extend(DevScene S, WfSlots W, Cou
     }
 }
 
+// The split form's completion of the extension rays traced last bounce, one thread per queue
+// entry: the hit becomes the slot's vertex (vp: position | mesh, vn: normal | depth) and its
+// emission is added with the MIS weight; a miss or a back-facing hit empties the slot. A small
+// kernel of scene gathers, at full residency; the shading kernel then reads the vertex.
+__global__ void __launch_bounds__(256, 8)
+    k_wf_complete(const __grid_constant__ DevScene S, const __grid_constant__ RenderArgs A, WfSlots W,
+                  Counters const *cnt, float4 *accum, float *path_rgb) {
+    const uint32_t n = cnt->ext_n;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        uint32_t s = __float_as_uint(W.ext_o[q].w);
+        float4 hv = W.hit[s];
+        Hit h;
+        h.t = hv.x;
+        h.tri = __float_as_uint(hv.y);
+        h.b1 = hv.z;
+        h.b2 = hv.w;
+        uint32_t state = kEmpty;
+        if (h.tri != 0xFFFFFFFFu) {
+            float4 od = W.o[s];
+            float3 o = xyz(od);
+            Vert nv = make_vert(S, h);
+            float cos_l2 = dot(nv.n, o);
+            if (cos_l2 > 0.0f) {
+                int32_t hl = __ldg(&S.mesh_light[nv.mesh]);
+                if (hl >= 0) {
+                    float4 b = W.beta_pdf[s];
+                    float pl = __ldg(&S.light_pnorm[hl]) / S.total_power;
+                    float inv_area = 1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]);
+                    float p_l = pl * inv_area * (nv.t * nv.t) / cos_l2;
+                    float w = power_heuristic(b.w, p_l);
+                    emit_to(A, accum, path_rgb, W.out[s], scale(mul(xyz(b), light_rad(S, hl)), w));
+                }
+                W.vp[s] = make_float4(nv.p.x, nv.p.y, nv.p.z, __int_as_float(nv.mesh));
+                W.vn[s] = make_float4(nv.n.x, nv.n.y, nv.n.z, __uint_as_float(__float_as_uint(od.w) + 1u));
+                state = kVertexReady;
+            }
+        }
+        W.state[s] = state;
+    }
+}
+
 // Persistent trace kernel with per-lane dynamic fetch: a lane whose ray is finished takes the
 // next queue entry; lanes are refilled together (one atomic) once at least `threshold` of them
 // are idle, or when none is busy. WIDE: the eight-wide tree (one node visit per step), else the
@@ -553,6 +604,8 @@ static WfSlots carve(char *base, uint32_t capacity, size_t *total) {
     W.sh_c = reinterpret_cast<float4 *>(take(Q * 16));
     W.ext_o = reinterpret_cast<float4 *>(take(Q * 16));
     W.ext_d = reinterpret_cast<float4 *>(take(Q * 16));
+    W.vp = reinterpret_cast<float4 *>(take(Q * 16));
+    W.vn = reinterpret_cast<float4 *>(take(Q * 16));
     W.counters = take(sizeof(Counters));
     W.next_path = base ? &reinterpret_cast<Counters *>(W.counters)->next_path : nullptr;
     *total = off;
@@ -589,8 +642,11 @@ int wf_trace_blocks_per_sm(uint32_t layout, uint32_t threshold) {
 
 // The shading kernel's shapes: threads per block, resident blocks per SM (the register cap is
 // 65536 / (threads x blocks)) and whether the materials' code is out of line.
-constexpr int kShadeShape[kWfShadeVariants][3] = {{256, 4, 0}, {256, 3, 0}, {256, 4, 1},
-                                                  {256, 3, 1}, {256, 5, 1}, {128, 8, 1}};
+constexpr int kShadeShape[kWfShadeVariants][3] = {{256, 4, 0}, {256, 3, 0}, {256, 4, 1}, {256, 3, 1},
+                                                  {256, 5, 1}, {128, 8, 1}, {256, 4, 0}, {256, 5, 0}};
+// Shapes 6 and 7 run the split form: k_wf_complete first, then the shading kernel without the
+// hit completion (fewer registers, a smaller instruction footprint).
+constexpr bool shade_split(uint32_t v) { return v == 6 || v == 7; }
 
 int wf_shade_threads(uint32_t variant) { return kShadeShape[variant < kWfShadeVariants ? variant : 0][0]; }
 int wf_shade_blocks(uint32_t variant) { return kShadeShape[variant < kWfShadeVariants ? variant : 0][1]; }
@@ -622,6 +678,14 @@ static void launch_shade(uint32_t variant, int grid, cudaStream_t st, DevScene c
     case 5:
         k_wf_shade<R, false, 128, 8, true><<<grid, 128, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
         break;
+    case 6:
+        k_wf_shade<R, false, 256, 4, false, true><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb,
+                                                                       total_paths);
+        break;
+    case 7:
+        k_wf_shade<R, false, 256, 5, false, true><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb,
+                                                                       total_paths);
+        break;
     default:
         k_wf_shade<R, false, 256, 4, false><<<grid, 256, 0, st>>>(S, A, none, fh, W, cnt, accum, path_rgb, total_paths);
     }
@@ -639,6 +703,8 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
             cudaEventRecordWithFlags(timing[k], st, cudaEventRecordExternal);
     };
     mark(0);
+    if (!B && shade_split(shade_variant))
+        k_wf_complete<<<shade_grid, 256, 0, st>>>(S, A, W, cnt, accum, path_rgb);
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
     if (B) { // the many-scene form shades with the first block shape
         if (A.rng == E8G_RNG_MINSTD)
@@ -673,6 +739,8 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
 void wf_enqueue_shade(DevScene const &S, RenderArgs const &A, FirstHit const *fh, WfSlots const &W, float4 *accum,
                       float *path_rgb, int shade_grid, uint64_t total_paths, cudaStream_t st, uint32_t shade_variant) {
     auto *cnt = reinterpret_cast<Counters *>(W.counters);
+    if (shade_split(shade_variant))
+        k_wf_complete<<<shade_grid, 256, 0, st>>>(S, A, W, cnt, accum, path_rgb);
     k_wf_reset<<<1, 1, 0, st>>>(cnt);
     if (A.rng == E8G_RNG_MINSTD)
         launch_shade<RngMinstd>(shade_variant, shade_grid, st, S, A, fh, W, cnt, accum, path_rgb, total_paths);

@@ -12,6 +12,7 @@ struct WfSlots {
     float4 *beta_pdf, *o, *hit; // o: direction towards the previous vertex | depth
     float4 *sh_o, *sh_d, *sh_c; // shadow queue: origin | out, direction | tmax, contribution
     float4 *ext_o, *ext_d;      // extension queue: origin | slot, direction
+    float4 *vp, *vn;            // split form: completed vertex (position | mesh, normal | depth)
     void *counters;
     unsigned long long *next_path; // the path counter refills draw from (shared by the pools of a
                                    // concurrent wavefront; the pool's own counter otherwise)
@@ -30,7 +31,7 @@ void wf_enqueue_bounce(DevScene const &S, RenderArgs const &A, FirstHit const *f
                        uint32_t shade_variant = 0);
 // Block shapes of the shading kernel (the tuner's choice): the number of them, the threads of
 // one, and the grid of a bounce over `capacity` slots.
-constexpr uint32_t kWfShadeVariants = 6;
+constexpr uint32_t kWfShadeVariants = 8;
 int wf_shade_threads(uint32_t variant);
 int wf_shade_grid(uint32_t variant, uint32_t capacity, int num_sms);
 uint32_t *wf_busy_ptr(WfSlots const &W);
