@@ -45,14 +45,14 @@ REF_ESTIMATOR = dict(name="unidirect_lt1 (the reference's direct-lighting tracer
 # The host arms' sample of the frame: the same scene and camera at a quarter of the resolution in
 # each axis, so its pixels are spread uniformly over the whole 1920x1080 view (sky included).
 REF_SAMPLE_W, REF_SAMPLE_H = 480, 270
-# DRAM traffic per path of a (tree, integrator) combination, from the ncu captures summarised in
-# profiles/ (dram__bytes_read.sum + dram__bytes_write.sum divided by the paths of the captured
-# frame, scaled to the timed frame by its path count): "kernel" is the dominant kernel alone, "loop"
-# every kernel of the integrator. SAH pairs + megakernel: one 480x270, 8-spp frame (1,036,800
-# paths; profiles/megakernel_icosphere_l8.md). Eight-wide tree + wavefront: the launches of a
-# 1080p 8-spp frame (16,588,800 paths in steady state; profiles/wavefront_wide_icosphere_l8.md).
-TRAFFIC_BYTES_PER_PATH = {("sah", "megakernel"): {"kernel": 217.1, "loop": 217.1},
-                          ("wide", "wavefront"): {"kernel": 206.3, "loop": 457.7}}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures summarised in
+# profiles/, one kernel per capture. Eight-wide tree + wavefront: one steady-state launch of each
+# wavefront kernel in the benchmark's own configuration (2^23 slots, 2 bounces per graph,
+# threshold 12; profiles/wavefront_wide_icosphere_l8.md): "kernel" is the trace kernel's bytes
+# per launch, "shade" the shading kernel's. SAH pairs + megakernel: one 480x270, 8-spp launch of
+# k_mega, 217.1 B per path (profiles/megakernel_icosphere_l8.md), scaled by the frame's paths.
+TRAFFIC = {("wide", "wavefront"): {"kernel_per_launch": 1.938e9, "shade_per_launch": 2.244e9},
+           ("sah", "megakernel"): {"kernel_per_path": 217.1}}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
 
 
@@ -837,7 +837,7 @@ def main():
     loop_ms = rb["kernel_ms"]  # the integrator's whole device time per frame (first hits and resolve excluded)
     node_bytes = bvh["node_bytes"] // max(bvh["num_nodes"], 1)  # 32 (binary node) or 96 (wide node)
     alg_bytes = node_bytes * counts["nodes"] + 48 * counts["tris"]
-    per_path = TRAFFIC_BYTES_PER_PATH.get(best)
+    tr = TRAFFIC.get(best, {})
     if best_integ == "wavefront":
         # the dominant kernel is the trace kernel: every traversal byte is fetched there
         dom_ms, dom_launches = rb["trace_ms"], rb["trace_launches_per_step"]
@@ -848,7 +848,12 @@ def main():
         dom_name = {"plain": "k_plain (baseline per-path kernel)", "megakernel": "k_mega (megakernel)"}[best_integ]
     achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
     achieved_loop = alg_bytes / (loop_ms / 1000.0) / 1e9
-    traffic = per_path["kernel"] * paths_per_step / dom_launches if per_path else None
+    if "kernel_per_launch" in tr:
+        traffic = tr["kernel_per_launch"]
+    elif "kernel_per_path" in tr:
+        traffic = tr["kernel_per_path"] * paths_per_step / dom_launches
+    else:
+        traffic = None
     commit_s = trees[best_lay]["build_s"]
 
     line = {
@@ -875,12 +880,12 @@ def main():
                      "l2_peak": l2_peak, "frac_l2": achieved / l2_peak if l2_peak else None,
                      "node_bytes": node_bytes, "algorithmic_bytes_per_step": alg_bytes, "rays": counts["rays"],
                      "nodes": counts["nodes"], "tris": counts["tris"],
-                     "traffic_note": "DRAM bytes per launch from the ncu capture summarised in profiles/ "
-                                     "(per path, scaled by the paths of a launch)"},
+                     "traffic_note": "DRAM bytes of one steady-state launch of this kernel in this configuration, "
+                                     "from the ncu capture summarised in profiles/ (one kernel, three launches)"},
         "roofline_loop": {"achieved": achieved_loop, "unit": "GB/s", "frac": achieved_loop / peak,
                           "frac_l2": achieved_loop / l2_peak if l2_peak else None, "loop_ms_per_step": loop_ms,
                           "trace_ms_per_step": rb.get("trace_ms"), "shade_ms_per_step": rb.get("shade_ms"),
-                          "traffic": per_path["loop"] * paths_per_step if per_path else None,
+                          "shade_traffic_per_launch": tr.get("shade_per_launch"),
                           "note": "the same algorithmic bytes over the integrator's whole device time per frame "
                                   "(shading included)"},
         "gpu_launches": launches,
