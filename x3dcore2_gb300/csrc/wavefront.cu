@@ -133,6 +133,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
                FirstHit const *__restrict__ fh, WfSlots W, Counters *cnt, float4 *accum, float *path_rgb,
                uint64_t total_paths) {
     const uint64_t mix0 = MULTI ? 0 : splitmix64(A0.seed);
+    // Read once per thread: once the path counter has passed the last path (it only grows), no
+    // slot can be refilled for the rest of the frame, and the tail bounces skip the refill atomics
+    // (one per warp and slot group on a single address).
+    const bool paths_left = __ldcg(W.next_path) < total_paths;
     uint32_t busy_local = 0;
     for (uint32_t s0 = blockIdx.x * blockDim.x; s0 < W.capacity; s0 += gridDim.x * blockDim.x) {
         uint32_t s = s0 + threadIdx.x;
@@ -202,7 +206,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         // scene (its cached first hit is a miss) has no vertex and contributes nothing, so the
         // lane draws again, up to kRefillRounds rounds, instead of leaving the slot idle for the
         // whole bounce; the megakernel's refill does the same.
-        bool want = in && state == kEmpty;
+        bool want = paths_left && in && state == kEmpty;
         bool refilled = false;
         for (int round = 0; round < kRefillRounds; round++) {
             uint32_t mask = __ballot_sync(~0u, want);
