@@ -345,18 +345,24 @@ def cornell_leg(ctx, threads, cpu_budget_s=6.0):
 
 def bdpt_leg(ctx):
     """Bidirectional MIS on the benchmark scene (still uploaded) at 1280x720, subpaths of at most 6
-    vertices, 32 spp: power-heuristic weights (E8G_MODE_BDPT_POWER) and the reference's uniform
-    weights (E8G_MODE_REF_BDPT). Per mode the traversal roofline of its kernel (one launch per
-    frame): algorithmic bytes from the counted run (node bytes per node box fetched + 48 B per
-    triangle tested) over the kernel's device time, against the measured HBM copy bandwidth."""
+    vertices, 32 spp: power-heuristic weights (E8G_MODE_BDPT_POWER) one thread per path
+    (`power`) and in the split form (`power_split`: a subpath kernel and a connection kernel per
+    chunk of paths, E8G_INTEGRATOR_WAVEFRONT), and the reference's uniform weights
+    (E8G_MODE_REF_BDPT). Per form the traversal roofline of its kernels: algorithmic bytes from
+    the counted run (node bytes per node box fetched + 48 B per triangle tested) over the
+    integrator's device time, against the measured HBM copy bandwidth."""
     from x3dcore2_gb300 import abi
     from x3dcore2_gb300.core import default_params
     peak, _ = read_peaks()
     st = ctx.bvh_stats()
     node_bytes = st["node_bytes"] // max(st["num_nodes"], 1)
     out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6, "node_bytes": node_bytes}
-    for name, mode, kern in (("power", abi.MODE_BDPT_POWER, "k_bdpt_power"), ("uniform", abi.MODE_REF_BDPT, "k_bdpt_ref")):
+    for name, mode, kern, integ in (("power", abi.MODE_BDPT_POWER, "k_bdpt_power", abi.INTEGRATOR_MEGAKERNEL),
+                                    ("power_split", abi.MODE_BDPT_POWER, "k_bdw_walk + k_bdw_connect",
+                                     abi.INTEGRATOR_WAVEFRONT),
+                                    ("uniform", abi.MODE_REF_BDPT, "k_bdpt_ref", abi.INTEGRATOR_MEGAKERNEL)):
         p = default_params(mode, 1280, 720, 32, seed=1, bdpt_max_len=6)
+        p.integrator = integ
         ctx.render(p)
         ms = []
         for _ in range(2):

@@ -197,7 +197,10 @@ enum {
 
 enum {
     E8G_INTEGRATOR_MEGAKERNEL = 0, /* persistent threads; a lane whose path ends takes the next one */
-    E8G_INTEGRATOR_WAVEFRONT = 1,  /* queues of path slots, bounce loop as a CUDA graph (E8G_MODE_MIS) */
+    E8G_INTEGRATOR_WAVEFRONT = 1,  /* E8G_MODE_MIS: queues of path slots, bounce loop as a CUDA graph;
+                                      E8G_MODE_BDPT_POWER: the split form, subpaths sampled by one
+                                      kernel and every (t, s) connection evaluated by one thread of
+                                      another; other modes: the megakernel */
     E8G_INTEGRATOR_PLAIN = 2       /* one thread per path for its whole length: the baseline kernel */
 };
 
@@ -414,8 +417,9 @@ e8g_status e8g_wavefront_tune_cached(e8g_ctx *ctx, const e8g_render_params *para
  *   - the first call on a device looks up the array's device address: make it before any
  *     stream capture;
  *   - all calls share the one array: calls that overlap on the GPU race, so serialise them;
- *   - E8G_INTEGRATOR_WAVEFRONT renders with the persistent megakernel here (its slot pool would
- *     need memory); the paths, and so the image, are the ones the wavefront renders;
+ *   - E8G_INTEGRATOR_WAVEFRONT renders with the persistent megakernel here, and
+ *     E8G_MODE_BDPT_POWER with its one-thread-per-path kernel (the slot pool and the subpath
+ *     buffers would need memory); the paths, and so the image, are the same;
  *     E8G_INTEGRATOR_PLAIN runs the plain kernel; the firefly clamp is refused
  *     (E8G_ERR_UNSUPPORTED);
  *   - the array's address is cached per device: a cudaDeviceReset frees the array with every

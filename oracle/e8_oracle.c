@@ -1805,21 +1805,23 @@ static v3 bdpt_power_path(octx *c, const oray *cam_ray, const overt *first) {
             }
             /* power-heuristic weight over strategies producing this path */
             /* strategies whose subpaths would exceed the cap are impossible: stop there */
-            double sum = 0.0, ri = 1.0;
+            /* single precision: a ratio product whose square overflows gives weight 0, where */
+            /* double precision would give a weight below 1e-38 */
+            float sum = 0.0f, ri = 1.0f;
             for (int i = (int)t - 1; i >= 1; i--) {
                 if (sl + t - (unsigned)i > maxlen)
                     break;
-                ri *= (cam[i].fwd > 0.0f) ? (double)cam[i].rev / cam[i].fwd : 0.0;
+                ri *= (cam[i].fwd > 0.0f) ? cam[i].rev / cam[i].fwd : 0.0f;
                 sum += ri * ri;
             }
-            ri = 1.0;
+            ri = 1.0f;
             for (int i = (int)sl - 1; i >= 0; i--) {
                 if (t + sl - (unsigned)i > maxlen)
                     break;
-                ri *= (lp[i].fwd > 0.0f) ? (double)lp[i].rev / lp[i].fwd : 0.0;
+                ri *= (lp[i].fwd > 0.0f) ? lp[i].rev / lp[i].fwd : 0.0f;
                 sum += ri * ri;
             }
-            float wgt = (float)(1.0 / (1.0 + sum));
+            float wgt = 1.0f / (1.0f + sum);
             L = vadd(L, vscale(contrib, wgt));
             cv->rev = save_c_rev;
             if (t >= 2)

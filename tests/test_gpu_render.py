@@ -322,6 +322,34 @@ def test_wavefront_tuner_cache_and_shade_shapes(ctx, tmp_path):
     assert ctx.lib.e8g_wavefront_set_shade(ctx.h, 8) == 1
 
 
+@pytest.mark.parametrize("layout", [abi.BVH_WIDE, abi.BVH_SAH])
+def test_bdpt_power_split_form_renders_the_same_image(ctx, layout):
+    """The split form of power-heuristic BDPT (E8G_INTEGRATOR_WAVEFRONT: a subpath kernel and a
+    connection kernel per chunk of paths) renders the same paths as one thread per path: the same
+    image (the terms of a path added in another order), the same traversal counts; a memory
+    limit that forces chunks of a few thousand paths changes neither."""
+    d = G.load("ico.npz")
+    sc = G.scene_from(d)
+    ctx.upload(sc, layout=layout)
+    w, h = int(d["width"]), int(d["height"])
+    p = default_params(abi.MODE_BDPT_POWER, w, h, 8, seed=4, bdpt_max_len=6)
+    one = ctx.render(p)
+    c1 = ctx.count_traversal(p)
+    p.integrator = abi.INTEGRATOR_WAVEFRONT
+    ctx.set_memory_limit(ctx.memory_used() + 4 * 1024 * 1024)  # chunks of about 5,000 paths
+    try:
+        chunked = ctx.render(p)
+        c2 = ctx.count_traversal(p)
+    finally:
+        ctx.set_memory_limit(0)
+    split = ctx.render(p)  # one chunk
+    for img, name in ((chunked, "chunked"), (split, "one chunk")):
+        close = np.all(np.abs(img - one) <= np.maximum(1e-4 * np.abs(one), 1e-6), axis=-1)
+        print(f"split bdpt layout {layout} {name}: {close.mean():.5f} of pixels within 1e-4")
+        assert close.mean() >= 0.999, (name, close.mean())
+    assert (c1["rays"], c1["nodes"], c1["tris"]) == (c2["rays"], c2["nodes"], c2["tris"])
+
+
 @pytest.mark.parametrize("mode", [abi.MODE_REF_BDPT, abi.MODE_BDPT_POWER])
 def test_bidirectional_traversal_counts(ctx, mode):
     """e8g_count_traversal covers the bidirectional kernels (the roofline's algorithmic bytes): the

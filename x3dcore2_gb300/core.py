@@ -208,6 +208,16 @@ class Context:
         self._check(self.lib.e8g_composite(self.h, _ptr(rgba), w, h, C.byref(cp), _ptr(out)), "e8g_composite")
         return out
 
+    def set_memory_limit(self, nbytes):
+        """e8g_set_memory_limit: cap on the context's device memory (0: none)."""
+        self._check(self.lib.e8g_set_memory_limit(self.h, int(nbytes)), "e8g_set_memory_limit")
+
+    def memory_used(self):
+        """e8g_memory_used: device bytes the context holds."""
+        v = C.c_uint64(0)
+        self._check(self.lib.e8g_memory_used(self.h, C.byref(v)), "e8g_memory_used")
+        return v.value
+
     def set_kernel_timing(self, on=True):
         """e8g_set_kernel_timing: the wavefront times its trace and shading kernels per bounce."""
         self._check(self.lib.e8g_set_kernel_timing(self.h, int(on)), "e8g_set_kernel_timing")

@@ -63,6 +63,7 @@ struct e8g_ctx {
     e8g::dev_buffer b_fh, b_accum, b_work, b_img, b_io0, b_io1, b_counts;
     // wavefront queues and adjoint state
     e8g::dev_buffer b_wf, b_grad, b_ff, b_batch; // b_ff: firefly per-sample images; b_batch: staged batch scenes
+    e8g::dev_buffer b_bdw; // subpaths and connection lists of the split bidirectional form
     e8g_render_params fwd_params{};
     bool have_forward = false;
     // wavefront configuration (autotuned per context) and a pinned word for its termination test
@@ -104,7 +105,7 @@ struct e8g_ctx {
         return {&b_nlo, &b_nhi, &b_wide, &b_tri, &b_tidx, &b_vpos, &b_vnrm, &b_vtx, &b_mesh_mat, &b_mesh_light, &b_mesh_toff,
                 &b_mesh_area, &b_tri_cum, &b_mats, &b_light_mesh, &b_light_rad, &b_light_cum, &b_light_pnorm,
                 &b_fh, &b_accum, &b_work, &b_img, &b_io0, &b_io1, &b_counts, &b_wf, &b_grad, &b_ff, &b_batch,
-                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild, &b_pipe, &b_check};
+                &b_refit, &b_vpos0, &b_vnrm0, &b_gbuild, &b_pipe, &b_check, &b_bdw};
     }
 };
 

@@ -274,21 +274,23 @@ __device__ float3 connect_power(DevScene const &S, BV *cam, uint32_t clen, BV *l
                 if (sl >= 2)
                     lp[sl - 2].rev = to_area(vpdf(S, lv, neg(dir), wo_l), lv.p, lp[sl - 2].p, lp[sl - 2].n);
             }
-            double sum = 0.0, ri = 1.0;
+            // single precision (FP64 issues at a small fraction of the FP32 rate on this GPU): a
+            // ratio product whose square overflows gives weight 0, where FP64 would give < 1e-38
+            float sum = 0.0f, ri = 1.0f;
             for (int i = static_cast<int>(t) - 1; i >= 1; i--) {
                 if (sl + t - static_cast<uint32_t>(i) > maxlen)
                     break;
-                ri *= (cam[i].fwd > 0.0f) ? static_cast<double>(cam[i].rev) / cam[i].fwd : 0.0;
+                ri *= (cam[i].fwd > 0.0f) ? cam[i].rev / cam[i].fwd : 0.0f;
                 sum += ri * ri;
             }
-            ri = 1.0;
+            ri = 1.0f;
             for (int i = static_cast<int>(sl) - 1; i >= 0; i--) {
                 if (t + sl - static_cast<uint32_t>(i) > maxlen)
                     break;
-                ri *= (lp[i].fwd > 0.0f) ? static_cast<double>(lp[i].rev) / lp[i].fwd : 0.0;
+                ri *= (lp[i].fwd > 0.0f) ? lp[i].rev / lp[i].fwd : 0.0f;
                 sum += ri * ri;
             }
-            float wgt = static_cast<float>(1.0 / (1.0 + sum));
+            float wgt = 1.0f / (1.0f + sum);
             L = add(L, scale(contrib, wgt));
             cv.rev = save_c_rev;
             if (t >= 2)
@@ -402,6 +404,62 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_ref(DevScene S, RenderArgs A, F
         flush_counts(cnt, counters);
 }
 
+// Both subpaths of one path (the draw order of k_bdpt_power): the camera subpath from the cached
+// first hit f, then the light pick, the emission point and direction and the light subpath.
+// Returns the light's index; clen = 0 when the camera ray missed.
+template <bool COUNT, class R>
+__device__ __forceinline__ int sample_subpaths(DevScene const &S, R &rng, FirstHit const &f, uint32_t max_len, BV *cam,
+                                               BV *lp, uint32_t &clen, uint32_t &llen, uint32_t *stk,
+                                               TraceCounters *cnt) {
+    int32_t mesh = __float_as_int(f.p.w);
+    float3 o0 = neg(xyz(f.d));
+    clen = 0;
+    llen = 0;
+    if (mesh >= 0 && max_len) {
+        cam[0].p = xyz(f.p);
+        cam[0].n = xyz(f.n);
+        cam[0].mesh = mesh;
+        cam[0].beta = f3(1.0f, 1.0f, 1.0f);
+        cam[0].fwd = 1.0f;
+        cam[0].rev = 0.0f;
+        clen = bdp_walk<COUNT>(S, rng, cam, 1, max_len, o0, stk, cnt);
+    }
+    float pmf;
+    int light = sample_light(S, rng, pmf);
+    uint32_t lmesh = __ldg(&S.light_mesh[light]);
+    Surf em = mesh_sample(S, lmesh, rng, true);
+    float3 w = cos_hemisphere(em.n, rng);
+    float pdf_w = dot(em.n, w) / kPi;
+    if (max_len) {
+        lp[0].p = em.p;
+        lp[0].n = em.n;
+        lp[0].mesh = static_cast<int32_t>(lmesh);
+        lp[0].fwd = pmf * em.area_dens;
+        lp[0].rev = 0.0f;
+        float ib = 1.0f / lp[0].fwd;
+        lp[0].beta = f3(ib, ib, ib);
+        llen = 1;
+        if (pdf_w > 0.0f && max_len > 1) {
+            if (COUNT)
+                cnt->rays++;
+            Hit h = trace_closest<COUNT>(S, em.p, w, stk, cnt);
+            if (h.tri != 0xFFFFFFFFu) {
+                Vert v0 = make_vert(S, h);
+                if (dot(v0.n, neg(w)) > 0.0f) {
+                    lp[1].p = v0.p;
+                    lp[1].n = v0.n;
+                    lp[1].mesh = v0.mesh;
+                    lp[1].beta = scale(light_rad(S, light), dot(em.n, w) / (pdf_w * lp[0].fwd));
+                    lp[1].fwd = to_area(pdf_w, em.p, lp[1].p, lp[1].n);
+                    lp[1].rev = 0.0f;
+                    llen = bdp_walk<COUNT>(S, rng, lp, 2, max_len, neg(w), stk, cnt);
+                }
+            }
+        }
+    }
+    return light;
+}
+
 template <class R, bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
                                                        float4 *accum, float *path_rgb, unsigned long long *work,
@@ -426,52 +484,10 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
             R rng;
             seed_path(rng, A, mix, pixel, sample);
             FirstHit f = fh[pixel];
-            int32_t mesh = __float_as_int(f.p.w);
-            float3 o0 = neg(xyz(f.d));
-            uint32_t clen = 0, llen = 0;
-            if (mesh >= 0 && max_len) {
-                cam[0].p = xyz(f.p);
-                cam[0].n = xyz(f.n);
-                cam[0].mesh = mesh;
-                cam[0].beta = f3(1.0f, 1.0f, 1.0f);
-                cam[0].fwd = 1.0f;
-                cam[0].rev = 0.0f;
-                clen = bdp_walk<COUNT>(S, rng, cam, 1, max_len, o0, stk, &cnt);
-            }
-            float pmf;
-            int light = sample_light(S, rng, pmf);
-            uint32_t lmesh = __ldg(&S.light_mesh[light]);
-            Surf em = mesh_sample(S, lmesh, rng, true);
-            float3 w = cos_hemisphere(em.n, rng);
-            float pdf_w = dot(em.n, w) / kPi;
-            if (max_len) {
-                lp[0].p = em.p;
-                lp[0].n = em.n;
-                lp[0].mesh = static_cast<int32_t>(lmesh);
-                lp[0].fwd = pmf * em.area_dens;
-                lp[0].rev = 0.0f;
-                float ib = 1.0f / lp[0].fwd;
-                lp[0].beta = f3(ib, ib, ib);
-                llen = 1;
-                if (pdf_w > 0.0f && max_len > 1) {
-                    if (COUNT)
-                        cnt.rays++;
-                    Hit h = trace_closest<COUNT>(S, em.p, w, stk, &cnt);
-                    if (h.tri != 0xFFFFFFFFu) {
-                        Vert v0 = make_vert(S, h);
-                        if (dot(v0.n, neg(w)) > 0.0f) {
-                            lp[1].p = v0.p;
-                            lp[1].n = v0.n;
-                            lp[1].mesh = v0.mesh;
-                            lp[1].beta = scale(light_rad(S, light), dot(em.n, w) / (pdf_w * lp[0].fwd));
-                            lp[1].fwd = to_area(pdf_w, em.p, lp[1].p, lp[1].n);
-                            lp[1].rev = 0.0f;
-                            llen = bdp_walk<COUNT>(S, rng, lp, 2, max_len, neg(w), stk, &cnt);
-                        }
-                    }
-                }
-            }
-            float3 L = clen ? connect_power<COUNT>(S, cam, clen, lp, llen, max_len, o0, light, stk, &cnt) : f3(0, 0, 0);
+            uint32_t clen, llen;
+            int light = sample_subpaths<COUNT>(S, rng, f, max_len, cam, lp, clen, llen, stk, &cnt);
+            float3 L = clen ? connect_power<COUNT>(S, cam, clen, lp, llen, max_len, neg(xyz(f.d)), light, stk, &cnt)
+                            : f3(0, 0, 0);
             if (path_rgb) {
                 path_rgb[3 * static_cast<size_t>(out)] = L.x;
                 path_rgb[3 * static_cast<size_t>(out) + 1] = L.y;
@@ -479,6 +495,221 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
             } else {
                 atomicAdd(&accum[out], make_float4(L.x, L.y, L.z, 0.0f));
             }
+        }
+    }
+    if (COUNT)
+        flush_counts(cnt, counters);
+}
+
+// ---- E8G_MODE_BDPT_POWER, split form (E8G_INTEGRATOR_WAVEFRONT) ----
+// One thread per path of k_bdpt_power waits, with its warp, for the path with the most
+// connections (every (t, s) pair traces a shadow ray), and its lanes diverge on every connection's
+// early exits. The split form runs the same estimator as two kernels per chunk of paths:
+//   k_bdw_walk     one thread per path samples both subpaths (the same draws, sample_subpaths)
+//                  and stores them, and appends one entry per (t, s) strategy that can contribute
+//                  (s = 0 only when the camera vertex lies on a light);
+//   k_bdw_connect  one thread per entry evaluates that connection (BSDFs, shadow ray, the
+//                  power-heuristic weight from the stored densities with the four it changes) and
+//                  adds its contribution to the path's output.
+// A path's radiance is the same sum of the same terms, added in another order.
+
+// Stored vertex: three float4 (p | mesh), (n | fwd), (beta | rev).
+__device__ __forceinline__ void bdw_store(float4 *dst, BV const &v) {
+    dst[0] = make_float4(v.p.x, v.p.y, v.p.z, __int_as_float(v.mesh));
+    dst[1] = make_float4(v.n.x, v.n.y, v.n.z, v.fwd);
+    dst[2] = make_float4(v.beta.x, v.beta.y, v.beta.z, v.rev);
+}
+__device__ __forceinline__ BV bdw_load(float4 const *src) {
+    float4 a = src[0], b = src[1], c = src[2];
+    BV v;
+    v.p = xyz(a);
+    v.mesh = __float_as_int(a.w);
+    v.n = xyz(b);
+    v.fwd = b.w;
+    v.beta = xyz(c);
+    v.rev = c.w;
+    return v;
+}
+
+template <class R, bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_bdw_walk(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
+                                                     float *path_rgb, BdwChunk C, unsigned long long *work,
+                                                     unsigned long long *counters) {
+    TraceCounters cnt{0, 0, 0};
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *stk = stk_all + threadIdx.x;
+    const uint64_t mix = splitmix64(A.seed);
+    const uint32_t lane = lane_id();
+    const uint32_t max_len = C.max_len;
+    BV cam[kMaxSub], lp[kMaxSub];
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32ull);
+        base = __shfl_sync(~0u, base, 0);
+        if (base >= C.count)
+            break;
+        const uint32_t local = static_cast<uint32_t>(base) + lane;
+        uint32_t pixel, sample, out, n_conn = 0;
+        if (local < C.count && path_coords(A, C.first + local, pixel, sample, out)) {
+            R rng;
+            seed_path(rng, A, mix, pixel, sample);
+            FirstHit f = fh[pixel];
+            uint32_t clen, llen;
+            int light = sample_subpaths<COUNT>(S, rng, f, max_len, cam, lp, clen, llen, stk, &cnt);
+            float4 *v = C.vtx + static_cast<size_t>(local) * 6 * max_len;
+            for (uint32_t k = 0; k < clen; k++)
+                bdw_store(v + 3 * k, cam[k]);
+            for (uint32_t k = 0; k < llen; k++)
+                bdw_store(v + 3 * (max_len + k), lp[k]);
+            C.info[local] = make_int4(static_cast<int>(clen | llen << 8), light, static_cast<int>(out), 0);
+            float3 o0 = neg(xyz(f.d));
+            C.o0[local] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+            if (path_rgb) { // the connections add into it
+                path_rgb[3 * static_cast<size_t>(out)] = 0.0f;
+                path_rgb[3 * static_cast<size_t>(out) + 1] = 0.0f;
+                path_rgb[3 * static_cast<size_t>(out) + 2] = 0.0f;
+            }
+            for (uint32_t t = 1; t <= clen; t++)
+                n_conn += llen + (__ldg(&S.mesh_light[cam[t - 1].mesh]) >= 0 ? 1u : 0u);
+        }
+        // warp-aggregated append of every lane's entries
+        uint32_t incl = n_conn;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(~0u, incl, off);
+            if (static_cast<int>(lane) >= off)
+                incl += y;
+        }
+        uint32_t total = __shfl_sync(~0u, incl, 31), start = 0;
+        if (lane == 31 && total)
+            start = atomicAdd(C.conn_n, total);
+        start = __shfl_sync(~0u, start, 31);
+        if (n_conn) {
+            uint32_t pos = start + incl - n_conn;
+            uint32_t clen = C.info[local].x & 0xFFu, llen = (C.info[local].x >> 8) & 0xFFu;
+            for (uint32_t t = 1; t <= clen; t++) {
+                uint32_t s0 = __ldg(&S.mesh_light[cam[t - 1].mesh]) >= 0 ? 0u : 1u;
+                for (uint32_t sl = s0; sl <= llen; sl++)
+                    C.conn[pos++] = local << 10 | (t - 1) << 5 | sl;
+            }
+        }
+    }
+    if (COUNT)
+        flush_counts(cnt, counters);
+}
+
+// Power-heuristic density of the BSDF at a stored vertex (vpdf on its mesh and normal).
+__device__ __forceinline__ float bdw_pdf(DevScene const &S, int32_t mesh, float3 n, float3 wo, float3 wi) {
+    return bsdf_pdf<true>(S, vert_mat(S, mesh), n, wo, wi);
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_bdw_connect(DevScene S, float4 *accum, float *path_rgb, BdwChunk C,
+                                                        unsigned long long *counters) {
+    TraceCounters cnt{0, 0, 0};
+    __shared__ uint32_t stk_all[kStackWords * kBlock];
+    uint32_t *stk = stk_all + threadIdx.x;
+    const uint32_t n = *C.conn_n;
+    const uint32_t maxlen = C.max_len;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint32_t e = C.conn[q];
+        const uint32_t path = e >> 10, t = ((e >> 5) & 31u) + 1u, sl = e & 31u;
+        const int4 inf = C.info[path];
+        float4 const *cam = C.vtx + static_cast<size_t>(path) * 6 * maxlen;
+        float4 const *lpv = cam + 3 * maxlen;
+        const BV cv = bdw_load(cam + 3 * (t - 1));
+        BV c2{};
+        if (t >= 2)
+            c2 = bdw_load(cam + 3 * (t - 2));
+        const float3 wo_c = t >= 2 ? normalize(sub(c2.p, cv.p)) : xyz(C.o0[path]);
+        // the densities this connection changes: camera vertices t-1, t-2; light vertices s-1, s-2
+        float rc1 = cv.rev, rc2 = c2.rev, rl1 = 0.0f, rl2 = 0.0f;
+        float3 contrib;
+        if (sl == 0) {
+            int hl = __ldg(&S.mesh_light[cv.mesh]);
+            if (hl < 0)
+                continue;
+            float3 le = light_radiance(S, hl, wo_c, cv.n);
+            if (vequals0(le))
+                continue;
+            contrib = mul(cv.beta, le);
+            float pl = __ldg(&S.light_pnorm[hl]) / S.total_power;
+            rc1 = pl * (1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]));
+            if (t >= 2) {
+                float ew = fmaxf(dot(cv.n, wo_c), 0.0f) / kPi;
+                rc2 = to_area(ew, cv.p, c2.p, c2.n);
+            }
+        } else {
+            const BV lv = bdw_load(lpv + 3 * (sl - 1));
+            float3 d = sub(lv.p, cv.p);
+            float d2 = dot(d, d);
+            if (d2 <= 0.0f)
+                continue;
+            float dist = sqrtf(d2);
+            float3 dir = divs(d, dist);
+            float cos_c = dot(cv.n, dir);
+            float cos_l = dot(lv.n, neg(dir));
+            if (cos_c <= 0.0f || cos_l <= 0.0f)
+                continue;
+            float3 fc = bsdf_eval<true>(S, vert_mat(S, cv.mesh), cv.n, wo_c, dir);
+            if (vequals0(fc))
+                continue;
+            float3 fl, wo_l = f3(0, 0, 0);
+            float4 l2p = make_float4(0, 0, 0, 0), l2n = make_float4(0, 0, 0, 0);
+            if (sl == 1) {
+                fl = light_radiance(S, inf.y, neg(dir), lv.n);
+            } else {
+                l2p = lpv[3 * (sl - 2)];
+                l2n = lpv[3 * (sl - 2) + 1];
+                wo_l = normalize(sub(xyz(l2p), lv.p));
+                fl = bsdf_eval<true>(S, vert_mat(S, lv.mesh), lv.n, neg(dir), wo_l);
+            }
+            if (vequals0(fl))
+                continue;
+            if (COUNT)
+                cnt.rays++;
+            if (trace_any<COUNT>(S, cv.p, dir, 1e-4f, dist - 1e-3f, stk, &cnt))
+                continue;
+            float G = cos_c * cos_l / d2;
+            contrib = scale(mul(mul(mul(cv.beta, fc), fl), lv.beta), G);
+            float pc = bdw_pdf(S, cv.mesh, cv.n, wo_c, dir);
+            rl1 = to_area(pc, cv.p, lv.p, lv.n);
+            if (sl == 1)
+                rc1 = to_area(cos_l / kPi, lv.p, cv.p, cv.n);
+            else
+                rc1 = to_area(bdw_pdf(S, lv.mesh, lv.n, wo_l, neg(dir)), lv.p, cv.p, cv.n);
+            if (t >= 2)
+                rc2 = to_area(bdw_pdf(S, cv.mesh, cv.n, dir, wo_c), cv.p, c2.p, c2.n);
+            if (sl >= 2)
+                rl2 = to_area(bdw_pdf(S, lv.mesh, lv.n, neg(dir), wo_l), lv.p, xyz(l2p), xyz(l2n));
+        }
+        // the weight of connect_power, densities read from the stored subpaths
+        float sum = 0.0f, ri = 1.0f;
+        for (int i = static_cast<int>(t) - 1; i >= 1; i--) {
+            if (sl + t - static_cast<uint32_t>(i) > maxlen)
+                break;
+            float fwd = cam[3 * i + 1].w;
+            float rev = i == static_cast<int>(t) - 1 ? rc1 : i == static_cast<int>(t) - 2 ? rc2 : cam[3 * i + 2].w;
+            ri *= (fwd > 0.0f) ? rev / fwd : 0.0f;
+            sum += ri * ri;
+        }
+        ri = 1.0f;
+        for (int i = static_cast<int>(sl) - 1; i >= 0; i--) {
+            if (t + sl - static_cast<uint32_t>(i) > maxlen)
+                break;
+            float fwd = lpv[3 * i + 1].w;
+            float rev = i == static_cast<int>(sl) - 1 ? rl1 : i == static_cast<int>(sl) - 2 ? rl2 : lpv[3 * i + 2].w;
+            ri *= (fwd > 0.0f) ? rev / fwd : 0.0f;
+            sum += ri * ri;
+        }
+        float3 L = scale(contrib, 1.0f / (1.0f + sum));
+        const uint32_t out = static_cast<uint32_t>(inf.z);
+        if (path_rgb) {
+            atomicAdd(&path_rgb[3 * static_cast<size_t>(out)], L.x);
+            atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 1], L.y);
+            atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 2], L.z);
+        } else {
+            atomicAdd(&accum[out], make_float4(L.x, L.y, L.z, 0.0f));
         }
     }
     if (COUNT)
@@ -611,6 +842,32 @@ __global__ void __launch_bounds__(kBlock) k_lt2(DevScene S, RenderArgs A, FirstH
             }
         }
     }
+}
+
+void bdpt_split_blocks_per_sm(int *walk, int *conn) {
+    *walk = *conn = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(walk, k_bdw_walk<RngPhilox, false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(conn, k_bdw_connect<false>, kBlock, 0);
+    *walk = *walk > 0 ? *walk : 1;
+    *conn = *conn > 0 ? *conn : 1;
+}
+
+void launch_bdpt_split(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
+                       BdwChunk const &C, unsigned long long *work, int grid_walk, int grid_conn, cudaStream_t st,
+                       unsigned long long *counters) {
+    bool minstd = A.rng == E8G_RNG_MINSTD;
+    if (counters && minstd)
+        k_bdw_walk<RngMinstd, true><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, counters);
+    else if (counters)
+        k_bdw_walk<RngPhilox, true><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, counters);
+    else if (minstd)
+        k_bdw_walk<RngMinstd, false><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, nullptr);
+    else
+        k_bdw_walk<RngPhilox, false><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, nullptr);
+    if (counters)
+        k_bdw_connect<true><<<grid_conn, kBlock, 0, st>>>(S, accum, path_rgb, C, counters);
+    else
+        k_bdw_connect<false><<<grid_conn, kBlock, 0, st>>>(S, accum, path_rgb, C, nullptr);
 }
 
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,

@@ -154,6 +154,29 @@ struct RngMinstd {
 };
 
 // Philox4x32-10 (Salmon et al., SC'11), counter (block, pixel, sample, tag), key = seed.
+// Philox4x32-10 block `block` of the stream keyed (k0, k1) at counter (block, pixel, sample, const).
+// Out of line: RngPhilox::next() is inlined at every draw site, and one copy of the ten rounds
+// serves all of them (the shading kernels' code otherwise overflows the instruction cache). Its
+// arguments and result are plain values, so the caller's stream state stays in registers.
+static __device__ __noinline__ uint4 philox_block(uint32_t k0, uint32_t k1, uint32_t block, uint32_t pixel,
+                                                  uint32_t sample) {
+    uint32_t c0 = block, c1 = pixel, c2 = sample, c3 = 0x0E8A0E8Au;
+    uint32_t a = k0, b = k1;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ a, n2 = hi0 ^ c3 ^ b;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        a += 0x9E3779B9u;
+        b += 0xBB67AE85u;
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+
 struct RngPhilox {
     uint32_t k0, k1, pixel, sample, block, lane;
     uint32_t buf[4];
@@ -165,27 +188,12 @@ struct RngPhilox {
         block = 0;
         lane = 4;
     }
-    // Out of line: next() is inlined at every draw site, and one copy of the ten rounds serves all
-    // of them (the shading kernels' code otherwise overflows the instruction cache).
-    __device__ __noinline__ void refill() {
-        uint32_t c0 = block, c1 = pixel, c2 = sample, c3 = 0x0E8A0E8Au;
-        uint32_t a = k0, b = k1;
-#pragma unroll
-        for (int r = 0; r < 10; r++) {
-            uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-            uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-            uint32_t n0 = hi1 ^ c1 ^ a, n2 = hi0 ^ c3 ^ b;
-            c0 = n0;
-            c1 = lo1;
-            c2 = n2;
-            c3 = lo0;
-            a += 0x9E3779B9u;
-            b += 0xBB67AE85u;
-        }
-        buf[0] = c0;
-        buf[1] = c1;
-        buf[2] = c2;
-        buf[3] = c3;
+    __device__ __forceinline__ void refill() {
+        uint4 r = philox_block(k0, k1, block, pixel, sample);
+        buf[0] = r.x;
+        buf[1] = r.y;
+        buf[2] = r.z;
+        buf[3] = r.w;
         block++;
         lane = 0;
     }

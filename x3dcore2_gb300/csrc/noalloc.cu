@@ -22,9 +22,10 @@
 //  * Every call on a device shares the one array and leaves the last call's contents in it; each
 //    call clears what must start at zero. Two calls that overlap on the GPU (other streams,
 //    other contexts on the same device, other host threads) race on the array: serialise them.
-//  * E8G_INTEGRATOR_WAVEFRONT runs as the persistent megakernel (the wavefront's slot pool is
-//    allocated memory); both render the same paths from the same streams, so the image is the
-//    wavefront's. E8G_INTEGRATOR_PLAIN runs the plain kernel.
+//  * E8G_INTEGRATOR_WAVEFRONT runs as the persistent megakernel, and E8G_MODE_BDPT_POWER as its
+//    one-thread-per-path kernel (the wavefront's slot pool and the split form's subpath buffers
+//    are allocated memory); they render the same paths from the same streams, so the image is
+//    the same. E8G_INTEGRATOR_PLAIN runs the plain kernel.
 //  * The address looked up per device stays cached for the life of the process. A
 //    cudaDeviceReset frees the array with every other allocation on that device; after one, the
 //    library must not be used on that device again.

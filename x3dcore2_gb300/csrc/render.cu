@@ -20,8 +20,70 @@ struct WfCounters { // mirrors the device Counters of wavefront.cu
     uint32_t shadow_n, ext_n, busy, pad[3];
 };
 
+// The split form of E8G_MODE_BDPT_POWER: paths in chunks whose subpaths and connection lists fit
+// in at most 2 GiB (fewer paths per chunk when the memory limit refuses that).
+e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb,
+                          unsigned long long *d_counts) {
+    const uint32_t ml = std::min<uint32_t>(A.bdpt_max_len, 16);
+    const size_t per_path = bdw_bytes_per_path(ml);
+    uint64_t chunk = std::min<uint64_t>({A.total_paths, kBdwMaxChunk, (size_t(2) << 30) / per_path});
+    chunk = std::max<uint64_t>(chunk, 1);
+    // the chunk's arrays from base (sizes only when base is null), each 256-byte aligned
+    auto carve = [&](char *base, uint64_t n, size_t *bytes) {
+        BdwChunk C{};
+        size_t off = 0;
+        auto take = [&](size_t sz) {
+            char *r = base ? base + off : nullptr;
+            off += (sz + 255) & ~size_t(255);
+            return r;
+        };
+        C.vtx = reinterpret_cast<float4 *>(take(n * ml * 6 * 16));
+        C.info = reinterpret_cast<int4 *>(take(n * 16));
+        C.o0 = reinterpret_cast<float4 *>(take(n * 16));
+        C.conn = reinterpret_cast<uint32_t *>(take(n * ml * (ml + 1) * 4));
+        C.conn_n = reinterpret_cast<uint32_t *>(take(16));
+        C.max_len = ml;
+        *bytes = off;
+        return C;
+    };
+    cudaError_t e = cudaErrorMemoryAllocation;
+    size_t need = 0;
+    while (true) {
+        carve(nullptr, chunk, &need);
+        e = c->b_bdw.reserve(need);
+        if (e == cudaSuccess || chunk <= 4096)
+            break;
+        cudaGetLastError();
+        chunk /= 2;
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "bidirectional subpath buffers");
+    BdwChunk C = carve(static_cast<char *>(c->b_bdw.ptr), chunk, &need);
+    int bw = 1, bc = 1;
+    bdpt_split_blocks_per_sm(&bw, &bc);
+    const int grid_walk = persistent_grid(c, bw), grid_conn = persistent_grid(c, bc);
+    auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
+    auto *work = static_cast<unsigned long long *>(c->b_work.ptr);
+    for (uint64_t first = 0; first < A.total_paths; first += chunk) {
+        if (take_cancel(c))
+            return fail(c, E8G_ERR_CANCELLED, "render cancelled");
+        C.first = first;
+        C.count = static_cast<uint32_t>(std::min<uint64_t>(chunk, A.total_paths - first));
+        e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(C.conn_n, 0, sizeof(uint32_t), c->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "bidirectional chunk counters");
+        launch_bdpt_split(c->dev, A, fh, accum, path_rgb, C, work, grid_walk, grid_conn, c->stream, d_counts);
+        c->launches += 2;
+    }
+    return E8G_OK;
+}
+
 e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs const &A, float4 *accum, float *path_rgb,
                           unsigned long long *d_counts) {
+    if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_BDPT_POWER)
+        return run_bdpt_split(c, A, accum, path_rgb, d_counts);
     if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_MIS && !d_counts)
         return c->wf_concurrent ? run_wavefront_concurrent(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces,
                                                            c->wf_threshold)

