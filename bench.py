@@ -356,9 +356,10 @@ def bdpt_leg(ctx):
     peak, _ = read_peaks()
     st = ctx.bvh_stats()
     node_bytes = st["node_bytes"] // max(st["num_nodes"], 1)
-    out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6, "node_bytes": node_bytes}
+    out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6, "node_bytes": node_bytes,
+           "tree": {0: "sah", 1: "reference", 2: "wide", 3: "linear"}.get(st.get("layout", -1), "?")}
     for name, mode, kern, integ in (("power", abi.MODE_BDPT_POWER, "k_bdpt_power", abi.INTEGRATOR_MEGAKERNEL),
-                                    ("power_split", abi.MODE_BDPT_POWER, "k_bdw_walk + k_bdw_connect",
+                                    ("power_split", abi.MODE_BDPT_POWER, "k_bdw_walk + k_bdw_eval + trace kernels",
                                      abi.INTEGRATOR_WAVEFRONT),
                                     ("uniform", abi.MODE_REF_BDPT, "k_bdpt_ref", abi.INTEGRATOR_MEGAKERNEL)):
         p = default_params(mode, 1280, 720, 32, seed=1, bdpt_max_len=6)
@@ -623,9 +624,11 @@ def run_leg(args):
     if args.leg == "obj":
         print(json.dumps({"leg": "obj", **obj_leg()}))
         return
+    from x3dcore2_gb300 import abi
     ctx = Context(0)
     scene, _, _, _ = make_scene(args.small)
-    ctx.upload(scene)
+    LAYOUTS = {"sah": abi.BVH_SAH, "wide": abi.BVH_WIDE, "reference": abi.BVH_REFERENCE}
+    ctx.upload(scene, layout=LAYOUTS[args.layout] if args.layout else abi.BVH_SAH)
     fn = {"bdpt": lambda: bdpt_leg(ctx), "batch": lambda: batch_leg(ctx), "adjoint": lambda: adjoint_leg(ctx),
           "update": lambda: update_leg(ctx, scene), "adjoint_fd": lambda: adjoint_fd_leg(ctx),
           "cornell": lambda: cornell_leg(ctx, os.cpu_count() or 1)}[args.leg]

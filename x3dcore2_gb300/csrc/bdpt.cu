@@ -8,6 +8,7 @@
 // direction (2), light subpath BSDF samples — the reference's order.
 #include "../../include/e8g.h"
 #include "launch.h"
+#include "wavefront.h"
 
 namespace e8g {
 
@@ -502,15 +503,20 @@ __global__ void __launch_bounds__(kBlock) k_bdpt_power(DevScene S, RenderArgs A,
 }
 
 // ---- E8G_MODE_BDPT_POWER, split form (E8G_INTEGRATOR_WAVEFRONT) ----
-// One thread per path of k_bdpt_power waits, with its warp, for the path with the most
-// connections (every (t, s) pair traces a shadow ray), and its lanes diverge on every connection's
-// early exits. The split form runs the same estimator as two kernels per chunk of paths:
-//   k_bdw_walk     one thread per path samples both subpaths (the same draws, sample_subpaths)
-//                  and stores them, and appends one entry per (t, s) strategy that can contribute
-//                  (s = 0 only when the camera vertex lies on a light);
-//   k_bdw_connect  one thread per entry evaluates that connection (BSDFs, shadow ray, the
-//                  power-heuristic weight from the stored densities with the four it changes) and
-//                  adds its contribution to the path's output.
+// One thread per path of k_bdpt_power waits, with its warp, for the path with the longest
+// subpaths and the most connections (every (t, s) pair traces a shadow ray), and its lanes diverge
+// on every early exit and traversal. The split form runs the same estimator per chunk of paths as
+// two wavefronts:
+//   the walk     path slots (WfSlots) advance both subpaths of their paths one vertex per
+//                bounce: k_bdw_walk shades (completes the last ray's vertex, samples the next
+//                direction, the same draws in the same order as sample_subpaths), the wavefront's
+//                trace kernel traces the extension queue; a finished path stores its record and
+//                appends one entry per (t, s) strategy that can contribute (s = 0 only when the
+//                camera vertex lies on a light), and its slot takes the next path;
+//   connections  k_bdw_eval evaluates one entry per thread without tracing (BSDFs, geometry
+//                term, the power-heuristic weight from the stored densities with the four it
+//                changes); s = 0 terms go to the output at once, the others become shadow rays
+//                carrying their weighted contribution, which the wavefront's trace kernel drains.
 // A path's radiance is the same sum of the same terms, added in another order.
 
 // Stored vertex: three float4 (p | mesh), (n | fwd), (beta | rev).
@@ -531,71 +537,267 @@ __device__ __forceinline__ BV bdw_load(float4 const *src) {
     return v;
 }
 
-template <class R, bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_bdw_walk(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh,
-                                                     float *path_rgb, BdwChunk C, unsigned long long *work,
-                                                     unsigned long long *counters) {
-    TraceCounters cnt{0, 0, 0};
-    __shared__ uint32_t stk_all[kStackWords * kBlock];
-    uint32_t *stk = stk_all + threadIdx.x;
+// One step of a subpath walk at stored vertex len-1 (the loop body of bdp_walk up to the trace):
+// samples the next direction; false when the walk ends there. On true: the ray, the throughput of
+// the vertex it will make, the sampling density and the reverse density at the current vertex.
+template <class R>
+__device__ __forceinline__ bool walk_sample(DevScene const &S, R &rng, float4 const *sub, uint32_t len, float3 wo,
+                                            float3 &org, float3 &dir, float3 &beta_next, float &pdf, float &prev_w) {
+    const BV cur = bdw_load(sub + 3 * (len - 1));
+    const DevMaterial &m = vert_mat(S, cur.mesh);
+    float3 i = bsdf_sample_mis<true>(S, m, rng, pdf, cur.n, wo);
+    if (!(pdf > 0.0f))
+        return false;
+    float cw = dot(cur.n, i);
+    if (cw <= 0.0f)
+        return false;
+    float3 f = bsdf_eval<true>(S, m, cur.n, wo, i);
+    beta_next = mul(cur.beta, scale(f, cw / pdf));
+    prev_w = vpdf(S, cur, i, wo);
+    org = cur.p;
+    dir = i;
+    return true;
+}
+
+// The rest of the step once the ray's hit is known: stores vertex len and the reverse density of
+// vertex len-2; false when the walk ends (miss or back face).
+__device__ __forceinline__ bool walk_complete(DevScene const &S, float4 *sub, uint32_t len, Hit const &h, float3 dir,
+                                              float3 beta_next, float pdf, float prev_w) {
+    if (h.tri == 0xFFFFFFFFu)
+        return false;
+    Vert nv = make_vert(S, h);
+    if (dot(nv.n, neg(dir)) <= 0.0f)
+        return false;
+    const float3 cp = xyz(sub[3 * (len - 1)]);
+    BV nx;
+    nx.p = nv.p;
+    nx.n = nv.n;
+    nx.mesh = nv.mesh;
+    nx.beta = beta_next;
+    nx.fwd = to_area(pdf, cp, nx.p, nx.n);
+    nx.rev = 0.0f;
+    bdw_store(sub + 3 * len, nx);
+    if (len >= 2) {
+        float4 pp = sub[3 * (len - 2)], pn = sub[3 * (len - 2) + 1];
+        reinterpret_cast<float *>(sub + 3 * (len - 2) + 2)[3] = to_area(prev_w, cp, xyz(pp), xyz(pn));
+    }
+    return true;
+}
+
+// Slot state of the walk: stage in bits 0-1 (kWkEmpty, kWkCam: a camera-subpath ray is pending,
+// kWkLight: a light-subpath ray is pending), the current subpath's stored vertices in bits 2-6,
+// the camera subpath's length in bits 7-11.
+enum : uint32_t { kWkEmpty = 0, kWkCam = 1, kWkLight = 2 };
+constexpr int kWalkRounds = 4; // paths a slot may start and finish without a ray in one bounce
+
+// One bounce of the walk over every slot. range: the chunk's first path index and path count
+// (device memory, so one captured graph serves every chunk). W.next_path: the chunk's path
+// counter; W.sid: the slot's path (index in the chunk), W.out: its light, W.beta_pdf: throughput
+// of the pending vertex | sampling density, W.o: ray direction | reverse density.
+template <class R>
+__global__ void __launch_bounds__(256, 3)
+    k_bdw_walk(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh, float *path_rgb, BdwChunk C, WfSlots W,
+               uint64_t const *range, uint32_t *ext_n, uint32_t *busy) {
     const uint64_t mix = splitmix64(A.seed);
-    const uint32_t lane = lane_id();
     const uint32_t max_len = C.max_len;
-    BV cam[kMaxSub], lp[kMaxSub];
-    while (true) {
-        unsigned long long base = 0;
-        if (lane == 0)
-            base = atomicAdd(work, 32ull);
-        base = __shfl_sync(~0u, base, 0);
-        if (base >= C.count)
-            break;
-        const uint32_t local = static_cast<uint32_t>(base) + lane;
-        uint32_t pixel, sample, out, n_conn = 0;
-        if (local < C.count && path_coords(A, C.first + local, pixel, sample, out)) {
-            R rng;
-            seed_path(rng, A, mix, pixel, sample);
-            FirstHit f = fh[pixel];
-            uint32_t clen, llen;
-            int light = sample_subpaths<COUNT>(S, rng, f, max_len, cam, lp, clen, llen, stk, &cnt);
-            float4 *v = C.vtx + static_cast<size_t>(local) * 6 * max_len;
-            for (uint32_t k = 0; k < clen; k++)
-                bdw_store(v + 3 * k, cam[k]);
-            for (uint32_t k = 0; k < llen; k++)
-                bdw_store(v + 3 * (max_len + k), lp[k]);
-            C.info[local] = make_int4(static_cast<int>(clen | llen << 8), light, static_cast<int>(out), 0);
-            float3 o0 = neg(xyz(f.d));
-            C.o0[local] = make_float4(o0.x, o0.y, o0.z, 0.0f);
-            if (path_rgb) { // the connections add into it
-                path_rgb[3 * static_cast<size_t>(out)] = 0.0f;
-                path_rgb[3 * static_cast<size_t>(out) + 1] = 0.0f;
-                path_rgb[3 * static_cast<size_t>(out) + 2] = 0.0f;
+    const uint64_t first = range[0];
+    const uint32_t count = static_cast<uint32_t>(range[1]);
+    const uint32_t lane = lane_id();
+    uint32_t busy_local = 0;
+    for (uint32_t s0 = blockIdx.x * blockDim.x; s0 < W.capacity; s0 += gridDim.x * blockDim.x) {
+        const uint32_t s = s0 + threadIdx.x;
+        const bool in = s < W.capacity;
+        const uint32_t st = in ? W.state[s] : kWkEmpty;
+        uint32_t stage = st & 3u, len = (st >> 2) & 31u, clen = (st >> 7) & 31u;
+        uint32_t path = 0, pixel = 0, sample = 0, light = 0;
+        R rng;
+        float3 wo = f3(0, 0, 0), org = f3(0, 0, 0), dir = f3(0, 0, 0), beta_next = f3(0, 0, 0);
+        float pdf = 0.0f, prev_w = 0.0f;
+        bool at_vertex = false; // at stored vertex len-1 with the walk going on (else it ended)
+        if (stage != kWkEmpty) { // complete the pending ray
+            path = W.sid[s];
+            pixel = W.pixel[s];
+            sample = W.sample[s];
+            light = W.out[s];
+            rng = RngSlot<R>::load(A, pixel, sample, W.rng[s]);
+            float4 hv = W.hit[s], od = W.o[s], bp = W.beta_pdf[s];
+            Hit h;
+            h.t = hv.x;
+            h.tri = __float_as_uint(hv.y);
+            h.b1 = hv.z;
+            h.b2 = hv.w;
+            float4 *sub = C.vtx + static_cast<size_t>(path) * 6 * max_len + (stage == kWkLight ? 3 * max_len : 0);
+            if (walk_complete(S, sub, len, h, xyz(od), xyz(bp), bp.w, od.w)) {
+                len++;
+                wo = neg(xyz(od));
+                at_vertex = true;
             }
-            for (uint32_t t = 1; t <= clen; t++)
-                n_conn += llen + (__ldg(&S.mesh_light[cam[t - 1].mesh]) >= 0 ? 1u : 0u);
         }
-        // warp-aggregated append of every lane's entries
-        uint32_t incl = n_conn;
-        for (int off = 1; off < 32; off <<= 1) {
-            uint32_t y = __shfl_up_sync(~0u, incl, off);
-            if (static_cast<int>(lane) >= off)
-                incl += y;
+        bool emitted = false, paths_left = true;
+        for (int round = 0; round < kWalkRounds; round++) {
+            // a new path for every empty slot, one atomic per warp
+            bool want = in && stage == kWkEmpty && paths_left;
+            uint32_t mask = __ballot_sync(~0u, want);
+            if (mask) {
+                int leader = __ffs(mask) - 1;
+                unsigned long long base = 0;
+                if (static_cast<int>(lane) == leader)
+                    base = atomicAdd(W.next_path, static_cast<unsigned long long>(__popc(mask)));
+                base = __shfl_sync(~0u, base, leader);
+                if (want) {
+                    uint64_t idx = base + __popc(mask & ((1u << lane) - 1u));
+                    uint32_t out;
+                    if (idx >= count) {
+                        paths_left = false;
+                    } else if (path_coords(A, first + idx, pixel, sample, out)) {
+                        path = static_cast<uint32_t>(idx);
+                        seed_path(rng, A, mix, pixel, sample);
+                        FirstHit f = fh[pixel];
+                        const float3 o0 = neg(xyz(f.d));
+                        C.o0[path] = make_float4(o0.x, o0.y, o0.z, 0.0f);
+                        stage = kWkCam;
+                        len = 0;
+                        at_vertex = false;
+                        int32_t mesh = __float_as_int(f.p.w);
+                        if (mesh >= 0 && max_len) {
+                            BV v0;
+                            v0.p = xyz(f.p);
+                            v0.n = xyz(f.n);
+                            v0.mesh = mesh;
+                            v0.beta = f3(1.0f, 1.0f, 1.0f);
+                            v0.fwd = 1.0f;
+                            v0.rev = 0.0f;
+                            bdw_store(C.vtx + static_cast<size_t>(path) * 6 * max_len, v0);
+                            len = 1;
+                            wo = o0;
+                            at_vertex = true;
+                        }
+                    }
+                }
+            }
+            // advance the lane's path until it waits for a ray or is finished
+            bool done = false;
+            for (int k = 0; k < 3 && !emitted && !done && stage != kWkEmpty; k++) {
+                float4 *sub = C.vtx + static_cast<size_t>(path) * 6 * max_len + (stage == kWkLight ? 3 * max_len : 0);
+                if (at_vertex && len < max_len &&
+                    walk_sample(S, rng, sub, len, wo, org, dir, beta_next, pdf, prev_w)) {
+                    emitted = true;
+                    break;
+                }
+                at_vertex = false;
+                if (stage == kWkLight) { // the light subpath ended: len vertices
+                    done = true;
+                    break;
+                }
+                // the camera subpath ended: the light's emission sample (sample_subpaths' order)
+                clen = len;
+                float pmf;
+                int li = sample_light(S, rng, pmf);
+                light = static_cast<uint32_t>(li);
+                uint32_t lmesh = __ldg(&S.light_mesh[li]);
+                Surf em = mesh_sample(S, lmesh, rng, true);
+                float3 w = cos_hemisphere(em.n, rng);
+                float pdf_w = dot(em.n, w) / kPi;
+                stage = kWkLight;
+                len = 0;
+                if (max_len) {
+                    BV l0;
+                    l0.p = em.p;
+                    l0.n = em.n;
+                    l0.mesh = static_cast<int32_t>(lmesh);
+                    l0.fwd = pmf * em.area_dens;
+                    l0.rev = 0.0f;
+                    float ib = 1.0f / l0.fwd;
+                    l0.beta = f3(ib, ib, ib);
+                    bdw_store(C.vtx + static_cast<size_t>(path) * 6 * max_len + 3 * max_len, l0);
+                    len = 1;
+                    if (pdf_w > 0.0f && max_len > 1) {
+                        org = em.p;
+                        dir = w;
+                        beta_next = scale(light_rad(S, li), dot(em.n, w) / (pdf_w * l0.fwd));
+                        pdf = pdf_w;
+                        prev_w = 0.0f;
+                        emitted = true;
+                        break;
+                    }
+                }
+                done = true; // a light subpath of at most one vertex
+            }
+            // finished paths: record, output cleared, connection entries (one atomic per warp)
+            uint32_t n_conn = 0;
+            float4 const *cam = C.vtx + static_cast<size_t>(path) * 6 * max_len;
+            if (done) {
+                uint32_t px, smp, out = 0;
+                path_coords(A, first + path, px, smp, out);
+                C.info[path] = make_int4(static_cast<int>(clen | len << 8), static_cast<int>(light),
+                                         static_cast<int>(out), 0);
+                if (path_rgb) {
+                    path_rgb[3 * static_cast<size_t>(out)] = 0.0f;
+                    path_rgb[3 * static_cast<size_t>(out) + 1] = 0.0f;
+                    path_rgb[3 * static_cast<size_t>(out) + 2] = 0.0f;
+                }
+                for (uint32_t t = 1; t <= clen; t++)
+                    n_conn += len + (__ldg(&S.mesh_light[__float_as_int(cam[3 * (t - 1)].w)]) >= 0 ? 1u : 0u);
+            }
+            uint32_t incl = n_conn;
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t y = __shfl_up_sync(~0u, incl, off);
+                if (static_cast<int>(lane) >= off)
+                    incl += y;
+            }
+            uint32_t total = __shfl_sync(~0u, incl, 31), start = 0;
+            if (lane == 31 && total)
+                start = atomicAdd(C.conn_n, total);
+            start = __shfl_sync(~0u, start, 31);
+            if (n_conn) {
+                uint32_t pos = start + incl - n_conn;
+                for (uint32_t t = 1; t <= clen; t++) {
+                    uint32_t sl0 = __ldg(&S.mesh_light[__float_as_int(cam[3 * (t - 1)].w)]) >= 0 ? 0u : 1u;
+                    for (uint32_t sl = sl0; sl <= len; sl++)
+                        C.conn[pos++] = path << 10 | (t - 1) << 5 | sl;
+                }
+            }
+            if (done) {
+                stage = kWkEmpty;
+                len = clen = 0;
+            }
+            if (__ballot_sync(~0u, in && stage == kWkEmpty && paths_left) == 0)
+                break;
         }
-        uint32_t total = __shfl_sync(~0u, incl, 31), start = 0;
-        if (lane == 31 && total)
-            start = atomicAdd(C.conn_n, total);
-        start = __shfl_sync(~0u, start, 31);
-        if (n_conn) {
-            uint32_t pos = start + incl - n_conn;
-            uint32_t clen = C.info[local].x & 0xFFu, llen = (C.info[local].x >> 8) & 0xFFu;
-            for (uint32_t t = 1; t <= clen; t++) {
-                uint32_t s0 = __ldg(&S.mesh_light[cam[t - 1].mesh]) >= 0 ? 0u : 1u;
-                for (uint32_t sl = s0; sl <= llen; sl++)
-                    C.conn[pos++] = local << 10 | (t - 1) << 5 | sl;
+        // the slot's ray to the extension queue, one atomic per warp
+        uint32_t mask = __ballot_sync(~0u, emitted);
+        uint32_t base = 0;
+        if (mask) {
+            int leader = __ffs(mask) - 1;
+            if (static_cast<int>(lane) == leader)
+                base = atomicAdd(ext_n, static_cast<uint32_t>(__popc(mask)));
+            base = __shfl_sync(~0u, base, leader);
+        }
+        if (in) {
+            if (emitted) {
+                uint32_t q = base + __popc(mask & ((1u << lane) - 1u));
+                if (E8G_CHK(S.check, q < W.capacity, kChkQueue, q)) {
+                    W.ext_o[q] = make_float4(org.x, org.y, org.z, __uint_as_float(s));
+                    W.ext_d[q] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                }
+                W.state[s] = stage | len << 2 | clen << 7;
+                W.sid[s] = path;
+                W.pixel[s] = pixel;
+                W.sample[s] = sample;
+                W.out[s] = light;
+                W.rng[s] = RngSlot<R>::store(rng);
+                W.beta_pdf[s] = make_float4(beta_next.x, beta_next.y, beta_next.z, pdf);
+                W.o[s] = make_float4(dir.x, dir.y, dir.z, prev_w);
+                busy_local++;
+            } else {
+                W.state[s] = kWkEmpty;
             }
         }
     }
-    if (COUNT)
-        flush_counts(cnt, counters);
+    for (int off = 16; off > 0; off >>= 1)
+        busy_local += __shfl_down_sync(~0u, busy_local, off);
+    if (lane == 0 && busy_local)
+        atomicAdd(busy, busy_local);
 }
 
 // Power-heuristic density of the BSDF at a stored vertex (vpdf on its mesh and normal).
@@ -603,117 +805,141 @@ __device__ __forceinline__ float bdw_pdf(DevScene const &S, int32_t mesh, float3
     return bsdf_pdf<true>(S, vert_mat(S, mesh), n, wo, wi);
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_bdw_connect(DevScene S, float4 *accum, float *path_rgb, BdwChunk C,
-                                                        unsigned long long *counters) {
-    TraceCounters cnt{0, 0, 0};
-    __shared__ uint32_t stk_all[kStackWords * kBlock];
-    uint32_t *stk = stk_all + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) k_bdw_eval(DevScene S, float4 *accum, float *path_rgb, BdwChunk C,
+                                                     WfSlots W, uint32_t *shadow_n) {
     const uint32_t n = *C.conn_n;
     const uint32_t maxlen = C.max_len;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const uint32_t e = C.conn[q];
-        const uint32_t path = e >> 10, t = ((e >> 5) & 31u) + 1u, sl = e & 31u;
-        const int4 inf = C.info[path];
-        float4 const *cam = C.vtx + static_cast<size_t>(path) * 6 * maxlen;
-        float4 const *lpv = cam + 3 * maxlen;
-        const BV cv = bdw_load(cam + 3 * (t - 1));
-        BV c2{};
-        if (t >= 2)
-            c2 = bdw_load(cam + 3 * (t - 2));
-        const float3 wo_c = t >= 2 ? normalize(sub(c2.p, cv.p)) : xyz(C.o0[path]);
-        // the densities this connection changes: camera vertices t-1, t-2; light vertices s-1, s-2
-        float rc1 = cv.rev, rc2 = c2.rev, rl1 = 0.0f, rl2 = 0.0f;
-        float3 contrib;
-        if (sl == 0) {
-            int hl = __ldg(&S.mesh_light[cv.mesh]);
-            if (hl < 0)
-                continue;
-            float3 le = light_radiance(S, hl, wo_c, cv.n);
-            if (vequals0(le))
-                continue;
-            contrib = mul(cv.beta, le);
-            float pl = __ldg(&S.light_pnorm[hl]) / S.total_power;
-            rc1 = pl * (1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]));
-            if (t >= 2) {
-                float ew = fmaxf(dot(cv.n, wo_c), 0.0f) / kPi;
-                rc2 = to_area(ew, cv.p, c2.p, c2.n);
-            }
-        } else {
-            const BV lv = bdw_load(lpv + 3 * (sl - 1));
-            float3 d = sub(lv.p, cv.p);
-            float d2 = dot(d, d);
-            if (d2 <= 0.0f)
-                continue;
-            float dist = sqrtf(d2);
-            float3 dir = divs(d, dist);
-            float cos_c = dot(cv.n, dir);
-            float cos_l = dot(lv.n, neg(dir));
-            if (cos_c <= 0.0f || cos_l <= 0.0f)
-                continue;
-            float3 fc = bsdf_eval<true>(S, vert_mat(S, cv.mesh), cv.n, wo_c, dir);
-            if (vequals0(fc))
-                continue;
-            float3 fl, wo_l = f3(0, 0, 0);
-            float4 l2p = make_float4(0, 0, 0, 0), l2n = make_float4(0, 0, 0, 0);
-            if (sl == 1) {
-                fl = light_radiance(S, inf.y, neg(dir), lv.n);
-            } else {
-                l2p = lpv[3 * (sl - 2)];
-                l2n = lpv[3 * (sl - 2) + 1];
-                wo_l = normalize(sub(xyz(l2p), lv.p));
-                fl = bsdf_eval<true>(S, vert_mat(S, lv.mesh), lv.n, neg(dir), wo_l);
-            }
-            if (vequals0(fl))
-                continue;
-            if (COUNT)
-                cnt.rays++;
-            if (trace_any<COUNT>(S, cv.p, dir, 1e-4f, dist - 1e-3f, stk, &cnt))
-                continue;
-            float G = cos_c * cos_l / d2;
-            contrib = scale(mul(mul(mul(cv.beta, fc), fl), lv.beta), G);
-            float pc = bdw_pdf(S, cv.mesh, cv.n, wo_c, dir);
-            rl1 = to_area(pc, cv.p, lv.p, lv.n);
-            if (sl == 1)
-                rc1 = to_area(cos_l / kPi, lv.p, cv.p, cv.n);
-            else
-                rc1 = to_area(bdw_pdf(S, lv.mesh, lv.n, wo_l, neg(dir)), lv.p, cv.p, cv.n);
+    const uint32_t lane = lane_id();
+    // warp-uniform loop: every lane reaches the shadow-queue append
+    for (uint32_t q0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); q0 < n; q0 += gridDim.x * blockDim.x) {
+        const uint32_t q = q0 + lane;
+        bool push = false;
+        float3 org = f3(0, 0, 0), dir = f3(0, 0, 0), L = f3(0, 0, 0);
+        float tmax = 0.0f;
+        uint32_t out = 0;
+        do {
+            if (q >= n)
+                break;
+            const uint32_t e = C.conn[q];
+            const uint32_t path = e >> 10, t = ((e >> 5) & 31u) + 1u, sl = e & 31u;
+            const int4 inf = C.info[path];
+            out = static_cast<uint32_t>(inf.z);
+            float4 const *cam = C.vtx + static_cast<size_t>(path) * 6 * maxlen;
+            float4 const *lpv = cam + 3 * maxlen;
+            const BV cv = bdw_load(cam + 3 * (t - 1));
+            BV c2{};
             if (t >= 2)
-                rc2 = to_area(bdw_pdf(S, cv.mesh, cv.n, dir, wo_c), cv.p, c2.p, c2.n);
-            if (sl >= 2)
-                rl2 = to_area(bdw_pdf(S, lv.mesh, lv.n, neg(dir), wo_l), lv.p, xyz(l2p), xyz(l2n));
+                c2 = bdw_load(cam + 3 * (t - 2));
+            const float3 wo_c = t >= 2 ? normalize(sub(c2.p, cv.p)) : xyz(C.o0[path]);
+            // the densities this connection changes: camera vertices t-1, t-2; light vertices s-1, s-2
+            float rc1 = cv.rev, rc2 = c2.rev, rl1 = 0.0f, rl2 = 0.0f;
+            float3 contrib;
+            if (sl == 0) {
+                int hl = __ldg(&S.mesh_light[cv.mesh]);
+                if (hl < 0)
+                    break;
+                float3 le = light_radiance(S, hl, wo_c, cv.n);
+                if (vequals0(le))
+                    break;
+                contrib = mul(cv.beta, le);
+                float pl = __ldg(&S.light_pnorm[hl]) / S.total_power;
+                rc1 = pl * (1.0f / __ldg(&S.mesh_area[__ldg(&S.light_mesh[hl])]));
+                if (t >= 2) {
+                    float ew = fmaxf(dot(cv.n, wo_c), 0.0f) / kPi;
+                    rc2 = to_area(ew, cv.p, c2.p, c2.n);
+                }
+            } else {
+                const BV lv = bdw_load(lpv + 3 * (sl - 1));
+                float3 d = sub(lv.p, cv.p);
+                float d2 = dot(d, d);
+                if (d2 <= 0.0f)
+                    break;
+                float dist = sqrtf(d2);
+                dir = divs(d, dist);
+                float cos_c = dot(cv.n, dir);
+                float cos_l = dot(lv.n, neg(dir));
+                if (cos_c <= 0.0f || cos_l <= 0.0f)
+                    break;
+                float3 fc = bsdf_eval<true>(S, vert_mat(S, cv.mesh), cv.n, wo_c, dir);
+                if (vequals0(fc))
+                    break;
+                float3 fl, wo_l = f3(0, 0, 0);
+                float4 l2p = make_float4(0, 0, 0, 0), l2n = make_float4(0, 0, 0, 0);
+                if (sl == 1) {
+                    fl = light_radiance(S, inf.y, neg(dir), lv.n);
+                } else {
+                    l2p = lpv[3 * (sl - 2)];
+                    l2n = lpv[3 * (sl - 2) + 1];
+                    wo_l = normalize(sub(xyz(l2p), lv.p));
+                    fl = bsdf_eval<true>(S, vert_mat(S, lv.mesh), lv.n, neg(dir), wo_l);
+                }
+                if (vequals0(fl))
+                    break;
+                float G = cos_c * cos_l / d2;
+                contrib = scale(mul(mul(mul(cv.beta, fc), fl), lv.beta), G);
+                float pc = bdw_pdf(S, cv.mesh, cv.n, wo_c, dir);
+                rl1 = to_area(pc, cv.p, lv.p, lv.n);
+                if (sl == 1)
+                    rc1 = to_area(cos_l / kPi, lv.p, cv.p, cv.n);
+                else
+                    rc1 = to_area(bdw_pdf(S, lv.mesh, lv.n, wo_l, neg(dir)), lv.p, cv.p, cv.n);
+                if (t >= 2)
+                    rc2 = to_area(bdw_pdf(S, cv.mesh, cv.n, dir, wo_c), cv.p, c2.p, c2.n);
+                if (sl >= 2)
+                    rl2 = to_area(bdw_pdf(S, lv.mesh, lv.n, neg(dir), wo_l), lv.p, xyz(l2p), xyz(l2n));
+                org = cv.p;
+                tmax = dist - 1e-3f;
+            }
+            // the weight of connect_power, densities read from the stored subpaths
+            float sum = 0.0f, ri = 1.0f;
+            for (int i = static_cast<int>(t) - 1; i >= 1; i--) {
+                if (sl + t - static_cast<uint32_t>(i) > maxlen)
+                    break;
+                float fwd = cam[3 * i + 1].w;
+                float rev = i == static_cast<int>(t) - 1 ? rc1 : i == static_cast<int>(t) - 2 ? rc2 : cam[3 * i + 2].w;
+                ri *= (fwd > 0.0f) ? rev / fwd : 0.0f;
+                sum += ri * ri;
+            }
+            ri = 1.0f;
+            for (int i = static_cast<int>(sl) - 1; i >= 0; i--) {
+                if (t + sl - static_cast<uint32_t>(i) > maxlen)
+                    break;
+                float fwd = lpv[3 * i + 1].w;
+                float rev = i == static_cast<int>(sl) - 1 ? rl1 : i == static_cast<int>(sl) - 2 ? rl2 : lpv[3 * i + 2].w;
+                ri *= (fwd > 0.0f) ? rev / fwd : 0.0f;
+                sum += ri * ri;
+            }
+            L = scale(contrib, 1.0f / (1.0f + sum));
+            if (sl == 0) { // no shadow ray: the camera subpath itself reached a light
+                if (path_rgb) {
+                    atomicAdd(&path_rgb[3 * static_cast<size_t>(out)], L.x);
+                    atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 1], L.y);
+                    atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 2], L.z);
+                } else {
+                    atomicAdd(&accum[out], make_float4(L.x, L.y, L.z, 0.0f));
+                }
+            } else {
+                push = true;
+            }
+        } while (false);
+        // warp-aggregated append to the shadow queue
+        uint32_t mask = __ballot_sync(~0u, push);
+        uint32_t base = 0;
+        if (mask) {
+            int leader = __ffs(mask) - 1;
+            if (static_cast<int>(lane) == leader)
+                base = atomicAdd(shadow_n, static_cast<uint32_t>(__popc(mask)));
+            base = __shfl_sync(~0u, base, leader);
         }
-        // the weight of connect_power, densities read from the stored subpaths
-        float sum = 0.0f, ri = 1.0f;
-        for (int i = static_cast<int>(t) - 1; i >= 1; i--) {
-            if (sl + t - static_cast<uint32_t>(i) > maxlen)
-                break;
-            float fwd = cam[3 * i + 1].w;
-            float rev = i == static_cast<int>(t) - 1 ? rc1 : i == static_cast<int>(t) - 2 ? rc2 : cam[3 * i + 2].w;
-            ri *= (fwd > 0.0f) ? rev / fwd : 0.0f;
-            sum += ri * ri;
-        }
-        ri = 1.0f;
-        for (int i = static_cast<int>(sl) - 1; i >= 0; i--) {
-            if (t + sl - static_cast<uint32_t>(i) > maxlen)
-                break;
-            float fwd = lpv[3 * i + 1].w;
-            float rev = i == static_cast<int>(sl) - 1 ? rl1 : i == static_cast<int>(sl) - 2 ? rl2 : lpv[3 * i + 2].w;
-            ri *= (fwd > 0.0f) ? rev / fwd : 0.0f;
-            sum += ri * ri;
-        }
-        float3 L = scale(contrib, 1.0f / (1.0f + sum));
-        const uint32_t out = static_cast<uint32_t>(inf.z);
-        if (path_rgb) {
-            atomicAdd(&path_rgb[3 * static_cast<size_t>(out)], L.x);
-            atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 1], L.y);
-            atomicAdd(&path_rgb[3 * static_cast<size_t>(out) + 2], L.z);
-        } else {
-            atomicAdd(&accum[out], make_float4(L.x, L.y, L.z, 0.0f));
+        if (push) {
+            uint32_t slot = base + __popc(mask & ((1u << lane) - 1u));
+            if (E8G_CHK(S.check, slot < W.capacity, kChkQueue, slot)) {
+                W.sh_o[slot] = make_float4(org.x, org.y, org.z, __uint_as_float(out));
+                W.sh_d[slot] = make_float4(dir.x, dir.y, dir.z, tmax);
+                W.sh_c[slot] = make_float4(L.x, L.y, L.z, 0.0f);
+            }
         }
     }
-    if (COUNT)
-        flush_counts(cnt, counters);
 }
 
 } // namespace
@@ -844,30 +1070,23 @@ __global__ void __launch_bounds__(kBlock) k_lt2(DevScene S, RenderArgs A, FirstH
     }
 }
 
-void bdpt_split_blocks_per_sm(int *walk, int *conn) {
-    *walk = *conn = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(walk, k_bdw_walk<RngPhilox, false>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(conn, k_bdw_connect<false>, kBlock, 0);
-    *walk = *walk > 0 ? *walk : 1;
-    *conn = *conn > 0 ? *conn : 1;
+int bdpt_eval_blocks_per_sm() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bdw_eval, kBlock, 0);
+    return n > 0 ? n : 1;
 }
 
-void launch_bdpt_split(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                       BdwChunk const &C, unsigned long long *work, int grid_walk, int grid_conn, cudaStream_t st,
-                       unsigned long long *counters) {
-    bool minstd = A.rng == E8G_RNG_MINSTD;
-    if (counters && minstd)
-        k_bdw_walk<RngMinstd, true><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, counters);
-    else if (counters)
-        k_bdw_walk<RngPhilox, true><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, counters);
-    else if (minstd)
-        k_bdw_walk<RngMinstd, false><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, nullptr);
+void launch_bdpt_walk(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float *path_rgb, BdwChunk const &C,
+                      WfSlots const &W, uint64_t const *range, int grid, cudaStream_t st) {
+    if (A.rng == E8G_RNG_MINSTD)
+        k_bdw_walk<RngMinstd><<<grid, 256, 0, st>>>(S, A, fh, path_rgb, C, W, range, wf_ext_count_ptr(W), wf_busy_ptr(W));
     else
-        k_bdw_walk<RngPhilox, false><<<grid_walk, kBlock, 0, st>>>(S, A, fh, path_rgb, C, work, nullptr);
-    if (counters)
-        k_bdw_connect<true><<<grid_conn, kBlock, 0, st>>>(S, accum, path_rgb, C, counters);
-    else
-        k_bdw_connect<false><<<grid_conn, kBlock, 0, st>>>(S, accum, path_rgb, C, nullptr);
+        k_bdw_walk<RngPhilox><<<grid, 256, 0, st>>>(S, A, fh, path_rgb, C, W, range, wf_ext_count_ptr(W), wf_busy_ptr(W));
+}
+
+void launch_bdpt_eval(DevScene const &S, float4 *accum, float *path_rgb, BdwChunk const &C, WfSlots const &Q, int grid,
+                      cudaStream_t st) {
+    k_bdw_eval<<<grid, kBlock, 0, st>>>(S, accum, path_rgb, C, Q, wf_shadow_count_ptr(Q));
 }
 
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,

@@ -87,14 +87,10 @@ struct BdwChunk {
     uint32_t count;
     uint64_t first;
 };
-// Bytes of a chunk's buffers per path.
+// Bytes of a chunk's buffers per path: subpaths, path records, connection entries and a shadow
+// ray (48 bytes) per entry.
 inline size_t bdw_bytes_per_path(uint32_t max_len) {
-    return static_cast<size_t>(max_len) * 6 * 16 + 32 + static_cast<size_t>(max_len) * (max_len + 1) * 4;
+    return static_cast<size_t>(max_len) * 6 * 16 + 32 + static_cast<size_t>(max_len) * (max_len + 1) * (4 + 48);
 }
-// Walk then connect one chunk; work: the walk kernel's path counter (zeroed before each chunk).
-void launch_bdpt_split(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,
-                       BdwChunk const &C, unsigned long long *work, int grid_walk, int grid_conn, cudaStream_t st,
-                       unsigned long long *counters = nullptr);
-void bdpt_split_blocks_per_sm(int *walk, int *conn);
 
 } // namespace e8g

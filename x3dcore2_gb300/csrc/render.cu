@@ -20,16 +20,17 @@ struct WfCounters { // mirrors the device Counters of wavefront.cu
     uint32_t shadow_n, ext_n, busy, pad[3];
 };
 
-// The split form of E8G_MODE_BDPT_POWER: paths in chunks whose subpaths and connection lists fit
-// in at most 2 GiB (fewer paths per chunk when the memory limit refuses that).
-e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb,
-                          unsigned long long *d_counts) {
+// The split form of E8G_MODE_BDPT_POWER: paths in chunks whose subpaths, connection lists and
+// shadow queue fit in at most 4 GiB (fewer paths per chunk when the memory limit refuses that).
+// Per chunk: the walk wavefront (a captured graph of two bounces, replayed until every slot is
+// idle and the chunk's paths are taken), then the connections and their shadow rays.
+e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb) {
     const uint32_t ml = std::min<uint32_t>(A.bdpt_max_len, 16);
     const size_t per_path = bdw_bytes_per_path(ml);
-    uint64_t chunk = std::min<uint64_t>({A.total_paths, kBdwMaxChunk, (size_t(2) << 30) / per_path});
+    uint64_t chunk = std::min<uint64_t>({A.total_paths, kBdwMaxChunk, (size_t(4) << 30) / per_path});
     chunk = std::max<uint64_t>(chunk, 1);
     // the chunk's arrays from base (sizes only when base is null), each 256-byte aligned
-    auto carve = [&](char *base, uint64_t n, size_t *bytes) {
+    auto carve = [&](char *base, uint64_t n, WfSlots *Q, uint64_t **range, size_t *bytes) {
         BdwChunk C{};
         size_t off = 0;
         auto take = [&](size_t sz) {
@@ -37,19 +38,29 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
             off += (sz + 255) & ~size_t(255);
             return r;
         };
+        const size_t entries = n * ml * (ml + 1);
         C.vtx = reinterpret_cast<float4 *>(take(n * ml * 6 * 16));
         C.info = reinterpret_cast<int4 *>(take(n * 16));
         C.o0 = reinterpret_cast<float4 *>(take(n * 16));
-        C.conn = reinterpret_cast<uint32_t *>(take(n * ml * (ml + 1) * 4));
+        C.conn = reinterpret_cast<uint32_t *>(take(entries * 4));
         C.conn_n = reinterpret_cast<uint32_t *>(take(16));
         C.max_len = ml;
+        *Q = WfSlots{};
+        Q->capacity = static_cast<uint32_t>(std::min<size_t>(entries, 0xFFFFFFFFu));
+        Q->sh_o = reinterpret_cast<float4 *>(take(entries * 16));
+        Q->sh_d = reinterpret_cast<float4 *>(take(entries * 16));
+        Q->sh_c = reinterpret_cast<float4 *>(take(entries * 16));
+        Q->counters = take(wf_counters_bytes());
+        *range = reinterpret_cast<uint64_t *>(take(16));
         *bytes = off;
         return C;
     };
     cudaError_t e = cudaErrorMemoryAllocation;
     size_t need = 0;
+    WfSlots Q{};
+    uint64_t *range = nullptr;
     while (true) {
-        carve(nullptr, chunk, &need);
+        carve(nullptr, chunk, &Q, &range, &need);
         e = c->b_bdw.reserve(need);
         if (e == cudaSuccess || chunk <= 4096)
             break;
@@ -58,32 +69,96 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
     }
     if (e != cudaSuccess)
         return cuda_fail(c, e, "bidirectional subpath buffers");
-    BdwChunk C = carve(static_cast<char *>(c->b_bdw.ptr), chunk, &need);
-    int bw = 1, bc = 1;
-    bdpt_split_blocks_per_sm(&bw, &bc);
-    const int grid_walk = persistent_grid(c, bw), grid_conn = persistent_grid(c, bc);
+    BdwChunk C = carve(static_cast<char *>(c->b_bdw.ptr), chunk, &Q, &range, &need);
+    // the walk's slots
+    const uint32_t slots = static_cast<uint32_t>(std::min<uint64_t>((chunk + 255) / 256 * 256, 1u << 21));
+    e = c->b_wf.reserve(wf_total_bytes(slots));
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "bidirectional walk slots");
+    WfSlots W = wf_carve(c->b_wf.ptr, slots);
+    const uint32_t threshold = c->dev.layout == 0 || c->dev.layout == 2 ? 16u : 0u;
+    const int grid_walk = static_cast<int>(std::min<uint64_t>((slots + 255) / 256, static_cast<uint64_t>(c->num_sms) * 8));
+    const int grid_eval = persistent_grid(c, bdpt_eval_blocks_per_sm());
+    const int grid_trace = persistent_grid(c, wf_trace_blocks_per_sm(c->dev.layout, threshold));
     auto const *fh = static_cast<FirstHit const *>(c->b_fh.ptr);
-    auto *work = static_cast<unsigned long long *>(c->b_work.ptr);
-    for (uint64_t first = 0; first < A.total_paths; first += chunk) {
-        if (take_cancel(c))
-            return fail(c, E8G_ERR_CANCELLED, "render cancelled");
+    constexpr uint32_t kBounces = 2;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "bidirectional walk capture");
+    for (uint32_t k = 0; k < kBounces; k++) {
+        wf_enqueue_reset(W, c->stream);
+        launch_bdpt_walk(c->dev, A, fh, path_rgb, C, W, range, grid_walk, c->stream);
+        wf_enqueue_trace(c->dev, A, W, nullptr, nullptr, grid_trace, threshold, c->stream);
+    }
+    e = cudaStreamEndCapture(c->stream, &graph);
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return cuda_fail(c, e, "bidirectional walk graph");
+    }
+    auto *host = static_cast<WfCounters *>(c->host_pinned);
+    auto *host_range = reinterpret_cast<uint64_t *>(static_cast<char *>(c->host_pinned) + 32);
+    // a path takes at most 2 max_len + 2 walk bounces; slots refill continuously
+    const uint64_t max_replays = ((chunk + slots - 1) / slots + 1) * (2 * ml + 4) / kBounces + 16;
+    bool cancelled = false, stuck = false;
+    for (uint64_t first = 0; first < A.total_paths && e == cudaSuccess; first += chunk) {
+        if (take_cancel(c)) {
+            cancelled = true;
+            break;
+        }
         C.first = first;
         C.count = static_cast<uint32_t>(std::min<uint64_t>(chunk, A.total_paths - first));
-        e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), c->stream);
+        host_range[0] = C.first;
+        host_range[1] = C.count;
+        e = cudaMemcpyAsync(range, host_range, 16, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = wf_init(W, c->stream);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(C.conn_n, 0, sizeof(uint32_t), c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(Q.counters, 0, wf_counters_bytes(), c->stream);
+        uint64_t r = 0;
+        for (; r < max_replays && e == cudaSuccess; r++) {
+            e = cudaGraphLaunch(exec, c->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(host, W.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(c->stream);
+            c->launches += 4 * kBounces;
+            if (e == cudaSuccess && host->busy == 0 && host->next_path >= C.count)
+                break;
+        }
         if (e != cudaSuccess)
-            return cuda_fail(c, e, "bidirectional chunk counters");
-        launch_bdpt_split(c->dev, A, fh, accum, path_rgb, C, work, grid_walk, grid_conn, c->stream, d_counts);
-        c->launches += 2;
+            break;
+        if (r == max_replays) {
+            stuck = true;
+            break;
+        }
+        launch_bdpt_eval(c->dev, accum, path_rgb, C, Q, grid_eval, c->stream);
+        wf_enqueue_trace(c->dev, A, Q, accum, path_rgb, grid_trace, threshold, c->stream);
+        c->launches += 3;
+        e = cudaGetLastError();
     }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "bidirectional split run");
+    if (cancelled)
+        return fail(c, E8G_ERR_CANCELLED, "render cancelled");
+    if (stuck)
+        return fail(c, E8G_ERR_INTERNAL, "bidirectional walk did not drain");
     return E8G_OK;
 }
 
 e8g_status run_integrator(e8g_ctx *c, e8g_render_params const *p, RenderArgs const &A, float4 *accum, float *path_rgb,
                           unsigned long long *d_counts) {
-    if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_BDPT_POWER)
-        return run_bdpt_split(c, A, accum, path_rgb, d_counts);
+    // the counted run traces the same rays one thread per path
+    if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_BDPT_POWER && !d_counts)
+        return run_bdpt_split(c, A, accum, path_rgb);
     if (p->integrator == E8G_INTEGRATOR_WAVEFRONT && p->mode == E8G_MODE_MIS && !d_counts)
         return c->wf_concurrent ? run_wavefront_concurrent(c, A, accum, path_rgb, c->wf_capacity, c->wf_bounces,
                                                            c->wf_threshold)

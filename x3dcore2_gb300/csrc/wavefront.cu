@@ -62,47 +62,6 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
-template <class R> struct RngSlot;
-template <> struct RngSlot<RngMinstd> {
-    __device__ static RngMinstd load(RenderArgs const &, uint32_t, uint32_t, uint32_t word) {
-        RngMinstd r;
-        r.x = word;
-        return r;
-    }
-    __device__ static uint32_t store(RngMinstd const &r) { return r.x; }
-    __device__ static RngMinstd fresh(RenderArgs const &, uint64_t mix, uint32_t px, uint32_t s) {
-        RngMinstd r;
-        r.seed(path_seed(mix, px, s));
-        return r;
-    }
-};
-template <> struct RngSlot<RngPhilox> {
-    // the slot keeps the number of draws taken; the 4-word block is regenerated on resume
-    __device__ static RngPhilox load(RenderArgs const &A, uint32_t px, uint32_t s, uint32_t drawn) {
-        RngPhilox r;
-        r.seed(A.seed, px, s);
-        r.block = drawn >> 2;
-        uint32_t skip = drawn & 3u;
-        if (skip) {
-            r.refill();
-            for (uint32_t k = 0; k < skip; k++) {
-                r.buf[0] = r.buf[1];
-                r.buf[1] = r.buf[2];
-                r.buf[2] = r.buf[3];
-            }
-            r.lane = skip;
-        }
-        return r;
-    }
-    __device__ static uint32_t store(RngPhilox const &r) { return r.lane == 4 ? r.block * 4 : (r.block - 1) * 4 + r.lane; }
-    __device__ static RngPhilox fresh(RenderArgs const &A, uint64_t, uint32_t px, uint32_t s) {
-        RngPhilox r;
-        r.seed(A.seed, px, s);
-        return r;
-    }
-};
-
-
 // The scene table of a many-scene wavefront: MULTI kernels look a path's scene and render
 // arguments up by its scene index; single-scene kernels use their parameters.
 template <bool MULTI>
@@ -776,6 +735,10 @@ cudaError_t wf_init(WfSlots const &W, cudaStream_t st) {
 
 // Busy slots after the last bounce (read back by the host between graph replays).
 uint32_t *wf_busy_ptr(WfSlots const &W) { return &reinterpret_cast<Counters *>(W.counters)->busy; }
+size_t wf_counters_bytes() { return sizeof(Counters); }
+uint32_t *wf_shadow_count_ptr(WfSlots const &W) { return &reinterpret_cast<Counters *>(W.counters)->shadow_n; }
+uint32_t *wf_ext_count_ptr(WfSlots const &W) { return &reinterpret_cast<Counters *>(W.counters)->ext_n; }
+void wf_enqueue_reset(WfSlots const &W, cudaStream_t st) { k_wf_reset<<<1, 1, 0, st>>>(reinterpret_cast<Counters *>(W.counters)); }
 unsigned long long *wf_next_ptr(WfSlots const &W) { return &reinterpret_cast<Counters *>(W.counters)->next_path; }
 
 } // namespace e8g
