@@ -537,39 +537,37 @@ __device__ __forceinline__ BV bdw_load(float4 const *src) {
     return v;
 }
 
-// One step of a subpath walk at stored vertex len-1 (the loop body of bdp_walk up to the trace):
+// One step of a subpath walk at its last vertex cur (the loop body of bdp_walk up to the trace):
 // samples the next direction; false when the walk ends there. On true: the ray, the throughput of
 // the vertex it will make, the sampling density and the reverse density at the current vertex.
 template <class R>
-__device__ __forceinline__ bool walk_sample(DevScene const &S, R &rng, float4 const *sub, uint32_t len, float3 wo,
-                                            float3 &org, float3 &dir, float3 &beta_next, float &pdf, float &prev_w) {
-    const BV cur = bdw_load(sub + 3 * (len - 1));
+__device__ __forceinline__ bool walk_sample(DevScene const &S, R &rng, BV const &cur, float3 wo, float3 &org,
+                                            float3 &dir, float3 &beta_next, float &pdf, float &prev_w) {
     const DevMaterial &m = vert_mat(S, cur.mesh);
-    float3 i = bsdf_sample_mis<true>(S, m, rng, pdf, cur.n, wo);
+    float3 i = bsdf_sample_mis<false>(S, m, rng, pdf, cur.n, wo);
     if (!(pdf > 0.0f))
         return false;
     float cw = dot(cur.n, i);
     if (cw <= 0.0f)
         return false;
-    float3 f = bsdf_eval<true>(S, m, cur.n, wo, i);
+    float3 f = bsdf_eval<false>(S, m, cur.n, wo, i);
     beta_next = mul(cur.beta, scale(f, cw / pdf));
-    prev_w = vpdf(S, cur, i, wo);
+    prev_w = bsdf_pdf<false>(S, m, cur.n, i, wo); // vpdf(cur, i, wo), the material's code inlined
     org = cur.p;
     dir = i;
     return true;
 }
 
-// The rest of the step once the ray's hit is known: stores vertex len and the reverse density of
-// vertex len-2; false when the walk ends (miss or back face).
-__device__ __forceinline__ bool walk_complete(DevScene const &S, float4 *sub, uint32_t len, Hit const &h, float3 dir,
-                                              float3 beta_next, float pdf, float prev_w) {
+// The rest of the step once the ray's hit is known: stores vertex len (also into nx) and the
+// reverse density of vertex len-2; false when the walk ends (miss or back face). cp: the ray's
+// origin, vertex len-1.
+__device__ __forceinline__ bool walk_complete(DevScene const &S, float4 *sub, uint32_t len, Hit const &h, float3 cp,
+                                              float3 dir, float3 beta_next, float pdf, float prev_w, BV &nx) {
     if (h.tri == 0xFFFFFFFFu)
         return false;
     Vert nv = make_vert(S, h);
     if (dot(nv.n, neg(dir)) <= 0.0f)
         return false;
-    const float3 cp = xyz(sub[3 * (len - 1)]);
-    BV nx;
     nx.p = nv.p;
     nx.n = nv.n;
     nx.mesh = nv.mesh;
@@ -613,7 +611,8 @@ __global__ void __launch_bounds__(256, 3)
         R rng;
         float3 wo = f3(0, 0, 0), org = f3(0, 0, 0), dir = f3(0, 0, 0), beta_next = f3(0, 0, 0);
         float pdf = 0.0f, prev_w = 0.0f;
-        bool at_vertex = false; // at stored vertex len-1 with the walk going on (else it ended)
+        bool at_vertex = false; // at stored vertex len-1 (cur) with the walk going on (else it ended)
+        BV cur{};
         if (stage != kWkEmpty) { // complete the pending ray
             path = W.sid[s];
             pixel = W.pixel[s];
@@ -627,7 +626,7 @@ __global__ void __launch_bounds__(256, 3)
             h.b1 = hv.z;
             h.b2 = hv.w;
             float4 *sub = C.vtx + static_cast<size_t>(path) * 6 * max_len + (stage == kWkLight ? 3 * max_len : 0);
-            if (walk_complete(S, sub, len, h, xyz(od), xyz(bp), bp.w, od.w)) {
+            if (walk_complete(S, sub, len, h, xyz(sub[3 * (len - 1)]), xyz(od), xyz(bp), bp.w, od.w, cur)) {
                 len++;
                 wo = neg(xyz(od));
                 at_vertex = true;
@@ -668,6 +667,7 @@ __global__ void __launch_bounds__(256, 3)
                             v0.fwd = 1.0f;
                             v0.rev = 0.0f;
                             bdw_store(C.vtx + static_cast<size_t>(path) * 6 * max_len, v0);
+                            cur = v0;
                             len = 1;
                             wo = o0;
                             at_vertex = true;
@@ -678,9 +678,7 @@ __global__ void __launch_bounds__(256, 3)
             // advance the lane's path until it waits for a ray or is finished
             bool done = false;
             for (int k = 0; k < 3 && !emitted && !done && stage != kWkEmpty; k++) {
-                float4 *sub = C.vtx + static_cast<size_t>(path) * 6 * max_len + (stage == kWkLight ? 3 * max_len : 0);
-                if (at_vertex && len < max_len &&
-                    walk_sample(S, rng, sub, len, wo, org, dir, beta_next, pdf, prev_w)) {
+                if (at_vertex && len < max_len && walk_sample(S, rng, cur, wo, org, dir, beta_next, pdf, prev_w)) {
                     emitted = true;
                     break;
                 }
@@ -754,7 +752,7 @@ __global__ void __launch_bounds__(256, 3)
                 for (uint32_t t = 1; t <= clen; t++) {
                     uint32_t sl0 = __ldg(&S.mesh_light[__float_as_int(cam[3 * (t - 1)].w)]) >= 0 ? 0u : 1u;
                     for (uint32_t sl = sl0; sl <= len; sl++)
-                        C.conn[pos++] = path << 10 | (t - 1) << 5 | sl;
+                        C.conn[pos++] = static_cast<uint64_t>(path) << 10 | (t - 1) << 5 | sl;
                 }
             }
             if (done) {
@@ -806,13 +804,13 @@ __device__ __forceinline__ float bdw_pdf(DevScene const &S, int32_t mesh, float3
 }
 
 __global__ void __launch_bounds__(kBlock) k_bdw_eval(DevScene S, float4 *accum, float *path_rgb, BdwChunk C,
-                                                     WfSlots W, uint32_t *shadow_n) {
-    const uint32_t n = *C.conn_n;
+                                                     WfSlots W, uint32_t *shadow_n, uint32_t first, uint32_t n) {
     const uint32_t maxlen = C.max_len;
     const uint32_t lane = lane_id();
     // warp-uniform loop: every lane reaches the shadow-queue append
     for (uint32_t q0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); q0 < n; q0 += gridDim.x * blockDim.x) {
         const uint32_t q = q0 + lane;
+        const uint32_t entry = first + q;
         bool push = false;
         float3 org = f3(0, 0, 0), dir = f3(0, 0, 0), L = f3(0, 0, 0);
         float tmax = 0.0f;
@@ -820,8 +818,9 @@ __global__ void __launch_bounds__(kBlock) k_bdw_eval(DevScene S, float4 *accum, 
         do {
             if (q >= n)
                 break;
-            const uint32_t e = C.conn[q];
-            const uint32_t path = e >> 10, t = ((e >> 5) & 31u) + 1u, sl = e & 31u;
+            const uint64_t e = C.conn[entry];
+            const uint32_t path = static_cast<uint32_t>(e >> 10), t = ((e >> 5) & 31u) + 1u,
+                           sl = static_cast<uint32_t>(e & 31u);
             const int4 inf = C.info[path];
             out = static_cast<uint32_t>(inf.z);
             float4 const *cam = C.vtx + static_cast<size_t>(path) * 6 * maxlen;
@@ -1084,9 +1083,9 @@ void launch_bdpt_walk(DevScene const &S, RenderArgs const &A, FirstHit const *fh
         k_bdw_walk<RngPhilox><<<grid, 256, 0, st>>>(S, A, fh, path_rgb, C, W, range, wf_ext_count_ptr(W), wf_busy_ptr(W));
 }
 
-void launch_bdpt_eval(DevScene const &S, float4 *accum, float *path_rgb, BdwChunk const &C, WfSlots const &Q, int grid,
-                      cudaStream_t st) {
-    k_bdw_eval<<<grid, kBlock, 0, st>>>(S, accum, path_rgb, C, Q, wf_shadow_count_ptr(Q));
+void launch_bdpt_eval(DevScene const &S, float4 *accum, float *path_rgb, BdwChunk const &C, WfSlots const &Q,
+                      uint32_t first, uint32_t n, int grid, cudaStream_t st) {
+    k_bdw_eval<<<grid, kBlock, 0, st>>>(S, accum, path_rgb, C, Q, wf_shadow_count_ptr(Q), first, n);
 }
 
 void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float4 *accum, float *path_rgb,

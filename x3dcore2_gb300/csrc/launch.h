@@ -74,23 +74,17 @@ void launch_bdpt(DevScene const &S, RenderArgs const &A, FirstHit const *fh, flo
 int bdpt_blocks_per_sm();
 
 // The split form of E8G_MODE_BDPT_POWER (E8G_INTEGRATOR_WAVEFRONT): a chunk of `count` paths
-// starting at path index `first`; its buffers are sized for at most kBdwMaxChunk paths and
-// max_len-vertex subpaths.
-constexpr uint32_t kBdwMaxChunk = 1u << 22; // connection entries keep the path in 22 bits
+// starting at path index `first` (at most kBdwMaxChunk), subpaths of at most max_len vertices.
+constexpr uint32_t kBdwMaxChunk = 1u << 26; // keeps a chunk's connection count within 32 bits
 struct BdwChunk {
     float4 *vtx;      // per path: max_len camera then max_len light vertices, three float4 each
     int4 *info;       // per path: (clen | llen << 8, light, output index, 0)
     float4 *o0;       // per path: the direction back along the camera ray
-    uint32_t *conn;   // connection entries: path << 10 | (t - 1) << 5 | s
+    uint64_t *conn;   // connection entries: path << 10 | (t - 1) << 5 | s
     uint32_t *conn_n; // entry count (zeroed before each chunk)
     uint32_t max_len;
     uint32_t count;
     uint64_t first;
 };
-// Bytes of a chunk's buffers per path: subpaths, path records, connection entries and a shadow
-// ray (48 bytes) per entry.
-inline size_t bdw_bytes_per_path(uint32_t max_len) {
-    return static_cast<size_t>(max_len) * 6 * 16 + 32 + static_cast<size_t>(max_len) * (max_len + 1) * (4 + 48);
-}
 
 } // namespace e8g

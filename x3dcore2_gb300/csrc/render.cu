@@ -20,16 +20,18 @@ struct WfCounters { // mirrors the device Counters of wavefront.cu
     uint32_t shadow_n, ext_n, busy, pad[3];
 };
 
-// The split form of E8G_MODE_BDPT_POWER: paths in chunks whose subpaths, connection lists and
-// shadow queue fit in at most 4 GiB (fewer paths per chunk when the memory limit refuses that).
-// Per chunk: the walk wavefront (a captured graph of two bounces, replayed until every slot is
-// idle and the chunk's paths are taken), then the connections and their shadow rays.
+// The split form of E8G_MODE_BDPT_POWER. Paths go in chunks (at most 2^26, and at most 16 GiB or
+// half the free device memory for subpaths, connection lists and shadow queue; fewer when the
+// memory limit refuses that). Per
+// chunk: the walk wavefront (a captured graph of two bounces, replayed until every slot is idle
+// and the chunk's paths are taken), then the connection list in pieces of at most the shadow
+// queue's length: evaluation, then the queue's shadow rays.
 e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float *path_rgb) {
     const uint32_t ml = std::min<uint32_t>(A.bdpt_max_len, 16);
-    const size_t per_path = bdw_bytes_per_path(ml);
-    uint64_t chunk = std::min<uint64_t>({A.total_paths, kBdwMaxChunk, (size_t(4) << 30) / per_path});
+    uint64_t chunk = std::min<uint64_t>({A.total_paths, kBdwMaxChunk});
     chunk = std::max<uint64_t>(chunk, 1);
-    // the chunk's arrays from base (sizes only when base is null), each 256-byte aligned
+    // the chunk's arrays from base (sizes only when base is null), each 256-byte aligned; the
+    // shadow queue holds every entry of a chunk of up to 2^24 entries, 2^24 beyond
     auto carve = [&](char *base, uint64_t n, WfSlots *Q, uint64_t **range, size_t *bytes) {
         BdwChunk C{};
         size_t off = 0;
@@ -39,29 +41,36 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
             return r;
         };
         const size_t entries = n * ml * (ml + 1);
+        const size_t qlen = std::max<size_t>(std::min<size_t>(entries, size_t(1) << 24), 1);
         C.vtx = reinterpret_cast<float4 *>(take(n * ml * 6 * 16));
         C.info = reinterpret_cast<int4 *>(take(n * 16));
         C.o0 = reinterpret_cast<float4 *>(take(n * 16));
-        C.conn = reinterpret_cast<uint32_t *>(take(entries * 4));
+        C.conn = reinterpret_cast<uint64_t *>(take(entries * 8));
         C.conn_n = reinterpret_cast<uint32_t *>(take(16));
         C.max_len = ml;
         *Q = WfSlots{};
-        Q->capacity = static_cast<uint32_t>(std::min<size_t>(entries, 0xFFFFFFFFu));
-        Q->sh_o = reinterpret_cast<float4 *>(take(entries * 16));
-        Q->sh_d = reinterpret_cast<float4 *>(take(entries * 16));
-        Q->sh_c = reinterpret_cast<float4 *>(take(entries * 16));
+        Q->capacity = static_cast<uint32_t>(qlen);
+        Q->sh_o = reinterpret_cast<float4 *>(take(qlen * 16));
+        Q->sh_d = reinterpret_cast<float4 *>(take(qlen * 16));
+        Q->sh_c = reinterpret_cast<float4 *>(take(qlen * 16));
         Q->counters = take(wf_counters_bytes());
         *range = reinterpret_cast<uint64_t *>(take(16));
         *bytes = off;
         return C;
     };
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = size_t(8) << 30;
+    }
+    const size_t budget = std::min<size_t>(size_t(16) << 30, (free_b + c->b_bdw.bytes) / 2);
     cudaError_t e = cudaErrorMemoryAllocation;
     size_t need = 0;
     WfSlots Q{};
     uint64_t *range = nullptr;
     while (true) {
         carve(nullptr, chunk, &Q, &range, &need);
-        e = c->b_bdw.reserve(need);
+        e = need <= budget || chunk <= 4096 ? c->b_bdw.reserve(need) : cudaErrorMemoryAllocation;
         if (e == cudaSuccess || chunk <= 4096)
             break;
         cudaGetLastError();
@@ -71,7 +80,7 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
         return cuda_fail(c, e, "bidirectional subpath buffers");
     BdwChunk C = carve(static_cast<char *>(c->b_bdw.ptr), chunk, &Q, &range, &need);
     // the walk's slots
-    const uint32_t slots = static_cast<uint32_t>(std::min<uint64_t>((chunk + 255) / 256 * 256, 1u << 21));
+    const uint32_t slots = static_cast<uint32_t>(std::min<uint64_t>((chunk + 255) / 256 * 256, 1u << 23));
     e = c->b_wf.reserve(wf_total_bytes(slots));
     if (e != cudaSuccess)
         return cuda_fail(c, e, "bidirectional walk slots");
@@ -102,6 +111,7 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
     }
     auto *host = static_cast<WfCounters *>(c->host_pinned);
     auto *host_range = reinterpret_cast<uint64_t *>(static_cast<char *>(c->host_pinned) + 32);
+    auto *host_conn = reinterpret_cast<uint32_t *>(static_cast<char *>(c->host_pinned) + 48);
     // a path takes at most 2 max_len + 2 walk bounces; slots refill continuously
     const uint64_t max_replays = ((chunk + slots - 1) / slots + 1) * (2 * ml + 4) / kBounces + 16;
     bool cancelled = false, stuck = false;
@@ -119,13 +129,13 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
             e = wf_init(W, c->stream);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(C.conn_n, 0, sizeof(uint32_t), c->stream);
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(Q.counters, 0, wf_counters_bytes(), c->stream);
         uint64_t r = 0;
         for (; r < max_replays && e == cudaSuccess; r++) {
             e = cudaGraphLaunch(exec, c->stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(host, W.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(host_conn, C.conn_n, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
             if (e == cudaSuccess)
                 e = cudaStreamSynchronize(c->stream);
             c->launches += 4 * kBounces;
@@ -138,10 +148,17 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
             stuck = true;
             break;
         }
-        launch_bdpt_eval(c->dev, accum, path_rgb, C, Q, grid_eval, c->stream);
-        wf_enqueue_trace(c->dev, A, Q, accum, path_rgb, grid_trace, threshold, c->stream);
-        c->launches += 3;
-        e = cudaGetLastError();
+        const uint32_t n_conn = *host_conn;
+        for (uint32_t q0 = 0; q0 < n_conn && e == cudaSuccess; q0 += Q.capacity) {
+            const uint32_t n = std::min<uint32_t>(Q.capacity, n_conn - q0);
+            e = cudaMemsetAsync(Q.counters, 0, wf_counters_bytes(), c->stream);
+            if (e != cudaSuccess)
+                break;
+            launch_bdpt_eval(c->dev, accum, path_rgb, C, Q, q0, n, grid_eval, c->stream);
+            wf_enqueue_trace(c->dev, A, Q, accum, path_rgb, grid_trace, threshold, c->stream);
+            c->launches += 3;
+            e = cudaGetLastError();
+        }
     }
     cudaGraphExecDestroy(exec);
     cudaGraphDestroy(graph);

@@ -89,13 +89,13 @@ void wf_enqueue_reset(WfSlots const &W, cudaStream_t st);
 // The split form of E8G_MODE_BDPT_POWER (bdpt.cu). The walk: one bounce over the slots of W
 // (advance every slot's path by one subpath vertex, refill finished slots from the chunk), whose
 // extension queue wf_enqueue_trace then traces; range: the chunk's first path index and path
-// count in device memory. The connections: one thread per entry of the chunk's list into the
-// shadow queue of Q (its counters zeroed beforehand, sh_* arrays sized for every entry), which
-// wf_enqueue_trace then drains.
+// count in device memory. The connections: one thread per entry [first, first + n) of the chunk's
+// list into the shadow queue of Q (its counters zeroed beforehand, sh_* arrays sized for n
+// entries), which wf_enqueue_trace then drains.
 void launch_bdpt_walk(DevScene const &S, RenderArgs const &A, FirstHit const *fh, float *path_rgb, BdwChunk const &C,
                       WfSlots const &W, uint64_t const *range, int grid, cudaStream_t st);
-void launch_bdpt_eval(DevScene const &S, float4 *accum, float *path_rgb, BdwChunk const &C, WfSlots const &Q, int grid,
-                      cudaStream_t st);
+void launch_bdpt_eval(DevScene const &S, float4 *accum, float *path_rgb, BdwChunk const &C, WfSlots const &Q,
+                      uint32_t first, uint32_t n, int grid, cudaStream_t st);
 int bdpt_eval_blocks_per_sm();
 unsigned long long *wf_next_ptr(WfSlots const &W);
 // The two halves of a bounce, for pools that interleave on two streams (concurrent wavefront):
