@@ -343,7 +343,7 @@ def cornell_leg(ctx, threads, cpu_budget_s=6.0):
     return out
 
 
-def bdpt_leg(ctx):
+def bdpt_leg(ctx, w=1280, h=720, spp=32):
     """Bidirectional MIS on the benchmark scene (still uploaded) at 1280x720, subpaths of at most 6
     vertices, 32 spp: power-heuristic weights (E8G_MODE_BDPT_POWER) one thread per path
     (`power`) and in the split form (`power_split`: a subpath kernel and a connection kernel per
@@ -356,13 +356,13 @@ def bdpt_leg(ctx):
     peak, _ = read_peaks()
     st = ctx.bvh_stats()
     node_bytes = st["node_bytes"] // max(st["num_nodes"], 1)
-    out = {"width": 1280, "height": 720, "spp": 32, "max_subpath": 6, "node_bytes": node_bytes,
+    out = {"width": w, "height": h, "spp": spp, "max_subpath": 6, "node_bytes": node_bytes,
            "tree": {0: "sah", 1: "reference", 2: "wide", 3: "linear"}.get(st.get("layout", -1), "?")}
     for name, mode, kern, integ in (("power", abi.MODE_BDPT_POWER, "k_bdpt_power", abi.INTEGRATOR_MEGAKERNEL),
                                     ("power_split", abi.MODE_BDPT_POWER, "k_bdw_walk + k_bdw_eval + trace kernels",
                                      abi.INTEGRATOR_WAVEFRONT),
                                     ("uniform", abi.MODE_REF_BDPT, "k_bdpt_ref", abi.INTEGRATOR_MEGAKERNEL)):
-        p = default_params(mode, 1280, 720, 32, seed=1, bdpt_max_len=6)
+        p = default_params(mode, w, h, spp, seed=1, bdpt_max_len=6)
         p.integrator = integ
         ctx.render(p)
         ms = []
@@ -372,7 +372,7 @@ def bdpt_leg(ctx):
         kms = statistics.mean(ms)
         c = ctx.count_traversal(p)
         alg = node_bytes * c["nodes"] + 48 * c["tris"]
-        out[name] = {"kernel_ms": kms, "paths_per_s": 1280 * 720 * 32 / (kms / 1000.0),
+        out[name] = {"kernel_ms": kms, "paths_per_s": w * h * spp / (kms / 1000.0),
                      "roofline": {"kernel": kern, "rays": c["rays"], "nodes": c["nodes"], "tris": c["tris"],
                                   "algorithmic_bytes": alg, "achieved_gbs": alg / (kms / 1e3) / 1e9,
                                   "frac": alg / (kms / 1e3) / 1e9 / peak}}
@@ -629,7 +629,8 @@ def run_leg(args):
     scene, _, _, _ = make_scene(args.small)
     LAYOUTS = {"sah": abi.BVH_SAH, "wide": abi.BVH_WIDE, "reference": abi.BVH_REFERENCE}
     ctx.upload(scene, layout=LAYOUTS[args.layout] if args.layout else abi.BVH_SAH)
-    fn = {"bdpt": lambda: bdpt_leg(ctx), "batch": lambda: batch_leg(ctx), "adjoint": lambda: adjoint_leg(ctx),
+    bw, bh = (int(x) for x in args.res.lower().split("x")) if args.res else (1280, 720)
+    fn = {"bdpt": lambda: bdpt_leg(ctx, bw, bh, args.spp or 32), "batch": lambda: batch_leg(ctx), "adjoint": lambda: adjoint_leg(ctx),
           "update": lambda: update_leg(ctx, scene), "adjoint_fd": lambda: adjoint_fd_leg(ctx),
           "cornell": lambda: cornell_leg(ctx, os.cpu_count() or 1)}[args.leg]
     print(json.dumps({"leg": args.leg, **fn()}))
@@ -829,9 +830,12 @@ def main():
     pc = default_params(abi.MODE_MIS, w, h, spp, seed=1, max_depth=8, rr_start=3, rr_prob=0.5)
     counts = ctx.count_traversal(pc)
 
-    # end to end through the public call: host buffer, image read back every step
+    # end to end through the public call: host buffer, image read back every step (two untimed
+    # calls first: the calls before them rendered other configurations)
     e2e_ms = []
-    for k in range(0 if args.no_e2e else max(2, min(args.steps, 3))):
+    for k in range(0 if args.no_e2e else 2):
+        abi.check(lib.e8g_render(ctx.h, C.byref(p), C.c_void_p(h_img.data_ptr())), ctx.h, "e8g_render")
+    for k in range(0 if args.no_e2e else max(3, min(args.steps, 5))):
         barrier()
         t = time.perf_counter()
         abi.check(lib.e8g_render(ctx.h, C.byref(p), C.c_void_p(h_img.data_ptr())), ctx.h, "e8g_render")

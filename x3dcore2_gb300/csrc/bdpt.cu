@@ -544,15 +544,15 @@ template <class R>
 __device__ __forceinline__ bool walk_sample(DevScene const &S, R &rng, BV const &cur, float3 wo, float3 &org,
                                             float3 &dir, float3 &beta_next, float &pdf, float &prev_w) {
     const DevMaterial &m = vert_mat(S, cur.mesh);
-    float3 i = bsdf_sample_mis<false>(S, m, rng, pdf, cur.n, wo);
+    float3 i = bsdf_sample_mis<true>(S, m, rng, pdf, cur.n, wo);
     if (!(pdf > 0.0f))
         return false;
     float cw = dot(cur.n, i);
     if (cw <= 0.0f)
         return false;
-    float3 f = bsdf_eval<false>(S, m, cur.n, wo, i);
+    float3 f = bsdf_eval<true>(S, m, cur.n, wo, i);
     beta_next = mul(cur.beta, scale(f, cw / pdf));
-    prev_w = bsdf_pdf<false>(S, m, cur.n, i, wo); // vpdf(cur, i, wo), the material's code inlined
+    prev_w = bsdf_pdf<true>(S, m, cur.n, i, wo); // vpdf(cur, i, wo)
     org = cur.p;
     dir = i;
     return true;
@@ -588,12 +588,15 @@ __device__ __forceinline__ bool walk_complete(DevScene const &S, float4 *sub, ui
 enum : uint32_t { kWkEmpty = 0, kWkCam = 1, kWkLight = 2 };
 constexpr int kWalkRounds = 4; // paths a slot may start and finish without a ray in one bounce
 
+// The materials' code is out of line and the kernel held to 64 registers (four blocks of 256 per
+// SM): the walk stalled on instruction fetch with it inlined, and at three blocks per SM (80
+// registers, no spills) it took 52.1 ms per 1280x720, 32-spp frame against 47.6 ms at four.
 // One bounce of the walk over every slot. range: the chunk's first path index and path count
 // (device memory, so one captured graph serves every chunk). W.next_path: the chunk's path
 // counter; W.sid: the slot's path (index in the chunk), W.out: its light, W.beta_pdf: throughput
 // of the pending vertex | sampling density, W.o: ray direction | reverse density.
 template <class R>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
     k_bdw_walk(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh, float *path_rgb, BdwChunk C, WfSlots W,
                uint64_t const *range, uint32_t *ext_n, uint32_t *busy) {
     const uint64_t mix = splitmix64(A.seed);
@@ -632,7 +635,9 @@ __global__ void __launch_bounds__(256, 3)
                 at_vertex = true;
             }
         }
-        bool emitted = false, paths_left = true;
+        // once the chunk's path counter has passed its last path (it only grows), no slot takes a
+        // path for the rest of the chunk: the tail bounces skip the refill atomics
+        bool emitted = false, paths_left = __ldcg(W.next_path) < count;
         for (int round = 0; round < kWalkRounds; round++) {
             // a new path for every empty slot, one atomic per warp
             bool want = in && stage == kWkEmpty && paths_left;
