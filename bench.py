@@ -47,11 +47,13 @@ REF_ESTIMATOR = dict(name="unidirect_lt1 (the reference's direct-lighting tracer
 REF_SAMPLE_W, REF_SAMPLE_H = 480, 270
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures summarised in
 # profiles/, one kernel per capture. Eight-wide tree + wavefront: one steady-state launch of each
-# wavefront kernel in the benchmark's own configuration (2^23 slots, 2 bounces per graph,
-# threshold 12; profiles/wavefront_wide_icosphere_l8.md): "kernel" is the trace kernel's bytes
-# per launch, "shade" the shading kernel's. SAH pairs + megakernel: one 480x270, 8-spp launch of
-# k_mega, 217.1 B per path (profiles/megakernel_icosphere_l8.md), scaled by the frame's paths.
-TRAFFIC = {("wide", "wavefront"): {"kernel_per_launch": 1.938e9, "shade_per_launch": 2.244e9},
+# wavefront kernel in the benchmark's own tuned configuration (2^24 slots, 2 bounces per graph,
+# threshold 8, shading shape 6; profiles/wavefront_headline_launches_icosphere_l8.md and
+# profiles/wavefront_wide_icosphere_l8.md): "kernel" is the trace kernel's bytes per launch,
+# "shade" the shading phase's (completion kernel + shading kernel) per bounce. SAH pairs +
+# megakernel: one 480x270, 8-spp launch of k_mega, 217.1 B per path
+# (profiles/megakernel_icosphere_l8.md), scaled by the frame's paths.
+TRAFFIC = {("wide", "wavefront"): {"kernel_per_launch": 3.822e9, "shade_per_launch": 5.76e9},
            ("sah", "megakernel"): {"kernel_per_path": 217.1}}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
 
@@ -701,7 +703,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the quality, BDPT, batch and adjoint legs")
     ap.add_argument("--no-tune", action="store_true", help="wavefront with the library defaults (profiling)")
     ap.add_argument("--wf-config", default=None,
-                    help="CAPACITY,BOUNCES,THRESHOLD: a fixed wavefront configuration instead of tuning (profiling)")
+                    help="CAPACITY,BOUNCES,THRESHOLD[,SHADE]: a fixed wavefront configuration (and shading "
+                         "shape) instead of tuning (profiling)")
     ap.add_argument("--leg", default=None, choices=["bdpt", "batch", "adjoint", "adjoint_fd", "update", "obj", "cornell"],
                     help="run one extra leg alone on the benchmark scene and print its JSON (not a bench line)")
     args = ap.parse_args()
@@ -774,8 +777,10 @@ def main():
         trees[lay] = {"nodes": st["num_nodes"], "node_bytes": st["node_bytes"], "depth": st["max_depth"],
                       "build_s": round(commit_s, 3)}
         if "wavefront" in integrators and args.wf_config:
-            cap, bn, th = (int(x) for x in args.wf_config.split(","))
-            abi.check(lib.e8g_wavefront_set(ctx.h, cap, bn, th), ctx.h, "e8g_wavefront_set")
+            cfg = [int(x) for x in args.wf_config.split(",")]
+            abi.check(lib.e8g_wavefront_set(ctx.h, cfg[0], cfg[1], cfg[2]), ctx.h, "e8g_wavefront_set")
+            if len(cfg) > 3:
+                abi.check(lib.e8g_wavefront_set_shade(ctx.h, cfg[3]), ctx.h, "e8g_wavefront_set_shade")
         elif "wavefront" in integrators and not args.no_tune:
             tunes[lay] = tune_wavefront()
         for integ in integrators:
