@@ -143,7 +143,7 @@ def test_wavefront_paths_match_oracle(ctx, rng, layout):
 
 @pytest.mark.parametrize("integ", [abi.INTEGRATOR_MEGAKERNEL, abi.INTEGRATOR_WAVEFRONT])
 @pytest.mark.parametrize("rng", [abi.RNG_PHILOX, abi.RNG_MINSTD])
-@pytest.mark.parametrize("max_len", [6, 3])
+@pytest.mark.parametrize("max_len", [6, 3, 1, 16])
 def test_bdpt_power_paths_match_oracle(ctx, rng, max_len, integ):
     """Bidirectional with power-heuristic MIS (product mode): per-path radiance equals the
     oracle's restatement fed the same stream, one thread per path and in the split form (every
