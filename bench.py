@@ -47,13 +47,14 @@ REF_ESTIMATOR = dict(name="unidirect_lt1 (the reference's direct-lighting tracer
 REF_SAMPLE_W, REF_SAMPLE_H = 480, 270
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures summarised in
 # profiles/, one kernel per capture. Eight-wide tree + wavefront: one steady-state launch of each
-# wavefront kernel in the benchmark's own tuned configuration (2^24 slots, 2 bounces per graph,
+# wavefront kernel in a tuned configuration of the benchmark (2^24 slots, 2 bounces per graph,
 # threshold 8, shading shape 6; profiles/wavefront_headline_launches_icosphere_l8.md and
-# profiles/wavefront_wide_icosphere_l8.md): "kernel" is the trace kernel's bytes per launch,
-# "shade" the shading phase's (completion kernel + shading kernel) per bounce. SAH pairs +
-# megakernel: one 480x270, 8-spp launch of k_mega, 217.1 B per path
-# (profiles/megakernel_icosphere_l8.md), scaled by the frame's paths.
-TRAFFIC = {("wide", "wavefront"): {"kernel_per_launch": 3.822e9, "shade_per_launch": 5.76e9},
+# profiles/wavefront_wide_icosphere_l8.md): 3.822 GB per trace launch and 5.76 GB per shading
+# phase (completion kernel + shading kernel) at 16 launches for the frame's 192.3 M rays, kept as
+# bytes per ray of the frame (318.0 and 479.2) and scaled to the run's own rays per launch, since
+# the tuner may pick another slot pool. SAH pairs + megakernel: one 480x270, 8-spp launch of
+# k_mega, 217.1 B per path (profiles/megakernel_icosphere_l8.md), scaled by the frame's paths.
+TRAFFIC = {("wide", "wavefront"): {"kernel_per_ray": 318.0, "shade_per_ray": 479.2},
            ("sah", "megakernel"): {"kernel_per_path": 217.1}}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
 
@@ -866,8 +867,10 @@ def main():
         dom_name = {"plain": "k_plain (baseline per-path kernel)", "megakernel": "k_mega (megakernel)"}[best_integ]
     achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
     achieved_loop = alg_bytes / (loop_ms / 1000.0) / 1e9
-    if "kernel_per_launch" in tr:
-        traffic = tr["kernel_per_launch"]
+    shade_traffic = None
+    if "kernel_per_ray" in tr:
+        traffic = tr["kernel_per_ray"] * counts["rays"] / dom_launches
+        shade_traffic = tr["shade_per_ray"] * counts["rays"] / dom_launches
     elif "kernel_per_path" in tr:
         traffic = tr["kernel_per_path"] * paths_per_step / dom_launches
     else:
@@ -898,12 +901,13 @@ def main():
                      "l2_peak": l2_peak, "frac_l2": achieved / l2_peak if l2_peak else None,
                      "node_bytes": node_bytes, "algorithmic_bytes_per_step": alg_bytes, "rays": counts["rays"],
                      "nodes": counts["nodes"], "tris": counts["tris"],
-                     "traffic_note": "DRAM bytes of one steady-state launch of this kernel in this configuration, "
-                                     "from the ncu capture summarised in profiles/ (one kernel, three launches)"},
+                     "traffic_note": "DRAM bytes per launch of this kernel: the DRAM bytes per ray of steady-state "
+                                     "launches captured with ncu in a tuned configuration (profiles/, one kernel, three "
+                                     "launches) times this run's rays per launch"},
         "roofline_loop": {"achieved": achieved_loop, "unit": "GB/s", "frac": achieved_loop / peak,
                           "frac_l2": achieved_loop / l2_peak if l2_peak else None, "loop_ms_per_step": loop_ms,
                           "trace_ms_per_step": rb.get("trace_ms"), "shade_ms_per_step": rb.get("shade_ms"),
-                          "shade_traffic_per_launch": tr.get("shade_per_launch"),
+                          "shade_traffic_per_launch": shade_traffic,
                           "note": "the same algorithmic bytes over the integrator's whole device time per frame "
                                   "(shading included)"},
         "gpu_launches": launches,
