@@ -409,6 +409,7 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
     bool exhausted = false;  // the same in every lane: the queue and the warp's reserve are empty
     uint32_t wb = 0, we = 0; // the warp's reserved entries [wb, we)
     bool gdrained = false;
+    uint32_t qw = 0; // the lane's ray's output (shadow) or slot (extension), kept from the refill
     TravState T;
     WideTrav TW;
     while (true) {
@@ -454,10 +455,13 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
                         ro = xyz(so);
                         rd = xyz(sd);
                         tmax = sd.w;
+                        qw = __float_as_uint(so.w);
                     } else {
-                        ro = xyz(W.ext_o[q]);
+                        float4 eo = W.ext_o[q];
+                        ro = xyz(eo);
                         rd = xyz(W.ext_d[q]);
                         tmax = 1000.0f;
+                        qw = __float_as_uint(eo.w);
                     }
                     if (WIDE)
                         wide_begin(TW, ro, rd, 1e-4f, tmax, ANY);
@@ -479,10 +483,10 @@ __global__ void __launch_bounds__(kBlock, WIDE ? kWfWideBlocks : 1)
             if (ANY) {
                 bool occluded = WIDE ? TW.h.tri != 0xFFFFFFFFu : T.found;
                 if (!occluded)
-                    emit_to(A, accum, path_rgb, __float_as_uint(W.sh_o[q].w), xyz(W.sh_c[q]));
+                    emit_to(A, accum, path_rgb, qw, xyz(W.sh_c[q]));
             } else {
                 Hit b = WIDE ? TW.h : T.best;
-                W.hit[__float_as_uint(W.ext_o[q].w)] = make_float4(b.t, __uint_as_float(b.tri), b.b1, b.b2);
+                W.hit[qw] = make_float4(b.t, __uint_as_float(b.tri), b.b1, b.b2);
             }
             q = kNone;
         }
