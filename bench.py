@@ -48,12 +48,12 @@ REF_SAMPLE_W, REF_SAMPLE_H = 480, 270
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures summarised in
 # profiles/, one kernel per capture. Eight-wide tree + wavefront: one steady-state launch of each
 # wavefront kernel in a tuned configuration of the benchmark (2^24 slots, 2 bounces per graph,
-# threshold 8, shading shape 6; profiles/wavefront_headline_launches_icosphere_l8.md and
-# profiles/wavefront_wide_icosphere_l8.md): 3.822 GB per trace launch and 5.76 GB per shading
-# phase (completion kernel + shading kernel) at 16 launches for the frame's 192.3 M rays, kept as
-# bytes per ray of the frame (318.0 and 479.2) and scaled to the run's own rays per launch, since
-# the tuner may pick another slot pool. SAH pairs + megakernel: one 480x270, 8-spp launch of
-# k_mega, 217.1 B per path (profiles/megakernel_icosphere_l8.md), scaled by the frame's paths.
+# threshold 8, shading shape 6; the headline launch list and the wavefront kernels' summaries
+# under profiles/): 3.822 GB per trace launch and 5.76 GB per shading phase (completion kernel +
+# shading kernel) at 16 launches for the frame's 192.3 M rays, kept as bytes per ray of the frame
+# (318.0 and 479.2) and scaled to the run's own rays per launch, since the tuner may pick another
+# slot pool. SAH pairs + megakernel: one 480x270, 8-spp launch of k_mega, 217.1 B per path (the
+# megakernel's summary under profiles/), scaled by the frame's paths.
 TRAFFIC = {("wide", "wavefront"): {"kernel_per_ray": 318.0, "shade_per_ray": 479.2},
            ("sah", "megakernel"): {"kernel_per_path": 217.1}}
 INTEGRATORS = {"megakernel": 0, "wavefront": 1, "plain": 2}  # E8G_INTEGRATOR_*
