@@ -86,7 +86,9 @@ e8g_status run_bdpt_split(e8g_ctx *c, RenderArgs const &A, float4 *accum, float 
     if (e != cudaSuccess)
         return cuda_fail(c, e, "bidirectional walk slots");
     WfSlots W = wf_carve(c->b_wf.ptr, slots);
-    const uint32_t threshold = c->dev.layout == 0 || c->dev.layout == 2 ? 16u : 0u;
+    // refill threshold of the trace kernels (threshold 8 against 16: 42.3 against 43.0 ms per
+    // 1280x720, 32-spp frame)
+    const uint32_t threshold = c->dev.layout == 0 || c->dev.layout == 2 ? 8u : 0u;
     const int grid_walk = static_cast<int>(std::min<uint64_t>((slots + 255) / 256, static_cast<uint64_t>(c->num_sms) * 8));
     const int grid_eval = persistent_grid(c, bdpt_eval_blocks_per_sm());
     const int grid_trace = persistent_grid(c, wf_trace_blocks_per_sm(c->dev.layout, threshold));
