@@ -588,13 +588,13 @@ __device__ __forceinline__ bool walk_complete(DevScene const &S, float4 *sub, ui
 enum : uint32_t { kWkEmpty = 0, kWkCam = 1, kWkLight = 2 };
 constexpr int kWalkRounds = 4; // paths a slot may start and finish without a ray in one bounce
 
-// The materials' code is out of line and the kernel held to 64 registers (four blocks of 256 per
-// SM): the walk stalled on instruction fetch with it inlined, and at three blocks per SM (80
-// registers, no spills) it took 52.1 ms per 1280x720, 32-spp frame against 47.6 ms at four.
 // One bounce of the walk over every slot. range: the chunk's first path index and path count
 // (device memory, so one captured graph serves every chunk). W.next_path: the chunk's path
 // counter; W.sid: the slot's path (index in the chunk), W.out: its light, W.beta_pdf: throughput
 // of the pending vertex | sampling density, W.o: ray direction | reverse density.
+// The materials' code is out of line and the kernel held to 64 registers (four blocks of 256 per
+// SM): the walk stalled on instruction fetch with it inlined, and at three blocks per SM (80
+// registers, no spills) it took 52.1 ms per 1280x720, 32-spp frame against 47.6 ms at four.
 template <class R>
 __global__ void __launch_bounds__(256, 4)
     k_bdw_walk(DevScene S, RenderArgs A, FirstHit const *__restrict__ fh, float *path_rgb, BdwChunk C, WfSlots W,
