@@ -92,7 +92,7 @@ __device__ __forceinline__ float grad_dlog(DevScene const &S, int32_t mi, float3
 template <bool FIRST, int LAYOUT>
 __device__ float3 replay(DevScene const &S, RenderArgs const &A, FirstHit const &f, uint32_t pixel, uint32_t sample,
                          float3 Ltot, float3 w, GradAcc &g, uint32_t *stk, ScatterRec *rec, uint32_t *nscatter) {
-    RngPhilox rng;
+    RngPhiloxMem rng;
     rng.seed(A.seed, pixel, sample);
     float3 p = xyz(f.p), n = xyz(f.n), o = neg(xyz(f.d));
     int32_t mesh = __float_as_int(f.p.w);
